@@ -1,0 +1,224 @@
+/*
+ * ps_gb300.h -- C ABI of the GB300 period-search engine.
+ *
+ * The engine replaces the hot path of the Asteroids@home period_search
+ * application (IanSteveC/PeriodSearch): for every trial period of a scan and
+ * each of the 10 fixed initial poles, a Levenberg-Marquardt fit of a convex
+ * Gaussian-image shape, spin axis, phase function and Lambert weight to the
+ * photometry, then the best pole per period.
+ *
+ * The reference has no plugin API; its in-process seam is the CUDA port's
+ * host interface (period_search_cuda/period_search/start_CUDA.h:2-14), and its
+ * process-level seam is the BOINC app contract (period_search_in ->
+ * period_search_out, period_search_state).  This header covers both:
+ *
+ *   ps_prepare       <- CUDAPrepare   (start_CUDA.cu:119-238)
+ *   ps_precalc_conw  <- CUDAPrecalc   (start_CUDA.cu:248-521)
+ *   ps_scan          <- CUDAStart     (start_CUDA.cu:523-801)
+ *   ps_destroy       <- CUDAUnprepare (start_CUDA.cu:240-246)
+ *   ps_run_files     <- main() of period_search/period_search_BOINC.cpp:147-954
+ *
+ * Differences from the CUDA port's seam, all deliberate:
+ *   - inputs are passed explicitly (ps_problem) instead of through extern
+ *     globals; every array is 0-based, caller-owned and only read during the
+ *     call that receives it;
+ *   - errors come back as ps_status, never through exit();
+ *   - rows are returned to the caller (ps_row) instead of being printed into
+ *     an MFILE; ps_format_row prints the reference's exact row format;
+ *   - a context is used by one host thread at a time; different contexts are
+ *     independent.
+ *
+ * All floating-point quantities are double.  Periods are in hours, epochs in
+ * Julian days, angles in degrees unless stated otherwise.
+ */
+#ifndef PS_GB300_H
+#define PS_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define PS_ABI_VERSION 1
+#define PS_N_POLES 10          /* period_search/constants.h:11 */
+#define PS_POINTS_MAX 1000     /* points per lightcurve, period_search/constants.h:1 */
+#define PS_MAX_N_OBS 20000     /* points per object, period_search/constants.h:2 */
+#define PS_MAX_LC 200          /* lightcurves per object, period_search/constants.h:3 */
+#define PS_MAX_N_FAC 1000      /* facets, period_search/constants.h:5 */
+#define PS_MAX_N_PAR 200       /* parameters, period_search/constants.h:7 */
+#define PS_MAX_LM 10           /* Laplace-series degree, period_search/constants.h:8 */
+
+typedef enum ps_status {
+    PS_OK = 0,
+    PS_ERR_ARG = 1,        /* NULL pointer, inconsistent sizes, bad index range */
+    PS_ERR_LIMIT = 2,      /* a reference size limit is exceeded (reference exit code 2) */
+    PS_ERR_SINGULAR = 4,   /* singular ellipsoid fit (reference ludcmp exit code 4) */
+    PS_ERR_IO = 5,         /* input file missing or malformed, output not writable */
+    PS_ERR_CUDA = 10,      /* a CUDA runtime call failed; see ps_last_error */
+    PS_ERR_NO_DEVICE = 11, /* no usable sm_103 device */
+    PS_ERR_TIMEOUT = 12    /* a device-side bounded wait expired; the context stays usable */
+} ps_status;
+
+/* Arithmetic form of the fit kernels. */
+typedef enum ps_form {
+    PS_FORM_FP64 = 0,  /* plain FP64: the drop-in for the reference fit */
+    PS_FORM_MIXED = 1  /* FP32 facet stage and contractions, FP64 phase/chi^2/solve */
+} ps_form;
+
+/* The 14-line header of period_search_in (period_search_BOINC.cpp:277-303). */
+typedef struct ps_header {
+    double per_start;       /* shortest trial period [h] */
+    double per_step_coef;   /* period step coefficient */
+    double per_end;         /* longest trial period [h] */
+    int32_t ia_prd;         /* 1: period free in the fit */
+    double jd00;            /* epoch of zero time; <= 0 selects floor(min JD) */
+    double phi0_deg;        /* initial rotation angle [deg] */
+    double conw;            /* convexity regularisation weight */
+    int32_t lmax, mmax;     /* degree and order of the Laplace series */
+    int32_t nrows;          /* triangulation rows per octant (8*nrows^2 facets) */
+    double par[3];          /* phase function a, d, k */
+    int32_t ia_par[3];      /* 1: free */
+    double cl;              /* Lambert weight (Lommel-Seeliger weight is 1) */
+    int32_t ia_cl;          /* 1: free */
+    double stop_condition;  /* > 1: iteration count; < 1: minimum rms improvement */
+    int32_t n_iter_min;     /* minimum iterations when stop_condition < 1 */
+    double alamda_incr;     /* LM lambda factor */
+    double alamda_start;    /* LM lambda start */
+} ps_header;
+
+/* One object's photometry, as read from period_search_in
+ * (period_search_BOINC.cpp:322-456).  Points are stored lightcurve after
+ * lightcurve. */
+typedef struct ps_problem {
+    ps_header hdr;
+    int32_t n_lc;                  /* lightcurves (without the convexity rows) */
+    const int32_t *lc_points;      /* [n_lc] points per lightcurve (1..PS_POINTS_MAX) */
+    const int32_t *lc_calibrated;  /* [n_lc] file flag: 1 calibrated, 0 relative */
+    const double *lc_weight;       /* [n_lc] weights, or NULL; -1 means "not given" */
+    int32_t ndata;                 /* sum of lc_points */
+    const double *jd;              /* [ndata] epochs [JD] */
+    const double *brightness;      /* [ndata] reduced intensities */
+    const double *sun;             /* [ndata*3] asteroid->Sun vectors [AU] */
+    const double *earth;           /* [ndata*3] asteroid->Earth vectors [AU] */
+} ps_problem;
+
+typedef struct ps_options {
+    int32_t device;        /* CUDA device ordinal */
+    int32_t form;          /* ps_form */
+    int32_t ctas_per_sm;   /* resident fit slots per SM; 0 = tuned default */
+    int32_t flags;         /* reserved, 0 */
+} ps_options;
+
+/* One output row (period_search_BOINC.cpp:927-931). */
+typedef struct ps_row {
+    double period_h;       /* best period [h] */
+    double rms;            /* best rms deviation */
+    double chi2;           /* rms^2 * ndata */
+    double dark_or_conw;   /* dark-facet %; row of period index 1: conw_r*escl^2 */
+    double lambda_deg;     /* pole longitude [deg], 0..360 */
+    double beta_deg;       /* pole latitude [deg] */
+} ps_row;
+
+/* One LM fit (one period index, one initial pole). */
+typedef struct ps_fit {
+    double dev;            /* final rms deviation */
+    double dark;           /* |sum Area*normal| of the last accepted shape */
+    double totarea;        /* sum of facet areas of the last evaluated shape */
+    double period_h;       /* fitted period [h] */
+    double lambda_deg;     /* fitted pole longitude [deg] (not wrapped) */
+    double beta_deg;       /* fitted pole latitude [deg] */
+    double chisq;          /* final chi^2 (with the convexity rows) */
+    int32_t niter;         /* LM iterations run */
+    int32_t err_code;      /* last gauss_errc code: 0, 1 or 2 */
+} ps_fit;
+
+/* Sizes of a prepared object. */
+typedef struct ps_info {
+    int32_t ndata, n_lc, ncoef, ma, mfit, nfac;
+    int64_t n_max;         /* trial periods in the scan */
+    double escl;           /* initial size scale */
+    double conw_r0;        /* conw / escl^2 */
+    double freq_start, freq_step;   /* [1/h] */
+    int32_t sm_count, slots;        /* device SMs and resident fit slots */
+} ps_info;
+
+/* Device timing of the last ps_scan / ps_fit_batch call, measured with CUDA
+ * events on the context's stream around the fit kernel launches. */
+typedef struct ps_timing {
+    double kernel_ms;      /* fit kernel(s) */
+    double total_ms;       /* kernels + result copy */
+    int64_t fits;          /* fits computed */
+    int64_t evals;         /* model evaluations (mrqcof calls) */
+    int32_t launches;      /* kernel launches */
+} ps_timing;
+
+typedef struct ps_ctx ps_ctx;
+typedef struct ps_input ps_input;
+
+const char *ps_status_string(ps_status st);
+int32_t ps_abi_version(void);
+
+/* ---- period_search_in parsing (host only) ---- */
+/* Parses a period_search_in file with the reference's reading rules
+ * (period_search_BOINC.cpp:277-427).  *out stays owned by the library. */
+ps_status ps_input_read(const char *path, ps_input **out);
+/* A view of the parsed data; valid until ps_input_free. */
+ps_status ps_input_problem(const ps_input *in, ps_problem *view);
+void ps_input_free(ps_input *in);
+
+/* ---- engine ---- */
+/* Prepares an object on a device: input preparation, shape tables,
+ * initial ellipsoid and the device-resident copies.  Replaces CUDAPrepare. */
+ps_status ps_prepare(const ps_problem *prob, const ps_options *opt, ps_ctx **out);
+ps_status ps_get_info(const ps_ctx *ctx, ps_info *out);
+/* Convexity-weight optimisation (period_search_BOINC.cpp:487-715).  On entry
+ * *conw_r is ignored; on exit it holds the final conw_r and *new_conw tells
+ * whether the loop accepted it.  Replaces CUDAPrecalc. */
+ps_status ps_precalc_conw(ps_ctx *ctx, double *conw_r, int32_t *new_conw);
+/* Rows for period indices n_lo..n_hi (1-based, inclusive) at convexity weight
+ * conw_r.  out has n_hi-n_lo+1 rows.  Replaces CUDAStart. */
+ps_status ps_scan(ps_ctx *ctx, double conw_r, int64_t n_lo, int64_t n_hi, ps_row *out);
+/* Individual fits: period index period_index[i] (1-based), pole pole[i]
+ * (1..10).  out has n_fits entries. */
+ps_status ps_fit_batch(ps_ctx *ctx, double conw_r, int64_t n_fits, const int64_t *period_index,
+                       const int32_t *pole, ps_fit *out);
+/* One model evaluation (the reference's mrqcof) at parameters cg[ma]
+ * (0-based, reference layout): alpha[mfit*mfit] row-major, beta[mfit],
+ * area[nfac] (may be NULL); returns chi^2 through *chisq. */
+ps_status ps_eval(ps_ctx *ctx, double conw_r, const double *cg, double *alpha, double *beta,
+                  double *chisq, double *area);
+ps_status ps_last_timing(const ps_ctx *ctx, ps_timing *out);
+const char *ps_last_error(const ps_ctx *ctx);
+void ps_destroy(ps_ctx *ctx);
+
+/* Measured FMA throughput of a device (TFLOP/s, 2 flops per FMA) for FP64
+ * and FP32 SIMT: the compute ceilings that bound the fit kernels. */
+ps_status ps_device_fma_peaks(int32_t device, double *fp64_tflops, double *fp32_tflops);
+
+/* ---- formats ---- */
+/* Writes one row in the reference's format "%.8f  %.6f  %.6f %4.1f %4.0f %4.0f\n"
+ * (period_search_BOINC.cpp:928,931).  Returns the number of characters. */
+int32_t ps_format_row(const ps_row *row, char *buf, size_t len);
+
+/* ---- process-level drop-in ---- */
+/* Runs the BOINC app's job on files: reads in_path (period_search_in), resumes
+ * from state_path (period_search_state, optional) and writes or appends rows
+ * to out_path (period_search_out), checkpointing every checkpoint_rows rows
+ * (0 = only at the end).  Mirrors period_search_BOINC.cpp:218-954. */
+ps_status ps_run_files(const char *in_path, const char *out_path, const char *state_path,
+                       const ps_options *opt, int32_t checkpoint_rows);
+
+/* ---- shape tables (host only) ---- */
+/* Facet normals nor[nfac*3], facet areas darea[nfac] and the Laplace-series
+ * basis dsph[nfac*ncoef] of the trifac grid (trifac.c, areanorm.c,
+ * sphfunc.c).  Sizes: nfac = 8*nrows^2, ncoef = sum over m of the (l,m)
+ * pairs with cos and sin terms.  Any output may be NULL. */
+ps_status ps_shape_tables(int32_t nrows, int32_t lmax, int32_t mmax, int32_t *nfac,
+                          int32_t *ncoef, double *nor, double *darea, double *dsph);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,1 @@
+/* empty stand-in for a BOINC header */

@@ -1,0 +1,608 @@
+// ps_api.cpp -- C ABI of the GB300 period-search engine (ps_gb300.h).
+//
+// A context owns one prepared object: its host copy (HostObject), one device
+// allocation holding every table, the per-slot scratch, the result buffers
+// and a CUDA stream with timing events.  Scans launch the persistent fit
+// kernel once per call; the best-of-poles reduction of the (at most a few
+// hundred kB of) per-fit results runs on the host in the reference's order.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "ps_engine.h"
+#include "ps_host.h"
+
+struct ps_input {
+    psg::ParsedInput data;
+};
+
+struct ps_ctx {
+    psg::HostObject obj;
+    ps_options opt{};
+    cudaStream_t stream = nullptr;
+    cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};
+    char *d_tables = nullptr;          // one allocation with every table
+    psg::DevObject dob{};
+    int sm_count = 0, slots = 0, P = 16;
+    size_t smem = 0;
+    double *d_scratch = nullptr;
+    size_t scratch_stride = 0;
+    unsigned long long *d_queue = nullptr;
+    ps_fit *d_out = nullptr;
+    size_t out_cap = 0;
+    int64_t *d_pidx = nullptr;
+    int *d_pole = nullptr;
+    size_t list_cap = 0;
+    double *d_eval = nullptr;          // cg, alpha, beta, chisq, area of ps_eval
+    std::vector<ps_fit> h_fits;
+    ps_timing timing{};
+    std::string err;
+};
+
+namespace {
+
+ps_status cuda_fail(ps_ctx *c, cudaError_t e, const char *what)
+{
+    if (c) c->err = std::string(what) + ": " + cudaGetErrorString(e);
+    return PS_ERR_CUDA;
+}
+
+#define PSG_CUDA(ctx, call)                                        \
+    do {                                                           \
+        cudaError_t e_ = (call);                                   \
+        if (e_ != cudaSuccess) return cuda_fail((ctx), e_, #call); \
+    } while (0)
+
+// Packs host arrays into one device allocation, 256-byte aligned each.
+struct Packer {
+    std::vector<char> bytes;
+    template <class T>
+    size_t add(const std::vector<T> &v)
+    {
+        size_t off = (bytes.size() + 255) & ~size_t(255);
+        bytes.resize(off + std::max<size_t>(v.size() * sizeof(T), 1));
+        if (!v.empty()) std::memcpy(bytes.data() + off, v.data(), v.size() * sizeof(T));
+        return off;
+    }
+};
+
+psg::FitConfig make_config(const ps_ctx *c, double conw_r)
+{
+    const psg::HostObject &o = c->obj;
+    const ps_header &h = o.hdr;
+    psg::FitConfig f{};
+    f.phi0 = o.phi0;
+    f.alamda_start = h.alamda_start;
+    f.alamda_incr = h.alamda_incr;
+    f.conw_r = conw_r;
+    f.freq_start = o.freq_start;
+    f.freq_step = o.freq_step;
+    f.log_cl = std::log(h.cl);
+    f.par0 = h.par[0];
+    f.par1 = h.par[1];
+    f.par2 = h.par[2];
+    // Stop rule of period_search_BOINC.cpp:847-860.
+    f.n_iter_max = 0;
+    f.iter_diff_max = -1;
+    f.n_iter_min = h.n_iter_min;
+    if (h.stop_condition > 1) {
+        f.n_iter_max = static_cast<int>(h.stop_condition);
+        f.iter_diff_max = 0;
+        f.n_iter_min = 0;
+    }
+    if (h.stop_condition < 1) {
+        f.n_iter_max = 100;  // MAX_N_ITER, period_search/constants.h:6
+        f.iter_diff_max = h.stop_condition;
+    }
+    return f;
+}
+
+ps_status ensure_out(ps_ctx *c, size_t nfits)
+{
+    if (nfits <= c->out_cap) return PS_OK;
+    if (c->d_out) cudaFree(c->d_out);
+    c->d_out = nullptr;
+    size_t cap = std::max(nfits, size_t(1024));
+    PSG_CUDA(c, cudaMalloc(&c->d_out, cap * sizeof(ps_fit)));
+    c->out_cap = cap;
+    return PS_OK;
+}
+
+// Launches the fits described by w (queue and outputs filled in here) and
+// copies the results back into c->h_fits.
+ps_status run_fits(ps_ctx *c, double conw_r, psg::FitWork w)
+{
+    psg::FitConfig cfg = make_config(c, conw_r);
+    ps_status st = ensure_out(c, static_cast<size_t>(w.nfits));
+    if (st != PS_OK) return st;
+    w.queue = c->d_queue;
+    w.scratch = c->d_scratch;
+    w.scratch_stride = c->scratch_stride;
+    w.out = c->d_out;
+    int grid = static_cast<int>(std::min<int64_t>(c->slots, std::max<int64_t>(w.nfits, 1)));
+    PSG_CUDA(c, cudaMemsetAsync(c->d_queue, 0, sizeof(unsigned long long), c->stream));
+    PSG_CUDA(c, cudaEventRecord(c->ev[0], c->stream));
+    int e = psg::launch_fits(c->opt.form, c->dob, cfg, w, grid, c->P, c->smem, c->stream);
+    if (e != 0) return cuda_fail(c, static_cast<cudaError_t>(e), "fit kernel launch");
+    PSG_CUDA(c, cudaEventRecord(c->ev[1], c->stream));
+    c->h_fits.resize(static_cast<size_t>(w.nfits));
+    PSG_CUDA(c, cudaMemcpyAsync(c->h_fits.data(), c->d_out, w.nfits * sizeof(ps_fit), cudaMemcpyDeviceToHost,
+                                c->stream));
+    PSG_CUDA(c, cudaEventRecord(c->ev[2], c->stream));
+    PSG_CUDA(c, cudaStreamSynchronize(c->stream));
+    float k_ms = 0, t_ms = 0;
+    cudaEventElapsedTime(&k_ms, c->ev[0], c->ev[1]);
+    cudaEventElapsedTime(&t_ms, c->ev[0], c->ev[2]);
+    c->timing.kernel_ms = k_ms;
+    c->timing.total_ms = t_ms;
+    c->timing.fits = w.nfits;
+    int64_t evals = 0;
+    for (const ps_fit &f : c->h_fits) evals += f.niter + 1;
+    c->timing.evals = evals;
+    c->timing.launches = 1;
+    return PS_OK;
+}
+
+ps_status scan_rows(ps_ctx *c, double conw_r, int64_t n_lo, int64_t n_hi, ps_row *out, bool prepass)
+{
+    psg::FitWork w{};
+    w.n_lo = n_lo;
+    w.nfits = (n_hi - n_lo + 1) * PS_N_POLES;
+    ps_status st = run_fits(c, conw_r, w);
+    if (st != PS_OK) return st;
+    for (int64_t n = n_lo; n <= n_hi; n++) {
+        ps_row r = psg::best_of_poles(&c->h_fits[static_cast<size_t>(n - n_lo) * PS_N_POLES], c->obj.ndata);
+        if (prepass && std::isnan(r.dark_or_conw)) r.dark_or_conw = 1.0;
+        out[n - n_lo] = r;
+    }
+    return PS_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char *ps_status_string(ps_status st)
+{
+    switch (st) {
+    case PS_OK: return "ok";
+    case PS_ERR_ARG: return "invalid argument";
+    case PS_ERR_LIMIT: return "a size limit of the reference is exceeded";
+    case PS_ERR_SINGULAR: return "singular matrix in the ellipsoid fit";
+    case PS_ERR_IO: return "input/output error";
+    case PS_ERR_CUDA: return "CUDA error";
+    case PS_ERR_NO_DEVICE: return "no usable CUDA device";
+    case PS_ERR_TIMEOUT: return "device wait timed out";
+    }
+    return "unknown status";
+}
+
+int32_t ps_abi_version(void) { return PS_ABI_VERSION; }
+
+ps_status ps_input_read(const char *path, ps_input **out)
+{
+    if (!path || !out) return PS_ERR_ARG;
+    *out = nullptr;
+    auto in = std::make_unique<ps_input>();
+    std::string err;
+    ps_status st = psg::parse_input_file(path, in->data, err);
+    if (st != PS_OK) {
+        std::fprintf(stderr, "ps_input_read: %s\n", err.c_str());
+        return st;
+    }
+    *out = in.release();
+    return PS_OK;
+}
+
+ps_status ps_input_problem(const ps_input *in, ps_problem *v)
+{
+    if (!in || !v) return PS_ERR_ARG;
+    const psg::ParsedInput &d = in->data;
+    v->hdr = d.hdr;
+    v->n_lc = static_cast<int32_t>(d.lc_points.size());
+    v->lc_points = d.lc_points.data();
+    v->lc_calibrated = d.lc_calibrated.data();
+    v->lc_weight = d.lc_weight.data();
+    v->ndata = static_cast<int32_t>(d.jd.size());
+    v->jd = d.jd.data();
+    v->brightness = d.brightness.data();
+    v->sun = d.sun.data();
+    v->earth = d.earth.data();
+    return PS_OK;
+}
+
+void ps_input_free(ps_input *in) { delete in; }
+
+ps_status ps_prepare(const ps_problem *prob, const ps_options *opt, ps_ctx **out)
+{
+    if (!prob || !out) return PS_ERR_ARG;
+    *out = nullptr;
+    auto c = std::make_unique<ps_ctx>();
+    if (opt) c->opt = *opt;
+    if (c->opt.form != PS_FORM_FP64 && c->opt.form != PS_FORM_MIXED) return PS_ERR_ARG;
+    std::string err;
+    ps_status st = psg::prepare_object(*prob, c->obj, err);
+    if (st != PS_OK) {
+        std::fprintf(stderr, "ps_prepare: %s\n", err.c_str());
+        return st;
+    }
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev <= c->opt.device || c->opt.device < 0)
+        return PS_ERR_NO_DEVICE;
+    cudaDeviceProp prop;
+    if (cudaGetDeviceProperties(&prop, c->opt.device) != cudaSuccess) return PS_ERR_NO_DEVICE;
+    if (prop.major < 10) return PS_ERR_NO_DEVICE;
+    ps_ctx *cp = c.get();
+    PSG_CUDA(cp, cudaSetDevice(c->opt.device));
+    c->sm_count = prop.multiProcessorCount;
+    PSG_CUDA(cp, cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
+    for (auto &e : c->ev) PSG_CUDA(cp, cudaEventCreate(&e));
+
+    psg::HostObject &o = c->obj;
+    const psg::ShapeTables &s = o.shape;
+    const int F = s.nfac;
+    // Facet-major tables transposed to [index][facet] where threads run over
+    // facets, and the Earth/Sun vectors split into coalesced components.
+    std::vector<double> nx(F), ny(F), nz(F), pleg(static_cast<size_t>(s.npairs) * F),
+        fc(static_cast<size_t>(s.mmax + 1) * F), fs(static_cast<size_t>(s.mmax + 1) * F);
+    for (int i = 0; i < F; i++) {
+        nx[i] = s.nor[3 * i];
+        ny[i] = s.nor[3 * i + 1];
+        nz[i] = s.nor[3 * i + 2];
+        for (int q = 0; q < s.npairs; q++) pleg[static_cast<size_t>(q) * F + i] = s.pleg[static_cast<size_t>(i) * s.npairs + q];
+        for (int m = 0; m <= s.mmax; m++) {
+            fc[static_cast<size_t>(m) * F + i] = s.fc[static_cast<size_t>(i) * (s.mmax + 1) + m];
+            fs[static_cast<size_t>(m) * F + i] = s.fs[static_cast<size_t>(i) * (s.mmax + 1) + m];
+        }
+    }
+    std::vector<double> ex(o.ndata), ey(o.ndata), ez(o.ndata), sx(o.ndata), sy(o.ndata), sz(o.ndata);
+    for (int q = 0; q < o.ndata; q++) {
+        ex[q] = o.ee[3 * q];
+        ey[q] = o.ee[3 * q + 1];
+        ez[q] = o.ee[3 * q + 2];
+        sx[q] = o.ee0[3 * q];
+        sy[q] = o.ee0[3 * q + 1];
+        sz[q] = o.ee0[3 * q + 2];
+    }
+    std::vector<float> dsph_f(s.dsph.begin(), s.dsph.end());
+    Packer pk;
+    size_t o_nx = pk.add(nx), o_ny = pk.add(ny), o_nz = pk.add(nz), o_darea = pk.add(s.darea),
+           o_dsph = pk.add(s.dsph), o_pleg = pk.add(pleg), o_fc = pk.add(fc), o_fs = pk.add(fs),
+           o_pm = pk.add(s.pair_m), o_pn = pk.add(s.pair_n), o_tim = pk.add(o.tim), o_br = pk.add(o.bright),
+           o_sig = pk.add(o.sig), o_w = pk.add(o.weight), o_ex = pk.add(ex), o_ey = pk.add(ey), o_ez = pk.add(ez),
+           o_sx = pk.add(sx), o_sy = pk.add(sy), o_sz = pk.add(sz), o_ls = pk.add(o.lc_start),
+           o_ln = pk.add(o.lc_points), o_lr = pk.add(o.lc_rel), o_fl = pk.add(o.free_list),
+           o_cgf = pk.add(o.cg_first), o_dsf = pk.add(dsph_f);
+    PSG_CUDA(cp, cudaMalloc(&c->d_tables, pk.bytes.size()));
+    PSG_CUDA(cp, cudaMemcpyAsync(c->d_tables, pk.bytes.data(), pk.bytes.size(), cudaMemcpyHostToDevice, c->stream));
+    char *b = c->d_tables;
+    psg::DevObject &d = c->dob;
+    d.nfac = F;
+    d.ncoef = o.ncoef;
+    d.ma = o.ma;
+    d.mfit = o.mfit;
+    d.npairs = s.npairs;
+    d.mmax = s.mmax;
+    d.n_lc = o.n_lc + 1;
+    d.ndata = o.ndata;
+    d.max_rel_points = o.max_rel_points;
+    d.nx = reinterpret_cast<const double *>(b + o_nx);
+    d.ny = reinterpret_cast<const double *>(b + o_ny);
+    d.nz = reinterpret_cast<const double *>(b + o_nz);
+    d.darea = reinterpret_cast<const double *>(b + o_darea);
+    d.dsph = reinterpret_cast<const double *>(b + o_dsph);
+    d.pleg = reinterpret_cast<const double *>(b + o_pleg);
+    d.fc = reinterpret_cast<const double *>(b + o_fc);
+    d.fs = reinterpret_cast<const double *>(b + o_fs);
+    d.pair_m = reinterpret_cast<const int *>(b + o_pm);
+    d.pair_n = reinterpret_cast<const int *>(b + o_pn);
+    d.tim = reinterpret_cast<const double *>(b + o_tim);
+    d.bright = reinterpret_cast<const double *>(b + o_br);
+    d.sig = reinterpret_cast<const double *>(b + o_sig);
+    d.weight = reinterpret_cast<const double *>(b + o_w);
+    d.eex = reinterpret_cast<const double *>(b + o_ex);
+    d.eey = reinterpret_cast<const double *>(b + o_ey);
+    d.eez = reinterpret_cast<const double *>(b + o_ez);
+    d.e0x = reinterpret_cast<const double *>(b + o_sx);
+    d.e0y = reinterpret_cast<const double *>(b + o_sy);
+    d.e0z = reinterpret_cast<const double *>(b + o_sz);
+    d.lc_start = reinterpret_cast<const int *>(b + o_ls);
+    d.lc_npts = reinterpret_cast<const int *>(b + o_ln);
+    d.lc_rel = reinterpret_cast<const int *>(b + o_lr);
+    d.free_list = reinterpret_cast<const int *>(b + o_fl);
+    d.cg_first = reinterpret_cast<const double *>(b + o_cgf);
+    d.dsph_f = reinterpret_cast<const float *>(b + o_dsf);
+
+    // Slot plan: the largest point tile whose shared-memory footprint fits.
+    size_t smem_max = static_cast<size_t>(prop.sharedMemPerBlockOptin);
+    int P = 16;
+    psg::SlotLayout L = psg::make_layout(o.ma, o.mfit, F, P);
+    while (L.bytes > smem_max && P > 2) {
+        P /= 2;
+        L = psg::make_layout(o.ma, o.mfit, F, P);
+    }
+    if (L.bytes > smem_max) {
+        c->err = "shared-memory plan of a fit slot exceeds the device limit";
+        std::fprintf(stderr, "ps_prepare: %s\n", c->err.c_str());
+        return PS_ERR_LIMIT;
+    }
+    c->P = P;
+    c->smem = L.bytes;
+    int e = psg::set_kernel_smem(c->opt.form, c->smem);
+    if (e != 0) return cuda_fail(cp, static_cast<cudaError_t>(e), "cudaFuncSetAttribute");
+    int per_sm = 0;
+    e = psg::occupancy_slots(c->opt.form, c->smem, &per_sm);
+    if (e != 0) return cuda_fail(cp, static_cast<cudaError_t>(e), "occupancy");
+    if (per_sm < 1) {
+        c->err = "fit slot does not fit on an SM";
+        return PS_ERR_LIMIT;
+    }
+    if (c->opt.ctas_per_sm > 0) per_sm = std::min(per_sm, c->opt.ctas_per_sm);
+    c->slots = per_sm * c->sm_count;
+    c->scratch_stride = static_cast<size_t>(std::max(o.max_rel_points, 1)) * (o.ma + 1);
+    c->scratch_stride = (c->scratch_stride + 31) & ~size_t(31);
+    PSG_CUDA(cp, cudaMalloc(&c->d_scratch, c->scratch_stride * c->slots * sizeof(double)));
+    PSG_CUDA(cp, cudaMalloc(&c->d_queue, 256));
+    size_t ev_doubles = static_cast<size_t>(o.ma) + static_cast<size_t>(o.mfit) * o.mfit + o.mfit + 1 + F;
+    PSG_CUDA(cp, cudaMalloc(&c->d_eval, ev_doubles * sizeof(double)));
+    PSG_CUDA(cp, cudaStreamSynchronize(c->stream));
+    *out = c.release();
+    return PS_OK;
+}
+
+ps_status ps_get_info(const ps_ctx *c, ps_info *out)
+{
+    if (!c || !out) return PS_ERR_ARG;
+    const psg::HostObject &o = c->obj;
+    out->ndata = o.ndata;
+    out->n_lc = o.n_lc;
+    out->ncoef = o.ncoef;
+    out->ma = o.ma;
+    out->mfit = o.mfit;
+    out->nfac = o.shape.nfac;
+    out->n_max = o.n_max;
+    out->escl = o.escl;
+    out->conw_r0 = o.conw_r0;
+    out->freq_start = o.freq_start;
+    out->freq_step = o.freq_step;
+    out->sm_count = c->sm_count;
+    out->slots = c->slots;
+    return PS_OK;
+}
+
+ps_status ps_precalc_conw(ps_ctx *c, double *conw_r, int32_t *new_conw)
+{
+    if (!c || !conw_r || !new_conw) return PS_ERR_ARG;
+    PSG_CUDA(c, cudaSetDevice(c->opt.device));
+    const psg::HostObject &o = c->obj;
+    double cw = o.conw_r0;
+    int nc = 0;
+    int64_t ntest = std::min<int64_t>(10, o.n_max);
+    std::vector<ps_row> rows(static_cast<size_t>(std::max<int64_t>(ntest, 1)));
+    double launches = 0, kms = 0, tms = 0;
+    int64_t fits = 0, evals = 0;
+    while (nc != 1 && (cw * o.escl * o.escl) < 10.0) {
+        if (ntest < 1) break;
+        ps_status st = scan_rows(c, cw, 1, ntest, rows.data(), true);
+        if (st != PS_OK) return st;
+        launches += 1;
+        kms += c->timing.kernel_ms;
+        tms += c->timing.total_ms;
+        fits += c->timing.fits;
+        evals += c->timing.evals;
+        double sum = 0.0;
+        for (int64_t n = 0; n < ntest; n++) sum = sum + rows[static_cast<size_t>(n)].dark_or_conw;
+        double ave = sum / ntest;
+        if (ave < 1.0) nc = 1;
+        if (ave >= 1.0) cw = cw * 2;
+    }
+    c->timing.kernel_ms = kms;
+    c->timing.total_ms = tms;
+    c->timing.fits = fits;
+    c->timing.evals = evals;
+    c->timing.launches = static_cast<int32_t>(launches);
+    *conw_r = cw;
+    *new_conw = nc;
+    return PS_OK;
+}
+
+ps_status ps_scan(ps_ctx *c, double conw_r, int64_t n_lo, int64_t n_hi, ps_row *out)
+{
+    if (!c || !out || n_lo < 1 || n_hi < n_lo || !(conw_r > 0)) return PS_ERR_ARG;
+    PSG_CUDA(c, cudaSetDevice(c->opt.device));
+    ps_status st = scan_rows(c, conw_r, n_lo, n_hi, out, false);
+    if (st != PS_OK) return st;
+    if (n_lo == 1) out[0].dark_or_conw = conw_r * c->obj.escl * c->obj.escl;
+    return PS_OK;
+}
+
+ps_status ps_fit_batch(ps_ctx *c, double conw_r, int64_t n_fits, const int64_t *period_index, const int32_t *pole,
+                       ps_fit *out)
+{
+    if (!c || !out || !period_index || !pole || n_fits < 1 || !(conw_r > 0)) return PS_ERR_ARG;
+    for (int64_t i = 0; i < n_fits; i++)
+        if (period_index[i] < 1 || pole[i] < 1 || pole[i] > PS_N_POLES) return PS_ERR_ARG;
+    PSG_CUDA(c, cudaSetDevice(c->opt.device));
+    if (static_cast<size_t>(n_fits) > c->list_cap) {
+        if (c->d_pidx) cudaFree(c->d_pidx);
+        if (c->d_pole) cudaFree(c->d_pole);
+        c->d_pidx = nullptr;
+        c->d_pole = nullptr;
+        PSG_CUDA(c, cudaMalloc(&c->d_pidx, n_fits * sizeof(int64_t)));
+        PSG_CUDA(c, cudaMalloc(&c->d_pole, n_fits * sizeof(int)));
+        c->list_cap = static_cast<size_t>(n_fits);
+    }
+    PSG_CUDA(c, cudaMemcpyAsync(c->d_pidx, period_index, n_fits * sizeof(int64_t), cudaMemcpyHostToDevice, c->stream));
+    PSG_CUDA(c, cudaMemcpyAsync(c->d_pole, pole, n_fits * sizeof(int), cudaMemcpyHostToDevice, c->stream));
+    psg::FitWork w{};
+    w.n_lo = 1;
+    w.nfits = n_fits;
+    w.period_index = c->d_pidx;
+    w.pole = c->d_pole;
+    ps_status st = run_fits(c, conw_r, w);
+    if (st != PS_OK) return st;
+    std::memcpy(out, c->h_fits.data(), n_fits * sizeof(ps_fit));
+    return PS_OK;
+}
+
+ps_status ps_eval(ps_ctx *c, double conw_r, const double *cg, double *alpha, double *beta, double *chisq,
+                  double *area)
+{
+    if (!c || !cg || !alpha || !beta || !chisq || !(conw_r > 0)) return PS_ERR_ARG;
+    PSG_CUDA(c, cudaSetDevice(c->opt.device));
+    const psg::HostObject &o = c->obj;
+    const int ma = o.ma, mf = o.mfit, F = o.shape.nfac;
+    double *d_cg = c->d_eval, *d_al = d_cg + ma, *d_be = d_al + static_cast<size_t>(mf) * mf, *d_c2 = d_be + mf,
+           *d_ar = d_c2 + 1;
+    PSG_CUDA(c, cudaMemcpyAsync(d_cg, cg, ma * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+    psg::FitConfig cfg = make_config(c, conw_r);
+    int e = psg::launch_eval(c->opt.form, c->dob, cfg, d_cg, d_al, d_be, d_c2, d_ar, c->d_scratch, c->P, c->smem,
+                             c->stream);
+    if (e != 0) return cuda_fail(c, static_cast<cudaError_t>(e), "eval kernel launch");
+    PSG_CUDA(c, cudaMemcpyAsync(alpha, d_al, static_cast<size_t>(mf) * mf * sizeof(double), cudaMemcpyDeviceToHost,
+                                c->stream));
+    PSG_CUDA(c, cudaMemcpyAsync(beta, d_be, mf * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+    PSG_CUDA(c, cudaMemcpyAsync(chisq, d_c2, sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+    if (area) PSG_CUDA(c, cudaMemcpyAsync(area, d_ar, F * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+    PSG_CUDA(c, cudaStreamSynchronize(c->stream));
+    return PS_OK;
+}
+
+ps_status ps_last_timing(const ps_ctx *c, ps_timing *out)
+{
+    if (!c || !out) return PS_ERR_ARG;
+    *out = c->timing;
+    return PS_OK;
+}
+
+const char *ps_last_error(const ps_ctx *c) { return c ? c->err.c_str() : ""; }
+
+void ps_destroy(ps_ctx *c)
+{
+    if (!c) return;
+    cudaSetDevice(c->opt.device);
+    if (c->stream) cudaStreamSynchronize(c->stream);
+    cudaFree(c->d_tables);
+    cudaFree(c->d_scratch);
+    cudaFree(c->d_queue);
+    cudaFree(c->d_out);
+    cudaFree(c->d_pidx);
+    cudaFree(c->d_pole);
+    cudaFree(c->d_eval);
+    for (auto &e : c->ev)
+        if (e) cudaEventDestroy(e);
+    if (c->stream) cudaStreamDestroy(c->stream);
+    delete c;
+}
+
+ps_status ps_device_fma_peaks(int32_t device, double *fp64_tflops, double *fp32_tflops)
+{
+    if (!fp64_tflops || !fp32_tflops) return PS_ERR_ARG;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || device < 0 || device >= ndev) return PS_ERR_NO_DEVICE;
+    if (cudaSetDevice(device) != cudaSuccess) return PS_ERR_NO_DEVICE;
+    int e = psg::measure_fma_peaks(fp64_tflops, fp32_tflops, nullptr);
+    return e == 0 ? PS_OK : PS_ERR_CUDA;
+}
+
+int32_t ps_format_row(const ps_row *r, char *buf, size_t len)
+{
+    if (!r || !buf) return -1;
+    return std::snprintf(buf, len, "%.8f  %.6f  %.6f %4.1f %4.0f %4.0f\n", r->period_h, r->rms, r->chi2,
+                         r->dark_or_conw, r->lambda_deg, r->beta_deg);
+}
+
+ps_status ps_shape_tables(int32_t nrows, int32_t lmax, int32_t mmax, int32_t *nfac, int32_t *ncoef, double *nor,
+                          double *darea, double *dsph)
+{
+    if (nrows < 1 || lmax < 0 || mmax < 0 || mmax > lmax || lmax > PS_MAX_LM || 8 * nrows * nrows > PS_MAX_N_FAC)
+        return PS_ERR_ARG;
+    psg::ShapeTables s;
+    psg::build_shape(s, nrows, lmax, mmax);
+    if (nfac) *nfac = s.nfac;
+    if (ncoef) *ncoef = s.ncoef;
+    if (nor) std::memcpy(nor, s.nor.data(), s.nor.size() * sizeof(double));
+    if (darea) std::memcpy(darea, s.darea.data(), s.darea.size() * sizeof(double));
+    if (dsph) std::memcpy(dsph, s.dsph.data(), s.dsph.size() * sizeof(double));
+    return PS_OK;
+}
+
+// Process-level drop-in (period_search_BOINC.cpp:218-954): resume from the
+// state file, run the convexity pre-pass, scan, append rows, checkpoint by
+// writing "temp" next to the state file and renaming it (do_checkpoint,
+// :85-101).
+ps_status ps_run_files(const char *in_path, const char *out_path, const char *state_path, const ps_options *opt,
+                       int32_t checkpoint_rows)
+{
+    if (!in_path || !out_path) return PS_ERR_ARG;
+    ps_input *in = nullptr;
+    ps_status st = ps_input_read(in_path, &in);
+    if (st != PS_OK) return st;
+    ps_problem prob;
+    ps_input_problem(in, &prob);
+    int64_t n_start_from = 1;
+    bool resume = false;
+    if (state_path) {
+        FILE *sf = std::fopen(state_path, "r");
+        if (sf) {
+            int nlines = 0;
+            if (std::fscanf(sf, "%d", &nlines) == 1) {
+                n_start_from = nlines + 1;
+                resume = true;
+            }
+            std::fclose(sf);
+        }
+    }
+    ps_ctx *c = nullptr;
+    st = ps_prepare(&prob, opt, &c);
+    if (st != PS_OK) {
+        ps_input_free(in);
+        return st;
+    }
+    double conw_r = 0;
+    int32_t new_conw = 0;
+    st = ps_precalc_conw(c, &conw_r, &new_conw);
+    FILE *f = nullptr;
+    if (st == PS_OK) {
+        f = std::fopen(out_path, resume ? "a" : "w");
+        if (!f) st = PS_ERR_IO;
+    }
+    const int64_t n_max = c->obj.n_max;
+    const int64_t chunk = std::max<int64_t>(checkpoint_rows > 0 ? checkpoint_rows : n_max, 1);
+    std::vector<ps_row> rows;
+    for (int64_t n0 = n_start_from; st == PS_OK && n0 <= n_max; n0 += chunk) {
+        int64_t n1 = std::min(n_max, n0 + chunk - 1);
+        rows.resize(static_cast<size_t>(n1 - n0 + 1));
+        st = ps_scan(c, conw_r, n0, n1, rows.data());
+        if (st != PS_OK) break;
+        char line[256];
+        for (const ps_row &r : rows) {
+            ps_format_row(&r, line, sizeof line);
+            std::fputs(line, f);
+        }
+        std::fflush(f);
+        if (state_path && checkpoint_rows > 0) {
+            std::string tmp = std::string(state_path) + ".temp";
+            FILE *t = std::fopen(tmp.c_str(), "w");
+            if (!t) {
+                st = PS_ERR_IO;
+                break;
+            }
+            std::fprintf(t, "%lld", static_cast<long long>(n1));
+            std::fclose(t);
+            if (std::rename(tmp.c_str(), state_path) != 0) st = PS_ERR_IO;
+        }
+    }
+    if (f) std::fclose(f);
+    ps_destroy(c);
+    ps_input_free(in);
+    return st;
+}
+
+}  // extern "C"

@@ -1,0 +1,135 @@
+"""Generates the golden fixtures of tests/golden/ from the reference tree.
+
+Run in a container where the reference project is mounted (default
+/root/reference) after `make -C oracle ref` has built the reference CPU app
+into oracle/_ref/ps_ref.  Writes:
+
+* period_search_in / period_search_out -- the reference's own committed
+  golden input/output pair (period_search/period_search_in and _out);
+* golden12.full -- the reference binary's rows 1..12 of that input at %.17g
+  (input truncated with per_end so that the scan has 12 periods);
+* <case>/period_search_in, <case>/period_search_out, <case>/ref.full -- the
+  seeded synthetic cases of periodsearch_gb300.synth and the reference
+  binary's output for each (text and %.17g);
+* unit_arrays.json -- golden arrays of the reference's unit tests
+  (period_search_pure_cpu_win/UnitTest_pure_cpu_win/arrangers.cpp and the
+  test inputs of InnerFunctionsTests.cpp): trifac vertex triplets, normal
+  angles, the Laplace basis, the ellipsoid coefficients and the phase function.
+
+Usage: python tests/golden/make_fixtures.py [REFERENCE_ROOT]
+"""
+from __future__ import annotations
+
+import json
+import math
+import re
+import shutil
+import subprocess
+import sys
+import tempfile
+from pathlib import Path
+
+HERE = Path(__file__).resolve().parent
+ROOT = HERE.parent.parent
+sys.path.insert(0, str(ROOT))
+sys.path.insert(0, str(ROOT / "tests"))
+
+from oracle_binding import REF_BIN  # noqa: E402
+from periodsearch_gb300 import synth  # noqa: E402
+
+SYNTH_CASES = ["tiny_cal", "tiny_rel", "tiny_mix", "tiny_stop", "c0_12"]
+
+
+def _truncate_periods(text: str, n_periods: int) -> str:
+    """Sets per_end so that the scan has exactly n_periods trial periods."""
+    lines = text.split("\n")
+    per_start, coef, _, ia = lines[0].split()[:4]
+    per_start, coef = float(per_start), float(coef)
+    jd = []
+    i = 15
+    n_lc = int(lines[14].split()[0])
+    for _ in range(n_lc):
+        npts = int(lines[i].split()[0])
+        jd.extend(float(l.split()[0]) for l in lines[i + 1:i + 1 + npts])
+        i += 1 + npts
+    step = 0.5 / (max(jd) - min(jd)) / 24 * coef
+    f_end = 1 / per_start - (n_periods - 0.5) * step
+    lines[0] = f"{per_start:g} {coef:g} {1 / f_end:.10f} {ia} period_start period_step period_end fixed/free"
+    return "\n".join(lines)
+
+
+def _run_ref(workdir: Path) -> None:
+    subprocess.run([str(REF_BIN)], cwd=workdir, check=True, capture_output=True)
+    shutil.move(str(workdir / "period_search_out.full"), str(workdir / "ref.full"))
+
+
+def _arrays(src: str, func: str) -> dict[str, list[float]]:
+    """Initialised arrays declared in the body of function `func`."""
+    m = re.search(r"\n\w[\w\s\*]*\b" + func + r"\s*\([^)]*\)\s*\{", src)
+    body_start = m.end()
+    depth, i = 1, body_start
+    while depth:
+        depth += {"{": 1, "}": -1}.get(src[i], 0)
+        i += 1
+    body = src[body_start:i]
+    out = {}
+    for am in re.finditer(r"(?:double|int)\s+(\w+)\s*\[[^\]]*\]\s*=\s*\{([^}]*)\}", body):
+        vals = [v.strip() for v in am.group(2).split(",") if v.strip()]
+        out[am.group(1)] = [float(v) for v in vals]
+    return out
+
+
+def unit_arrays(ref_root: Path) -> dict:
+    ut = ref_root / "period_search_pure_cpu_win" / "UnitTest_pure_cpu_win"
+    src = (ut / "arrangers.cpp").read_text()
+    out: dict = {"source": "period_search_pure_cpu_win/UnitTest_pure_cpu_win/arrangers.cpp"}
+    a = _arrays(src, "get_ifp")
+    out["ifp"] = [[int(a[f"_ifp_{j}"][i]) for j in (1, 2, 3)] for i in range(1, 289)]
+    out["at"] = _arrays(src, "get_at")["_at"][1:289]
+    out["af"] = _arrays(src, "get_af")["_af"][1:289]
+    d = _arrays(src, "get_dsph")
+    # _dsph_k[i] = Dsph[i][k] for facets 1..146, coefficients 1..16
+    out["dsph_146x16"] = [[d[f"_dsph_{k}"][i] for k in range(1, 17)] for i in range(1, 147)]
+    out["cg_first_l3"] = _arrays(src, "get_cg_first")["_cg_first_local"][1:17]
+    # TestEllfit inputs (InnerFunctionsTests.cpp:356-421): Lmax = Mmax = 3,
+    # calibrated data (escl * 0.8), mean brightness and solar phase angle of
+    # the reference object's first lightcurve.
+    out["ellfit_inputs"] = {"ave": 0.382008772881355651573898057904, "al0": 0.069555451868686835048549710336,
+                            "onlyrel": 0, "lmax": 3, "nrows": 6}
+    x1 = _arrays(src, "get_xx1")["__xx1"][1:4]
+    x2 = _arrays(src, "get_xx2")["__xx2"][1:4]
+    cg = _arrays(src, "get_cg24")["_cg"]
+    out["phasec"] = {"xx1": x1, "xx2": x2, "par": cg[20:23], "dphp": _arrays(src, "get_dphp")["__dphp"][1:4],
+                     "scale": 1.214621163362573641464337015350}
+    return out
+
+
+def main(ref_root: Path) -> None:
+    if not REF_BIN.exists():
+        subprocess.run(["make", "-s", "-C", str(ROOT / "oracle"), "ref", f"REF_DIR={ref_root / 'period_search'}"],
+                       check=True)
+    gold_in = ref_root / "period_search" / "period_search_in"
+    shutil.copy(gold_in, HERE / "period_search_in")
+    shutil.copy(ref_root / "period_search" / "period_search_out", HERE / "period_search_out")
+    with tempfile.TemporaryDirectory() as td:
+        td = Path(td)
+        (td / "period_search_in").write_text(_truncate_periods(gold_in.read_text(), 12))
+        _run_ref(td)
+        shutil.copy(td / "ref.full", HERE / "golden12.full")
+    for case in SYNTH_CASES:
+        d = HERE / case
+        d.mkdir(exist_ok=True)
+        if case == "c0_12":
+            text = _truncate_periods(synth.make_object("c0").text, 12)
+        else:
+            text = synth.make_object(case).text
+        (d / "period_search_in").write_text(text)
+        _run_ref(d)
+        for junk in ("temp", "period_search_state"):
+            (d / junk).unlink(missing_ok=True)
+    (HERE / "unit_arrays.json").write_text(json.dumps(unit_arrays(ref_root)))
+    print("fixtures written to", HERE)
+
+
+if __name__ == "__main__":
+    main(Path(sys.argv[1]) if len(sys.argv) > 1 else Path("/root/reference"))

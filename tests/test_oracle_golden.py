@@ -1,0 +1,143 @@
+"""The oracle against the reference's golden vectors.
+
+Pins: period_search_out of the reference project (text), the reference
+binary's full-precision rows for the same input and for seeded synthetic
+cases (generated by tests/golden/make_fixtures.py), and the golden arrays of
+the reference's unit tests.  The oracle must be bit-identical on x86-64.
+"""
+from __future__ import annotations
+
+import json
+import math
+import platform
+from concurrent.futures import ThreadPoolExecutor
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN, SYNTH_CASES
+
+BITEXACT = platform.machine() == "x86_64"
+
+
+def _rows_array(rows):
+    return np.array([list(r) for r in rows])
+
+
+def _format(r):
+    return "%.8f  %.6f  %.6f %4.1f %4.0f %4.0f\n" % tuple(r)
+
+
+@pytest.mark.parametrize("case", [c for c in SYNTH_CASES if c != "c0_12"])
+def test_synthetic_cases_match_reference_binary(oracle, case):
+    d = GOLDEN / case
+    p = oracle.OracleProblem(d / "period_search_in")
+    cw, _ = p.precalc_conw()
+    rows = p.scan(cw, 1, p.info()["n_max"])
+    got = _rows_array(rows)
+    ref = np.loadtxt(d / "ref.full", ndmin=2)
+    assert got.shape == ref.shape
+    if BITEXACT:
+        assert np.array_equal(got, ref)
+    else:
+        np.testing.assert_allclose(got, ref, rtol=1e-6, atol=1e-9)
+    text = "".join(_format(r) for r in got)
+    assert text == (d / "period_search_out").read_text()
+
+
+def test_golden_rows_match_reference_output(oracle):
+    """Rows 1..3 of the reference's period_search_out (N = 500 relative
+    points, L = 6, 288 facets), with the pre-pass weight taken from row 1
+    (0.1 = conw * escl^2 / escl^2: no doubling), fitted in parallel."""
+    p0 = oracle.OracleProblem(GOLDEN / "period_search_in")
+    conw_r = p0.info()["conw_r"]
+
+    def one(n):
+        p = oracle.OracleProblem(GOLDEN / "period_search_in")
+        p.setup(conw_r)
+        return p.scan(conw_r, n, n)[0]
+
+    with ThreadPoolExecutor(3) as ex:
+        rows = list(ex.map(one, [1, 2, 3]))
+    got = _rows_array(rows)
+    got[0][3] = conw_r * p0.info()["escl"] ** 2
+    full = np.loadtxt(GOLDEN / "golden12.full", ndmin=2)[:3]
+    if BITEXACT:
+        assert np.array_equal(got, full)
+    else:
+        np.testing.assert_allclose(got, full, rtol=1e-6)
+    golden_text = (GOLDEN / "period_search_out").read_text().splitlines(keepends=True)[:3]
+    assert "".join(_format(r) for r in got) == "".join(golden_text)
+
+
+def test_golden12_is_prefix_of_reference_output():
+    full = np.loadtxt(GOLDEN / "golden12.full", ndmin=2)
+    golden_text = (GOLDEN / "period_search_out").read_text().splitlines(keepends=True)[:12]
+    assert "".join(_format(r) for r in full) == "".join(golden_text)
+
+
+# ---- unit-level golden arrays (reference unit tests) ----
+
+@pytest.fixture(scope="module")
+def unit():
+    return json.loads((GOLDEN / "unit_arrays.json").read_text())
+
+
+def _shape(oracle, nrows, lmax):
+    import ctypes as C
+
+    L = oracle.lib()
+    nf = 8 * nrows * nrows
+    nc = sum(1 if m == 0 else 2 for m in range(lmax + 1) for _ in range(m, lmax + 1))
+    ifp = np.zeros(nf * 3, np.int32)
+    at, af, darea = np.zeros(nf), np.zeros(nf), np.zeros(nf)
+    nor = np.zeros(nf * 3)
+    dsph = np.zeros(nf * nc)
+    dp = lambda a: a.ctypes.data_as(C.POINTER(C.c_double))
+    L.pso_shape_export.argtypes = [C.c_int] * 3 + [C.POINTER(C.c_int)] + [C.POINTER(C.c_double)] * 5
+    L.pso_shape_export(nrows, lmax, lmax, ifp.ctypes.data_as(C.POINTER(C.c_int)), dp(at), dp(af), dp(nor),
+                       dp(darea), dp(dsph))
+    return ifp.reshape(nf, 3), at, af, nor.reshape(nf, 3), darea, dsph.reshape(nf, nc)
+
+
+def test_trifac_matches_golden(oracle, unit):
+    ifp, *_ = _shape(oracle, 6, 3)
+    assert ifp.tolist() == unit["ifp"]
+
+
+def test_areanorm_and_sphfunc_match_golden(oracle, unit):
+    _, at, af, _, _, dsph = _shape(oracle, 6, 3)
+    np.testing.assert_allclose(at, unit["at"], rtol=0, atol=2e-15)
+    # af of facets on the -x half-plane sit at +-pi; compare on the circle
+    d = np.angle(np.exp(1j * (af - np.array(unit["af"]))))
+    assert np.abs(d).max() < 2e-15
+    np.testing.assert_allclose(dsph[:146], unit["dsph_146x16"], rtol=1e-13, atol=1e-14)
+
+
+def test_ellfit_matches_golden(oracle, unit):
+    import ctypes as C
+
+    inp = unit["ellfit_inputs"]
+    a, b, c = 1.05, 1.00, 0.95
+    rfit = math.sqrt(2 * inp["ave"] / (0.5 * math.pi * (1 + math.cos(inp["al0"]))))
+    escl = rfit / math.sqrt((a * b + b * c + a * c) / 3) * 0.8
+    cg = np.zeros(16)
+    L = oracle.lib()
+    L.pso_ellfit_export.argtypes = [C.c_int] * 3 + [C.c_double] * 3 + [C.POINTER(C.c_double)]
+    L.pso_ellfit_export(6, 3, 3, a * escl, b * escl, c * escl, cg.ctypes.data_as(C.POINTER(C.c_double)))
+    np.testing.assert_allclose(cg, unit["cg_first_l3"], rtol=1e-12, atol=1e-14)
+
+
+def test_phasec_matches_golden(oracle, unit):
+    import ctypes as C
+
+    ph = unit["phasec"]
+    alpha = math.acos(sum(x * y for x, y in zip(ph["xx1"], ph["xx2"])))
+    d = np.zeros(3)
+    L = oracle.lib()
+    L.pso_phasec_export.argtypes = [C.c_double, C.POINTER(C.c_double), C.POINTER(C.c_double)]
+    L.pso_phasec_export.restype = C.c_double
+    par = np.array(ph["par"])
+    scale = L.pso_phasec_export(alpha, par.ctypes.data_as(C.POINTER(C.c_double)), d.ctypes.data_as(C.POINTER(C.c_double)))
+    assert abs(scale - ph["scale"]) < 1e-15
+    np.testing.assert_allclose(d, ph["dphp"], rtol=1e-14)
