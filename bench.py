@@ -1,0 +1,363 @@
+"""Benchmark: LM period fits/s on one GB300 (per GPU under torchrun).
+
+Workload: the batched plain-FP64 scan of one synthetic asteroid with 8 dense
+relative lightcurves (3 h, 60 points each, 0.02 mag) and 500 sparse
+calibrated points over 8 years (Ndata = 980), trial periods 2-50 h with the
+reference's step rule (~40k periods x 10 initial poles), Laplace series
+L = M = 6 on the 288-facet grid, 50 LM iterations per fit.  A step is one
+contiguous chunk of the period scan (all 10 poles of each period), fitted by
+one launch of the persistent fit kernel; successive steps take chunks spread
+over the whole 2-50 h range.  Seeded synthetic data (no external dataset).
+
+value      fits/s with the object resident in HBM, from CUDA events around
+           the fit kernel on its own stream (sum over steps);
+e2e        the same through the C ABI with host buffers: ps_prepare (host ->
+           device copy of the tables), ps_scan (rows back to the host) and
+           ps_destroy per step, wall clock;
+roofline   algorithmic FLOP of the fits (2 N F C + 60 N F + N m(m+1) + 9 F C
+           per evaluation, 2 m^3 per solve) per launch over the launch time,
+           against the FP64 FMA ceiling measured live on the device;
+cpu_baseline  the CPU oracle (a restatement of the reference's FP64 path)
+           on all host cores, one fit per thread, on a bounded sample.
+
+`--impl reference` times that CPU implementation alone as the reference arm.
+Between timed steps a 256 MiB buffer is rewritten to flush the 126 MB L2.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "LM period fits/s on 1 GB300: chosen form vs plain FP64, same best P, χ² in tol"
+WORKLOAD = "c1: 8 dense relative LCs + 500 sparse points (Ndata 980), scan 2-50 h, L=M=6, 288 facets, 10 poles, 50 LM iterations"
+PROFILE = ROOT / "profiles" / "fit_kernel_fp64_c1.md"
+
+
+def _args():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="engine", choices=["engine", "reference"])
+    ap.add_argument("--form", default="fp64", choices=["fp64", "mixed"])
+    ap.add_argument("--periods-per-step", type=int, default=64)
+    ap.add_argument("--cpu-sample-fits", type=int, default=0, help="fits in the CPU baseline sample (0: 2 per core)")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+def _dist():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def make_workload(tmpdir: Path):
+    from periodsearch_gb300 import read_input, synth
+
+    path = tmpdir / "period_search_in"
+    obj = synth.write_object(path, "c1")
+    return path, read_input(path), obj
+
+
+def flops_per_eval(ndata, nfac, ncoef, mfit):
+    return 2.0 * ndata * nfac * ncoef + 60.0 * ndata * nfac + ndata * mfit * (mfit + 1) + 9.0 * nfac * ncoef
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.lines: list[str] = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self._t = threading.Thread(target=self._read, daemon=True)
+            self._t.start()
+        except FileNotFoundError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+            self._t.join(timeout=2)
+
+    def summary(self):
+        sm, smax, reasons = [], 0.0, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for l in self.lines:
+            p = [x.strip() for x in l.split(",")]
+            if len(p) < 9:
+                continue
+            try:
+                sm.append(float(p[1]))
+                smax = max(smax, float(p[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, p[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": smax or None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def cpu_baseline(path: Path, periods, sample_fits: int):
+    """The CPU oracle on all host cores: one fit per thread (ctypes releases
+    the GIL), a bounded sample of fits of the same scan."""
+    sys.path.insert(0, str(ROOT / "tests"))
+    import oracle_binding
+    from concurrent.futures import ThreadPoolExecutor
+
+    oracle_binding.build_oracle()
+    cores = os.cpu_count() or 1
+    n = sample_fits or 2 * cores
+    probs = [oracle_binding.OracleProblem(path) for _ in range(cores)]
+    cw = probs[0].info()["conw_r"]
+    for p in probs:
+        p.setup(cw)
+    jobs = [(int(periods[i % len(periods)]), 1 + i % 10) for i in range(n)]
+    lock = threading.Lock()
+    free = list(range(cores))
+
+    def one(job):
+        with lock:
+            k = free.pop()
+        try:
+            p = probs[k]
+            return p.fit(p.freq(job[0]), job[1])
+        finally:
+            with lock:
+                free.append(k)
+
+    t0 = time.perf_counter()
+    with ThreadPoolExecutor(cores) as ex:
+        list(ex.map(one, jobs))
+    dt = time.perf_counter() - t0
+    return {"value": n / dt, "unit": "fits/s", "cores": cores, "kind": "port",
+            "sample": f"{n} fits (period indices of the timed chunks x poles 1-10) of the c1 scan, {cores} threads, "
+                      f"{dt:.1f} s wall"}
+
+
+def run_reference_arm(args):
+    rank, world, _ = _dist()
+    if rank != 0:
+        return
+    with tempfile.TemporaryDirectory() as td:
+        path, data, _ = make_workload(Path(td))
+        sys.path.insert(0, str(ROOT / "tests"))
+        import oracle_binding
+
+        probe = oracle_binding.OracleProblem(path)
+        n_max = probe.info()["n_max"]
+        cores = os.cpu_count() or 1
+        periods = [1 + (k * 7919) % n_max for k in range(4 * cores)]
+        for _ in range(args.warmup):
+            cpu_baseline(path, periods, cores)
+        vals = []
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            vals.append(cpu_baseline(path, periods, cores))
+        dt = time.perf_counter() - t0
+        fits = cores * args.steps
+        v = fits / dt
+        cb = dict(vals[-1])
+        cb["value"] = v
+        cb["sample"] = f"{args.steps} steps of {cores} fits (one per core) of the c1 scan, oracle port of the reference FP64 path"
+        line = {"metric": METRIC, "value": v, "unit": "fits/s", "n_gpus": world, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": 1000 * dt / args.steps, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded generator, c1)",
+                "config": {"workload": WORKLOAD, "form": "cpu fp64 (reference algorithm)"}, "impl": "reference",
+                "cpu_baseline": cb, "e2e": {"value": v, "unit": "fits/s", "h2d_bytes_per_step": 0,
+                                            "d2h_bytes_per_step": 0}}
+        print(json.dumps(line))
+
+
+def _profile_traffic():
+    """DRAM bytes per fit from the committed ncu summary, if present."""
+    if not PROFILE.exists():
+        return None
+    for line in PROFILE.read_text().splitlines():
+        if line.startswith("dram_bytes_per_fit:"):
+            try:
+                return float(line.split(":", 1)[1].split()[0])
+            except ValueError:
+                return None
+    return None
+
+
+def run_engine_arm(args):
+    import numpy as np
+    import torch
+
+    from periodsearch_gb300 import Engine, PS_FORM_FP64, PS_FORM_MIXED, _abi, build
+
+    rank, world, local = _dist()
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    build.build()
+    torch.cuda.set_device(local)
+    form = PS_FORM_MIXED if args.form == "mixed" else PS_FORM_FP64
+    L = _abi.lib()
+    import ctypes as C
+
+    p64, p32 = C.c_double(), C.c_double()
+    _abi.check(L.ps_device_fma_peaks(local, C.byref(p64), C.byref(p32)), "ps_device_fma_peaks")
+
+    with tempfile.TemporaryDirectory() as td:
+        path, data, obj = make_workload(Path(td))
+        eng = Engine(data, device=local, form=form)
+        info = eng.info
+        n_max = int(info.n_max)
+        chunk = args.periods_per_step
+        conw_r, _ = eng.precalc_conw()
+        fe = flops_per_eval(info.ndata, info.nfac, info.ncoef, info.mfit)
+        fs = 2.0 * info.mfit ** 3
+        total_steps = args.warmup + args.steps
+        # chunks spread over the scan, distinct per rank (weak scaling: each
+        # rank fits its own chunks)
+        starts = [1 + ((k * world + rank) * 7919) % (n_max - chunk) for k in range(total_steps)]
+        flush = torch.empty(256 << 20, dtype=torch.uint8, device=f"cuda:{local}")
+
+        for k in range(args.warmup):
+            flush.zero_()
+            torch.cuda.synchronize()
+            eng.scan(conw_r, starts[k], starts[k] + chunk - 1)
+
+        if world > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize()
+        kernel_ms, fits_done, flops, launches = 0.0, 0, 0.0, 0
+        periods_timed = []
+        sampler = ClockSampler(local) if rank == 0 else None
+        t0 = time.perf_counter()
+        if sampler:
+            sampler.__enter__()
+        try:
+            for k in range(args.warmup, total_steps):
+                flush.zero_()
+                torch.cuda.synchronize()
+                n0 = starts[k]
+                eng.scan(conw_r, n0, n0 + chunk - 1)
+                t = eng.timing()
+                kernel_ms += t["kernel_ms"]
+                fits_done += t["fits"]
+                launches += t["launches"]
+                periods_timed.extend(range(n0, n0 + chunk))
+                # evaluations actually run (niter + 1 per fit) and solves (niter per fit)
+                flops += t["evals"] * fe + (t["evals"] - t["fits"]) * fs
+        finally:
+            if sampler:
+                sampler.__exit__(None, None, None)
+        torch.cuda.synchronize()
+        if world > 1:
+            torch.distributed.barrier()
+        wall = time.perf_counter() - t0
+
+        # e2e: the whole C-ABI path with host buffers, per step
+        e2e_t, e2e_fits = 0.0, 0
+        h2d = d2h = 0
+        for k in range(args.steps):
+            n0 = starts[args.warmup + k]
+            flush.zero_()
+            torch.cuda.synchronize()
+            s0 = time.perf_counter()
+            e2 = Engine(data, device=local, form=form)
+            rows = e2.scan(conw_r, n0, n0 + chunk - 1)
+            h2d = e2.info.h2d_bytes
+            e2.close()
+            e2e_t += time.perf_counter() - s0
+            e2e_fits += chunk * 10
+            d2h = chunk * 10 * C.sizeof(_abi.Fit)
+            assert np.isfinite(rows["rms"]).any()
+
+        vals = torch.tensor([kernel_ms / 1e3, e2e_t, float(fits_done), float(e2e_fits)], dtype=torch.float64,
+                            device=f"cuda:{local}")
+        if world > 1:
+            import torch.distributed as dist
+
+            mx = vals[:2].clone()
+            dist.all_reduce(mx, op=dist.ReduceOp.MAX)
+            sm = vals[2:].clone()
+            dist.all_reduce(sm, op=dist.ReduceOp.SUM)
+            vals = torch.cat([mx, sm])
+        dev_s, e2e_s, fits_all, e2e_fits_all = vals.tolist()
+
+        if rank == 0:
+            value = fits_all / dev_s
+            per_launch_s = (kernel_ms / 1e3) / max(launches, 1)
+            achieved = flops / max(launches, 1) / per_launch_s / 1e12
+            traffic_fit = _profile_traffic()
+            roof = {"bound": "fp64", "achieved": achieved, "peak": p64.value, "unit": "TFLOP/s",
+                    "frac": achieved / p64.value if p64.value else None,
+                    "traffic": traffic_fit * chunk * 10 if traffic_fit else None,
+                    "peak_source": "FP64 FMA ceiling measured live on this device by ps_device_fma_peaks "
+                                   "(MEASURED_PEAKS.json has no FP64 figure)",
+                    "algorithmic_flop_per_launch": flops / max(launches, 1),
+                    "fp32_fma_peak_tflops": p32.value}
+            cb = None
+            if not args.no_cpu_baseline:
+                cb = cpu_baseline(path, periods_timed, args.cpu_sample_fits)
+            line = {"metric": METRIC, "value": value, "unit": "fits/s", "n_gpus": world, "steps": args.steps,
+                    "warmup": args.warmup, "ms_per_step": kernel_ms / args.steps, "higher_is_better": True,
+                    "scaling": "weak", "vs_baseline": None, "dtype": "f64" if form == PS_FORM_FP64 else "f32+f64",
+                    "data": "synthetic (seeded generator, c1 shapes; no external dataset)",
+                    "config": {"workload": WORKLOAD, "form": args.form, "periods_per_step": chunk,
+                               "fits_per_step": chunk * 10, "ndata": info.ndata, "nfac": info.nfac,
+                               "ncoef": info.ncoef, "mfit": info.mfit, "n_max": n_max, "conw_r": conw_r,
+                               "slots": info.slots, "l2": "flushed between steps (256 MiB rewrite)",
+                               "truth": obj.truth},
+                    "e2e": {"value": e2e_fits_all / e2e_s, "unit": "fits/s", "h2d_bytes_per_step": h2d,
+                            "d2h_bytes_per_step": d2h},
+                    "gpu_launches": launches, "roofline": roof, "cpu_baseline": cb,
+                    "clocks": sampler.summary() if sampler else None, "wall_s": wall}
+            print(json.dumps(line))
+        eng.close()
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.destroy_process_group()
+
+
+def main():
+    args = _args()
+    if args.impl == "reference":
+        run_reference_arm(args)
+    else:
+        run_engine_arm(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -142,6 +142,7 @@ typedef struct ps_info {
     double conw_r0;        /* conw / escl^2 */
     double freq_start, freq_step;   /* [1/h] */
     int32_t sm_count, slots;        /* device SMs and resident fit slots */
+    int64_t h2d_bytes;              /* bytes ps_prepare copied host -> device */
 } ps_info;
 
 /* Device timing of the last ps_scan / ps_fit_batch call, measured with CUDA

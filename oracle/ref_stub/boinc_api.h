@@ -31,4 +31,9 @@ inline int boinc_time_to_checkpoint() { return 0; }
 inline int boinc_checkpoint_completed() { return 0; }
 inline int boinc_rename(const char *a, const char *b) { return std::rename(a, b); }
 inline void boinc_finish(int status) { std::exit(status); }
+// used by the AVX/FMA variant of the reference app
+struct APP_INIT_DATA {
+    int major_version = 0, minor_version = 0, release = 0;
+};
+inline int boinc_get_init_data(APP_INIT_DATA &) { return 0; }
 #endif

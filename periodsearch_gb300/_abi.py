@@ -64,7 +64,7 @@ class Info(C.Structure):
     _fields_ = [("ndata", C.c_int32), ("n_lc", C.c_int32), ("ncoef", C.c_int32), ("ma", C.c_int32),
                 ("mfit", C.c_int32), ("nfac", C.c_int32), ("n_max", C.c_int64), ("escl", C.c_double),
                 ("conw_r0", C.c_double), ("freq_start", C.c_double), ("freq_step", C.c_double),
-                ("sm_count", C.c_int32), ("slots", C.c_int32)]
+                ("sm_count", C.c_int32), ("slots", C.c_int32), ("h2d_bytes", C.c_int64)]
 
 
 class Timing(C.Structure):

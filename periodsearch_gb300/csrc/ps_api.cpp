@@ -30,6 +30,7 @@ struct ps_ctx {
     char *d_tables = nullptr;          // one allocation with every table
     psg::DevObject dob{};
     int sm_count = 0, slots = 0, P = 16;
+    int64_t h2d_bytes = 0;
     size_t smem = 0;
     double *d_scratch = nullptr;
     size_t scratch_stride = 0;
@@ -279,6 +280,7 @@ ps_status ps_prepare(const ps_problem *prob, const ps_options *opt, ps_ctx **out
            o_sx = pk.add(sx), o_sy = pk.add(sy), o_sz = pk.add(sz), o_ls = pk.add(o.lc_start),
            o_ln = pk.add(o.lc_points), o_lr = pk.add(o.lc_rel), o_fl = pk.add(o.free_list),
            o_cgf = pk.add(o.cg_first), o_dsf = pk.add(dsph_f);
+    c->h2d_bytes = static_cast<int64_t>(pk.bytes.size());
     PSG_CUDA(cp, cudaMalloc(&c->d_tables, pk.bytes.size()));
     PSG_CUDA(cp, cudaMemcpyAsync(c->d_tables, pk.bytes.data(), pk.bytes.size(), cudaMemcpyHostToDevice, c->stream));
     char *b = c->d_tables;
@@ -373,6 +375,7 @@ ps_status ps_get_info(const ps_ctx *c, ps_info *out)
     out->freq_step = o.freq_step;
     out->sm_count = c->sm_count;
     out->slots = c->slots;
+    out->h2d_bytes = c->h2d_bytes;
     return PS_OK;
 }
 

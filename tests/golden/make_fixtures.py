@@ -58,6 +58,32 @@ def _truncate_periods(text: str, n_periods: int) -> str:
     return "\n".join(lines)
 
 
+def _run_chunked(binary: Path, text: str, n_total: int, n_chunks: int) -> "list[str]":
+    """Rows 1..n_total of a reference binary, computed by n_chunks processes
+    over contiguous period ranges: each process gets the same input with
+    per_end truncated to its last period and a period_search_state holding
+    its first period - 1 (the reference's own resume path); every process
+    re-runs the convexity pre-pass on periods 1..10."""
+    from concurrent.futures import ThreadPoolExecutor
+
+    bounds = [round(i * n_total / n_chunks) for i in range(n_chunks + 1)]
+
+    def one(k):
+        lo, hi = bounds[k] + 1, bounds[k + 1]
+        with tempfile.TemporaryDirectory() as td:
+            td = Path(td)
+            (td / "period_search_in").write_text(_truncate_periods(text, max(hi, 10)))
+            if lo > 1:
+                (td / "period_search_state").write_text(str(lo - 1))
+            subprocess.run([str(binary)], cwd=td, check=True, capture_output=True)
+            rows = (td / "period_search_out.full").read_text().splitlines()
+            return rows[: hi - lo + 1]
+
+    with ThreadPoolExecutor(n_chunks) as ex:
+        parts = list(ex.map(one, range(n_chunks)))
+    return [r for p in parts for r in p]
+
+
 def _run_ref(workdir: Path) -> None:
     subprocess.run([str(REF_BIN)], cwd=workdir, check=True, capture_output=True)
     shutil.move(str(workdir / "period_search_out.full"), str(workdir / "ref.full"))
@@ -128,6 +154,21 @@ def main(ref_root: Path) -> None:
         for junk in ("temp", "period_search_state"):
             (d / junk).unlink(missing_ok=True)
     (HERE / "unit_arrays.json").write_text(json.dumps(unit_arrays(ref_root)))
+    # rows 1..134 (the length of the reference's period_search_out) at full
+    # precision, from the base build and, on x86-64, from the reference's own
+    # AVX2/FMA build: the cross-build agreement of the reference itself
+    import os
+
+    cores = os.cpu_count() or 1
+    rows = _run_chunked(REF_BIN, gold_in.read_text(), 134, cores)
+    (HERE / "golden134.full").write_text("\n".join(rows) + "\n")
+    fma = REF_BIN.parent / "ps_ref_fma"
+    if not fma.exists():
+        subprocess.run(["make", "-s", "-C", str(ROOT / "oracle"), "ref_fma",
+                        f"FMA_DIR={ref_root / 'period_search_optimization_avx_fma' / 'period_search'}"], check=False)
+    if fma.exists():
+        rows = _run_chunked(fma, gold_in.read_text(), 134, cores)
+        (HERE / "golden134_fma.full").write_text("\n".join(rows) + "\n")
     print("fixtures written to", HERE)
 
 
