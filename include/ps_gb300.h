@@ -185,6 +185,30 @@ ps_status ps_scan(ps_ctx *ctx, double conw_r, int64_t n_lo, int64_t n_hi, ps_row
  * (1..10).  out has n_fits entries. */
 ps_status ps_fit_batch(ps_ctx *ctx, double conw_r, int64_t n_fits, const int64_t *period_index,
                        const int32_t *pole, ps_fit *out);
+/* Allocation-free variant of ps_fit_batch.  No counterpart in the reference.
+ * For callers that cannot let a library allocate device memory when it is
+ * called: applications that give all device memory to their own pool
+ * allocator, processes under a fixed device-memory budget, and pipelines that
+ * cannot take the device-wide synchronisation of cudaMalloc/cudaFree.  The
+ * call allocates nothing (no cudaMalloc, cudaFree or allocating library
+ * routine): d_period_index[n_fits] (1-based period indices),
+ * d_pole[n_fits] (1..10) and d_out[n_fits] are caller-owned DEVICE memory,
+ * the object's tables are those ps_prepare placed on the device, and the work
+ * counter and per-slot scratch come from a file-scope device array of 4 MiB
+ * that every GPU loading the library reserves until the process exits.
+ * The fits are enqueued on `stream` (a cudaStream_t, NULL for the default
+ * stream); the call returns without waiting, and d_out is valid once the
+ * stream has reached it.  The first call on a device looks up the array's
+ * device address (cudaGetSymbolAddress); make that first call before any
+ * stream capture.  Every call shares the one array, so calls whose work
+ * overlaps on the GPU (other streams, other contexts, other threads) race;
+ * serialise them.  An object whose single fit slot needs more scratch than
+ * the array holds (max relative-lightcurve points * (ma+1) doubles > 4 MiB)
+ * is rejected with PS_ERR_LIMIT.  FP64 form only.  Entries of the device
+ * lists must be valid (period index >= 1, pole 1..10); they are not checked.
+ * ps_last_timing is not updated. */
+ps_status ps_fit_batch_noalloc(ps_ctx *ctx, double conw_r, int64_t n_fits, const int64_t *d_period_index,
+                               const int32_t *d_pole, ps_fit *d_out, void *stream);
 /* One model evaluation (the reference's mrqcof) at parameters cg[ma]
  * (0-based, reference layout): alpha[mfit*mfit] row-major, beta[mfit],
  * area[nfac] (may be NULL); returns chi^2 through *chisq. */

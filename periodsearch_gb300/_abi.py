@@ -88,6 +88,8 @@ SIGNATURES = {
     "ps_precalc_conw": (C.c_int, [_CTX, _D, _I32]),
     "ps_scan": (C.c_int, [_CTX, C.c_double, C.c_int64, C.c_int64, C.POINTER(Row)]),
     "ps_fit_batch": (C.c_int, [_CTX, C.c_double, C.c_int64, _I64, _I32, C.POINTER(Fit)]),
+    "ps_fit_batch_noalloc": (C.c_int, [_CTX, C.c_double, C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p,
+                                       C.c_void_p]),
     "ps_eval": (C.c_int, [_CTX, C.c_double, _D, _D, _D, _D, _D]),
     "ps_last_timing": (C.c_int, [_CTX, C.POINTER(Timing)]),
     "ps_last_error": (C.c_char_p, [_CTX]),

@@ -454,6 +454,42 @@ ps_status ps_fit_batch(ps_ctx *c, double conw_r, int64_t n_fits, const int64_t *
     return PS_OK;
 }
 
+// Allocation-free variant of ps_fit_batch for callers that cannot allocate
+// device memory at call time (see ps_gb300.h).  Everything it touches is
+// either the caller's (work lists, outputs, stream), the context's tables from
+// ps_prepare, or the file-scope scratch array of ps_engine.cu.
+ps_status ps_fit_batch_noalloc(ps_ctx *c, double conw_r, int64_t n_fits, const int64_t *d_period_index,
+                               const int32_t *d_pole, ps_fit *d_out, void *stream)
+{
+    if (!c || !d_period_index || !d_pole || !d_out || n_fits < 1 || !(conw_r > 0)) return PS_ERR_ARG;
+    if (c->opt.form != PS_FORM_FP64) {
+        c->err = "ps_fit_batch_noalloc supports the FP64 form only";
+        return PS_ERR_ARG;
+    }
+    PSG_CUDA(c, cudaSetDevice(c->opt.device));
+    psg::FitConfig cfg = make_config(c, conw_r);
+    psg::FitWork w{};
+    w.n_lo = 1;
+    w.nfits = n_fits;
+    w.period_index = d_period_index;
+    w.pole = d_pole;
+    w.scratch_stride = c->scratch_stride;
+    w.out = d_out;
+    int grid = 0;
+    int e = psg::launch_fits_noalloc(c->opt.form, c->dob, cfg, w, c->slots, c->P, c->smem, stream, &grid);
+    if (e == -1) {
+        char msg[256];
+        std::snprintf(msg, sizeof msg,
+                      "one fit slot needs %zu doubles of scratch; the allocation-free path holds %zu "
+                      "(4 MiB minus the work counter)",
+                      c->scratch_stride, psg::kStaticScratchDoubles - 32);
+        c->err = msg;
+        return PS_ERR_LIMIT;
+    }
+    if (e != 0) return cuda_fail(c, static_cast<cudaError_t>(e), "allocation-free fit launch");
+    return PS_OK;
+}
+
 ps_status ps_eval(ps_ctx *c, double conw_r, const double *cg, double *alpha, double *beta, double *chisq,
                   double *area)
 {

@@ -27,6 +27,7 @@
 
 #include <cmath>
 #include <cstdint>
+#include <mutex>
 
 #include "ps_engine.h"
 
@@ -792,6 +793,65 @@ int measure_fma_peaks(double *fp64_tflops, double *fp32_tflops, void *stream)
     cudaFree(sink);
     *fp64_tflops = best64;
     *fp32_tflops = best32;
+    return static_cast<int>(cudaGetLastError());
+}
+
+// ---------------------------------------------------------------------------
+// Scratch for the allocation-free entry point (ps_fit_batch_noalloc).
+//
+// Some hosts cannot let a library allocate device memory when it is called:
+// applications that hand all of the GPU's memory to their own pool allocator
+// up front, processes running under a fixed device-memory budget where a
+// failed allocation in the middle of a job is not acceptable, and pipelines
+// that keep other streams busy and cannot afford the device-wide
+// synchronisation that cudaMalloc/cudaFree imply.  For them the fit kernel
+// can take its work counter and its per-slot scratch from this file-scope
+// array instead.  Every GPU that loads the library reserves it until the
+// process exits.  Layout: the first 32 doubles hold the work counter (cleared
+// before each launch), then one scratch block per fit slot.
+// ---------------------------------------------------------------------------
+constexpr size_t kStaticCounterDoubles = 32;
+static __device__ __align__(256) double g_noalloc_scratch[kStaticScratchDoubles];
+
+namespace {
+std::mutex g_noalloc_mutex;
+double *g_noalloc_ptr[64] = {};  // device address of g_noalloc_scratch, per device ordinal
+}  // namespace
+
+int launch_fits_noalloc(int form, const DevObject &ob, const FitConfig &cfg, FitWork w, int max_grid, int P,
+                        size_t smem, void *stream, int *grid_used)
+{
+    if (form != PS_FORM_FP64) return static_cast<int>(cudaErrorInvalidValue);
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return static_cast<int>(e);
+    if (dev < 0 || dev >= 64) return static_cast<int>(cudaErrorInvalidDevice);
+    double *base = nullptr;
+    {
+        // Host code cannot use the array's name as a device address; look the
+        // address up once per device, with that device current.
+        std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+        if (!g_noalloc_ptr[dev]) {
+            e = cudaGetSymbolAddress(reinterpret_cast<void **>(&g_noalloc_ptr[dev]), g_noalloc_scratch);
+            if (e != cudaSuccess) {
+                g_noalloc_ptr[dev] = nullptr;
+                return static_cast<int>(e);
+            }
+        }
+        base = g_noalloc_ptr[dev];
+    }
+    const size_t usable = kStaticScratchDoubles - kStaticCounterDoubles;
+    const int64_t slots = static_cast<int64_t>(usable / w.scratch_stride);
+    if (slots < 1) return -1;  // one slot's scratch exceeds the array
+    int64_t grid = slots < max_grid ? slots : max_grid;
+    if (grid > w.nfits) grid = w.nfits;
+    w.queue = reinterpret_cast<unsigned long long *>(base);
+    w.scratch = base + kStaticCounterDoubles;
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    e = cudaMemsetAsync(base, 0, sizeof(unsigned long long), st);
+    if (e != cudaSuccess) return static_cast<int>(e);
+    fit_kernel<0><<<static_cast<int>(grid), kThreads, smem, st>>>(ob, cfg, w, P);
+    *grid_used = static_cast<int>(grid);
     return static_cast<int>(cudaGetLastError());
 }
 

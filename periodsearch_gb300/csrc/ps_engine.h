@@ -113,4 +113,12 @@ int set_kernel_smem(int form, size_t smem);
 int occupancy_slots(int form, size_t smem, int *per_sm);
 int measure_fma_peaks(double *fp64_tflops, double *fp32_tflops, void *stream);
 
+// Allocation-free launch of the FP64 fit kernel: the work counter and the
+// per-slot scratch come from a file-scope device array of
+// kStaticScratchDoubles doubles (ps_engine.cu).  Returns -1 when one slot's
+// scratch (w.scratch_stride doubles) does not fit, else a cudaError_t.
+constexpr size_t kStaticScratchDoubles = size_t(1) << 19;  // 4 MiB
+int launch_fits_noalloc(int form, const DevObject &ob, const FitConfig &cfg, FitWork w, int max_grid, int P,
+                        size_t smem, void *stream, int *grid_used);
+
 }  // namespace psg
