@@ -1,6 +1,6 @@
 """Benchmark: LM period fits/s on one GB300 (per GPU under torchrun).
 
-Workload: the batched plain-FP64 scan of one synthetic asteroid with 8 dense
+Workload: the batched scan of one synthetic asteroid with 8 dense
 relative lightcurves (3 h, 60 points each, 0.02 mag) and 500 sparse
 calibrated points over 8 years (Ndata = 980), trial periods 2-50 h with the
 reference's step rule (~40k periods x 10 initial poles), Laplace series
@@ -9,8 +9,11 @@ contiguous chunk of the period scan (all 10 poles of each period), fitted by
 one launch of the persistent fit kernel; successive steps take chunks spread
 over the whole 2-50 h range.  Seeded synthetic data (no external dataset).
 
-value      fits/s with the object resident in HBM, from CUDA events around
-           the fit kernel on its own stream (sum over steps);
+value      fits/s of the chosen form (--form, default mixed) with the object
+           resident in HBM, from CUDA events around the fit kernel on its own
+           stream (sum over steps); the plain FP64 form is timed on the same
+           chunks (plain_fp64), and both forms fit a window around the true
+           period (validation: same best period, chi^2 difference);
 e2e        the same through the C ABI with host buffers: ps_prepare (host ->
            device copy of the tables), ps_scan (rows back to the host) and
            ps_destroy per step, wall clock;
@@ -42,7 +45,7 @@ sys.path.insert(0, str(ROOT))
 
 METRIC = "LM period fits/s on 1 GB300: chosen form vs plain FP64, same best P, χ² in tol"
 WORKLOAD = "c1: 8 dense relative LCs + 500 sparse points (Ndata 980), scan 2-50 h, L=M=6, 288 facets, 10 poles, 50 LM iterations"
-PROFILE = ROOT / "profiles" / "fit_kernel_fp64_c1.md"
+PROFILES = {False: ROOT / "profiles" / "fit_kernel_fp64_c1.md", True: ROOT / "profiles" / "fit_kernel_mixed_c1.md"}
 
 
 def _args():
@@ -51,7 +54,8 @@ def _args():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="engine", choices=["engine", "reference"])
-    ap.add_argument("--form", default="fp64", choices=["fp64", "mixed"])
+    ap.add_argument("--form", default="mixed", choices=["fp64", "mixed"])
+    ap.add_argument("--no-fp64-compare", action="store_true", help="skip timing the plain FP64 form")
     ap.add_argument("--periods-per-step", type=int, default=64)
     ap.add_argument("--cpu-sample-fits", type=int, default=0, help="fits in the CPU baseline sample (0: 2 per core)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -203,11 +207,12 @@ def run_reference_arm(args):
         print(json.dumps(line))
 
 
-def _profile_traffic():
-    """DRAM bytes per fit from the committed ncu summary, if present."""
-    if not PROFILE.exists():
+def _profile_traffic(mixed: bool):
+    """DRAM bytes per fit from the committed ncu summary of that form, if present."""
+    prof = PROFILES[mixed]
+    if not prof.exists():
         return None
-    for line in PROFILE.read_text().splitlines():
+    for line in prof.read_text().splitlines():
         if line.startswith("dram_bytes_per_fit:"):
             try:
                 return float(line.split(":", 1)[1].split()[0])
@@ -216,7 +221,45 @@ def _profile_traffic():
     return None
 
 
+def _time_form(Engine, data, form, local, starts, chunk, warmup, steps, flush, sampler=None):
+    """Warm-up and timed steps of one form on the given chunk starts."""
+    import torch
+
+    eng = Engine(data, device=local, form=form)
+    info = eng.info
+    conw_r, _ = eng.precalc_conw()
+    fe = flops_per_eval(info.ndata, info.nfac, info.ncoef, info.mfit)
+    fs = 2.0 * info.mfit ** 3
+    for k in range(warmup):
+        flush.zero_()
+        torch.cuda.synchronize()
+        eng.scan(conw_r, starts[k], starts[k] + chunk - 1)
+    torch.cuda.synchronize()
+    kernel_ms, fits, flops, launches, rows = 0.0, 0, 0.0, 0, []
+    if sampler:
+        sampler.__enter__()
+    try:
+        for k in range(warmup, warmup + steps):
+            flush.zero_()
+            torch.cuda.synchronize()
+            r = eng.scan(conw_r, starts[k], starts[k] + chunk - 1)
+            t = eng.timing()
+            kernel_ms += t["kernel_ms"]
+            fits += t["fits"]
+            launches += t["launches"]
+            flops += t["evals"] * fe + (t["evals"] - t["fits"]) * fs
+            rows.append(r)
+    finally:
+        if sampler:
+            sampler.__exit__(None, None, None)
+    torch.cuda.synchronize()
+    return {"engine": eng, "conw_r": conw_r, "kernel_ms": kernel_ms, "fits": fits, "flops": flops,
+            "launches": launches, "rows": rows}
+
+
 def run_engine_arm(args):
+    import ctypes as C
+
     import numpy as np
     import torch
 
@@ -229,73 +272,45 @@ def run_engine_arm(args):
         dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
     build.build()
     torch.cuda.set_device(local)
-    form = PS_FORM_MIXED if args.form == "mixed" else PS_FORM_FP64
+    chosen = PS_FORM_MIXED if args.form == "mixed" else PS_FORM_FP64
     L = _abi.lib()
-    import ctypes as C
-
     p64, p32 = C.c_double(), C.c_double()
     _abi.check(L.ps_device_fma_peaks(local, C.byref(p64), C.byref(p32)), "ps_device_fma_peaks")
 
     with tempfile.TemporaryDirectory() as td:
         path, data, obj = make_workload(Path(td))
-        eng = Engine(data, device=local, form=form)
-        info = eng.info
-        n_max = int(info.n_max)
         chunk = args.periods_per_step
-        conw_r, _ = eng.precalc_conw()
-        fe = flops_per_eval(info.ndata, info.nfac, info.ncoef, info.mfit)
-        fs = 2.0 * info.mfit ** 3
+        probe = Engine(data, device=local, form=chosen)
+        n_max = int(probe.info.n_max)
+        info = probe.info
+        probe.close()
         total_steps = args.warmup + args.steps
-        # chunks spread over the scan, distinct per rank (weak scaling: each
-        # rank fits its own chunks)
+        # chunks spread over the scan, distinct per rank (weak scaling)
         starts = [1 + ((k * world + rank) * 7919) % (n_max - chunk) for k in range(total_steps)]
         flush = torch.empty(256 << 20, dtype=torch.uint8, device=f"cuda:{local}")
 
-        for k in range(args.warmup):
-            flush.zero_()
-            torch.cuda.synchronize()
-            eng.scan(conw_r, starts[k], starts[k] + chunk - 1)
-
         if world > 1:
             torch.distributed.barrier()
-        torch.cuda.synchronize()
-        kernel_ms, fits_done, flops, launches = 0.0, 0, 0.0, 0
-        periods_timed = []
         sampler = ClockSampler(local) if rank == 0 else None
         t0 = time.perf_counter()
-        if sampler:
-            sampler.__enter__()
-        try:
-            for k in range(args.warmup, total_steps):
-                flush.zero_()
-                torch.cuda.synchronize()
-                n0 = starts[k]
-                eng.scan(conw_r, n0, n0 + chunk - 1)
-                t = eng.timing()
-                kernel_ms += t["kernel_ms"]
-                fits_done += t["fits"]
-                launches += t["launches"]
-                periods_timed.extend(range(n0, n0 + chunk))
-                # evaluations actually run (niter + 1 per fit) and solves (niter per fit)
-                flops += t["evals"] * fe + (t["evals"] - t["fits"]) * fs
-        finally:
-            if sampler:
-                sampler.__exit__(None, None, None)
-        torch.cuda.synchronize()
+        main = _time_form(Engine, data, chosen, local, starts, chunk, args.warmup, args.steps, flush, sampler)
         if world > 1:
             torch.distributed.barrier()
         wall = time.perf_counter() - t0
+        # plain FP64 on the same chunks (the comparison the metric asks for)
+        plain = None
+        if chosen != PS_FORM_FP64 and not args.no_fp64_compare:
+            plain = _time_form(Engine, data, PS_FORM_FP64, local, starts, chunk, 1, args.steps, flush)
 
         # e2e: the whole C-ABI path with host buffers, per step
-        e2e_t, e2e_fits = 0.0, 0
-        h2d = d2h = 0
+        e2e_t, e2e_fits, h2d, d2h = 0.0, 0, 0, 0
         for k in range(args.steps):
             n0 = starts[args.warmup + k]
             flush.zero_()
             torch.cuda.synchronize()
             s0 = time.perf_counter()
-            e2 = Engine(data, device=local, form=form)
-            rows = e2.scan(conw_r, n0, n0 + chunk - 1)
+            e2 = Engine(data, device=local, form=chosen)
+            rows = e2.scan(main["conw_r"], n0, n0 + chunk - 1)
             h2d = e2.info.h2d_bytes
             e2.close()
             e2e_t += time.perf_counter() - s0
@@ -303,8 +318,26 @@ def run_engine_arm(args):
             d2h = chunk * 10 * C.sizeof(_abi.Fit)
             assert np.isfinite(rows["rms"]).any()
 
-        vals = torch.tensor([kernel_ms / 1e3, e2e_t, float(fits_done), float(e2e_fits)], dtype=torch.float64,
-                            device=f"cuda:{local}")
+        # validation window around the true period: same best period?
+        valid = None
+        if plain is not None and rank == 0:
+            n_truth = int(round((info.freq_start - 1 / obj.truth["period_h"]) / info.freq_step)) + 1
+            lo, hi = max(1, n_truth - 16), min(n_max, n_truth + 15)
+            w_main = main["engine"].scan(main["conw_r"], lo, hi)
+            w_plain = plain["engine"].scan(plain["conw_r"], lo, hi)
+            rel_w = np.abs(w_main["rms"] - w_plain["rms"]) / w_plain["rms"]
+            rel_c = np.concatenate([np.abs(a["rms"] - b["rms"]) / b["rms"] for a, b in zip(main["rows"], plain["rows"])])
+            bm, bp = int(np.argmin(w_main["rms"])), int(np.argmin(w_plain["rms"]))
+            valid = {"window": [lo, hi], "truth_period_h": obj.truth["period_h"],
+                     "best_index_chosen": lo + bm, "best_index_fp64": lo + bp, "same_best_period": bm == bp,
+                     "best_period_h_chosen": float(w_main["period_h"][bm]),
+                     "best_period_h_fp64": float(w_plain["period_h"][bp]),
+                     "chi2_rel_at_best": float(abs(w_main["chi2"][bm] - w_plain["chi2"][bp]) / w_plain["chi2"][bp]),
+                     "rms_rel_window_median": float(np.median(rel_w)), "rms_rel_window_max": float(rel_w.max()),
+                     "rms_rel_timed_median": float(np.median(rel_c)), "rms_rel_timed_max": float(rel_c.max())}
+
+        vals = torch.tensor([main["kernel_ms"] / 1e3, e2e_t, float(main["fits"]), float(e2e_fits)],
+                            dtype=torch.float64, device=f"cuda:{local}")
         if world > 1:
             import torch.distributed as dist
 
@@ -317,34 +350,50 @@ def run_engine_arm(args):
 
         if rank == 0:
             value = fits_all / dev_s
-            per_launch_s = (kernel_ms / 1e3) / max(launches, 1)
-            achieved = flops / max(launches, 1) / per_launch_s / 1e12
-            traffic_fit = _profile_traffic()
-            roof = {"bound": "fp64", "achieved": achieved, "peak": p64.value, "unit": "TFLOP/s",
-                    "frac": achieved / p64.value if p64.value else None,
+            launches = main["launches"]
+            per_launch_s = (main["kernel_ms"] / 1e3) / max(launches, 1)
+            achieved = main["flops"] / max(launches, 1) / per_launch_s / 1e12
+            mixed = chosen == PS_FORM_MIXED
+            peak = p32.value if mixed else p64.value
+            traffic_fit = _profile_traffic(mixed)
+            roof = {"bound": "fp32" if mixed else "fp64", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                    "frac": achieved / peak if peak else None,
                     "traffic": traffic_fit * chunk * 10 if traffic_fit else None,
-                    "peak_source": "FP64 FMA ceiling measured live on this device by ps_device_fma_peaks "
-                                   "(MEASURED_PEAKS.json has no FP64 figure)",
-                    "algorithmic_flop_per_launch": flops / max(launches, 1),
-                    "fp32_fma_peak_tflops": p32.value}
+                    "peak_source": ("FP32" if mixed else "FP64") + " FMA ceiling measured live on this device by "
+                                   "ps_device_fma_peaks (MEASURED_PEAKS.json has no FP32/FP64 SIMT figure)",
+                    "kernel": "fit_kernel<mixed>" if mixed else "fit_kernel<fp64>",
+                    "algorithmic_flop_per_launch": main["flops"] / max(launches, 1),
+                    "fp64_fma_peak_tflops": p64.value, "fp32_fma_peak_tflops": p32.value}
+            fp64 = None
+            if plain is not None:
+                pv = plain["fits"] / (plain["kernel_ms"] / 1e3)
+                pl = plain["launches"]
+                pa = plain["flops"] / max(pl, 1) / ((plain["kernel_ms"] / 1e3) / max(pl, 1)) / 1e12
+                fp64 = {"value": pv, "unit": "fits/s", "speedup_chosen_over_fp64": value / pv,
+                        "roofline": {"bound": "fp64", "achieved": pa, "peak": p64.value, "unit": "TFLOP/s",
+                                     "frac": pa / p64.value,
+                                     "traffic": (_profile_traffic(False) or 0) * chunk * 10 or None}}
             cb = None
             if not args.no_cpu_baseline:
-                cb = cpu_baseline(path, periods_timed, args.cpu_sample_fits)
+                periods = [n for st in starts[args.warmup:] for n in range(st, st + chunk)]
+                cb = cpu_baseline(path, periods, args.cpu_sample_fits)
             line = {"metric": METRIC, "value": value, "unit": "fits/s", "n_gpus": world, "steps": args.steps,
-                    "warmup": args.warmup, "ms_per_step": kernel_ms / args.steps, "higher_is_better": True,
-                    "scaling": "weak", "vs_baseline": None, "dtype": "f64" if form == PS_FORM_FP64 else "f32+f64",
+                    "warmup": args.warmup, "ms_per_step": main["kernel_ms"] / args.steps, "higher_is_better": True,
+                    "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64" if mixed else "f64",
                     "data": "synthetic (seeded generator, c1 shapes; no external dataset)",
                     "config": {"workload": WORKLOAD, "form": args.form, "periods_per_step": chunk,
                                "fits_per_step": chunk * 10, "ndata": info.ndata, "nfac": info.nfac,
-                               "ncoef": info.ncoef, "mfit": info.mfit, "n_max": n_max, "conw_r": conw_r,
+                               "ncoef": info.ncoef, "mfit": info.mfit, "n_max": n_max, "conw_r": main["conw_r"],
                                "slots": info.slots, "l2": "flushed between steps (256 MiB rewrite)",
                                "truth": obj.truth},
                     "e2e": {"value": e2e_fits_all / e2e_s, "unit": "fits/s", "h2d_bytes_per_step": h2d,
                             "d2h_bytes_per_step": d2h},
-                    "gpu_launches": launches, "roofline": roof, "cpu_baseline": cb,
-                    "clocks": sampler.summary() if sampler else None, "wall_s": wall}
+                    "gpu_launches": launches, "roofline": roof, "plain_fp64": fp64, "validation": valid,
+                    "cpu_baseline": cb, "clocks": sampler.summary() if sampler else None, "wall_s": wall}
             print(json.dumps(line))
-        eng.close()
+        main["engine"].close()
+        if plain is not None:
+            plain["engine"].close()
     if world > 1:
         import torch.distributed as dist
 

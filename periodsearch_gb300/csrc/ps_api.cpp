@@ -29,7 +29,7 @@ struct ps_ctx {
     cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};
     char *d_tables = nullptr;          // one allocation with every table
     psg::DevObject dob{};
-    int sm_count = 0, slots = 0, P = 16;
+    int sm_count = 0, slots = 0, P = 16, dsph_smem = 0;
     int64_t h2d_bytes = 0;
     size_t smem = 0;
     double *d_scratch = nullptr;
@@ -129,7 +129,7 @@ ps_status run_fits(ps_ctx *c, double conw_r, psg::FitWork w)
     int grid = static_cast<int>(std::min<int64_t>(c->slots, std::max<int64_t>(w.nfits, 1)));
     PSG_CUDA(c, cudaMemsetAsync(c->d_queue, 0, sizeof(unsigned long long), c->stream));
     PSG_CUDA(c, cudaEventRecord(c->ev[0], c->stream));
-    int e = psg::launch_fits(c->opt.form, c->dob, cfg, w, grid, c->P, c->smem, c->stream);
+    int e = psg::launch_fits(c->opt.form, c->dob, cfg, w, grid, c->P, c->smem, c->dsph_smem, c->stream);
     if (e != 0) return cuda_fail(c, static_cast<cudaError_t>(e), "fit kernel launch");
     PSG_CUDA(c, cudaEventRecord(c->ev[1], c->stream));
     c->h_fits.resize(static_cast<size_t>(w.nfits));
@@ -262,7 +262,12 @@ ps_status ps_prepare(const ps_problem *prob, const ps_options *opt, ps_ctx **out
             fs[static_cast<size_t>(m) * F + i] = s.fs[static_cast<size_t>(i) * (s.mmax + 1) + m];
         }
     }
-    std::vector<double> ex(o.ndata), ey(o.ndata), ez(o.ndata), sx(o.ndata), sy(o.ndata), sz(o.ndata);
+    // Solar phase angle of every point: it depends on the data only, so it is
+    // computed once here with the host libm, as the reference computes it in
+    // every evaluation (bright.c:30-31: acos of the dot product of the unit
+    // vectors, in the same order).
+    std::vector<double> ex(o.ndata), ey(o.ndata), ez(o.ndata), sx(o.ndata), sy(o.ndata), sz(o.ndata),
+        alpha_pt(o.ndata);
     for (int q = 0; q < o.ndata; q++) {
         ex[q] = o.ee[3 * q];
         ey[q] = o.ee[3 * q + 1];
@@ -270,8 +275,13 @@ ps_status ps_prepare(const ps_problem *prob, const ps_options *opt, ps_ctx **out
         sx[q] = o.ee0[3 * q];
         sy[q] = o.ee0[3 * q + 1];
         sz[q] = o.ee0[3 * q + 2];
+        alpha_pt[q] = std::acos(ex[q] * sx[q] + ey[q] * sy[q] + ez[q] * sz[q]);
     }
+    std::vector<double> sig2i(o.ndata);
+    for (int q = 0; q < o.ndata; q++) sig2i[q] = 1 / (o.sig[q] * o.sig[q]);
     std::vector<float> dsph_f(s.dsph.begin(), s.dsph.end());
+    std::vector<float> nx_f(nx.begin(), nx.end()), ny_f(ny.begin(), ny.end()), nz_f(nz.begin(), nz.end()),
+        darea_f(s.darea.begin(), s.darea.end());
     Packer pk;
     size_t o_nx = pk.add(nx), o_ny = pk.add(ny), o_nz = pk.add(nz), o_darea = pk.add(s.darea),
            o_dsph = pk.add(s.dsph), o_pleg = pk.add(pleg), o_fc = pk.add(fc), o_fs = pk.add(fs),
@@ -279,7 +289,8 @@ ps_status ps_prepare(const ps_problem *prob, const ps_options *opt, ps_ctx **out
            o_sig = pk.add(o.sig), o_w = pk.add(o.weight), o_ex = pk.add(ex), o_ey = pk.add(ey), o_ez = pk.add(ez),
            o_sx = pk.add(sx), o_sy = pk.add(sy), o_sz = pk.add(sz), o_ls = pk.add(o.lc_start),
            o_ln = pk.add(o.lc_points), o_lr = pk.add(o.lc_rel), o_fl = pk.add(o.free_list),
-           o_cgf = pk.add(o.cg_first), o_dsf = pk.add(dsph_f);
+           o_cgf = pk.add(o.cg_first), o_dsf = pk.add(dsph_f), o_alp = pk.add(alpha_pt), o_nxf = pk.add(nx_f),
+           o_nyf = pk.add(ny_f), o_nzf = pk.add(nz_f), o_daf = pk.add(darea_f), o_s2i = pk.add(sig2i);
     c->h2d_bytes = static_cast<int64_t>(pk.bytes.size());
     PSG_CUDA(cp, cudaMalloc(&c->d_tables, pk.bytes.size()));
     PSG_CUDA(cp, cudaMemcpyAsync(c->d_tables, pk.bytes.data(), pk.bytes.size(), cudaMemcpyHostToDevice, c->stream));
@@ -320,14 +331,27 @@ ps_status ps_prepare(const ps_problem *prob, const ps_options *opt, ps_ctx **out
     d.free_list = reinterpret_cast<const int *>(b + o_fl);
     d.cg_first = reinterpret_cast<const double *>(b + o_cgf);
     d.dsph_f = reinterpret_cast<const float *>(b + o_dsf);
+    d.alpha_pt = reinterpret_cast<const double *>(b + o_alp);
+    d.nx_f = reinterpret_cast<const float *>(b + o_nxf);
+    d.ny_f = reinterpret_cast<const float *>(b + o_nyf);
+    d.nz_f = reinterpret_cast<const float *>(b + o_nzf);
+    d.darea_f = reinterpret_cast<const float *>(b + o_daf);
+    d.sig2i = reinterpret_cast<const double *>(b + o_s2i);
 
     // Slot plan: the largest point tile whose shared-memory footprint fits.
     size_t smem_max = static_cast<size_t>(prop.sharedMemPerBlockOptin);
-    int P = 16;
-    psg::SlotLayout L = psg::make_layout(o.ma, o.mfit, F, P);
+    // Mixed form: 32-point tiles (the register tile of the contraction) and
+    // the FP32 basis in shared memory when it fits; FP64 form: 16-point tiles.
+    const bool mixed = c->opt.form == PS_FORM_MIXED;
+    int P = mixed ? 32 : 16, dsph_smem = mixed ? 1 : 0;
+    psg::SlotLayout L = psg::make_layout(c->opt.form, o.ma, o.mfit, F, o.ncoef, P, dsph_smem);
+    if (L.bytes > smem_max && dsph_smem) {
+        dsph_smem = 0;
+        L = psg::make_layout(c->opt.form, o.ma, o.mfit, F, o.ncoef, P, dsph_smem);
+    }
     while (L.bytes > smem_max && P > 2) {
         P /= 2;
-        L = psg::make_layout(o.ma, o.mfit, F, P);
+        L = psg::make_layout(c->opt.form, o.ma, o.mfit, F, o.ncoef, P, dsph_smem);
     }
     if (L.bytes > smem_max) {
         c->err = "shared-memory plan of a fit slot exceeds the device limit";
@@ -335,11 +359,12 @@ ps_status ps_prepare(const ps_problem *prob, const ps_options *opt, ps_ctx **out
         return PS_ERR_LIMIT;
     }
     c->P = P;
+    c->dsph_smem = dsph_smem;
     c->smem = L.bytes;
-    int e = psg::set_kernel_smem(c->opt.form, c->smem);
+    int e = psg::set_kernel_smem(c->opt.form, c->smem, o.ncoef);
     if (e != 0) return cuda_fail(cp, static_cast<cudaError_t>(e), "cudaFuncSetAttribute");
     int per_sm = 0;
-    e = psg::occupancy_slots(c->opt.form, c->smem, &per_sm);
+    e = psg::occupancy_slots(c->opt.form, c->smem, o.ncoef, &per_sm);
     if (e != 0) return cuda_fail(cp, static_cast<cudaError_t>(e), "occupancy");
     if (per_sm < 1) {
         c->err = "fit slot does not fit on an SM";
@@ -502,7 +527,7 @@ ps_status ps_eval(ps_ctx *c, double conw_r, const double *cg, double *alpha, dou
     PSG_CUDA(c, cudaMemcpyAsync(d_cg, cg, ma * sizeof(double), cudaMemcpyHostToDevice, c->stream));
     psg::FitConfig cfg = make_config(c, conw_r);
     int e = psg::launch_eval(c->opt.form, c->dob, cfg, d_cg, d_al, d_be, d_c2, d_ar, c->d_scratch, c->P, c->smem,
-                             c->stream);
+                             c->dsph_smem, c->stream);
     if (e != 0) return cuda_fail(c, static_cast<cudaError_t>(e), "eval kernel launch");
     PSG_CUDA(c, cudaMemcpyAsync(alpha, d_al, static_cast<size_t>(mf) * mf * sizeof(double), cudaMemcpyDeviceToHost,
                                 c->stream));

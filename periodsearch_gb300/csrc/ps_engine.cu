@@ -28,6 +28,7 @@
 #include <cmath>
 #include <cstdint>
 #include <mutex>
+#include <type_traits>
 
 #include "ps_engine.h"
 
@@ -40,35 +41,53 @@ constexpr double kTwoPi = 2 * kPi;
 constexpr double kRad2Deg = 180 / kPi;
 constexpr double kDeg2Rad = kPi / 180;
 constexpr double kTinyMu = 1e-8;
+// 2*pi split for the mixed form's phase reduction: hi = 2*pi rounded to
+// double, lo = 2*pi - hi.
+constexpr double kTwoPiHi = 6.283185307179586;
+constexpr double kTwoPiLo = 2.4492935982947064e-16;
+constexpr double kInvTwoPi = 0.15915494309189535;
 
 __constant__ double c_beta_pole[PS_N_POLES] = {0, 0, 0, 0, 60, 60, 60, -60, -60, -60};
 __constant__ double c_lambda_pole[PS_N_POLES] = {0, 90, 180, 270, 60, 180, 300, 60, 180, 300};
 
+// Arithmetic type of the facet stage, the contraction and the model rows.
+template <int FORM> struct RealOf { using T = double; };
+template <> struct RealOf<PS_FORM_MIXED> { using T = float; };
+
+template <int FORM>
 struct Smem {
-    double *cg, *atry, *beta, *da, *alpha, *covar, *area, *gv, *W, *J, *ym, *pt, *red, *dave, *col, *misc;
+    using R = typename RealOf<FORM>::T;
+    double *cg, *atry, *beta, *da, *alpha, *covar, *area, *gv, *ym, *red, *dave, *col, *misc;
+    R *areaR, *gvR, *W, *J, *pt;
     int *ipiv;
+    float *dsph;  // FP32 basis in shared memory (mixed form), or nullptr
 };
 
-__device__ inline Smem carve(double *base, const SlotLayout &L)
+template <int FORM>
+__device__ inline Smem<FORM> carve(char *base, const SlotLayout &L)
 {
-    Smem s;
-    s.cg = base + L.o_cg;
-    s.atry = base + L.o_atry;
-    s.beta = base + L.o_beta;
-    s.da = base + L.o_da;
-    s.alpha = base + L.o_alpha;
-    s.covar = base + L.o_covar;
-    s.area = base + L.o_area;
-    s.gv = base + L.o_gv;
-    s.W = base + L.o_W;
-    s.J = base + L.o_J;
-    s.ym = base + L.o_ym;
-    s.pt = base + L.o_pt;
-    s.red = base + L.o_red;
-    s.dave = base + L.o_dave;
-    s.col = base + L.o_col;
-    s.misc = base + L.o_misc;
-    s.ipiv = reinterpret_cast<int *>(reinterpret_cast<char *>(base) + L.o_ipiv);
+    using R = typename RealOf<FORM>::T;
+    Smem<FORM> s;
+    s.cg = reinterpret_cast<double *>(base + L.cg);
+    s.atry = reinterpret_cast<double *>(base + L.atry);
+    s.beta = reinterpret_cast<double *>(base + L.beta);
+    s.da = reinterpret_cast<double *>(base + L.da);
+    s.alpha = reinterpret_cast<double *>(base + L.alpha);
+    s.covar = reinterpret_cast<double *>(base + L.covar);
+    s.area = reinterpret_cast<double *>(base + L.area);
+    s.gv = reinterpret_cast<double *>(base + L.gv);
+    s.areaR = reinterpret_cast<R *>(base + L.areaR);
+    s.gvR = reinterpret_cast<R *>(base + L.gvR);
+    s.W = reinterpret_cast<R *>(base + L.W);
+    s.J = reinterpret_cast<R *>(base + L.J);
+    s.pt = reinterpret_cast<R *>(base + L.pt);
+    s.ym = reinterpret_cast<double *>(base + L.ym);
+    s.red = reinterpret_cast<double *>(base + L.red);
+    s.dave = reinterpret_cast<double *>(base + L.dave);
+    s.col = reinterpret_cast<double *>(base + L.col);
+    s.misc = reinterpret_cast<double *>(base + L.misc);
+    s.ipiv = reinterpret_cast<int *>(base + L.ipiv);
+    s.dsph = L.dsph_smem ? reinterpret_cast<float *>(base + L.dsph) : nullptr;
     return s;
 }
 
@@ -94,16 +113,19 @@ __device__ inline int tri_row(int e)
 
 // Thread that sets up point p of a tile: points are spread over the warps
 // (p % 8 -> warp, p / 8 -> lane) so that all four SM sub-partitions work.
-__device__ inline int setup_thread(int p) { return (p % (kThreads / 32)) * 32 + p / (kThreads / 32); }
+template <int NT>
+__device__ inline int setup_thread(int p) { return (p % (NT / 32)) * 32 + p / (NT / 32); }
 
-__device__ inline double warp_sum(double v)
+template <class T>
+__device__ inline T warp_sum(T v)
 {
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
     return v;
 }
 
-// Sum over the block; every thread gets the result.  red holds >= 8 doubles.
+// Sum over the block; every thread gets the result.  red holds >= NT/32 doubles.
+template <int NT>
 __device__ inline double block_sum(double v, double *red)
 {
     v = warp_sum(v);
@@ -113,9 +135,240 @@ __device__ inline double block_sum(double v, double *red)
     __syncthreads();
     double t = 0;
 #pragma unroll
-    for (int i = 0; i < kThreads / 32; i++) t += red[i];
+    for (int i = 0; i < NT / 32; i++) t += red[i];
     __syncthreads();
     return t;
+}
+
+// Rotation phase omega*t + phi0 reduced to [0, 2*pi).  The FP64 form rounds
+// the product and the sum separately and reduces with fmod, as the
+// reference does (matrix.c:21-22); the mixed form reduces with a two-part
+// 2*pi (the product rounded once), which is exact to ~1e-16 rad.
+template <int FORM>
+__device__ inline double rotation_phase(double omg, double t, double phi0)
+{
+    if constexpr (FORM == PS_FORM_FP64) {
+        return fmod(__dadd_rn(__dmul_rn(omg, t), phi0), kTwoPi);
+    } else {
+        const double x = fma(omg, t, phi0);
+        const double q = floor(x * kInvTwoPi);
+        double f = fma(-q, kTwoPiHi, x);
+        f = fma(-q, kTwoPiLo, f);
+        if (f < 0) f += kTwoPi;
+        if (f >= kTwoPi) f -= kTwoPi;
+        return f;
+    }
+}
+
+// Lit-facet terms of the Lommel-Seeliger + Lambert law (bright.c:65-74,
+// 116-117).  The FP64 form divides as the reference does; the mixed form
+// multiplies by one reciprocal.
+template <class R, int FORM>
+struct LitTerms {
+    R sv, dsmu, dsmu0, dcls_w;  // s, ds/dmu, ds/dmu0, mu*mu0/(mu+mu0)
+    __device__ inline LitTerms(R mu, R mu0, R cl, R cls)
+    {
+        const R dnom = mu + mu0;
+        if constexpr (FORM == PS_FORM_FP64) {
+            sv = mu * mu0 * (cl + cls / dnom);
+            const R q0 = mu0 / dnom, q1 = mu / dnom;
+            dsmu = cls * (q0 * q0) + cl * mu0;
+            dsmu0 = cls * (q1 * q1) + cl * mu;
+            dcls_w = mu * mu0 / dnom;
+        } else {
+            const R r = __frcp_rn(dnom);
+            sv = mu * mu0 * (cl + cls * r);
+            const R q0 = mu0 * r, q1 = mu * r;
+            dsmu = cls * (q0 * q0) + cl * mu0;
+            dsmu0 = cls * (q1 * q1) + cl * mu;
+            dcls_w = mu * mu0 * r;
+        }
+    }
+};
+
+// Accumulates the rows J[0..np) (model values in ym) of one tile into the
+// normal matrix M (lower triangle), bv and chi^2 (mrqcof.c:106-136).  The
+// FP64 form sums every alpha element over points in data order in FP64; the
+// mixed form sums the tile in FP32 and adds the tile sum to the FP64 total.
+// Mixed form: every thread keeps its share of the alpha lower triangle
+// (elements tid + u*256) and of beta (element tid) as FP32 partial sums in
+// registers and adds them to the FP64 totals every few tiles.
+constexpr int kAccPerThread = 8;    // with 512 threads: mfit <= 90
+constexpr int kTilesPerFlush = 8;
+
+template <int FORM>
+__device__ inline void flush_partials(double *M, double *bv, int mf, float (&accA)[kAccPerThread], float &accB)
+{
+    constexpr int NT = threads_of<FORM>();
+    const int tid = threadIdx.x;
+    const int ntri = mf * (mf + 1) / 2;
+#pragma unroll
+    for (int u = 0; u < kAccPerThread; u++) {
+        const int e = tid + u * NT;
+        if (e < ntri) {
+            const int j = tri_row(e);
+            const int k = e - j * (j + 1) / 2;
+            M[j * mf + k] += static_cast<double>(accA[u]);
+        }
+        accA[u] = 0.f;
+    }
+    if (tid < mf) bv[tid] += static_cast<double>(accB);
+    accB = 0.f;
+}
+
+template <int FORM>
+__device__ void accumulate_tile(const DevObject &ob, Smem<FORM> &s, double *M, double *bv, int np, int q0pt,
+                                bool conv, double conv_sig, float (&accA)[kAccPerThread], float &accB)
+{
+    using R = typename RealOf<FORM>::T;
+    constexpr int NT = threads_of<FORM>();
+    const int tid = threadIdx.x;
+    const int ma = ob.ma, mf = ob.mfit;
+    R *wt = s.W;  // [np][mf], reuses the facet-weight tile
+    for (int e = tid; e < np * mf; e += NT) {
+        const int p = e / mf, j = e - p * mf;
+        const int q = q0pt + p;
+        const double sig2i = conv ? 1 / (conv_sig * conv_sig) : ob.sig2i[q];
+        const double wg = ob.weight[q];
+        if constexpr (FORM == PS_FORM_FP64)
+            wt[p * mf + j] = s.J[p * ma + ob.free_list[j]] * sig2i * wg;
+        else
+            wt[p * mf + j] = s.J[p * ma + ob.free_list[j]] * static_cast<float>(sig2i * wg);
+    }
+    __syncthreads();
+    const int ntri = mf * (mf + 1) / 2;
+    if constexpr (FORM == PS_FORM_FP64) {
+        for (int e = tid; e < ntri; e += NT) {
+            const int j = tri_row(e);
+            const int k = e - j * (j + 1) / 2;
+            const int lk = ob.free_list[k];
+            double acc = M[j * mf + k];
+            for (int p = 0; p < np; p++) acc = acc + wt[p * mf + j] * s.J[p * ma + lk];
+            M[j * mf + k] = acc;
+        }
+        for (int j = tid; j < mf; j += NT) {
+            double acc = bv[j];
+            for (int p = 0; p < np; p++) {
+                const double y = conv ? 0.0 : ob.bright[q0pt + p];
+                acc = acc + (y - s.ym[p]) * wt[p * mf + j];
+            }
+            bv[j] = acc;
+        }
+    } else {
+        // residuals of the tile in FP32 (the model value is FP32-accurate)
+        float *dyv = reinterpret_cast<float *>(s.pt);
+        if (tid < np) dyv[tid] = static_cast<float>((conv ? 0.0 : ob.bright[q0pt + tid]) - s.ym[tid]);
+        __syncthreads();
+#pragma unroll
+        for (int u = 0; u < kAccPerThread; u++) {
+            const int e = tid + u * NT;
+            if (e < ntri) {
+                const int j = tri_row(e);
+                const int k = e - j * (j + 1) / 2;
+                const int lk = ob.free_list[k];
+                float acc = accA[u];
+                for (int p = 0; p < np; p++) acc = fmaf(wt[p * mf + j], s.J[p * ma + lk], acc);
+                accA[u] = acc;
+            }
+        }
+        if (tid < mf) {
+            float acc = accB;
+            for (int p = 0; p < np; p++) acc = fmaf(dyv[p], wt[p * mf + tid], acc);
+            accB = acc;
+        }
+    }
+    if (tid == NT - 1) {
+        double c2 = s.misc[M_CHISQ];
+        for (int p = 0; p < np; p++) {
+            const int q = q0pt + p;
+            const double sig2i = conv ? 1 / (conv_sig * conv_sig) : ob.sig2i[q];
+            const double y = conv ? 0.0 : ob.bright[q];
+            const double dy = y - s.ym[p];
+            c2 = c2 + dy * dy * sig2i * ob.weight[q];
+        }
+        s.misc[M_CHISQ] = c2;
+    }
+    __syncthreads();
+}
+
+// Basis element Dsph[i][k] of the mixed form: from shared memory with an
+// explicit shared-space load, or from global memory through the read-only
+// path.
+template <bool SMEM_D>
+__device__ inline float load_basis(const float *d, int idx)
+{
+    if constexpr (SMEM_D) {
+        float v;
+        const unsigned addr = static_cast<unsigned>(__cvta_generic_to_shared(d + idx));
+        asm("ld.shared.f32 %0, [%1];" : "=f"(v) : "r"(addr));
+        return v;
+    } else {
+        return __ldg(d + idx);
+    }
+}
+
+// Mixed-form shape contraction J[p][k] = Scale_p * sum_i W[p][i] Dsph[i][k]
+// of one tile, FP32 on the SIMT pipes.  Register tile: warp w owns points
+// (w % 8) + 8 r (r < 4) and coefficients lane + 32 ((w / 8) + 2 u) (u < KU);
+// W is read four facets at a time (float4 broadcast), Dsph one coalesced row
+// per facet.
+template <int NT, int KU, bool SMEM_D>
+__device__ void contract_mixed(Smem<PS_FORM_MIXED> &s, const float *dsph, int np, int F, int C, int ma, int wcols,
+                               bool conv)
+{
+    static_assert(NT == 512, "the register tile assumes 16 warps");
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int g = warp & 7, half = warp >> 3;
+    constexpr int kPW = 4;
+    float acc[kPW][KU];
+#pragma unroll
+    for (int r = 0; r < kPW; r++)
+#pragma unroll
+        for (int u = 0; u < KU; u++) acc[r][u] = 0.f;
+    int kk[KU];
+    bool kv[KU];
+#pragma unroll
+    for (int u = 0; u < KU; u++) {
+        kk[u] = lane + 32 * (half + 2 * u);
+        kv[u] = kk[u] < C;
+    }
+    bool any = false;
+#pragma unroll
+    for (int u = 0; u < KU; u++) any |= kv[u];
+    const float *Wf = s.W;
+    if (any) {
+        for (int i = 0; i < F; i += 4) {
+            float4 w4[kPW];
+#pragma unroll
+            for (int r = 0; r < kPW; r++) {
+                const int p = g + 8 * r;
+                w4[r] = (p < np) ? *reinterpret_cast<const float4 *>(Wf + static_cast<size_t>(p) * wcols + i)
+                                 : make_float4(0.f, 0.f, 0.f, 0.f);
+            }
+#pragma unroll
+            for (int ii = 0; ii < 4; ii++) {
+                float d[KU];
+#pragma unroll
+                for (int u = 0; u < KU; u++) d[u] = kv[u] ? load_basis<SMEM_D>(dsph, (i + ii) * C + kk[u]) : 0.f;
+#pragma unroll
+                for (int r = 0; r < kPW; r++) {
+                    const float wv = ii == 0 ? w4[r].x : ii == 1 ? w4[r].y : ii == 2 ? w4[r].z : w4[r].w;
+#pragma unroll
+                    for (int u = 0; u < KU; u++) acc[r][u] = fmaf(wv, d[u], acc[r][u]);
+                }
+            }
+        }
+    }
+#pragma unroll
+    for (int r = 0; r < kPW; r++) {
+        const int p = g + 8 * r;
+        if (p < np) {
+            const float sc = conv ? 1.f : s.pt[p * kPointStride + 24];
+#pragma unroll
+            for (int u = 0; u < KU; u++)
+                if (kv[u]) s.J[p * ma + kk[u]] = sc * acc[r][u];
+        }
+    }
 }
 
 // ---------------------------------------------------------------------------
@@ -123,17 +376,35 @@ __device__ inline double block_sum(double v, double *red)
 // lower triangle accumulated then mirrored) and vector bv.  Leaves chi^2,
 // the facet-area sum and the convexity residuals in misc.
 // ---------------------------------------------------------------------------
-template <int FORM>
-__device__ void evaluate(const DevObject &ob, const FitConfig &cfg, const SlotLayout &L, Smem &s,
-                         const double *a, double *M, double *bv, double *scratch)
+template <int FORM, int KU>
+__device__ void evaluate(const DevObject &ob, const FitConfig &cfg, const SlotLayout &L, Smem<FORM> &s,
+                         const double *a, double *M, double *bv, typename RealOf<FORM>::T *scratch)
 {
+    using R = typename RealOf<FORM>::T;
+    constexpr bool kFP64 = FORM == PS_FORM_FP64;
+    constexpr int NT = threads_of<FORM>();
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int F = ob.nfac, C = ob.ncoef, ma = ob.ma, mf = ob.mfit, P = L.P;
-    const int wcols = L.nfac > L.mfit ? L.nfac : L.mfit;
+    const int wcols = L.wcols;
+    const R *nxR, *nyR, *nzR, *dareaR;
+    const R *dsphR;
+    if constexpr (kFP64) {
+        nxR = ob.nx;
+        nyR = ob.ny;
+        nzR = ob.nz;
+        dareaR = ob.darea;
+        dsphR = ob.dsph;
+    } else {
+        nxR = ob.nx_f;
+        nyR = ob.ny_f;
+        nzR = ob.nz_f;
+        dareaR = ob.darea_f;
+        dsphR = ob.dsph_f;
+    }
 
-    // curv.c:10-39 -- g_i = exp(sum over (m,l) of P_l^m (c cos + c' sin)).
+    // curv.c:10-39 -- g_i = exp(sum over (m,l) of P_l^m (c cos + c' sin)), FP64.
     double asum = 0;
-    for (int i = tid; i < F; i += kThreads) {
+    for (int i = tid; i < F; i += NT) {
         double g = 0;
         for (int q = 0; q < ob.npairs; q++) {
             int m = ob.pair_m[q], n = ob.pair_n[q];
@@ -145,38 +416,48 @@ __device__ void evaluate(const DevObject &ob, const FitConfig &cfg, const SlotLa
         double ar = ob.darea[i] * g;
         s.area[i] = ar;
         s.gv[i] = g;
+        if constexpr (!kFP64) {
+            s.areaR[i] = static_cast<R>(ar);
+            s.gvR[i] = static_cast<R>(g);
+        }
         asum += ar;
     }
-    double tot = block_sum(asum, s.misc + M_RED);
+    double tot = block_sum<NT>(asum, s.misc + M_RED);
     if (tid == 0) {
         s.misc[M_AREA] = tot;
         s.misc[M_CHISQ] = 0;
         s.misc[M_CL] = exp(a[ma - 2]);
     }
-    for (int e = tid; e < mf * mf; e += kThreads) M[e] = 0;
-    for (int j = tid; j < mf; j += kThreads) bv[j] = 0;
+    for (int e = tid; e < mf * mf; e += NT) M[e] = 0;
+    for (int j = tid; j < mf; j += NT) bv[j] = 0;
 
+    // blmatrix.c:9-46 in FP64, then in the facet-stage type.
     const double bet = a[C], lam = a[C + 1];
     const double cb = cos(bet), sb = sin(bet), clm = cos(lam), slm = sin(lam);
-    // Blmat and its derivatives (row-major 3x3 each), registers of every thread.
-    const double B[9] = {cb * clm, cb * slm, -sb, -slm, clm, 0, sb * clm, sb * slm, cb};
-    const double DB0[9] = {-sb * clm, -sb * slm, -cb, 0, 0, 0, cb * clm, cb * slm, -sb};
-    const double DB1[9] = {-cb * slm, cb * clm, 0, -clm, -slm, 0, -sb * slm, sb * clm, 0};
+    const R B[9] = {R(cb * clm), R(cb * slm), R(-sb), R(-slm), R(clm), R(0), R(sb * clm), R(sb * slm), R(cb)};
+    const R DB0[9] = {R(-sb * clm), R(-sb * slm), R(-cb), R(0), R(0), R(0), R(cb * clm), R(cb * slm), R(-sb)};
+    const R DB1[9] = {R(-cb * slm), R(cb * clm), R(0), R(-clm), R(-slm), R(0), R(-sb * slm), R(sb * clm), R(0)};
     const double omg = a[C + 2];
-    const double php0 = a[C + 3], php1 = a[C + 4], php2 = a[C + 5];
-    const double cls = a[C + 7];
+    const R php0 = R(a[C + 3]), php1 = R(a[C + 4]), php2 = R(a[C + 5]);
+    const R cls = R(a[C + 7]);
     __syncthreads();
-    const double cl = s.misc[M_CL];
+    const R cl = R(s.misc[M_CL]);
 
     const double conv_sig = 1 / cfg.conw_r;
-    const double conv_sig2i = 1 / (conv_sig * conv_sig);
+    float accA[kAccPerThread];
+    float accB = 0.f;
+#pragma unroll
+    for (int u = 0; u < kAccPerThread; u++) accA[u] = 0.f;
+    int tiles_since_flush = 0;
+    const float *dsphF = nullptr;
+    if constexpr (!kFP64) dsphF = s.dsph ? s.dsph : ob.dsph_f;
 
     for (int lc = 0; lc < ob.n_lc; lc++) {
         const int start = ob.lc_start[lc], npts = ob.lc_npts[lc];
         const bool rel = ob.lc_rel[lc] != 0;
         const bool conv = (lc == ob.n_lc - 1);
         if (rel) {
-            for (int l = tid; l < ma; l += kThreads) s.dave[l] = 0;
+            for (int l = tid; l < ma; l += NT) s.dave[l] = 0;
             if (tid == 0) s.misc[M_AVE] = 0;
         }
         // ---- pass 1: model rows of this lightcurve, tile by tile ----
@@ -185,27 +466,34 @@ __device__ void evaluate(const DevObject &ob, const FitConfig &cfg, const SlotLa
             if (!conv) {
                 // 1. point set-up (bright.c:27-57, phasec.c, matrix.c)
                 // point sp is set up by thread setup_thread(sp) == tid
-                const int sp = (tid % 32) * (kThreads / 32) + tid / 32;
+                const int sp = (tid % 32) * (NT / 32) + tid / 32;
                 if (sp < np) {
                     const int q = start + t0 + sp;
-                    const double ee[3] = {ob.eex[q], ob.eey[q], ob.eez[q]};
-                    const double e0v[3] = {ob.e0x[q], ob.e0y[q], ob.e0z[q]};
-                    const double t = ob.tim[q];
-                    double cos_alpha = ee[0] * e0v[0] + ee[1] * e0v[1] + ee[2] * e0v[2];
-                    double alpha = acos(cos_alpha);
-                    double ex = exp(-alpha / php1);
-                    double scale = 1 + php0 * ex + php2 * alpha;
-                    double f = omg * t + cfg.phi0;
-                    f = fmod(f, kTwoPi);
-                    double cf = cos(f), sf = sin(f);
-                    const double fm[9] = {cf, sf, 0, -sf, cf, 0, 0, 0, 1};
-                    const double dfm[9] = {-t * sf, t * cf, 0, -t * cf, -t * sf, 0, 0, 0, 0};
-                    double tm[9], d0[9], d1[9], d2[9];
+                    const R ee[3] = {R(ob.eex[q]), R(ob.eey[q]), R(ob.eez[q])};
+                    const R e0v[3] = {R(ob.e0x[q]), R(ob.e0y[q]), R(ob.e0z[q])};
+                    const double td = ob.tim[q];
+                    const R t = R(td);
+                    const R alpha = R(ob.alpha_pt[q]);
+                    R ex;
+                    if constexpr (kFP64) ex = exp(-alpha / php1);
+                    else ex = expf(-alpha / php1);
+                    const R scale = 1 + php0 * ex + php2 * alpha;
+                    const double f = rotation_phase<FORM>(omg, td, cfg.phi0);
+                    R cf, sf;
+                    if constexpr (kFP64) {
+                        cf = cos(f);
+                        sf = sin(f);
+                    } else {
+                        sincosf(static_cast<float>(f), &sf, &cf);
+                    }
+                    const R fm[9] = {cf, sf, R(0), -sf, cf, R(0), R(0), R(0), R(1)};
+                    const R dfm[9] = {-t * sf, t * cf, R(0), -t * cf, -t * sf, R(0), R(0), R(0), R(0)};
+                    R tm[9], d0[9], d1[9], d2[9];
 #pragma unroll
                     for (int i = 0; i < 3; i++)
 #pragma unroll
                         for (int j = 0; j < 3; j++) {
-                            double x = 0, y0 = 0, y1 = 0, y2 = 0;
+                            R x = 0, y0 = 0, y1 = 0, y2 = 0;
 #pragma unroll
                             for (int k = 0; k < 3; k++) {
                                 x = x + fm[i * 3 + k] * B[k * 3 + j];
@@ -218,10 +506,10 @@ __device__ void evaluate(const DevObject &ob, const FitConfig &cfg, const SlotLa
                             d1[i * 3 + j] = y1;
                             d2[i * 3 + j] = y2;
                         }
-                    double *pt = s.pt + sp * kPointStride;
+                    R *pt = s.pt + sp * kPointStride;
 #pragma unroll
                     for (int i = 0; i < 3; i++) {
-                        double x = 0, y = 0;
+                        R x = 0, y = 0;
 #pragma unroll
                         for (int j = 0; j < 3; j++) {
                             x = x + tm[i * 3 + j] * ee[j];
@@ -231,12 +519,12 @@ __device__ void evaluate(const DevObject &ob, const FitConfig &cfg, const SlotLa
                         pt[3 + i] = y;
                     }
                     // de[i][j] = sum_k dtm[j][i][k] ee[k]; stored de[i*3+j] (j = derivative)
-                    const double *dd[3] = {d0, d1, d2};
+                    const R *dd[3] = {d0, d1, d2};
 #pragma unroll
                     for (int i = 0; i < 3; i++)
 #pragma unroll
                         for (int j = 0; j < 3; j++) {
-                            double x = 0, y = 0;
+                            R x = 0, y = 0;
 #pragma unroll
                             for (int k = 0; k < 3; k++) {
                                 x = x + dd[j][i * 3 + k] * ee[k];
@@ -252,43 +540,39 @@ __device__ void evaluate(const DevObject &ob, const FitConfig &cfg, const SlotLa
                 }
                 __syncthreads();
                 // 2. facet stage (bright.c:59-120), one warp per point
-                for (int p = warp; p < np; p += kThreads / 32) {
-                    const double *pt = s.pt + p * kPointStride;
-                    const double e1 = pt[0], e2 = pt[1], e3 = pt[2];
-                    const double f1 = pt[3], f2 = pt[4], f3 = pt[5];
-                    double de[9], de0[9];
+                for (int p = warp; p < np; p += NT / 32) {
+                    const R *pt = s.pt + p * kPointStride;
+                    const R e1 = pt[0], e2 = pt[1], e3 = pt[2];
+                    const R f1 = pt[3], f2 = pt[4], f3 = pt[5];
+                    R de[9], de0[9];
 #pragma unroll
                     for (int k = 0; k < 9; k++) {
                         de[k] = pt[6 + k];
                         de0[k] = pt[15 + k];
                     }
-                    double br = 0, r0 = 0, r1 = 0, r2 = 0, dcl = 0, dcls = 0;
-                    double *Wp = s.W + static_cast<size_t>(p) * wcols;
+                    R br = 0, r0 = 0, r1 = 0, r2 = 0, dcl = 0, dcls = 0;
+                    R *Wp = s.W + static_cast<size_t>(p) * wcols;
                     for (int i = lane; i < F; i += 32) {
-                        const double nx = ob.nx[i], ny = ob.ny[i], nz = ob.nz[i];
-                        const double mu = e1 * nx + e2 * ny + e3 * nz;
-                        const double mu0 = f1 * nx + f2 * ny + f3 * nz;
-                        double w = 0;
-                        if (mu > kTinyMu && mu0 > kTinyMu) {
-                            const double ar = s.area[i];
-                            const double dnom = mu + mu0;
-                            const double sv = mu * mu0 * (cl + cls / dnom);
-                            br = br + ar * sv;
-                            const double q0 = mu0 / dnom, q1 = mu / dnom;
-                            const double dsmu = cls * (q0 * q0) + cl * mu0;
-                            const double dsmu0 = cls * (q1 * q1) + cl * mu;
-                            w = ob.darea[i] * sv * s.gv[i];
-                            const double s0 = nx * de[0] + ny * de[3] + nz * de[6];
-                            const double s1 = nx * de[1] + ny * de[4] + nz * de[7];
-                            const double s2 = nx * de[2] + ny * de[5] + nz * de[8];
-                            const double t0v = nx * de0[0] + ny * de0[3] + nz * de0[6];
-                            const double t1v = nx * de0[1] + ny * de0[4] + nz * de0[7];
-                            const double t2v = nx * de0[2] + ny * de0[5] + nz * de0[8];
-                            r0 = r0 + ar * (dsmu * s0 + dsmu0 * t0v);
-                            r1 = r1 + ar * (dsmu * s1 + dsmu0 * t1v);
-                            r2 = r2 + ar * (dsmu * s2 + dsmu0 * t2v);
+                        const R nx = nxR[i], ny = nyR[i], nz = nzR[i];
+                        const R mu = e1 * nx + e2 * ny + e3 * nz;
+                        const R mu0 = f1 * nx + f2 * ny + f3 * nz;
+                        R w = 0;
+                        if (mu > R(kTinyMu) && mu0 > R(kTinyMu)) {
+                            const R ar = s.areaR[i];
+                            const LitTerms<R, FORM> lt(mu, mu0, cl, cls);
+                            br = br + ar * lt.sv;
+                            w = dareaR[i] * lt.sv * s.gvR[i];
+                            const R s0 = nx * de[0] + ny * de[3] + nz * de[6];
+                            const R s1 = nx * de[1] + ny * de[4] + nz * de[7];
+                            const R s2 = nx * de[2] + ny * de[5] + nz * de[8];
+                            const R t0v = nx * de0[0] + ny * de0[3] + nz * de0[6];
+                            const R t1v = nx * de0[1] + ny * de0[4] + nz * de0[7];
+                            const R t2v = nx * de0[2] + ny * de0[5] + nz * de0[8];
+                            r0 = r0 + ar * (lt.dsmu * s0 + lt.dsmu0 * t0v);
+                            r1 = r1 + ar * (lt.dsmu * s1 + lt.dsmu0 * t1v);
+                            r2 = r2 + ar * (lt.dsmu * s2 + lt.dsmu0 * t2v);
                             dcl = dcl + mu * mu0 * ar;
-                            dcls = dcls + ar * mu * mu0 / dnom;
+                            dcls = dcls + ar * lt.dcls_w;
                         }
                         Wp[i] = w;
                     }
@@ -309,14 +593,15 @@ __device__ void evaluate(const DevObject &ob, const FitConfig &cfg, const SlotLa
                     }
                 }
             } else {
-                // convexity rows (conv.c:12-29): W = Darea g n_c, residual = sum Area n_c
-                for (int p = warp; p < np; p += kThreads / 32) {
+                // convexity rows (conv.c:12-29): W = Darea g n_c, residual =
+                // sum Area n_c (the residual in FP64 in both forms)
+                for (int p = warp; p < np; p += NT / 32) {
                     const double *nc = (p == 0) ? ob.nx : (p == 1) ? ob.ny : ob.nz;
                     double res = 0;
-                    double *Wp = s.W + static_cast<size_t>(p) * wcols;
+                    R *Wp = s.W + static_cast<size_t>(p) * wcols;
                     for (int i = lane; i < F; i += 32) {
                         res = res + s.area[i] * nc[i];
-                        Wp[i] = ob.darea[i] * s.gv[i] * nc[i];
+                        Wp[i] = R(ob.darea[i] * s.gv[i] * nc[i]);
                     }
                     res = warp_sum(res);
                     if (lane == 0) s.red[p * kRedStride] = res;
@@ -324,30 +609,38 @@ __device__ void evaluate(const DevObject &ob, const FitConfig &cfg, const SlotLa
             }
             __syncthreads();
             // 3. shape contraction and the remaining columns of J
-            for (int o = tid; o < np * C; o += kThreads) {
-                const int p = o / C, k = o - p * C;
-                const double *Wp = s.W + static_cast<size_t>(p) * wcols;
-                const double *ds = ob.dsph + k;
-                double acc = 0;
-                for (int i = 0; i < F; i++) acc = acc + Wp[i] * ds[static_cast<size_t>(i) * C];
-                s.J[p * ma + k] = conv ? acc : s.pt[p * kPointStride + 24] * acc;
+            if constexpr (kFP64) {
+                for (int o = tid; o < np * C; o += NT) {
+                    const int p = o / C, k = o - p * C;
+                    const R *Wp = s.W + static_cast<size_t>(p) * wcols;
+                    const R *ds = dsphR + k;
+                    R acc = 0;
+                    for (int i = 0; i < F; i++) acc = acc + Wp[i] * ds[static_cast<size_t>(i) * C];
+                    s.J[p * ma + k] = conv ? acc : s.pt[p * kPointStride + 24] * acc;
+                }
+            } else {
+                if (s.dsph)
+                    contract_mixed<NT, KU, true>(s, dsphF, np, F, C, ma, wcols, conv);
+                else
+                    contract_mixed<NT, KU, false>(s, dsphF, np, F, C, ma, wcols, conv);
             }
             if (tid < np) {
                 const int p = tid;
-                double *Jp = s.J + p * ma;
+                R *Jp = s.J + p * ma;
                 const double *rd = s.red + p * kRedStride;
                 if (!conv) {
-                    const double *pt = s.pt + p * kPointStride;
-                    const double scale = pt[24];
-                    Jp[C] = scale * rd[1];
-                    Jp[C + 1] = scale * rd[2];
-                    Jp[C + 2] = scale * rd[3];
-                    Jp[C + 3] = rd[0] * pt[25];
-                    Jp[C + 4] = rd[0] * pt[26];
-                    Jp[C + 5] = rd[0] * pt[27];
-                    Jp[C + 6] = scale * rd[4] * cl;
-                    Jp[C + 7] = scale * rd[5];
-                    s.ym[p] = rd[0] * scale;
+                    const R *pt = s.pt + p * kPointStride;
+                    const R scale = pt[24];
+                    const R br = R(rd[0]);
+                    Jp[C] = scale * R(rd[1]);
+                    Jp[C + 1] = scale * R(rd[2]);
+                    Jp[C + 2] = scale * R(rd[3]);
+                    Jp[C + 3] = br * pt[25];
+                    Jp[C + 4] = br * pt[26];
+                    Jp[C + 5] = br * pt[27];
+                    Jp[C + 6] = scale * R(rd[4]) * cl;
+                    Jp[C + 7] = scale * R(rd[5]);
+                    s.ym[p] = static_cast<double>(br * scale);
                 } else {
                     for (int k = C; k < ma; k++) Jp[k] = 0;
                     s.ym[p] = rd[0];
@@ -357,16 +650,22 @@ __device__ void evaluate(const DevObject &ob, const FitConfig &cfg, const SlotLa
             __syncthreads();
             if (rel) {
                 // 4a. lightcurve sums and a copy of the rows (mrqcof.c:51-88)
-                double *dst = scratch + static_cast<size_t>(t0) * (ma + 1);
-                for (int e = tid; e < np * ma; e += kThreads) {
+                R *dst = scratch + static_cast<size_t>(t0) * (ma + 1);
+                for (int e = tid; e < np * ma; e += NT) {
                     int p = e / ma, l = e - p * ma;
                     dst[static_cast<size_t>(p) * (ma + 1) + l] = s.J[e];
                 }
-                if (tid < np) dst[static_cast<size_t>(tid) * (ma + 1) + ma] = s.ym[tid];
-                for (int l = tid; l < ma; l += kThreads) {
-                    double d = s.dave[l];
-                    for (int p = 0; p < np; p++) d = d + s.J[p * ma + l];
-                    s.dave[l] = d;
+                if (tid < np) dst[static_cast<size_t>(tid) * (ma + 1) + ma] = R(s.ym[tid]);
+                for (int l = tid; l < ma; l += NT) {
+                    if constexpr (kFP64) {
+                        double d = s.dave[l];
+                        for (int p = 0; p < np; p++) d = d + s.J[p * ma + l];
+                        s.dave[l] = d;
+                    } else {
+                        float d = 0.f;
+                        for (int p = 0; p < np; p++) d += s.J[p * ma + l];
+                        s.dave[l] += static_cast<double>(d);
+                    }
                 }
                 if (tid == 0) {
                     double av = s.misc[M_AVE];
@@ -377,49 +676,12 @@ __device__ void evaluate(const DevObject &ob, const FitConfig &cfg, const SlotLa
                 continue;
             }
             // 5. accumulate (mrqcof.c:106-136)
-            {
-                double *wt = s.W;  // reuse: [P][mfit]
-                for (int e = tid; e < np * mf; e += kThreads) {
-                    const int p = e / mf, j = e - p * mf;
-                    const int q = start + t0 + p;
-                    const double sg = conv ? conv_sig : ob.sig[q];
-                    const double sig2i = 1 / (sg * sg);
-                    const double wg = ob.weight[q];
-                    wt[p * mf + j] = s.J[p * ma + ob.free_list[j]] * sig2i * wg;
+            accumulate_tile<FORM>(ob, s, M, bv, np, start + t0, conv, conv_sig, accA, accB);
+            if constexpr (!kFP64) {
+                if (++tiles_since_flush == kTilesPerFlush) {
+                    flush_partials<FORM>(M, bv, mf, accA, accB);
+                    tiles_since_flush = 0;
                 }
-                __syncthreads();
-                const int ntri = mf * (mf + 1) / 2;
-                for (int e = tid; e < ntri; e += kThreads) {
-                    const int j = tri_row(e);
-                    const int k = e - j * (j + 1) / 2;
-                    const int lk = ob.free_list[k];
-                    double acc = M[j * mf + k];
-                    for (int p = 0; p < np; p++) acc = acc + wt[p * mf + j] * s.J[p * ma + lk];
-                    M[j * mf + k] = acc;
-                }
-                for (int j = tid; j < mf; j += kThreads) {
-                    double acc = bv[j];
-                    for (int p = 0; p < np; p++) {
-                        const int q = start + t0 + p;
-                        const double y = conv ? 0.0 : ob.bright[q];
-                        const double dy = y - s.ym[p];
-                        acc = acc + dy * wt[p * mf + j];
-                    }
-                    bv[j] = acc;
-                }
-                if (tid == kThreads - 1) {
-                    double c2 = s.misc[M_CHISQ];
-                    for (int p = 0; p < np; p++) {
-                        const int q = start + t0 + p;
-                        const double sg = conv ? conv_sig : ob.sig[q];
-                        const double sig2i = conv ? conv_sig2i : 1 / (sg * sg);
-                        const double y = conv ? 0.0 : ob.bright[q];
-                        const double dy = y - s.ym[p];
-                        c2 = c2 + dy * dy * sig2i * ob.weight[q];
-                    }
-                    s.misc[M_CHISQ] = c2;
-                }
-                __syncthreads();
             }
         }
         if (!rel) continue;
@@ -427,61 +689,47 @@ __device__ void evaluate(const DevObject &ob, const FitConfig &cfg, const SlotLa
         const double ave = s.misc[M_AVE];
         for (int t0 = 0; t0 < npts; t0 += P) {
             const int np = min(P, npts - t0);
-            const double *src = scratch + static_cast<size_t>(t0) * (ma + 1);
-            for (int e = tid; e < np * ma; e += kThreads) {
-                const int p = e / ma, l = e - p * ma;
-                const int q = start + t0 + p;
-                const double coef = ob.sig[q] * npts / ave;
-                const double yt = src[static_cast<size_t>(p) * (ma + 1) + ma];
-                double v = coef * (src[static_cast<size_t>(p) * (ma + 1) + l] - yt * s.dave[l] / ave);
-                s.J[e] = (l == 0) ? 0.0 : v;
-            }
+            const R *src = scratch + static_cast<size_t>(t0) * (ma + 1);
+            // model values of the tile in FP64 (the FP64 form keeps its own
+            // values; the mixed form parks them as FP32)
             if (tid < np) {
                 const int q = start + t0 + tid;
                 const double coef = ob.sig[q] * npts / ave;
-                s.ym[tid] = coef * src[static_cast<size_t>(tid) * (ma + 1) + ma];
+                const double yt = static_cast<double>(src[static_cast<size_t>(tid) * (ma + 1) + ma]);
+                s.ym[tid] = coef * yt;
+                s.red[tid * kRedStride + 6] = coef;
+                s.red[tid * kRedStride + 7] = yt / ave;
             }
             __syncthreads();
-            double *wt = s.W;
-            for (int e = tid; e < np * mf; e += kThreads) {
-                const int p = e / mf, j = e - p * mf;
-                const int q = start + t0 + p;
-                const double sig2i = 1 / (ob.sig[q] * ob.sig[q]);
-                wt[p * mf + j] = s.J[p * ma + ob.free_list[j]] * sig2i * ob.weight[q];
-            }
-            __syncthreads();
-            const int ntri = mf * (mf + 1) / 2;
-            for (int e = tid; e < ntri; e += kThreads) {
-                const int j = tri_row(e);
-                const int k = e - j * (j + 1) / 2;
-                const int lk = ob.free_list[k];
-                double acc = M[j * mf + k];
-                for (int p = 0; p < np; p++) acc = acc + wt[p * mf + j] * s.J[p * ma + lk];
-                M[j * mf + k] = acc;
-            }
-            for (int j = tid; j < mf; j += kThreads) {
-                double acc = bv[j];
-                for (int p = 0; p < np; p++) {
-                    const double dy = ob.bright[start + t0 + p] - s.ym[p];
-                    acc = acc + dy * wt[p * mf + j];
-                }
-                bv[j] = acc;
-            }
-            if (tid == kThreads - 1) {
-                double c2 = s.misc[M_CHISQ];
-                for (int p = 0; p < np; p++) {
+            for (int e = tid; e < np * ma; e += NT) {
+                const int p = e / ma, l = e - p * ma;
+                const R v = src[static_cast<size_t>(p) * (ma + 1) + l];
+                R out;
+                if constexpr (kFP64) {
                     const int q = start + t0 + p;
-                    const double sig2i = 1 / (ob.sig[q] * ob.sig[q]);
-                    const double dy = ob.bright[q] - s.ym[p];
-                    c2 = c2 + dy * dy * sig2i * ob.weight[q];
+                    const double coef = ob.sig[q] * npts / ave;
+                    const double yt = src[static_cast<size_t>(p) * (ma + 1) + ma];
+                    out = coef * (v - yt * s.dave[l] / ave);
+                } else {
+                    out = float(s.red[p * kRedStride + 6]) *
+                          (v - float(s.red[p * kRedStride + 7]) * float(s.dave[l]));
                 }
-                s.misc[M_CHISQ] = c2;
+                s.J[e] = (l == 0) ? R(0) : out;
             }
             __syncthreads();
+            accumulate_tile<FORM>(ob, s, M, bv, np, start + t0, false, conv_sig, accA, accB);
+            if constexpr (!kFP64) {
+                if (++tiles_since_flush == kTilesPerFlush) {
+                    flush_partials<FORM>(M, bv, mf, accA, accB);
+                    tiles_since_flush = 0;
+                }
+            }
         }
     }
+    if constexpr (!kFP64) flush_partials<FORM>(M, bv, mf, accA, accB);
+    __syncthreads();
     // mirror the lower triangle (mrqcof.c:139-141)
-    for (int e = tid; e < mf * mf; e += kThreads) {
+    for (int e = tid; e < mf * mf; e += NT) {
         const int j = e / mf, k = e - j * mf;
         if (k > j) M[e] = M[k * mf + j];
     }
@@ -494,17 +742,18 @@ __device__ void evaluate(const DevObject &ob, const FitConfig &cfg, const SlotLa
 // inverse are not updated and the final column unscrambling is skipped; the
 // pivot choices and the solution are those of the full algorithm.
 // Returns 0, 1 (no usable pivot: NaN entries) or 2 (zero pivot).
+template <int NT>
 __device__ int gauss_jordan(double *A, double *b, int n, double *col, int *ipiv, double *red)
 {
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    for (int k = tid; k < n; k += kThreads) ipiv[k] = 0;
+    for (int k = tid; k < n; k += NT) ipiv[k] = 0;
     __syncthreads();
     for (int step = 0; step < n; step++) {
         // pivot search: largest |a| over unpivoted rows and columns; ties go
         // to the last element in row-major order (the reference's >=).
         double bv = -1.0;
         int bi = -1;
-        for (int e = tid; e < n * n; e += kThreads) {
+        for (int e = tid; e < n * n; e += NT) {
             const int j = e / n, k = e - j * n;
             if (ipiv[j] != 1 && ipiv[k] == 0) {
                 const double v = fabs(A[e]);
@@ -531,7 +780,7 @@ __device__ int gauss_jordan(double *A, double *b, int n, double *col, int *ipiv,
         if (tid == 0) {
             double v = red[0];
             int idx = ipiv[n + 2];
-            for (int w = 1; w < kThreads / 32; w++) {
+            for (int w = 1; w < NT / 32; w++) {
                 const double ov = red[w];
                 const int oi = ipiv[n + 2 + w];
                 if (ov > v || (ov == v && oi > idx)) {
@@ -547,7 +796,7 @@ __device__ int gauss_jordan(double *A, double *b, int n, double *col, int *ipiv,
         if (idx < 0) return 1;
         const int irow = idx / n, icol = idx - irow * n;
         if (irow != icol) {
-            for (int l = tid; l < n; l += kThreads) {
+            for (int l = tid; l < n; l += NT) {
                 const double t = A[irow * n + l];
                 A[irow * n + l] = A[icol * n + l];
                 A[icol * n + l] = t;
@@ -564,34 +813,89 @@ __device__ int gauss_jordan(double *A, double *b, int n, double *col, int *ipiv,
         const double pivinv = 1.0 / piv;
         __syncthreads();
         // scale the pivot row over the columns not yet pivoted
-        for (int l = tid; l < n; l += kThreads)
+        for (int l = tid; l < n; l += NT)
             if (ipiv[l] == 0) A[icol * n + l] *= pivinv;
         if (tid == 0) b[icol] *= pivinv;
-        for (int r = tid; r < n; r += kThreads) col[r] = A[r * n + icol];
+        for (int r = tid; r < n; r += NT) col[r] = A[r * n + icol];
         __syncthreads();
-        for (int e = tid; e < n * n; e += kThreads) {
+        for (int e = tid; e < n * n; e += NT) {
             const int r = e / n, l = e - r * n;
             if (r != icol && ipiv[l] == 0) A[e] -= A[icol * n + l] * col[r];
         }
-        for (int r = tid; r < n; r += kThreads)
+        for (int r = tid; r < n; r += NT)
             if (r != icol) b[r] -= b[icol] * col[r];
         __syncthreads();
     }
     return 0;
 }
 
+// Cholesky factorisation A = L L^T of the damped normal matrix (symmetric
+// positive definite; lower triangle used, overwritten by L) and the two
+// triangular solves for b, in FP64.  Returns 2 when a pivot is not positive.
+template <int NT>
+__device__ int cholesky_solve(double *A, double *b, int n, double *col)
+{
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    (void)col;
+    __syncthreads();
+    for (int j = 0; j < n; j++) {
+        const double d = A[j * n + j];
+        if (!(d > 0.0)) return 2;
+        const double ljj = sqrt(d);
+        const double inv = 1.0 / ljj;
+        __syncthreads();
+        for (int i = j + 1 + tid; i < n; i += NT) A[i * n + j] *= inv;
+        if (tid == 0) A[j * n + j] = ljj;
+        __syncthreads();
+        const int m = n - j - 1;
+        const int ntri = m * (m + 1) / 2;
+        for (int e = tid; e < ntri; e += NT) {
+            const int r = tri_row(e);
+            const int c = e - r * (r + 1) / 2;
+            const int i = j + 1 + r, k = j + 1 + c;
+            A[i * n + k] -= A[i * n + j] * A[k * n + j];
+        }
+        __syncthreads();
+    }
+    if (warp == 0) {
+        for (int j = 0; j < n; j++) {
+            double y = 0;
+            if (lane == 0) {
+                y = b[j] / A[j * n + j];
+                b[j] = y;
+            }
+            y = __shfl_sync(0xffffffffu, y, 0);
+            for (int i = j + 1 + lane; i < n; i += 32) b[i] -= A[i * n + j] * y;
+            __syncwarp();
+        }
+        for (int j = n - 1; j >= 0; j--) {
+            double x = 0;
+            if (lane == 0) {
+                x = b[j] / A[j * n + j];
+                b[j] = x;
+            }
+            x = __shfl_sync(0xffffffffu, x, 0);
+            for (int i = lane; i < j; i += 32) b[i] -= A[j * n + i] * x;
+            __syncwarp();
+        }
+    }
+    __syncthreads();
+    return 0;
+}
+
 // ---------------------------------------------------------------------------
 // One fit (period_search_BOINC.cpp:817-921 with mrqmin.c:11-110).
 // ---------------------------------------------------------------------------
-template <int FORM>
-__device__ void run_fit(const DevObject &ob, const FitConfig &cfg, const SlotLayout &L, Smem &s,
-                        double *scratch, int64_t n, int pole, ps_fit *out)
+template <int FORM, int KU>
+__device__ void run_fit(const DevObject &ob, const FitConfig &cfg, const SlotLayout &L, Smem<FORM> &s,
+                        typename RealOf<FORM>::T *scratch, int64_t n, int pole, ps_fit *out)
 {
+    constexpr int NT = threads_of<FORM>();
     const int tid = threadIdx.x;
     const int C = ob.ncoef, ma = ob.ma, mf = ob.mfit;
     const double freq = cfg.freq_start - (n - 1) * cfg.freq_step;
     const double prd = 1 / freq;
-    for (int i = tid; i < ma; i += kThreads) {
+    for (int i = tid; i < ma; i += NT) {
         double v;
         if (i < C) v = ob.cg_first[i];
         else if (i == C) v = kDeg2Rad * (90 - c_beta_pole[pole - 1]);
@@ -614,31 +918,46 @@ __device__ void run_fit(const DevObject &ob, const FitConfig &cfg, const SlotLay
     int niter = 0, last_err = 0;
     while (((niter < cfg.n_iter_max) && (iter_diff > cfg.iter_diff_max)) || (niter < cfg.n_iter_min)) {
         bool accepted = false;
-        bool evaluated_trial = false;
         if (alamda < 0) {
             alamda = cfg.alamda_start;
-            evaluate<FORM>(ob, cfg, L, s, s.cg, s.alpha, s.beta, scratch);
+            evaluate<FORM, KU>(ob, cfg, L, s, s.cg, s.alpha, s.beta, scratch);
             ochisq = s.misc[M_CHISQ];
             area_first = s.misc[M_AREA];
             for (int c = 0; c < 3; c++) chk_first[c] = s.misc[M_CHK + c];
             totarea = area_first;
         }
-        for (int e = tid; e < mf * mf; e += kThreads) {
+        for (int e = tid; e < mf * mf; e += NT) {
             const int j = e / mf, k = e - j * mf;
             s.covar[e] = (j == k) ? s.alpha[e] * (1 + alamda) : s.alpha[e];
         }
-        for (int j = tid; j < mf; j += kThreads) s.da[j] = s.beta[j];
+        for (int j = tid; j < mf; j += NT) s.da[j] = s.beta[j];
         __syncthreads();
-        const int err = gauss_jordan(s.covar, s.da, mf, s.col, s.ipiv, s.misc + M_RED);
+        int err;
+        if constexpr (FORM == PS_FORM_FP64) {
+            err = gauss_jordan<NT>(s.covar, s.da, mf, s.col, s.ipiv, s.misc + M_RED);
+        } else {
+            // The damped normal matrix is symmetric positive definite: solve
+            // it by Cholesky in FP64; if a pivot is not positive (rounding on
+            // a nearly singular alpha), redo the step with Gauss-Jordan.
+            err = cholesky_solve<NT>(s.covar, s.da, mf, s.col);
+            if (err) {
+                for (int e = tid; e < mf * mf; e += NT) {
+                    const int j = e / mf, k = e - j * mf;
+                    s.covar[e] = (j == k) ? s.alpha[e] * (1 + alamda) : s.alpha[e];
+                }
+                for (int j = tid; j < mf; j += NT) s.da[j] = s.beta[j];
+                __syncthreads();
+                err = gauss_jordan<NT>(s.covar, s.da, mf, s.col, s.ipiv, s.misc + M_RED);
+            }
+        }
         __syncthreads();
         if (err == 0) {
-            for (int j = tid; j < mf; j += kThreads) {
+            for (int j = tid; j < mf; j += NT) {
                 const int l = ob.free_list[j];
                 s.atry[l] = s.cg[l] + s.da[j];
             }
             __syncthreads();
-            evaluate<FORM>(ob, cfg, L, s, s.atry, s.covar, s.da, scratch);
-            evaluated_trial = true;
+            evaluate<FORM, KU>(ob, cfg, L, s, s.atry, s.covar, s.da, scratch);
             chisq = s.misc[M_CHISQ];
             area_trial = s.misc[M_AREA];
             for (int c = 0; c < 3; c++) chk_trial[c] = s.misc[M_CHK + c];
@@ -646,9 +965,9 @@ __device__ void run_fit(const DevObject &ob, const FitConfig &cfg, const SlotLay
             if (chisq < ochisq) {
                 accepted = true;
                 alamda = alamda / cfg.alamda_incr;
-                for (int e = tid; e < mf * mf; e += kThreads) s.alpha[e] = s.covar[e];
-                for (int j = tid; j < mf; j += kThreads) s.beta[j] = s.da[j];
-                for (int l = tid; l < ma; l += kThreads) s.cg[l] = s.atry[l];
+                for (int e = tid; e < mf * mf; e += NT) s.alpha[e] = s.covar[e];
+                for (int j = tid; j < mf; j += NT) s.beta[j] = s.da[j];
+                for (int l = tid; l < ma; l += NT) s.cg[l] = s.atry[l];
                 __syncthreads();
             } else {
                 alamda = cfg.alamda_incr * alamda;
@@ -657,7 +976,6 @@ __device__ void run_fit(const DevObject &ob, const FitConfig &cfg, const SlotLay
         } else {
             last_err = err;
         }
-        (void)evaluated_trial;
         niter++;
         if ((niter == 1) || (chisq < ochisq)) {
             ochisq = chisq;
@@ -692,13 +1010,18 @@ __device__ void run_fit(const DevObject &ob, const FitConfig &cfg, const SlotLay
     __syncthreads();
 }
 
-template <int FORM>
-__global__ void __launch_bounds__(kThreads) fit_kernel(DevObject ob, FitConfig cfg, FitWork w, int P)
+template <int FORM, int KU>
+__global__ void __launch_bounds__(threads_of<FORM>(), 1)
+    fit_kernel(DevObject ob, FitConfig cfg, FitWork w, int P, int dsph_smem)
 {
-    extern __shared__ __align__(16) double smem[];
-    const SlotLayout L = make_layout(ob.ma, ob.mfit, ob.nfac, P);
-    Smem s = carve(smem, L);
-    double *scratch = w.scratch + static_cast<size_t>(blockIdx.x) * w.scratch_stride;
+    using R = typename RealOf<FORM>::T;
+    constexpr int NT = threads_of<FORM>();
+    extern __shared__ __align__(16) char smem[];
+    const SlotLayout L = make_layout(FORM, ob.ma, ob.mfit, ob.nfac, ob.ncoef, P, dsph_smem);
+    Smem<FORM> s = carve<FORM>(smem, L);
+    if (s.dsph)
+        for (int e = threadIdx.x; e < ob.nfac * ob.ncoef; e += NT) s.dsph[e] = ob.dsph_f[e];
+    R *scratch = reinterpret_cast<R *>(w.scratch + static_cast<size_t>(blockIdx.x) * w.scratch_stride);
     __shared__ long long next;
     for (;;) {
         if (threadIdx.x == 0) next = static_cast<long long>(atomicAdd(w.queue, 1ULL));
@@ -715,26 +1038,30 @@ __global__ void __launch_bounds__(kThreads) fit_kernel(DevObject ob, FitConfig c
             n = w.n_lo + f / PS_N_POLES;
             pole = static_cast<int>(f % PS_N_POLES) + 1;
         }
-        run_fit<FORM>(ob, cfg, L, s, scratch, n, pole, w.out + f);
+        run_fit<FORM, KU>(ob, cfg, L, s, scratch, n, pole, w.out + f);
     }
 }
 
-template <int FORM>
-__global__ void __launch_bounds__(kThreads) eval_kernel(DevObject ob, FitConfig cfg, const double *cg, double *alpha,
+template <int FORM, int KU>
+__global__ void __launch_bounds__(threads_of<FORM>(), 1) eval_kernel(DevObject ob, FitConfig cfg, const double *cg, double *alpha,
                                                         double *beta, double *chisq, double *area, double *scratch,
-                                                        int P)
+                                                        int P, int dsph_smem)
 {
-    extern __shared__ __align__(16) double smem[];
-    const SlotLayout L = make_layout(ob.ma, ob.mfit, ob.nfac, P);
-    Smem s = carve(smem, L);
-    for (int i = threadIdx.x; i < ob.ma; i += kThreads) s.cg[i] = cg[i];
+    using R = typename RealOf<FORM>::T;
+    constexpr int NT = threads_of<FORM>();
+    extern __shared__ __align__(16) char smem[];
+    const SlotLayout L = make_layout(FORM, ob.ma, ob.mfit, ob.nfac, ob.ncoef, P, dsph_smem);
+    Smem<FORM> s = carve<FORM>(smem, L);
+    if (s.dsph)
+        for (int e = threadIdx.x; e < ob.nfac * ob.ncoef; e += NT) s.dsph[e] = ob.dsph_f[e];
+    for (int i = threadIdx.x; i < ob.ma; i += NT) s.cg[i] = cg[i];
     __syncthreads();
-    evaluate<FORM>(ob, cfg, L, s, s.cg, s.alpha, s.beta, scratch);
+    evaluate<FORM, KU>(ob, cfg, L, s, s.cg, s.alpha, s.beta, reinterpret_cast<R *>(scratch));
     const int mf = ob.mfit;
-    for (int e = threadIdx.x; e < mf * mf; e += kThreads) alpha[e] = s.alpha[e];
-    for (int j = threadIdx.x; j < mf; j += kThreads) beta[j] = s.beta[j];
+    for (int e = threadIdx.x; e < mf * mf; e += NT) alpha[e] = s.alpha[e];
+    for (int j = threadIdx.x; j < mf; j += NT) beta[j] = s.beta[j];
     if (area)
-        for (int i = threadIdx.x; i < ob.nfac; i += kThreads) area[i] = s.area[i];
+        for (int i = threadIdx.x; i < ob.nfac; i += NT) area[i] = s.area[i];
     if (threadIdx.x == 0) *chisq = s.misc[M_CHISQ];
 }
 
@@ -850,44 +1177,98 @@ int launch_fits_noalloc(int form, const DevObject &ob, const FitConfig &cfg, Fit
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     e = cudaMemsetAsync(base, 0, sizeof(unsigned long long), st);
     if (e != cudaSuccess) return static_cast<int>(e);
-    fit_kernel<0><<<static_cast<int>(grid), kThreads, smem, st>>>(ob, cfg, w, P);
+    fit_kernel<PS_FORM_FP64, 1><<<static_cast<int>(grid), kThreads, smem, st>>>(ob, cfg, w, P, 0);
     *grid_used = static_cast<int>(grid);
     return static_cast<int>(cudaGetLastError());
 }
 
-int set_kernel_smem(int form, size_t smem)
+namespace {
+
+// Coefficient slots per lane of the mixed contraction: 1 for C <= 64, 2 up
+// to 128 (the largest Laplace series, L = 10, has 121 coefficients).
+inline int ku_of(int ncoef) { return ncoef <= 64 ? 1 : 2; }
+
+template <class Fn>
+cudaError_t for_mixed(int ncoef, Fn fn)
+{
+    return ku_of(ncoef) == 1 ? fn(std::integral_constant<int, 1>{}) : fn(std::integral_constant<int, 2>{});
+}
+
+}  // namespace
+
+int set_kernel_smem(int form, size_t smem, int ncoef)
 {
     cudaError_t e;
+    const int bytes = static_cast<int>(smem);
     if (form == PS_FORM_FP64) {
-        e = cudaFuncSetAttribute(fit_kernel<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
+        e = cudaFuncSetAttribute(fit_kernel<PS_FORM_FP64, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
         if (e == cudaSuccess)
-            e = cudaFuncSetAttribute(eval_kernel<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
+            e = cudaFuncSetAttribute(eval_kernel<PS_FORM_FP64, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    } else if (form == PS_FORM_MIXED) {
+        e = for_mixed(ncoef, [&](auto ku) {
+            constexpr int KU = decltype(ku)::value;
+            cudaError_t r = cudaFuncSetAttribute(fit_kernel<PS_FORM_MIXED, KU>,
+                                                 cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+            if (r == cudaSuccess)
+                r = cudaFuncSetAttribute(eval_kernel<PS_FORM_MIXED, KU>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         bytes);
+            return r;
+        });
     } else {
         return static_cast<int>(cudaErrorInvalidValue);
     }
     return static_cast<int>(e);
 }
 
-int occupancy_slots(int form, size_t smem, int *per_sm)
+int occupancy_slots(int form, size_t smem, int ncoef, int *per_sm)
 {
-    if (form != PS_FORM_FP64) return static_cast<int>(cudaErrorInvalidValue);
-    return static_cast<int>(cudaOccupancyMaxActiveBlocksPerMultiprocessor(per_sm, fit_kernel<0>, kThreads, smem));
+    if (form == PS_FORM_FP64)
+        return static_cast<int>(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+            per_sm, fit_kernel<PS_FORM_FP64, 1>, threads_of<PS_FORM_FP64>(), smem));
+    if (form == PS_FORM_MIXED)
+        return static_cast<int>(for_mixed(ncoef, [&](auto ku) {
+            constexpr int KU = decltype(ku)::value;
+            return cudaOccupancyMaxActiveBlocksPerMultiprocessor(per_sm, fit_kernel<PS_FORM_MIXED, KU>,
+                                                                 threads_of<PS_FORM_MIXED>(), smem);
+        }));
+    return static_cast<int>(cudaErrorInvalidValue);
 }
 
 int launch_fits(int form, const DevObject &ob, const FitConfig &cfg, const FitWork &w, int grid, int P, size_t smem,
-                void *stream)
+                int dsph_smem, void *stream)
 {
-    if (form != PS_FORM_FP64) return static_cast<int>(cudaErrorInvalidValue);
-    fit_kernel<0><<<grid, kThreads, smem, static_cast<cudaStream_t>(stream)>>>(ob, cfg, w, P);
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    if (form == PS_FORM_FP64) {
+        fit_kernel<PS_FORM_FP64, 1><<<grid, threads_of<PS_FORM_FP64>(), smem, st>>>(ob, cfg, w, P, 0);
+    } else if (form == PS_FORM_MIXED) {
+        for_mixed(ob.ncoef, [&](auto ku) {
+            constexpr int KU = decltype(ku)::value;
+            fit_kernel<PS_FORM_MIXED, KU><<<grid, threads_of<PS_FORM_MIXED>(), smem, st>>>(ob, cfg, w, P, dsph_smem);
+            return cudaSuccess;
+        });
+    } else {
+        return static_cast<int>(cudaErrorInvalidValue);
+    }
     return static_cast<int>(cudaGetLastError());
 }
 
 int launch_eval(int form, const DevObject &ob, const FitConfig &cfg, const double *cg, double *alpha, double *beta,
-                double *chisq, double *area, double *scratch, int P, size_t smem, void *stream)
+                double *chisq, double *area, double *scratch, int P, size_t smem, int dsph_smem, void *stream)
 {
-    if (form != PS_FORM_FP64) return static_cast<int>(cudaErrorInvalidValue);
-    eval_kernel<0><<<1, kThreads, smem, static_cast<cudaStream_t>(stream)>>>(ob, cfg, cg, alpha, beta, chisq, area,
-                                                                               scratch, P);
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    if (form == PS_FORM_FP64) {
+        eval_kernel<PS_FORM_FP64, 1><<<1, threads_of<PS_FORM_FP64>(), smem, st>>>(ob, cfg, cg, alpha, beta, chisq,
+                                                                                   area, scratch, P, 0);
+    } else if (form == PS_FORM_MIXED) {
+        for_mixed(ob.ncoef, [&](auto ku) {
+            constexpr int KU = decltype(ku)::value;
+            eval_kernel<PS_FORM_MIXED, KU><<<1, threads_of<PS_FORM_MIXED>(), smem, st>>>(
+                ob, cfg, cg, alpha, beta, chisq, area, scratch, P, dsph_smem);
+            return cudaSuccess;
+        });
+    } else {
+        return static_cast<int>(cudaErrorInvalidValue);
+    }
     return static_cast<int>(cudaGetLastError());
 }
 

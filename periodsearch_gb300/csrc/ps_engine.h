@@ -21,6 +21,9 @@ struct DevObject {
     const int *pair_m, *pair_n;          // [npairs]
     const double *tim, *bright, *sig, *weight;  // [ndata+3]; sig of the last 3 rows unused
     const double *eex, *eey, *eez, *e0x, *e0y, *e0z;  // [ndata]
+    const double *alpha_pt;              // [ndata] solar phase angle acos(ee . ee0), host libm
+    const double *sig2i;                 // [ndata] 1 / sig^2 of every point (mrqcof.c:112)
+    const float *nx_f, *ny_f, *nz_f, *darea_f;  // [nfac] FP32 copies for the mixed form
     const int *lc_start, *lc_npts, *lc_rel;  // [n_lc]
     const int *free_list;                // [mfit]
     const double *cg_first;              // [ncoef]
@@ -46,19 +49,14 @@ struct FitWork {
     ps_fit *out;                  // [nfits]
 };
 
-// Shared-memory plan of a fit slot; identical on host and device.
+// Shared-memory plan of a fit slot; identical on host and device.  Offsets
+// are in bytes; every block starts on a 16-byte boundary.  Blocks of type
+// "real" hold doubles in the FP64 form and floats in the mixed form.
 struct SlotLayout {
-    int ma, mfit, nfac, P;
-    size_t o_cg, o_atry, o_beta, o_da, o_alpha, o_covar, o_area, o_gv, o_W, o_J, o_ym, o_pt, o_red,
-        o_dave, o_col, o_misc, o_end;  // offsets in doubles
-    size_t o_ipiv;                     // offset in bytes of the int area
+    int form, ma, mfit, nfac, ncoef, P, wcols, dsph_smem;
+    size_t cg, atry, beta, da, alpha, covar, area, gv, areaR, gvR, W, J, pt, ym, red, dave, col, misc, ipiv, dsph;
     size_t bytes;
 };
-
-constexpr int kThreads = 256;
-constexpr int kPointStride = 32;   // doubles of per-point set-up
-constexpr int kRedStride = 8;      // doubles of per-point facet sums
-constexpr int kMisc = 32;
 
 #if defined(__CUDACC__)
 #define PSG_HD __host__ __device__
@@ -66,51 +64,72 @@ constexpr int kMisc = 32;
 #define PSG_HD
 #endif
 
-PSG_HD inline SlotLayout make_layout(int ma, int mfit, int nfac, int P)
+constexpr int kThreads = 256;   // threads of an FP64-form fit slot
+// Threads of a fit slot: the FP64 form is register-limited to 256; the mixed
+// form runs 512 (16 warps) to hide FP32/shared-memory latency.
+template <int FORM>
+PSG_HD constexpr int threads_of()
+{
+    return FORM == PS_FORM_MIXED ? 512 : 256;
+}
+constexpr int kPointStride = 32;   // reals of per-point set-up
+constexpr int kRedStride = 8;      // doubles of per-point facet sums
+constexpr int kMisc = 32;
+
+
+// dsph_smem: the mixed form keeps the FP32 basis Dsph[F][C] in shared memory
+// for the whole launch (it is read once per point tile by every warp).
+PSG_HD inline SlotLayout make_layout(int form, int ma, int mfit, int nfac, int ncoef, int P, int dsph_smem)
 {
     SlotLayout L{};
+    L.form = form;
     L.ma = ma;
     L.mfit = mfit;
     L.nfac = nfac;
+    L.ncoef = ncoef;
     L.P = P;
+    L.dsph_smem = dsph_smem;
+    L.wcols = ((nfac > mfit ? nfac : mfit) + 3) & ~3;
+    const size_t rs = form == PS_FORM_MIXED ? sizeof(float) : sizeof(double);
     size_t o = 0;
-    auto take = [&o](size_t n) {
+    auto take = [&o](size_t bytes) {
         size_t r = o;
-        o += (n + 1) & ~size_t(1);  // keep 16-byte alignment of every block
+        o += (bytes + 15) & ~size_t(15);
         return r;
     };
-    int wcols = nfac > mfit ? nfac : mfit;
-    L.o_cg = take(ma);
-    L.o_atry = take(ma);
-    L.o_beta = take(mfit);
-    L.o_da = take(mfit);
-    L.o_alpha = take(static_cast<size_t>(mfit) * mfit);
-    L.o_covar = take(static_cast<size_t>(mfit) * mfit);
-    L.o_area = take(nfac);
-    L.o_gv = take(nfac);
-    L.o_W = take(static_cast<size_t>(P) * wcols);
-    L.o_J = take(static_cast<size_t>(P) * ma);
-    L.o_ym = take(P);
-    L.o_pt = take(static_cast<size_t>(P) * kPointStride);
-    L.o_red = take(static_cast<size_t>(P) * kRedStride);
-    L.o_dave = take(ma);
-    L.o_col = take(mfit + 1);
-    L.o_misc = take(kMisc);
-    L.o_end = o;
-    L.o_ipiv = o * sizeof(double);
-    L.bytes = L.o_ipiv + sizeof(int) * static_cast<size_t>(mfit + 2 + 8);
-    L.bytes = (L.bytes + 15) & ~size_t(15);
+    const size_t d = sizeof(double);
+    L.cg = take(ma * d);
+    L.atry = take(ma * d);
+    L.beta = take(mfit * d);
+    L.da = take(mfit * d);
+    L.alpha = take(static_cast<size_t>(mfit) * mfit * d);
+    L.covar = take(static_cast<size_t>(mfit) * mfit * d);
+    L.area = take(nfac * d);
+    L.gv = take(nfac * d);
+    L.areaR = form == PS_FORM_MIXED ? take(nfac * rs) : L.area;
+    L.gvR = form == PS_FORM_MIXED ? take(nfac * rs) : L.gv;
+    L.W = take(static_cast<size_t>(P) * L.wcols * rs);
+    L.J = take(static_cast<size_t>(P) * ma * rs);
+    L.pt = take(static_cast<size_t>(P) * kPointStride * rs);
+    L.ym = take(P * d);
+    L.red = take(static_cast<size_t>(P) * kRedStride * d);
+    L.dave = take(ma * d);
+    L.col = take((mfit + 1) * d);
+    L.misc = take(kMisc * d);
+    L.ipiv = take(sizeof(int) * static_cast<size_t>(mfit + 2 + 16));
+    L.dsph = dsph_smem ? take(static_cast<size_t>(nfac) * ncoef * sizeof(float)) : 0;
+    L.bytes = o;
     return L;
 }
 
 // Launchers (ps_engine.cu).  All enqueue on `stream`; return cudaError_t as int.
 int launch_fits(int form, const DevObject &ob, const FitConfig &cfg, const FitWork &w, int grid,
-                int P, size_t smem, void *stream);
+                int P, size_t smem, int dsph_smem, void *stream);
 int launch_eval(int form, const DevObject &ob, const FitConfig &cfg, const double *cg, double *alpha,
                 double *beta, double *chisq, double *area, double *scratch, int P, size_t smem,
-                void *stream);
-int set_kernel_smem(int form, size_t smem);
-int occupancy_slots(int form, size_t smem, int *per_sm);
+                int dsph_smem, void *stream);
+int set_kernel_smem(int form, size_t smem, int ncoef);
+int occupancy_slots(int form, size_t smem, int ncoef, int *per_sm);
 int measure_fma_peaks(double *fp64_tflops, double *fp32_tflops, void *stream);
 
 // Allocation-free launch of the FP64 fit kernel: the work counter and the
