@@ -98,6 +98,8 @@ enum : int {
     M_AREA = 2,    // sum of facet areas of the current evaluation
     M_CHK = 3,     // 3 convexity residuals (sum Area*n) of the current evaluation
     M_CL = 7,      // exp(log cl)
+    M_TRIG = 8,    // cos/sin of the pole angles beta, lambda (4 doubles)
+    M_PIV = 12,    // pivot broadcast of the solvers (2 doubles + status)
     M_RED = 16     // 16 doubles of block-reduction scratch
 };
 
@@ -225,15 +227,38 @@ __device__ void accumulate_tile(const DevObject &ob, Smem<FORM> &s, double *M, d
     const int tid = threadIdx.x;
     const int ma = ob.ma, mf = ob.mfit;
     R *wt = s.W;  // [np][mf], reuses the facet-weight tile
-    for (int e = tid; e < np * mf; e += NT) {
-        const int p = e / mf, j = e - p * mf;
-        const int q = q0pt + p;
-        const double sig2i = conv ? 1 / (conv_sig * conv_sig) : ob.sig2i[q];
-        const double wg = ob.weight[q];
-        if constexpr (FORM == PS_FORM_FP64)
+    if constexpr (FORM == PS_FORM_FP64) {
+        for (int e = tid; e < np * mf; e += NT) {
+            const int p = e / mf, j = e - p * mf;
+            const int q = q0pt + p;
+            const double sig2i = conv ? 1 / (conv_sig * conv_sig) : ob.sig2i[q];
+            const double wg = ob.weight[q];
             wt[p * mf + j] = s.J[p * ma + ob.free_list[j]] * sig2i * wg;
-        else
-            wt[p * mf + j] = s.J[p * ma + ob.free_list[j]] * static_cast<float>(sig2i * wg);
+        }
+    } else {
+        // per point: FP32 weight sig2i*w and residual; chi^2 of the tile
+        // summed over one warp in FP64
+        float *dyv = reinterpret_cast<float *>(s.pt);
+        float *wtp = dyv + 32;
+        if (tid < 32) {
+            double c2 = 0;
+            if (tid < np) {
+                const int q = q0pt + tid;
+                const double sig2i = conv ? 1 / (conv_sig * conv_sig) : ob.sig2i[q];
+                const double wg = ob.weight[q];
+                const double dy = (conv ? 0.0 : ob.bright[q]) - s.ym[tid];
+                dyv[tid] = static_cast<float>(dy);
+                wtp[tid] = static_cast<float>(sig2i * wg);
+                c2 = dy * dy * sig2i * wg;
+            }
+            c2 = warp_sum(c2);
+            if (tid == 0) s.misc[M_CHISQ] += c2;
+        }
+        __syncthreads();
+        for (int e = tid; e < np * mf; e += NT) {
+            const int p = e / mf, j = e - p * mf;
+            wt[p * mf + j] = s.J[p * ma + ob.free_list[j]] * wtp[p];
+        }
     }
     __syncthreads();
     const int ntri = mf * (mf + 1) / 2;
@@ -255,10 +280,7 @@ __device__ void accumulate_tile(const DevObject &ob, Smem<FORM> &s, double *M, d
             bv[j] = acc;
         }
     } else {
-        // residuals of the tile in FP32 (the model value is FP32-accurate)
-        float *dyv = reinterpret_cast<float *>(s.pt);
-        if (tid < np) dyv[tid] = static_cast<float>((conv ? 0.0 : ob.bright[q0pt + tid]) - s.ym[tid]);
-        __syncthreads();
+        const float *dyv = reinterpret_cast<const float *>(s.pt);
 #pragma unroll
         for (int u = 0; u < kAccPerThread; u++) {
             const int e = tid + u * NT;
@@ -277,7 +299,7 @@ __device__ void accumulate_tile(const DevObject &ob, Smem<FORM> &s, double *M, d
             accB = acc;
         }
     }
-    if (tid == NT - 1) {
+    if (FORM == PS_FORM_FP64 && tid == NT - 1) {
         double c2 = s.misc[M_CHISQ];
         for (int p = 0; p < np; p++) {
             const int q = q0pt + p;
@@ -427,13 +449,18 @@ __device__ void evaluate(const DevObject &ob, const FitConfig &cfg, const SlotLa
         s.misc[M_AREA] = tot;
         s.misc[M_CHISQ] = 0;
         s.misc[M_CL] = exp(a[ma - 2]);
+        s.misc[M_TRIG] = cos(a[C]);
+        s.misc[M_TRIG + 1] = sin(a[C]);
+        s.misc[M_TRIG + 2] = cos(a[C + 1]);
+        s.misc[M_TRIG + 3] = sin(a[C + 1]);
     }
     for (int e = tid; e < mf * mf; e += NT) M[e] = 0;
     for (int j = tid; j < mf; j += NT) bv[j] = 0;
 
-    // blmatrix.c:9-46 in FP64, then in the facet-stage type.
-    const double bet = a[C], lam = a[C + 1];
-    const double cb = cos(bet), sb = sin(bet), clm = cos(lam), slm = sin(lam);
+    // blmatrix.c:9-46 in FP64 (angles' cos/sin from thread 0), then in the
+    // facet-stage type.
+    __syncthreads();
+    const double cb = s.misc[M_TRIG], sb = s.misc[M_TRIG + 1], clm = s.misc[M_TRIG + 2], slm = s.misc[M_TRIG + 3];
     const R B[9] = {R(cb * clm), R(cb * slm), R(-sb), R(-slm), R(clm), R(0), R(sb * clm), R(sb * slm), R(cb)};
     const R DB0[9] = {R(-sb * clm), R(-sb * slm), R(-cb), R(0), R(0), R(0), R(cb * clm), R(cb * slm), R(-sb)};
     const R DB1[9] = {R(-cb * slm), R(cb * clm), R(0), R(-clm), R(-slm), R(0), R(-sb * slm), R(sb * clm), R(0)};
@@ -810,8 +837,9 @@ __device__ int gauss_jordan(double *A, double *b, int n, double *col, int *ipiv,
         }
         const double piv = A[icol * n + icol];
         if (piv == 0.0) return 2;
-        const double pivinv = 1.0 / piv;
+        if (tid == 0) red[0] = 1.0 / piv;
         __syncthreads();
+        const double pivinv = red[0];
         // scale the pivot row over the columns not yet pivoted
         for (int l = tid; l < n; l += NT)
             if (ipiv[l] == 0) A[icol * n + l] *= pivinv;
@@ -836,17 +864,21 @@ template <int NT>
 __device__ int cholesky_solve(double *A, double *b, int n, double *col)
 {
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    (void)col;
     __syncthreads();
     for (int j = 0; j < n; j++) {
-        const double d = A[j * n + j];
-        if (!(d > 0.0)) return 2;
-        const double ljj = sqrt(d);
-        const double inv = 1.0 / ljj;
+        if (tid == 0) {
+            const double d = A[j * n + j];
+            const double ljj = sqrt(d);
+            col[0] = d > 0.0 ? 1.0 : 0.0;
+            col[1] = ljj;
+            col[2] = 1.0 / ljj;
+        }
         __syncthreads();
+        if (col[0] == 0.0) return 2;
+        const double ljj = col[1], inv = col[2];
         for (int i = j + 1 + tid; i < n; i += NT) A[i * n + j] *= inv;
-        if (tid == 0) A[j * n + j] = ljj;
         __syncthreads();
+        if (tid == 0) A[j * n + j] = ljj;
         const int m = n - j - 1;
         const int ntri = m * (m + 1) / 2;
         for (int e = tid; e < ntri; e += NT) {
