@@ -132,6 +132,9 @@ typedef struct ps_fit {
     double chisq;          /* final chi^2 (with the convexity rows) */
     int32_t niter;         /* LM iterations run */
     int32_t err_code;      /* last gauss_errc code: 0, 1 or 2 */
+    double pred_dev;       /* learned prediction of the final rms (screened fits), else 0 */
+    int32_t screened;      /* 1: stopped after the screening iterations */
+    int32_t reserved;
 } ps_fit;
 
 /* Sizes of a prepared object. */
@@ -221,6 +224,75 @@ void ps_destroy(ps_ctx *ctx);
 /* Measured FMA throughput of a device (TFLOP/s, 2 flops per FMA) for FP64
  * and FP32 SIMT: the compute ceilings that bound the fit kernels. */
 ps_status ps_device_fma_peaks(int32_t device, double *fp64_tflops, double *fp32_tflops);
+
+/* ---- learned early stop ----
+ * A 10-64-64-1 GELU perceptron (FP32) predicts, from the first 4 LM
+ * iterations of a fit (log ratios of the accepted chi^2 to the starting
+ * chi^2, log10 lambda after each iteration, log Ndata, log trial period [h]),
+ * log(final rms / rms after 4 iterations).  Weights: PS_MLP_FLOATS floats
+ * (input mean/std, W1[64][10], b1, W2[64][64], b2, W3[64], b3, target
+ * mean/std).  No counterpart in the reference. */
+#define PS_MLP_FEATURES 10
+#define PS_MLP_FLOATS 4951
+#define PS_TRAJ_FLOATS 16   /* features[10], rms after 4 iterations, final rms, iterations, 3 spare */
+
+typedef struct ps_learned_stats {
+    int64_t fits_total;        /* fits of the scan (periods x 10 poles) */
+    int64_t fits_screened_out; /* never run beyond the screening iterations */
+    int64_t fits_completed;    /* run in full in the mixed form (stages 2 and 3) */
+    int64_t fits_refit;        /* refitted in full in the FP64 form (stage 4) */
+    int64_t evals;             /* model evaluations of all stages */
+    double screen_ms, complete_ms, refit_ms;   /* kernel time of the stages */
+    int64_t best_index;        /* period index of the best row */
+    int64_t region_periods;    /* periods completed in all poles at stage 3 */
+} ps_learned_stats;
+
+/* Full fits of periods n_lo..n_hi (10 poles each) in the context's form,
+ * recording for every fit PS_TRAJ_FLOATS floats into traj (host). */
+ps_status ps_trajectories(ps_ctx *ctx, double conw_r, int64_t n_lo, int64_t n_hi, float *traj);
+/* Trains the predictor on n samples (features x[n][10], targets y[n]) with
+ * the engine's own CUDA kernels (mini-batch Adam on mean squared error).
+ * weights: in = initial parameters with the standardisation constants set,
+ * out = trained.  loss_history[epochs] may be NULL. */
+ps_status ps_mlp_train(int32_t device, float *weights, const float *x, const float *y, int64_t n, int32_t epochs,
+                       int32_t batch, float lr, uint64_t seed, float *loss_history);
+ps_status ps_mlp_predict(int32_t device, const float *weights, const float *x, int64_t n, float *y);
+/* Full-batch loss and gradient (for gradient checks); grad[PS_MLP_FLOATS]
+ * holds d loss / d W1..b3 at their offsets, zero elsewhere. */
+ps_status ps_mlp_grad(int32_t device, const float *weights, const float *x, const float *y, int64_t n, float *loss,
+                      float *grad);
+/* The screening pass alone: every fit of periods n_lo..n_hi runs 4 LM
+ * iterations in the mixed form; out[fit] holds the rms after them (dev), the
+ * predicted final rms (pred_dev) and screened = 1.  Fit f is period
+ * n_lo + f / 10, pole f % 10 + 1. */
+ps_status ps_screen(ps_ctx *ctx, double conw_r, int64_t n_lo, int64_t n_hi, const float *weights, ps_fit *out);
+/* Options of the learned scan (ps_scan_learned). */
+typedef struct ps_learned_opts {
+    int32_t top_k;           /* complete the top_k best-predicted poles of every period (>= 1) */
+    double margin;           /* and every fit predicted within (1 + margin) of the scan's best prediction;
+                                < 0 disables (the default: in flat scans it would complete everything) */
+    double region_rel;       /* complete all poles of the periods whose row lies within region_rel
+                                (relative) of the best row, and of region_halfwidth periods around it */
+    int32_t region_halfwidth;
+    double refit_rel;        /* refit in full with the FP64 form the periods within refit_rel of the
+                                best row after the region pass, */
+    int32_t refit_halfwidth; /* and refit_halfwidth periods on each side of the best */
+} ps_learned_opts;
+
+/* Period scan with the learned early stop, a cascade in which only the fits
+ * that can matter run in full: (1) every fit runs 4 LM iterations in the
+ * mixed form and the predictor estimates its final rms (ps_screen); (2) the
+ * top_k best-predicted poles of every period (and fits within `margin` of
+ * the best prediction) run in full in the mixed form, giving an upper bound
+ * of every period's row; (3) every pole of the periods near the best row
+ * runs in full in the mixed form; (4) the periods nearest the best row are
+ * refitted in full by the plain FP64 form, so that the reported minimum
+ * carries FP64 values.  Rows of periods that stopped at stage (2) carry the
+ * best completed pole.  opts NULL selects the defaults (top_k 1, margin off,
+ * region 3 % and +-2 periods, FP64 refit 0.5 % and +-2 periods).  stats may
+ * be NULL. */
+ps_status ps_scan_learned(ps_ctx *ctx, double conw_r, int64_t n_lo, int64_t n_hi, const float *weights,
+                          const ps_learned_opts *opts, ps_row *out, ps_learned_stats *stats);
 
 /* ---- formats ---- */
 /* Writes one row in the reference's format "%.8f  %.6f  %.6f %4.1f %4.0f %4.0f\n"

@@ -30,7 +30,8 @@ __all__ = ["Engine", "InputData", "read_input", "run_files", "format_row", "shap
 
 ROW_DTYPE = np.dtype([(n, "f8") for n in ("period_h", "rms", "chi2", "dark_or_conw", "lambda_deg", "beta_deg")])
 FIT_DTYPE = np.dtype([(n, "f8") for n in ("dev", "dark", "totarea", "period_h", "lambda_deg", "beta_deg", "chisq")]
-                     + [("niter", "i4"), ("err_code", "i4")])
+                     + [("niter", "i4"), ("err_code", "i4"), ("pred_dev", "f8"), ("screened", "i4"),
+                        ("reserved", "i4")])
 HEADER_FIELDS = [f for f, _ in _abi.Header._fields_]
 
 
@@ -198,6 +199,43 @@ class Engine:
         st = self._L.ps_eval(self._ctx, conw_r, dp(cg), dp(alpha), dp(beta), C.byref(c2), dp(area))
         _abi.check(st, "ps_eval", self._ctx)
         return alpha, beta, c2.value, area
+
+    def trajectories(self, conw_r: float, n_lo: int, n_hi: int) -> np.ndarray:
+        from . import learned
+
+        return learned.trajectories(self, conw_r, n_lo, n_hi)
+
+    def screen(self, conw_r: float, n_lo: int, n_hi: int, weights) -> np.ndarray:
+        """The screening pass alone (ps_screen): per fit the rms after four
+        iterations and the predicted final rms."""
+        w = np.ascontiguousarray(weights, np.float32)
+        out = np.zeros((n_hi - n_lo + 1) * N_POLES, FIT_DTYPE)
+        r = self._L.ps_screen(self._ctx, conw_r, n_lo, n_hi, w.ctypes.data_as(C.POINTER(C.c_float)),
+                              out.ctypes.data_as(C.POINTER(_abi.Fit)))
+        _abi.check(r, "ps_screen", self._ctx)
+        return out
+
+    def scan_learned(self, conw_r: float, n_lo: int, n_hi: int, weights=None, **opts):
+        """Period scan with the learned early stop (ps_scan_learned); returns
+        the rows and the stage statistics.  Options (ps_learned_opts): top_k,
+        margin, region_rel, region_halfwidth, refit_rel, refit_halfwidth.
+        Without weights the committed predictor is used."""
+        from . import learned
+
+        if weights is None:
+            weights, _ = learned.load_default()
+            if weights is None:
+                raise EngineError(_abi.PS_ERR_ARG, "scan_learned", "no trained predictor available")
+        o = _abi.LearnedOpts(1, -1.0, 0.03, 2, 0.005, 2)
+        for k, v in opts.items():
+            setattr(o, k, v)
+        w = np.ascontiguousarray(weights, np.float32)
+        out = np.zeros(n_hi - n_lo + 1, ROW_DTYPE)
+        st = _abi.LearnedStats()
+        r = self._L.ps_scan_learned(self._ctx, conw_r, n_lo, n_hi, w.ctypes.data_as(C.POINTER(C.c_float)),
+                                    C.byref(o), out.ctypes.data_as(C.POINTER(_abi.Row)), C.byref(st))
+        _abi.check(r, "ps_scan_learned", self._ctx)
+        return out, {k: getattr(st, k) for k, _ in _abi.LearnedStats._fields_}
 
     def timing(self) -> dict:
         t = _abi.Timing()

@@ -57,7 +57,8 @@ class Row(C.Structure):
 
 class Fit(C.Structure):
     _fields_ = [(n, C.c_double) for n in ("dev", "dark", "totarea", "period_h", "lambda_deg", "beta_deg", "chisq")] + [
-        ("niter", C.c_int32), ("err_code", C.c_int32)]
+        ("niter", C.c_int32), ("err_code", C.c_int32), ("pred_dev", C.c_double), ("screened", C.c_int32),
+        ("reserved", C.c_int32)]
 
 
 class Info(C.Structure):
@@ -65,6 +66,23 @@ class Info(C.Structure):
                 ("mfit", C.c_int32), ("nfac", C.c_int32), ("n_max", C.c_int64), ("escl", C.c_double),
                 ("conw_r0", C.c_double), ("freq_start", C.c_double), ("freq_step", C.c_double),
                 ("sm_count", C.c_int32), ("slots", C.c_int32), ("h2d_bytes", C.c_int64)]
+
+
+class LearnedStats(C.Structure):
+    _fields_ = [("fits_total", C.c_int64), ("fits_screened_out", C.c_int64), ("fits_completed", C.c_int64),
+                ("fits_refit", C.c_int64), ("evals", C.c_int64), ("screen_ms", C.c_double),
+                ("complete_ms", C.c_double), ("refit_ms", C.c_double), ("best_index", C.c_int64),
+                ("region_periods", C.c_int64)]
+
+
+class LearnedOpts(C.Structure):
+    _fields_ = [("top_k", C.c_int32), ("margin", C.c_double), ("region_rel", C.c_double),
+                ("region_halfwidth", C.c_int32), ("refit_rel", C.c_double), ("refit_halfwidth", C.c_int32)]
+
+
+MLP_FEATURES = 10
+MLP_FLOATS = 4951
+TRAJ_FLOATS = 16
 
 
 class Timing(C.Structure):
@@ -92,6 +110,16 @@ SIGNATURES = {
                                        C.c_void_p]),
     "ps_eval": (C.c_int, [_CTX, C.c_double, _D, _D, _D, _D, _D]),
     "ps_last_timing": (C.c_int, [_CTX, C.POINTER(Timing)]),
+    "ps_trajectories": (C.c_int, [_CTX, C.c_double, C.c_int64, C.c_int64, C.POINTER(C.c_float)]),
+    "ps_mlp_train": (C.c_int, [C.c_int32, C.POINTER(C.c_float), C.POINTER(C.c_float), C.POINTER(C.c_float),
+                               C.c_int64, C.c_int32, C.c_int32, C.c_float, C.c_uint64, C.POINTER(C.c_float)]),
+    "ps_mlp_predict": (C.c_int, [C.c_int32, C.POINTER(C.c_float), C.POINTER(C.c_float), C.c_int64,
+                                 C.POINTER(C.c_float)]),
+    "ps_mlp_grad": (C.c_int, [C.c_int32, C.POINTER(C.c_float), C.POINTER(C.c_float), C.POINTER(C.c_float),
+                              C.c_int64, C.POINTER(C.c_float), C.POINTER(C.c_float)]),
+    "ps_screen": (C.c_int, [_CTX, C.c_double, C.c_int64, C.c_int64, C.POINTER(C.c_float), C.POINTER(Fit)]),
+    "ps_scan_learned": (C.c_int, [_CTX, C.c_double, C.c_int64, C.c_int64, C.POINTER(C.c_float),
+                                  C.POINTER(LearnedOpts), C.POINTER(Row), C.POINTER(LearnedStats)]),
     "ps_last_error": (C.c_char_p, [_CTX]),
     "ps_destroy": (None, [_CTX]),
     "ps_device_fma_peaks": (C.c_int, [C.c_int32, _D, _D]),

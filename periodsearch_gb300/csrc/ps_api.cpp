@@ -8,6 +8,8 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <climits>
+#include <cstdlib>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -22,9 +24,17 @@ struct ps_input {
     psg::ParsedInput data;
 };
 
+// Launch plan of one arithmetic form: point-tile size, shared memory, slots.
+struct FormPlan {
+    bool ready = false;
+    int P = 16, dsph_smem = 0, slots = 0;
+    size_t smem = 0;
+};
+
 struct ps_ctx {
     psg::HostObject obj;
     ps_options opt{};
+    FormPlan plan[2];
     cudaStream_t stream = nullptr;
     cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};
     char *d_tables = nullptr;          // one allocation with every table
@@ -115,21 +125,76 @@ ps_status ensure_out(ps_ctx *c, size_t nfits)
     return PS_OK;
 }
 
-// Launches the fits described by w (queue and outputs filled in here) and
-// copies the results back into c->h_fits.
-ps_status run_fits(ps_ctx *c, double conw_r, psg::FitWork w)
+// Shared-memory plan, kernel attributes and resident slots of one form.
+ps_status make_plan(ps_ctx *c, int form)
 {
+    FormPlan &pl = c->plan[form];
+    if (pl.ready) return PS_OK;
+    const psg::HostObject &o = c->obj;
+    const int F = o.shape.nfac;
+    cudaDeviceProp prop;
+    PSG_CUDA(c, cudaGetDeviceProperties(&prop, c->opt.device));
+    size_t smem_max = static_cast<size_t>(prop.sharedMemPerBlockOptin);
+    // Mixed form: 32-point tiles (the register tile of the contraction) and
+    // the FP32 basis in shared memory when it fits; FP64 form: 16-point tiles.
+    const bool mixed = form == PS_FORM_MIXED;
+    int P = mixed ? 32 : 16, dsph_smem = mixed ? 1 : 0;
+    psg::SlotLayout L = psg::make_layout(form, o.ma, o.mfit, F, o.ncoef, P, dsph_smem);
+    if (L.bytes > smem_max && dsph_smem) {
+        dsph_smem = 0;
+        L = psg::make_layout(form, o.ma, o.mfit, F, o.ncoef, P, dsph_smem);
+    }
+    while (L.bytes > smem_max && P > 2) {
+        P /= 2;
+        L = psg::make_layout(form, o.ma, o.mfit, F, o.ncoef, P, dsph_smem);
+    }
+    if (L.bytes > smem_max) {
+        c->err = "shared-memory plan of a fit slot exceeds the device limit";
+        return PS_ERR_LIMIT;
+    }
+    int e = psg::set_kernel_smem(form, L.bytes, o.ncoef);
+    if (e != 0) return cuda_fail(c, static_cast<cudaError_t>(e), "cudaFuncSetAttribute");
+    int per_sm = 0;
+    e = psg::occupancy_slots(form, L.bytes, o.ncoef, &per_sm);
+    if (e != 0) return cuda_fail(c, static_cast<cudaError_t>(e), "occupancy");
+    if (per_sm < 1) {
+        c->err = "fit slot does not fit on an SM";
+        return PS_ERR_LIMIT;
+    }
+    if (c->opt.ctas_per_sm > 0) per_sm = std::min(per_sm, c->opt.ctas_per_sm);
+    pl.P = P;
+    pl.dsph_smem = dsph_smem;
+    pl.smem = L.bytes;
+    pl.slots = per_sm * c->sm_count;
+    pl.ready = true;
+    return PS_OK;
+}
+
+// Launches the fits described by w in the given form (queue and outputs
+// filled in here) and copies the results back into c->h_fits.
+ps_status run_fits(ps_ctx *c, double conw_r, psg::FitWork w, int form)
+{
+    ps_status st = make_plan(c, form);
+    if (st != PS_OK) return st;
+    const FormPlan &pl = c->plan[form];
+    if (pl.slots > c->slots) {
+        // a second form with more slots than the scratch was sized for
+        cudaFree(c->d_scratch);
+        c->d_scratch = nullptr;
+        PSG_CUDA(c, cudaMalloc(&c->d_scratch, c->scratch_stride * pl.slots * sizeof(double)));
+        c->slots = pl.slots;
+    }
     psg::FitConfig cfg = make_config(c, conw_r);
-    ps_status st = ensure_out(c, static_cast<size_t>(w.nfits));
+    st = ensure_out(c, static_cast<size_t>(w.nfits));
     if (st != PS_OK) return st;
     w.queue = c->d_queue;
     w.scratch = c->d_scratch;
     w.scratch_stride = c->scratch_stride;
     w.out = c->d_out;
-    int grid = static_cast<int>(std::min<int64_t>(c->slots, std::max<int64_t>(w.nfits, 1)));
+    int grid = static_cast<int>(std::min<int64_t>(pl.slots, std::max<int64_t>(w.nfits, 1)));
     PSG_CUDA(c, cudaMemsetAsync(c->d_queue, 0, sizeof(unsigned long long), c->stream));
     PSG_CUDA(c, cudaEventRecord(c->ev[0], c->stream));
-    int e = psg::launch_fits(c->opt.form, c->dob, cfg, w, grid, c->P, c->smem, c->dsph_smem, c->stream);
+    int e = psg::launch_fits(form, c->dob, cfg, w, grid, pl.P, pl.smem, pl.dsph_smem, c->stream);
     if (e != 0) return cuda_fail(c, static_cast<cudaError_t>(e), "fit kernel launch");
     PSG_CUDA(c, cudaEventRecord(c->ev[1], c->stream));
     c->h_fits.resize(static_cast<size_t>(w.nfits));
@@ -155,7 +220,7 @@ ps_status scan_rows(ps_ctx *c, double conw_r, int64_t n_lo, int64_t n_hi, ps_row
     psg::FitWork w{};
     w.n_lo = n_lo;
     w.nfits = (n_hi - n_lo + 1) * PS_N_POLES;
-    ps_status st = run_fits(c, conw_r, w);
+    ps_status st = run_fits(c, conw_r, w, c->opt.form);
     if (st != PS_OK) return st;
     for (int64_t n = n_lo; n <= n_hi; n++) {
         ps_row r = psg::best_of_poles(&c->h_fits[static_cast<size_t>(n - n_lo) * PS_N_POLES], c->obj.ndata);
@@ -338,40 +403,15 @@ ps_status ps_prepare(const ps_problem *prob, const ps_options *opt, ps_ctx **out
     d.darea_f = reinterpret_cast<const float *>(b + o_daf);
     d.sig2i = reinterpret_cast<const double *>(b + o_s2i);
 
-    // Slot plan: the largest point tile whose shared-memory footprint fits.
-    size_t smem_max = static_cast<size_t>(prop.sharedMemPerBlockOptin);
-    // Mixed form: 32-point tiles (the register tile of the contraction) and
-    // the FP32 basis in shared memory when it fits; FP64 form: 16-point tiles.
-    const bool mixed = c->opt.form == PS_FORM_MIXED;
-    int P = mixed ? 32 : 16, dsph_smem = mixed ? 1 : 0;
-    psg::SlotLayout L = psg::make_layout(c->opt.form, o.ma, o.mfit, F, o.ncoef, P, dsph_smem);
-    if (L.bytes > smem_max && dsph_smem) {
-        dsph_smem = 0;
-        L = psg::make_layout(c->opt.form, o.ma, o.mfit, F, o.ncoef, P, dsph_smem);
-    }
-    while (L.bytes > smem_max && P > 2) {
-        P /= 2;
-        L = psg::make_layout(c->opt.form, o.ma, o.mfit, F, o.ncoef, P, dsph_smem);
-    }
-    if (L.bytes > smem_max) {
-        c->err = "shared-memory plan of a fit slot exceeds the device limit";
+    ps_status pst = make_plan(cp, c->opt.form);
+    if (pst != PS_OK) {
         std::fprintf(stderr, "ps_prepare: %s\n", c->err.c_str());
-        return PS_ERR_LIMIT;
+        return pst;
     }
-    c->P = P;
-    c->dsph_smem = dsph_smem;
-    c->smem = L.bytes;
-    int e = psg::set_kernel_smem(c->opt.form, c->smem, o.ncoef);
-    if (e != 0) return cuda_fail(cp, static_cast<cudaError_t>(e), "cudaFuncSetAttribute");
-    int per_sm = 0;
-    e = psg::occupancy_slots(c->opt.form, c->smem, o.ncoef, &per_sm);
-    if (e != 0) return cuda_fail(cp, static_cast<cudaError_t>(e), "occupancy");
-    if (per_sm < 1) {
-        c->err = "fit slot does not fit on an SM";
-        return PS_ERR_LIMIT;
-    }
-    if (c->opt.ctas_per_sm > 0) per_sm = std::min(per_sm, c->opt.ctas_per_sm);
-    c->slots = per_sm * c->sm_count;
+    c->P = c->plan[c->opt.form].P;
+    c->dsph_smem = c->plan[c->opt.form].dsph_smem;
+    c->smem = c->plan[c->opt.form].smem;
+    c->slots = c->plan[c->opt.form].slots;
     c->scratch_stride = static_cast<size_t>(std::max(o.max_rel_points, 1)) * (o.ma + 1);
     c->scratch_stride = (c->scratch_stride + 31) & ~size_t(31);
     PSG_CUDA(cp, cudaMalloc(&c->d_scratch, c->scratch_stride * c->slots * sizeof(double)));
@@ -473,7 +513,7 @@ ps_status ps_fit_batch(ps_ctx *c, double conw_r, int64_t n_fits, const int64_t *
     w.nfits = n_fits;
     w.period_index = c->d_pidx;
     w.pole = c->d_pole;
-    ps_status st = run_fits(c, conw_r, w);
+    ps_status st = run_fits(c, conw_r, w, c->opt.form);
     if (st != PS_OK) return st;
     std::memcpy(out, c->h_fits.data(), n_fits * sizeof(ps_fit));
     return PS_OK;
@@ -535,6 +575,228 @@ ps_status ps_eval(ps_ctx *c, double conw_r, const double *cg, double *alpha, dou
     PSG_CUDA(c, cudaMemcpyAsync(chisq, d_c2, sizeof(double), cudaMemcpyDeviceToHost, c->stream));
     if (area) PSG_CUDA(c, cudaMemcpyAsync(area, d_ar, F * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
     PSG_CUDA(c, cudaStreamSynchronize(c->stream));
+    return PS_OK;
+}
+
+ps_status ps_trajectories(ps_ctx *c, double conw_r, int64_t n_lo, int64_t n_hi, float *traj)
+{
+    if (!c || !traj || n_lo < 1 || n_hi < n_lo || !(conw_r > 0)) return PS_ERR_ARG;
+    PSG_CUDA(c, cudaSetDevice(c->opt.device));
+    const int64_t nfits = (n_hi - n_lo + 1) * PS_N_POLES;
+    float *d_traj = nullptr;
+    PSG_CUDA(c, cudaMalloc(&d_traj, nfits * psg::kTrajFloats * sizeof(float)));
+    PSG_CUDA(c, cudaMemsetAsync(d_traj, 0, nfits * psg::kTrajFloats * sizeof(float), c->stream));
+    psg::FitWork w{};
+    w.n_lo = n_lo;
+    w.nfits = nfits;
+    w.traj = d_traj;
+    ps_status st = run_fits(c, conw_r, w, c->opt.form);
+    if (st == PS_OK) {
+        cudaError_t e = cudaMemcpy(traj, d_traj, nfits * psg::kTrajFloats * sizeof(float), cudaMemcpyDeviceToHost);
+        if (e != cudaSuccess) st = cuda_fail(c, e, "trajectory copy");
+    }
+    cudaFree(d_traj);
+    return st;
+}
+
+ps_status ps_mlp_train(int32_t device, float *weights, const float *x, const float *y, int64_t n, int32_t epochs,
+                       int32_t batch, float lr, uint64_t seed, float *loss_history)
+{
+    if (!weights || !x || !y || n < 1 || epochs < 1 || batch < 1 || n > INT32_MAX) return PS_ERR_ARG;
+    if (cudaSetDevice(device) != cudaSuccess) return PS_ERR_NO_DEVICE;
+    int e = psg::mlp_train(weights, x, y, static_cast<int>(n), epochs, batch, lr, seed, loss_history);
+    return e == 0 ? PS_OK : PS_ERR_CUDA;
+}
+
+ps_status ps_mlp_predict(int32_t device, const float *weights, const float *x, int64_t n, float *y)
+{
+    if (!weights || !x || !y || n < 1 || n > INT32_MAX) return PS_ERR_ARG;
+    if (cudaSetDevice(device) != cudaSuccess) return PS_ERR_NO_DEVICE;
+    int e = psg::mlp_predict(weights, x, static_cast<int>(n), y);
+    return e == 0 ? PS_OK : PS_ERR_CUDA;
+}
+
+ps_status ps_mlp_grad(int32_t device, const float *weights, const float *x, const float *y, int64_t n, float *loss,
+                      float *grad)
+{
+    if (!weights || !x || !y || !loss || !grad || n < 1 || n > INT32_MAX) return PS_ERR_ARG;
+    if (cudaSetDevice(device) != cudaSuccess) return PS_ERR_NO_DEVICE;
+    int e = psg::mlp_grad(weights, x, y, static_cast<int>(n), loss, grad);
+    return e == 0 ? PS_OK : PS_ERR_CUDA;
+}
+
+namespace {
+
+// Screening launch: kScreenIters iterations of every fit of n_lo..n_hi in the
+// mixed form with the in-kernel predictor; results in c->h_fits.
+ps_status screen_fits(ps_ctx *c, double conw_r, int64_t n_lo, int64_t n_hi, const float *weights)
+{
+    float *d_w = nullptr;
+    PSG_CUDA(c, cudaMalloc(&d_w, psg::kMlpFloats * sizeof(float)));
+    cudaError_t ce = cudaMemcpy(d_w, weights, psg::kMlpFloats * sizeof(float), cudaMemcpyHostToDevice);
+    if (ce != cudaSuccess) {
+        cudaFree(d_w);
+        return cuda_fail(c, ce, "predictor weights copy");
+    }
+    psg::FitWork w{};
+    w.n_lo = n_lo;
+    w.nfits = (n_hi - n_lo + 1) * PS_N_POLES;
+    w.iter_limit = psg::kScreenIters;
+    w.mlp = d_w;
+    ps_status st = run_fits(c, conw_r, w, PS_FORM_MIXED);
+    cudaFree(d_w);
+    return st;
+}
+
+}  // namespace
+
+ps_status ps_screen(ps_ctx *c, double conw_r, int64_t n_lo, int64_t n_hi, const float *weights, ps_fit *out)
+{
+    if (!c || !weights || !out || n_lo < 1 || n_hi < n_lo || !(conw_r > 0)) return PS_ERR_ARG;
+    PSG_CUDA(c, cudaSetDevice(c->opt.device));
+    ps_status st = screen_fits(c, conw_r, n_lo, n_hi, weights);
+    if (st != PS_OK) return st;
+    std::memcpy(out, c->h_fits.data(), c->h_fits.size() * sizeof(ps_fit));
+    return PS_OK;
+}
+
+ps_status ps_scan_learned(ps_ctx *c, double conw_r, int64_t n_lo, int64_t n_hi, const float *weights,
+                          const ps_learned_opts *opts, ps_row *out, ps_learned_stats *stats)
+{
+    ps_learned_opts o{1, -1.0, 0.03, 2, 0.005, 2};
+    if (opts) o = *opts;
+    if (!c || !weights || !out || n_lo < 1 || n_hi < n_lo || !(conw_r > 0) || o.top_k < 1 ||
+        !(o.region_rel >= 0) || !(o.refit_rel >= 0) || o.region_halfwidth < 0 || o.refit_halfwidth < 0)
+        return PS_ERR_ARG;
+    PSG_CUDA(c, cudaSetDevice(c->opt.device));
+    const int64_t nper = n_hi - n_lo + 1, nfits = nper * PS_N_POLES;
+    ps_learned_stats stt{};
+    stt.fits_total = nfits;
+    // (1) screening: 4 iterations of every fit, predicted final rms
+    ps_status st = screen_fits(c, conw_r, n_lo, n_hi, weights);
+    if (st != PS_OK) return st;
+    stt.screen_ms = c->timing.kernel_ms;
+    stt.evals += c->timing.evals;
+    std::vector<ps_fit> fits = c->h_fits;
+    std::vector<char> done(static_cast<size_t>(nfits), 0);  // run in full
+    std::vector<int64_t> pidx;
+    std::vector<int32_t> pole;
+    std::vector<size_t> slot;
+    auto queue = [&](int64_t i) {
+        if (done[static_cast<size_t>(i)]) return;
+        done[static_cast<size_t>(i)] = 1;
+        pidx.push_back(n_lo + i / PS_N_POLES);
+        pole.push_back(static_cast<int32_t>(i % PS_N_POLES) + 1);
+        slot.push_back(static_cast<size_t>(i));
+    };
+    auto run_list = [&](int form, double *ms) -> ps_status {
+        const int64_t n = static_cast<int64_t>(pidx.size());
+        if (n == 0) return PS_OK;
+        if (static_cast<size_t>(n) > c->list_cap) {
+            cudaFree(c->d_pidx);
+            cudaFree(c->d_pole);
+            c->d_pidx = nullptr;
+            c->d_pole = nullptr;
+            PSG_CUDA(c, cudaMalloc(&c->d_pidx, n * sizeof(int64_t)));
+            PSG_CUDA(c, cudaMalloc(&c->d_pole, n * sizeof(int)));
+            c->list_cap = static_cast<size_t>(n);
+        }
+        PSG_CUDA(c, cudaMemcpyAsync(c->d_pidx, pidx.data(), n * sizeof(int64_t), cudaMemcpyHostToDevice, c->stream));
+        PSG_CUDA(c, cudaMemcpyAsync(c->d_pole, pole.data(), n * sizeof(int), cudaMemcpyHostToDevice, c->stream));
+        psg::FitWork wl{};
+        wl.n_lo = 1;
+        wl.nfits = n;
+        wl.period_index = c->d_pidx;
+        wl.pole = c->d_pole;
+        ps_status r = run_fits(c, conw_r, wl, form);
+        if (r != PS_OK) return r;
+        *ms += c->timing.kernel_ms;
+        stt.evals += c->timing.evals;
+        for (int64_t k = 0; k < n; k++) fits[slot[static_cast<size_t>(k)]] = c->h_fits[static_cast<size_t>(k)];
+        pidx.clear();
+        pole.clear();
+        slot.clear();
+        return PS_OK;
+    };
+    // (2) the top_k predicted poles of every period, and fits near the best prediction
+    double best_pred = 1e300;
+    for (const ps_fit &f : fits)
+        if (f.pred_dev > 0 && f.pred_dev < best_pred) best_pred = f.pred_dev;
+    for (int64_t n = 0; n < nper; n++) {
+        int order[PS_N_POLES];
+        for (int m = 0; m < PS_N_POLES; m++) order[m] = m;
+        const ps_fit *pf = &fits[static_cast<size_t>(n * PS_N_POLES)];
+        std::stable_sort(order, order + PS_N_POLES, [&](int a, int b) {
+            const double pa = std::isnan(pf[a].pred_dev) ? 1e300 : pf[a].pred_dev;
+            const double pb = std::isnan(pf[b].pred_dev) ? 1e300 : pf[b].pred_dev;
+            return pa < pb;
+        });
+        for (int k = 0; k < std::min(o.top_k, PS_N_POLES); k++) queue(n * PS_N_POLES + order[k]);
+        if (o.margin >= 0)
+            for (int m = 0; m < PS_N_POLES; m++)
+                if (pf[m].pred_dev <= best_pred * (1 + o.margin)) queue(n * PS_N_POLES + m);
+    }
+    st = run_list(PS_FORM_MIXED, &stt.complete_ms);
+    if (st != PS_OK) return st;
+    // rows from the completed poles only (an upper bound of the full row)
+    auto rows_from = [&](std::vector<ps_row> &rows) {
+        rows.resize(static_cast<size_t>(nper));
+        for (int64_t n = 0; n < nper; n++) {
+            ps_fit tmp[PS_N_POLES];
+            for (int m = 0; m < PS_N_POLES; m++) {
+                tmp[m] = fits[static_cast<size_t>(n * PS_N_POLES + m)];
+                if (!done[static_cast<size_t>(n * PS_N_POLES + m)]) tmp[m].dev = NAN;  // not a candidate
+            }
+            rows[static_cast<size_t>(n)] = psg::best_of_poles(tmp, c->obj.ndata);
+        }
+    };
+    auto best_of = [&](const std::vector<ps_row> &rows) {
+        int64_t b = 0;
+        for (int64_t n = 1; n < nper; n++)
+            if (rows[static_cast<size_t>(n)].rms < rows[static_cast<size_t>(b)].rms) b = n;
+        return b;
+    };
+    std::vector<ps_row> rows;
+    rows_from(rows);
+    // (3) all poles of the periods near the best row, in the mixed form
+    int64_t best = best_of(rows);
+    double lim = rows[static_cast<size_t>(best)].rms * (1 + o.region_rel);
+    for (int64_t n = 0; n < nper; n++) {
+        if (!(std::llabs(n - best) <= o.region_halfwidth || rows[static_cast<size_t>(n)].rms <= lim)) continue;
+        stt.region_periods++;
+        for (int m = 0; m < PS_N_POLES; m++) queue(n * PS_N_POLES + m);
+    }
+    st = run_list(PS_FORM_MIXED, &stt.complete_ms);
+    if (st != PS_OK) return st;
+    int64_t ndone = 0;
+    for (char d : done) ndone += d;
+    stt.fits_completed = ndone;
+    stt.fits_screened_out = nfits - ndone;
+    rows_from(rows);
+    // (4) FP64 refit of the periods nearest the best row
+    best = best_of(rows);
+    lim = rows[static_cast<size_t>(best)].rms * (1 + o.refit_rel);
+    for (int64_t n = 0; n < nper; n++) {
+        if (!(std::llabs(n - best) <= o.refit_halfwidth || rows[static_cast<size_t>(n)].rms <= lim)) continue;
+        for (int m = 0; m < PS_N_POLES; m++) {
+            pidx.push_back(n_lo + n);
+            pole.push_back(m + 1);
+            slot.push_back(static_cast<size_t>(n * PS_N_POLES + m));
+        }
+    }
+    stt.fits_refit = static_cast<int64_t>(pidx.size());
+    st = run_list(PS_FORM_FP64, &stt.refit_ms);
+    if (st != PS_OK) return st;
+    rows_from(rows);
+    best = best_of(rows);
+    for (int64_t n = 0; n < nper; n++) out[n] = rows[static_cast<size_t>(n)];
+    if (n_lo == 1) out[0].dark_or_conw = conw_r * c->obj.escl * c->obj.escl;
+    stt.best_index = n_lo + best;
+    c->timing.kernel_ms = stt.screen_ms + stt.complete_ms + stt.refit_ms;
+    c->timing.fits = nfits;
+    c->timing.evals = stt.evals;
+    c->timing.launches = 3 + (stt.fits_refit > 0);
+    if (stats) *stats = stt;
     return PS_OK;
 }
 

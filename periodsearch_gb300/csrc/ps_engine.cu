@@ -915,12 +915,49 @@ __device__ int cholesky_solve(double *A, double *b, int n, double *col)
     return 0;
 }
 
+// Learned stop predictor, evaluated by warp 0: standardised features f[10]
+// -> 64 GELU -> 64 GELU -> 1, output de-standardised.  Predicts
+// log(final rms / rms after kScreenIters iterations).  sh: 64 floats.
+__device__ inline float gelu(float x) { return 0.5f * x * (1.f + erff(x * 0.70710678118654752f)); }
+
+__device__ float mlp_predict_warp(const float *W, const float *f, float *sh)
+{
+    const int lane = threadIdx.x & 31;
+    float x[kFeat];
+#pragma unroll
+    for (int i = 0; i < kFeat; i++) x[i] = (f[i] - W[kMlpMu + i]) / W[kMlpSd + i];
+    float h1[2];
+#pragma unroll
+    for (int h = 0; h < 2; h++) {
+        const int u = lane + 32 * h;
+        float z = W[kMlpB1 + u];
+#pragma unroll
+        for (int i = 0; i < kFeat; i++) z = fmaf(W[kMlpW1 + u * kFeat + i], x[i], z);
+        h1[h] = gelu(z);
+    }
+    sh[lane] = h1[0];
+    sh[lane + 32] = h1[1];
+    __syncwarp();
+    float y = 0.f;
+#pragma unroll
+    for (int h = 0; h < 2; h++) {
+        const int u = lane + 32 * h;
+        float z = W[kMlpB2 + u];
+        for (int j = 0; j < kHidden; j++) z = fmaf(W[kMlpW2 + u * kHidden + j], sh[j], z);
+        y = fmaf(W[kMlpW3 + u], gelu(z), y);
+    }
+    y = warp_sum(y) + W[kMlpB3];
+    __syncwarp();
+    return y * W[kMlpYSd] + W[kMlpYMu];
+}
+
 // ---------------------------------------------------------------------------
 // One fit (period_search_BOINC.cpp:817-921 with mrqmin.c:11-110).
 // ---------------------------------------------------------------------------
 template <int FORM, int KU>
 __device__ void run_fit(const DevObject &ob, const FitConfig &cfg, const SlotLayout &L, Smem<FORM> &s,
-                        typename RealOf<FORM>::T *scratch, int64_t n, int pole, ps_fit *out)
+                        typename RealOf<FORM>::T *scratch, int64_t n, int pole, ps_fit *out, const FitWork &w,
+                        long long fidx)
 {
     constexpr int NT = threads_of<FORM>();
     const int tid = threadIdx.x;
@@ -948,12 +985,17 @@ __device__ void run_fit(const DevObject &ob, const FitConfig &cfg, const SlotLay
     double chk_acc[3] = {0, 0, 0}, chk_first[3] = {0, 0, 0}, chk_trial[3] = {0, 0, 0};
     double area_first = 0, area_trial = 0, totarea = 0;
     int niter = 0, last_err = 0;
+    // learned early stop: accepted chi^2 and lambda of the first iterations
+    double hist[kScreenIters + 1], lam_hist[kScreenIters];
+    double pred_dev = 0;
+    bool screened = false;
     while (((niter < cfg.n_iter_max) && (iter_diff > cfg.iter_diff_max)) || (niter < cfg.n_iter_min)) {
         bool accepted = false;
         if (alamda < 0) {
             alamda = cfg.alamda_start;
             evaluate<FORM, KU>(ob, cfg, L, s, s.cg, s.alpha, s.beta, scratch);
             ochisq = s.misc[M_CHISQ];
+            hist[0] = ochisq;
             area_first = s.misc[M_AREA];
             for (int c = 0; c < 3; c++) chk_first[c] = s.misc[M_CHK + c];
             totarea = area_first;
@@ -1025,6 +1067,42 @@ __device__ void run_fit(const DevObject &ob, const FitConfig &cfg, const SlotLay
             iter_diff = dev_old - dev_new;
             dev_old = dev_new;
         }
+        if (niter <= kScreenIters) {
+            hist[niter] = ochisq;
+            lam_hist[niter - 1] = alamda;
+        }
+        if (niter == kScreenIters && (w.traj || w.mlp)) {
+            float f[kFeat];
+#pragma unroll
+            for (int i = 0; i < kScreenIters; i++) {
+                f[i] = static_cast<float>(log(hist[i + 1] / hist[0]));
+                f[kScreenIters + i] = static_cast<float>(log10(lam_hist[i]));
+            }
+            f[8] = static_cast<float>(log(static_cast<double>(ob.ndata)));
+            f[9] = static_cast<float>(log(prd));
+            if (w.traj && tid == 0) {
+                float *rec = w.traj + static_cast<size_t>(fidx) * kTrajFloats;
+                for (int i = 0; i < kFeat; i++) rec[i] = f[i];
+                rec[10] = static_cast<float>(dev_new);
+            }
+            if (w.mlp && w.iter_limit == kScreenIters) {
+                if (tid < 32) {
+                    const float y = mlp_predict_warp(w.mlp, f, reinterpret_cast<float *>(s.pt));
+                    if (tid == 0) s.misc[M_PIV + 2] = static_cast<double>(y);
+                }
+                __syncthreads();
+                pred_dev = dev_new * exp(s.misc[M_PIV + 2]);
+            }
+        }
+        if (w.iter_limit > 0 && niter >= w.iter_limit) {
+            screened = true;
+            break;
+        }
+    }
+    if (w.traj && tid == 0) {
+        float *rec = w.traj + static_cast<size_t>(fidx) * kTrajFloats;
+        rec[11] = static_cast<float>(dev_new);
+        rec[12] = static_cast<float>(niter);
     }
     if (tid == 0) {
         ps_fit r;
@@ -1037,6 +1115,9 @@ __device__ void run_fit(const DevObject &ob, const FitConfig &cfg, const SlotLay
         r.chisq = chisq;
         r.niter = niter;
         r.err_code = last_err;
+        r.pred_dev = pred_dev;
+        r.screened = screened ? 1 : 0;
+        r.reserved = 0;
         *out = r;
     }
     __syncthreads();
@@ -1070,7 +1151,7 @@ __global__ void __launch_bounds__(threads_of<FORM>(), 1)
             n = w.n_lo + f / PS_N_POLES;
             pole = static_cast<int>(f % PS_N_POLES) + 1;
         }
-        run_fit<FORM, KU>(ob, cfg, L, s, scratch, n, pole, w.out + f);
+        run_fit<FORM, KU>(ob, cfg, L, s, scratch, n, pole, w.out + f, w, f);
     }
 }
 

@@ -47,7 +47,22 @@ struct FitWork {
     double *scratch;              // per-slot scratch for relative lightcurves
     size_t scratch_stride;        // doubles per slot
     ps_fit *out;                  // [nfits]
+    // learned early stop (all optional)
+    int iter_limit;               // > 0: stop every fit after this many LM iterations (screening)
+    float *traj;                  // [nfits][kTrajFloats] trajectory records, or nullptr
+    const float *mlp;             // stop-predictor weights (layout of kMlp*), or nullptr
 };
+
+// Learned early stop: features of a fit after kScreenIters LM iterations,
+// the record written per fit, and the layout of the predictor's weights
+// (a 10-64-64-1 GELU MLP with input and output standardisation).
+constexpr int kScreenIters = 4;
+constexpr int kFeat = 10;
+constexpr int kHidden = 64;
+constexpr int kTrajFloats = 16;   // features[10], dev_k, dev_final, niter, spare[3]
+constexpr int kMlpMu = 0, kMlpSd = kFeat, kMlpW1 = 2 * kFeat, kMlpB1 = kMlpW1 + kHidden * kFeat,
+              kMlpW2 = kMlpB1 + kHidden, kMlpB2 = kMlpW2 + kHidden * kHidden, kMlpW3 = kMlpB2 + kHidden,
+              kMlpB3 = kMlpW3 + kHidden, kMlpYMu = kMlpB3 + 1, kMlpYSd = kMlpYMu + 1, kMlpFloats = kMlpYSd + 1;
 
 // Shared-memory plan of a fit slot; identical on host and device.  Offsets
 // are in bytes; every block starts on a 16-byte boundary.  Blocks of type
@@ -131,6 +146,11 @@ int launch_eval(int form, const DevObject &ob, const FitConfig &cfg, const doubl
 int set_kernel_smem(int form, size_t smem, int ncoef);
 int occupancy_slots(int form, size_t smem, int ncoef, int *per_sm);
 int measure_fma_peaks(double *fp64_tflops, double *fp32_tflops, void *stream);
+// Learned early stop (ps_mlp.cu).
+int mlp_train(float *h_P, const float *h_x, const float *h_y, int n, int epochs, int batch, float lr, uint64_t seed,
+              float *h_loss_hist);
+int mlp_predict(const float *h_P, const float *h_x, int n, float *h_out);
+int mlp_grad(const float *h_P, const float *h_x, const float *h_y, int n, float *h_loss, float *h_G);
 
 // Allocation-free launch of the FP64 fit kernel: the work counter and the
 // per-slot scratch come from a file-scope device array of
