@@ -266,6 +266,18 @@ ps_status ps_mlp_grad(int32_t device, const float *weights, const float *x, cons
  * predicted final rms (pred_dev) and screened = 1.  Fit f is period
  * n_lo + f / 10, pole f % 10 + 1. */
 ps_status ps_screen(ps_ctx *ctx, double conw_r, int64_t n_lo, int64_t n_hi, const float *weights, ps_fit *out);
+/* Period scan in the context's form followed by a full FP64 refit of the
+ * minimum region: every period whose row lies within refit_rel (relative)
+ * of the best row, or within refit_halfwidth periods of it, is refitted by
+ * the plain FP64 form, repeated with the new rows until no further period
+ * qualifies.  With the mixed form this gives the FP64 form's best period
+ * and FP64 values there at close to the mixed form's cost.  Statistics in
+ * the ps_learned_stats fields fits_total, fits_completed (the scan),
+ * fits_refit, complete_ms (scan), refit_ms, evals, best_index.  stats may
+ * be NULL. */
+ps_status ps_scan_refined(ps_ctx *ctx, double conw_r, int64_t n_lo, int64_t n_hi, double refit_rel,
+                          int32_t refit_halfwidth, ps_row *out, ps_learned_stats *stats);
+
 /* Options of the learned scan (ps_scan_learned). */
 typedef struct ps_learned_opts {
     int32_t top_k;           /* complete the top_k best-predicted poles of every period (>= 1) */

@@ -215,6 +215,17 @@ class Engine:
         _abi.check(r, "ps_screen", self._ctx)
         return out
 
+    def scan_refined(self, conw_r: float, n_lo: int, n_hi: int, refit_rel: float = 0.01, refit_halfwidth: int = 2):
+        """Scan in the engine's form, then refit the minimum region in full
+        with the FP64 form (ps_scan_refined); returns the rows and the
+        statistics."""
+        out = np.zeros(n_hi - n_lo + 1, ROW_DTYPE)
+        st = _abi.LearnedStats()
+        r = self._L.ps_scan_refined(self._ctx, conw_r, n_lo, n_hi, refit_rel, refit_halfwidth,
+                                    out.ctypes.data_as(C.POINTER(_abi.Row)), C.byref(st))
+        _abi.check(r, "ps_scan_refined", self._ctx)
+        return out, {k: getattr(st, k) for k, _ in _abi.LearnedStats._fields_}
+
     def scan_learned(self, conw_r: float, n_lo: int, n_hi: int, weights=None, **opts):
         """Period scan with the learned early stop (ps_scan_learned); returns
         the rows and the stage statistics.  Options (ps_learned_opts): top_k,

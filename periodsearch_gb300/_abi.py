@@ -118,6 +118,8 @@ SIGNATURES = {
     "ps_mlp_grad": (C.c_int, [C.c_int32, C.POINTER(C.c_float), C.POINTER(C.c_float), C.POINTER(C.c_float),
                               C.c_int64, C.POINTER(C.c_float), C.POINTER(C.c_float)]),
     "ps_screen": (C.c_int, [_CTX, C.c_double, C.c_int64, C.c_int64, C.POINTER(C.c_float), C.POINTER(Fit)]),
+    "ps_scan_refined": (C.c_int, [_CTX, C.c_double, C.c_int64, C.c_int64, C.c_double, C.c_int32,
+                                  C.POINTER(Row), C.POINTER(LearnedStats)]),
     "ps_scan_learned": (C.c_int, [_CTX, C.c_double, C.c_int64, C.c_int64, C.POINTER(C.c_float),
                                   C.POINTER(LearnedOpts), C.POINTER(Row), C.POINTER(LearnedStats)]),
     "ps_last_error": (C.c_char_p, [_CTX]),

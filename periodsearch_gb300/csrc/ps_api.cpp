@@ -50,6 +50,7 @@ struct ps_ctx {
     int64_t *d_pidx = nullptr;
     int *d_pole = nullptr;
     size_t list_cap = 0;
+    int64_t launch_total = 0;   // fit-kernel launches since ps_prepare
     double *d_eval = nullptr;          // cg, alpha, beta, chisq, area of ps_eval
     std::vector<ps_fit> h_fits;
     ps_timing timing{};
@@ -212,6 +213,7 @@ ps_status run_fits(ps_ctx *c, double conw_r, psg::FitWork w, int form)
     for (const ps_fit &f : c->h_fits) evals += f.niter + 1;
     c->timing.evals = evals;
     c->timing.launches = 1;
+    c->launch_total++;
     return PS_OK;
 }
 
@@ -226,6 +228,105 @@ ps_status scan_rows(ps_ctx *c, double conw_r, int64_t n_lo, int64_t n_hi, ps_row
         ps_row r = psg::best_of_poles(&c->h_fits[static_cast<size_t>(n - n_lo) * PS_N_POLES], c->obj.ndata);
         if (prepass && std::isnan(r.dark_or_conw)) r.dark_or_conw = 1.0;
         out[n - n_lo] = r;
+    }
+    return PS_OK;
+}
+
+// Fits given as (period index, pole) lists on the host: copied to the
+// device and launched in the given form; results in c->h_fits.
+ps_status run_list(ps_ctx *c, double conw_r, const int64_t *pidx, const int32_t *pole, int64_t n, int form)
+{
+    if (static_cast<size_t>(n) > c->list_cap) {
+        cudaFree(c->d_pidx);
+        cudaFree(c->d_pole);
+        c->d_pidx = nullptr;
+        c->d_pole = nullptr;
+        PSG_CUDA(c, cudaMalloc(&c->d_pidx, n * sizeof(int64_t)));
+        PSG_CUDA(c, cudaMalloc(&c->d_pole, n * sizeof(int)));
+        c->list_cap = static_cast<size_t>(n);
+    }
+    PSG_CUDA(c, cudaMemcpyAsync(c->d_pidx, pidx, n * sizeof(int64_t), cudaMemcpyHostToDevice, c->stream));
+    PSG_CUDA(c, cudaMemcpyAsync(c->d_pole, pole, n * sizeof(int), cudaMemcpyHostToDevice, c->stream));
+    psg::FitWork w{};
+    w.n_lo = 1;
+    w.nfits = n;
+    w.period_index = c->d_pidx;
+    w.pole = c->d_pole;
+    return run_fits(c, conw_r, w, form);
+}
+
+// The fits of a scan window on the host: period n_lo + i / 10, pole i % 10 + 1.
+struct ScanFits {
+    int64_t n_lo = 1, nper = 0;
+    std::vector<ps_fit> fits;
+    std::vector<char> done;     // run in full (a candidate of its period's row)
+    std::vector<char> fp64;     // period refitted in full by the FP64 form
+
+    ps_row row(int64_t n, int32_t ndata) const
+    {
+        ps_fit tmp[PS_N_POLES];
+        for (int m = 0; m < PS_N_POLES; m++) {
+            tmp[m] = fits[static_cast<size_t>(n * PS_N_POLES + m)];
+            if (!done[static_cast<size_t>(n * PS_N_POLES + m)]) tmp[m].dev = NAN;  // not a candidate
+        }
+        return psg::best_of_poles(tmp, ndata);
+    }
+    void rows(std::vector<ps_row> &r, int32_t ndata) const
+    {
+        r.resize(static_cast<size_t>(nper));
+        for (int64_t n = 0; n < nper; n++) r[static_cast<size_t>(n)] = row(n, ndata);
+    }
+    static int64_t best(const std::vector<ps_row> &r)
+    {
+        int64_t b = 0;
+        for (size_t n = 1; n < r.size(); n++)
+            if (r[n].rms < r[static_cast<size_t>(b)].rms) b = static_cast<int64_t>(n);
+        return b;
+    }
+};
+
+// Refits in full by the FP64 form every period whose row lies within
+// rel (relative) of the best row or within halfwidth periods of it, and
+// repeats with the new rows until the set is closed: the best row and its
+// neighbourhood then carry FP64 values, and no row outside the set comes
+// within rel of it.
+ps_status refit_minimum(ps_ctx *c, double conw_r, ScanFits &sf, double rel, int32_t halfwidth, double *ms,
+                        int64_t *nrefit, int64_t *evals)
+{
+    std::vector<ps_row> rows;
+    std::vector<int64_t> pidx;
+    std::vector<int32_t> pole;
+    std::vector<int64_t> per;
+    for (int round = 0; round < 64; round++) {
+        sf.rows(rows, c->obj.ndata);
+        const int64_t best = ScanFits::best(rows);
+        const double lim = rows[static_cast<size_t>(best)].rms * (1 + rel);
+        pidx.clear();
+        pole.clear();
+        per.clear();
+        for (int64_t n = 0; n < sf.nper; n++) {
+            if (sf.fp64[static_cast<size_t>(n)]) continue;
+            if (!(std::llabs(n - best) <= halfwidth || rows[static_cast<size_t>(n)].rms <= lim)) continue;
+            per.push_back(n);
+            for (int m = 0; m < PS_N_POLES; m++) {
+                pidx.push_back(sf.n_lo + n);
+                pole.push_back(m + 1);
+            }
+        }
+        if (per.empty()) return PS_OK;
+        ps_status st = run_list(c, conw_r, pidx.data(), pole.data(), static_cast<int64_t>(pidx.size()), PS_FORM_FP64);
+        if (st != PS_OK) return st;
+        *ms += c->timing.kernel_ms;
+        *evals += c->timing.evals;
+        *nrefit += static_cast<int64_t>(pidx.size());
+        for (size_t k = 0; k < per.size(); k++) {
+            const int64_t n = per[k];
+            sf.fp64[static_cast<size_t>(n)] = 1;
+            for (int m = 0; m < PS_N_POLES; m++) {
+                sf.fits[static_cast<size_t>(n * PS_N_POLES + m)] = c->h_fits[k * PS_N_POLES + m];
+                sf.done[static_cast<size_t>(n * PS_N_POLES + m)] = 1;
+            }
+        }
     }
     return PS_OK;
 }
@@ -497,23 +598,7 @@ ps_status ps_fit_batch(ps_ctx *c, double conw_r, int64_t n_fits, const int64_t *
     for (int64_t i = 0; i < n_fits; i++)
         if (period_index[i] < 1 || pole[i] < 1 || pole[i] > PS_N_POLES) return PS_ERR_ARG;
     PSG_CUDA(c, cudaSetDevice(c->opt.device));
-    if (static_cast<size_t>(n_fits) > c->list_cap) {
-        if (c->d_pidx) cudaFree(c->d_pidx);
-        if (c->d_pole) cudaFree(c->d_pole);
-        c->d_pidx = nullptr;
-        c->d_pole = nullptr;
-        PSG_CUDA(c, cudaMalloc(&c->d_pidx, n_fits * sizeof(int64_t)));
-        PSG_CUDA(c, cudaMalloc(&c->d_pole, n_fits * sizeof(int)));
-        c->list_cap = static_cast<size_t>(n_fits);
-    }
-    PSG_CUDA(c, cudaMemcpyAsync(c->d_pidx, period_index, n_fits * sizeof(int64_t), cudaMemcpyHostToDevice, c->stream));
-    PSG_CUDA(c, cudaMemcpyAsync(c->d_pole, pole, n_fits * sizeof(int), cudaMemcpyHostToDevice, c->stream));
-    psg::FitWork w{};
-    w.n_lo = 1;
-    w.nfits = n_fits;
-    w.period_index = c->d_pidx;
-    w.pole = c->d_pole;
-    ps_status st = run_fits(c, conw_r, w, c->opt.form);
+    ps_status st = run_list(c, conw_r, period_index, pole, n_fits, c->opt.form);
     if (st != PS_OK) return st;
     std::memcpy(out, c->h_fits.data(), n_fits * sizeof(ps_fit));
     return PS_OK;
@@ -669,50 +754,39 @@ ps_status ps_scan_learned(ps_ctx *c, double conw_r, int64_t n_lo, int64_t n_hi, 
         !(o.region_rel >= 0) || !(o.refit_rel >= 0) || o.region_halfwidth < 0 || o.refit_halfwidth < 0)
         return PS_ERR_ARG;
     PSG_CUDA(c, cudaSetDevice(c->opt.device));
-    const int64_t nper = n_hi - n_lo + 1, nfits = nper * PS_N_POLES;
+    ScanFits sf;
+    sf.n_lo = n_lo;
+    sf.nper = n_hi - n_lo + 1;
+    const int64_t nfits = sf.nper * PS_N_POLES;
     ps_learned_stats stt{};
     stt.fits_total = nfits;
+    const int64_t launch0 = c->launch_total;
     // (1) screening: 4 iterations of every fit, predicted final rms
     ps_status st = screen_fits(c, conw_r, n_lo, n_hi, weights);
     if (st != PS_OK) return st;
     stt.screen_ms = c->timing.kernel_ms;
     stt.evals += c->timing.evals;
-    std::vector<ps_fit> fits = c->h_fits;
-    std::vector<char> done(static_cast<size_t>(nfits), 0);  // run in full
-    std::vector<int64_t> pidx;
+    sf.fits = c->h_fits;
+    sf.done.assign(static_cast<size_t>(nfits), 0);
+    sf.fp64.assign(static_cast<size_t>(sf.nper), 0);
+    std::vector<int64_t> pidx, slot;
     std::vector<int32_t> pole;
-    std::vector<size_t> slot;
     auto queue = [&](int64_t i) {
-        if (done[static_cast<size_t>(i)]) return;
-        done[static_cast<size_t>(i)] = 1;
+        if (sf.done[static_cast<size_t>(i)]) return;
+        sf.done[static_cast<size_t>(i)] = 1;
         pidx.push_back(n_lo + i / PS_N_POLES);
         pole.push_back(static_cast<int32_t>(i % PS_N_POLES) + 1);
-        slot.push_back(static_cast<size_t>(i));
+        slot.push_back(i);
     };
-    auto run_list = [&](int form, double *ms) -> ps_status {
+    auto complete = [&]() -> ps_status {
         const int64_t n = static_cast<int64_t>(pidx.size());
         if (n == 0) return PS_OK;
-        if (static_cast<size_t>(n) > c->list_cap) {
-            cudaFree(c->d_pidx);
-            cudaFree(c->d_pole);
-            c->d_pidx = nullptr;
-            c->d_pole = nullptr;
-            PSG_CUDA(c, cudaMalloc(&c->d_pidx, n * sizeof(int64_t)));
-            PSG_CUDA(c, cudaMalloc(&c->d_pole, n * sizeof(int)));
-            c->list_cap = static_cast<size_t>(n);
-        }
-        PSG_CUDA(c, cudaMemcpyAsync(c->d_pidx, pidx.data(), n * sizeof(int64_t), cudaMemcpyHostToDevice, c->stream));
-        PSG_CUDA(c, cudaMemcpyAsync(c->d_pole, pole.data(), n * sizeof(int), cudaMemcpyHostToDevice, c->stream));
-        psg::FitWork wl{};
-        wl.n_lo = 1;
-        wl.nfits = n;
-        wl.period_index = c->d_pidx;
-        wl.pole = c->d_pole;
-        ps_status r = run_fits(c, conw_r, wl, form);
+        ps_status r = run_list(c, conw_r, pidx.data(), pole.data(), n, PS_FORM_MIXED);
         if (r != PS_OK) return r;
-        *ms += c->timing.kernel_ms;
+        stt.complete_ms += c->timing.kernel_ms;
         stt.evals += c->timing.evals;
-        for (int64_t k = 0; k < n; k++) fits[slot[static_cast<size_t>(k)]] = c->h_fits[static_cast<size_t>(k)];
+        for (int64_t k = 0; k < n; k++)
+            sf.fits[static_cast<size_t>(slot[static_cast<size_t>(k)])] = c->h_fits[static_cast<size_t>(k)];
         pidx.clear();
         pole.clear();
         slot.clear();
@@ -720,12 +794,12 @@ ps_status ps_scan_learned(ps_ctx *c, double conw_r, int64_t n_lo, int64_t n_hi, 
     };
     // (2) the top_k predicted poles of every period, and fits near the best prediction
     double best_pred = 1e300;
-    for (const ps_fit &f : fits)
+    for (const ps_fit &f : sf.fits)
         if (f.pred_dev > 0 && f.pred_dev < best_pred) best_pred = f.pred_dev;
-    for (int64_t n = 0; n < nper; n++) {
+    for (int64_t n = 0; n < sf.nper; n++) {
         int order[PS_N_POLES];
         for (int m = 0; m < PS_N_POLES; m++) order[m] = m;
-        const ps_fit *pf = &fits[static_cast<size_t>(n * PS_N_POLES)];
+        const ps_fit *pf = &sf.fits[static_cast<size_t>(n * PS_N_POLES)];
         std::stable_sort(order, order + PS_N_POLES, [&](int a, int b) {
             const double pa = std::isnan(pf[a].pred_dev) ? 1e300 : pf[a].pred_dev;
             const double pb = std::isnan(pf[b].pred_dev) ? 1e300 : pf[b].pred_dev;
@@ -736,66 +810,74 @@ ps_status ps_scan_learned(ps_ctx *c, double conw_r, int64_t n_lo, int64_t n_hi, 
             for (int m = 0; m < PS_N_POLES; m++)
                 if (pf[m].pred_dev <= best_pred * (1 + o.margin)) queue(n * PS_N_POLES + m);
     }
-    st = run_list(PS_FORM_MIXED, &stt.complete_ms);
+    st = complete();
     if (st != PS_OK) return st;
-    // rows from the completed poles only (an upper bound of the full row)
-    auto rows_from = [&](std::vector<ps_row> &rows) {
-        rows.resize(static_cast<size_t>(nper));
-        for (int64_t n = 0; n < nper; n++) {
-            ps_fit tmp[PS_N_POLES];
-            for (int m = 0; m < PS_N_POLES; m++) {
-                tmp[m] = fits[static_cast<size_t>(n * PS_N_POLES + m)];
-                if (!done[static_cast<size_t>(n * PS_N_POLES + m)]) tmp[m].dev = NAN;  // not a candidate
-            }
-            rows[static_cast<size_t>(n)] = psg::best_of_poles(tmp, c->obj.ndata);
-        }
-    };
-    auto best_of = [&](const std::vector<ps_row> &rows) {
-        int64_t b = 0;
-        for (int64_t n = 1; n < nper; n++)
-            if (rows[static_cast<size_t>(n)].rms < rows[static_cast<size_t>(b)].rms) b = n;
-        return b;
-    };
+    // (3) all poles of the periods near the best row (rows of the completed
+    // poles only: an upper bound of the full rows), in the mixed form
     std::vector<ps_row> rows;
-    rows_from(rows);
-    // (3) all poles of the periods near the best row, in the mixed form
-    int64_t best = best_of(rows);
-    double lim = rows[static_cast<size_t>(best)].rms * (1 + o.region_rel);
-    for (int64_t n = 0; n < nper; n++) {
+    sf.rows(rows, c->obj.ndata);
+    int64_t best = ScanFits::best(rows);
+    const double lim = rows[static_cast<size_t>(best)].rms * (1 + o.region_rel);
+    for (int64_t n = 0; n < sf.nper; n++) {
         if (!(std::llabs(n - best) <= o.region_halfwidth || rows[static_cast<size_t>(n)].rms <= lim)) continue;
         stt.region_periods++;
         for (int m = 0; m < PS_N_POLES; m++) queue(n * PS_N_POLES + m);
     }
-    st = run_list(PS_FORM_MIXED, &stt.complete_ms);
+    st = complete();
     if (st != PS_OK) return st;
-    int64_t ndone = 0;
-    for (char d : done) ndone += d;
-    stt.fits_completed = ndone;
-    stt.fits_screened_out = nfits - ndone;
-    rows_from(rows);
+    for (char d : sf.done) stt.fits_completed += d;
+    stt.fits_screened_out = nfits - stt.fits_completed;
     // (4) FP64 refit of the periods nearest the best row
-    best = best_of(rows);
-    lim = rows[static_cast<size_t>(best)].rms * (1 + o.refit_rel);
-    for (int64_t n = 0; n < nper; n++) {
-        if (!(std::llabs(n - best) <= o.refit_halfwidth || rows[static_cast<size_t>(n)].rms <= lim)) continue;
-        for (int m = 0; m < PS_N_POLES; m++) {
-            pidx.push_back(n_lo + n);
-            pole.push_back(m + 1);
-            slot.push_back(static_cast<size_t>(n * PS_N_POLES + m));
-        }
-    }
-    stt.fits_refit = static_cast<int64_t>(pidx.size());
-    st = run_list(PS_FORM_FP64, &stt.refit_ms);
+    st = refit_minimum(c, conw_r, sf, o.refit_rel, o.refit_halfwidth, &stt.refit_ms, &stt.fits_refit, &stt.evals);
     if (st != PS_OK) return st;
-    rows_from(rows);
-    best = best_of(rows);
-    for (int64_t n = 0; n < nper; n++) out[n] = rows[static_cast<size_t>(n)];
+    sf.rows(rows, c->obj.ndata);
+    best = ScanFits::best(rows);
+    for (int64_t n = 0; n < sf.nper; n++) out[n] = rows[static_cast<size_t>(n)];
     if (n_lo == 1) out[0].dark_or_conw = conw_r * c->obj.escl * c->obj.escl;
     stt.best_index = n_lo + best;
     c->timing.kernel_ms = stt.screen_ms + stt.complete_ms + stt.refit_ms;
     c->timing.fits = nfits;
     c->timing.evals = stt.evals;
-    c->timing.launches = 3 + (stt.fits_refit > 0);
+    c->timing.launches = static_cast<int32_t>(c->launch_total - launch0);
+    if (stats) *stats = stt;
+    return PS_OK;
+}
+
+ps_status ps_scan_refined(ps_ctx *c, double conw_r, int64_t n_lo, int64_t n_hi, double refit_rel,
+                          int32_t refit_halfwidth, ps_row *out, ps_learned_stats *stats)
+{
+    if (!c || !out || n_lo < 1 || n_hi < n_lo || !(conw_r > 0) || !(refit_rel >= 0) || refit_halfwidth < 0)
+        return PS_ERR_ARG;
+    PSG_CUDA(c, cudaSetDevice(c->opt.device));
+    ScanFits sf;
+    sf.n_lo = n_lo;
+    sf.nper = n_hi - n_lo + 1;
+    const int64_t nfits = sf.nper * PS_N_POLES;
+    ps_learned_stats stt{};
+    stt.fits_total = nfits;
+    const int64_t launch0 = c->launch_total;
+    psg::FitWork w{};
+    w.n_lo = n_lo;
+    w.nfits = nfits;
+    ps_status st = run_fits(c, conw_r, w, c->opt.form);
+    if (st != PS_OK) return st;
+    stt.complete_ms = c->timing.kernel_ms;
+    stt.evals = c->timing.evals;
+    stt.fits_completed = nfits;
+    sf.fits = c->h_fits;
+    sf.done.assign(static_cast<size_t>(nfits), 1);
+    sf.fp64.assign(static_cast<size_t>(sf.nper), c->opt.form == PS_FORM_FP64 ? 1 : 0);
+    st = refit_minimum(c, conw_r, sf, refit_rel, refit_halfwidth, &stt.refit_ms, &stt.fits_refit, &stt.evals);
+    if (st != PS_OK) return st;
+    std::vector<ps_row> rows;
+    sf.rows(rows, c->obj.ndata);
+    for (int64_t n = 0; n < sf.nper; n++) out[n] = rows[static_cast<size_t>(n)];
+    if (n_lo == 1) out[0].dark_or_conw = conw_r * c->obj.escl * c->obj.escl;
+    stt.best_index = n_lo + ScanFits::best(rows);
+    c->timing.kernel_ms = stt.complete_ms + stt.refit_ms;
+    c->timing.fits = nfits;
+    c->timing.evals = stt.evals;
+    c->timing.launches = static_cast<int32_t>(c->launch_total - launch0);
     if (stats) *stats = stt;
     return PS_OK;
 }

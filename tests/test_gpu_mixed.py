@@ -96,3 +96,41 @@ def test_mixed_finds_truth_period(engine_lib, tmp_path):
             rows = eng.scan(conw_r, lo, min(int(eng.info.n_max), n_truth + 12))
             best[form] = lo + int(np.argmin(rows["rms"]))
     assert best[PS_FORM_FP64] == best[PS_FORM_MIXED]
+
+
+def test_refined_golden134(mixed):
+    """The mixed scan refined by the FP64 form around the minimum: the best
+    period of the reference, the refitted rows within the FP64 form's
+    tolerance (1e-3 for any row), the others within the mixed form's."""
+    eng = mixed("golden")
+    conw_r, _ = eng.precalc_conw()
+    ref = np.loadtxt(GOLDEN / "golden134.full", ndmin=2)
+    rows, st = eng.scan_refined(conw_r, 1, 134, refit_rel=0.01, refit_halfwidth=2)
+    b = int(np.argmin(ref[:, 1]))
+    assert st["best_index"] == b + 1 and int(np.argmin(rows["rms"])) == b
+    assert st["fits_refit"] >= 50 and st["fits_refit"] % 10 == 0 and st["fits_completed"] == 1340
+    rel = np.abs(rows["rms"] - ref[:, 1]) / ref[:, 1]
+    lo, hi = max(0, b - 2), min(133, b + 2)
+    assert rel[lo:hi + 1].max() <= 1e-3
+    assert rel.max() <= MAX_REL
+    print("refined golden134: best row rel %.2e, refit %d fits" % (rel[b], st["fits_refit"]))
+
+
+def test_refined_matches_fp64_scan_window(engine_lib, tmp_path):
+    """On a synthetic object (c0 generator, seed 902, a window of 60
+    periods around the true period) the refined mixed scan reports the best
+    period of the full FP64 scan with its FP64 row values."""
+    from periodsearch_gb300 import Engine, PS_FORM_FP64, PS_FORM_MIXED, read_input, synth
+
+    obj = synth.write_object(tmp_path / "period_search_in", "c0", seed=902)
+    data = read_input(tmp_path / "period_search_in")
+    with Engine(data, form=PS_FORM_FP64) as e64:
+        conw_r, _ = e64.precalc_conw()
+        n_t = int(round((e64.info.freq_start - 1 / obj.truth["period_h"]) / e64.info.freq_step)) + 1
+        lo, hi = max(1, n_t - 30), min(int(e64.info.n_max), n_t + 29)
+        full = e64.scan(conw_r, lo, hi)
+    with Engine(data, form=PS_FORM_MIXED) as eng:
+        rows, st = eng.scan_refined(conw_r, lo, hi)
+    b = int(np.argmin(full["rms"]))
+    assert int(st["best_index"]) == lo + b
+    assert rows["rms"][b] == pytest.approx(full["rms"][b], rel=1e-12)
