@@ -306,6 +306,37 @@ typedef struct ps_learned_opts {
 ps_status ps_scan_learned(ps_ctx *ctx, double conw_r, int64_t n_lo, int64_t n_hi, const float *weights,
                           const ps_learned_opts *opts, ps_row *out, ps_learned_stats *stats);
 
+/* ---- replica validator ---- */
+
+/* Agreement of two replicas of one work unit under the project's validator
+ * rule (validator/period_search_validator4.cpp:71-109): same number of
+ * entries (at least one) and, on every entry, |(a - b) / (a + b)| / 2
+ * within tol = {period 0.1, rms 0.1, chi^2 0.5}. */
+typedef struct ps_validate_report {
+    int32_t match;            /* 1 when the replicas agree */
+    int32_t mismatch_column;  /* column of the first failing entry: 0 period, 1 rms, 2 chi^2; -1 none */
+    int64_t entries_a, entries_b;
+    int64_t first_mismatch;   /* 0-based entry of the first failure, -1 none */
+    double max_dev[3];        /* largest |(a - b) / (a + b)| / 2 per column over all compared entries */
+    int64_t argmax_dev[3];    /* entry where it occurs, -1 none */
+    int32_t parse_error_a;    /* the reader rejected file a (ps_validate_files) */
+    int32_t parse_error_b;
+} ps_validate_report;
+
+/* Rows as ps_scan returns them.  tol NULL selects the validator's
+ * tolerances. */
+ps_status ps_validate_rows(const ps_row *a, int64_t na, const ps_row *b, int64_t nb, const double *tol,
+                           ps_validate_report *report);
+
+/* period_search_out files, read the way the validator reads them: fscanf
+ * of six numbers until end of file; a partial entry or a NaN period, rms or
+ * chi^2 rejects the file (parse_error_*, match 0); the end-of-file read
+ * repeats the last entry, so a file ending in a newline has one entry more
+ * than rows.  An empty file is rejected.  PS_ERR_IO when a file cannot be
+ * opened. */
+ps_status ps_validate_files(const char *path_a, const char *path_b, const double *tol,
+                            ps_validate_report *report);
+
 /* ---- formats ---- */
 /* Writes one row in the reference's format "%.8f  %.6f  %.6f %4.1f %4.0f %4.0f\n"
  * (period_search_BOINC.cpp:928,931).  Returns the number of characters. */

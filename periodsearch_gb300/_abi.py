@@ -75,6 +75,12 @@ class LearnedStats(C.Structure):
                 ("region_periods", C.c_int64)]
 
 
+class ValidateReport(C.Structure):
+    _fields_ = [("match", C.c_int32), ("mismatch_column", C.c_int32), ("entries_a", C.c_int64),
+                ("entries_b", C.c_int64), ("first_mismatch", C.c_int64), ("max_dev", C.c_double * 3),
+                ("argmax_dev", C.c_int64 * 3), ("parse_error_a", C.c_int32), ("parse_error_b", C.c_int32)]
+
+
 class LearnedOpts(C.Structure):
     _fields_ = [("top_k", C.c_int32), ("margin", C.c_double), ("region_rel", C.c_double),
                 ("region_halfwidth", C.c_int32), ("refit_rel", C.c_double), ("refit_halfwidth", C.c_int32)]
@@ -118,6 +124,9 @@ SIGNATURES = {
     "ps_mlp_grad": (C.c_int, [C.c_int32, C.POINTER(C.c_float), C.POINTER(C.c_float), C.POINTER(C.c_float),
                               C.c_int64, C.POINTER(C.c_float), C.POINTER(C.c_float)]),
     "ps_screen": (C.c_int, [_CTX, C.c_double, C.c_int64, C.c_int64, C.POINTER(C.c_float), C.POINTER(Fit)]),
+    "ps_validate_rows": (C.c_int, [C.POINTER(Row), C.c_int64, C.POINTER(Row), C.c_int64, C.POINTER(C.c_double),
+                                   C.POINTER(ValidateReport)]),
+    "ps_validate_files": (C.c_int, [C.c_char_p, C.c_char_p, C.POINTER(C.c_double), C.POINTER(ValidateReport)]),
     "ps_scan_refined": (C.c_int, [_CTX, C.c_double, C.c_int64, C.c_int64, C.c_double, C.c_int32,
                                   C.POINTER(Row), C.POINTER(LearnedStats)]),
     "ps_scan_learned": (C.c_int, [_CTX, C.c_double, C.c_int64, C.c_int64, C.POINTER(C.c_float),

@@ -1,6 +1,6 @@
 """Builds the engine in-tree: libps_gb300.so (C ABI) and the ps_gb300 CLI.
 
-Three translation units are compiled in parallel: the sm_103a kernels with
+The translation units are compiled in parallel: the sm_103a kernels with
 nvcc, the host code with g++ (-ffp-contract=off keeps the reference's
 rounding in the per-object set-up on FMA hosts such as aarch64).
 """
@@ -60,9 +60,11 @@ def build(force: bool = False, verbose: bool = False) -> Path:
                      "-I", str(cuda / "include"), "-c", str(CSRC / "ps_api.cpp"), "-o", str(BUILD / "ps_api.o")],
         "ps_setup.o": ["g++", "-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", *inc,
                        "-c", str(CSRC / "ps_setup.cpp"), "-o", str(BUILD / "ps_setup.o")],
+        "ps_validate.o": ["g++", "-O2", "-std=c++17", "-fPIC", *inc,
+                          "-c", str(CSRC / "ps_validate.cpp"), "-o", str(BUILD / "ps_validate.o")],
     }
     srcs = {"ps_engine.o": CSRC / "ps_engine.cu", "ps_mlp.o": CSRC / "ps_mlp.cu", "ps_api.o": CSRC / "ps_api.cpp",
-            "ps_setup.o": CSRC / "ps_setup.cpp"}
+            "ps_setup.o": CSRC / "ps_setup.cpp", "ps_validate.o": CSRC / "ps_validate.cpp"}
     todo = [cmd for obj, cmd in units.items() if force or _stale(BUILD / obj, [srcs[obj], *headers])]
     with ThreadPoolExecutor(max_workers=4) as ex:
         list(ex.map(_run, todo))

@@ -134,3 +134,26 @@ def test_refined_matches_fp64_scan_window(engine_lib, tmp_path):
     b = int(np.argmin(full["rms"]))
     assert int(st["best_index"]) == lo + b
     assert rows["rms"][b] == pytest.approx(full["rms"][b], rel=1e-12)
+
+
+def test_cross_build_agreement_report(mixed, engine_lib):
+    """Agreement report of the reference output (full-precision capture),
+    the FP64 form, the mixed form and the refined mixed scan on the golden
+    work unit: every pair passes the project's replica validator and has the
+    same best period."""
+    from periodsearch_gb300 import ROW_DTYPE, Engine, PS_FORM_FP64, read_input, validate
+
+    ref = np.loadtxt(GOLDEN / "golden134.full", ndmin=2)
+    golden = np.zeros(len(ref), ROW_DTYPE)
+    for k, name in enumerate(ROW_DTYPE.names):
+        golden[name] = ref[:, k]
+    eng = mixed("golden")
+    conw_r, _ = eng.precalc_conw()
+    builds = {"reference": golden, "mixed": eng.scan(conw_r, 1, 134),
+              "refined": eng.scan_refined(conw_r, 1, 134)[0]}
+    with Engine(read_input(_path("golden")), form=PS_FORM_FP64) as e64:
+        builds["fp64"] = e64.scan(conw_r, 1, 134)
+    rpt = validate.agreement_report(builds)
+    for name, pair in rpt["pairs"].items():
+        assert pair["validator_match"] and pair["same_best_index"], (name, pair)
+    assert rpt["pairs"]["reference|fp64"]["rms_rel_median"] <= 1e-6
