@@ -104,11 +104,15 @@ typedef struct ps_problem {
     const double *earth;           /* [ndata*3] asteroid->Earth vectors [AU] */
 } ps_problem;
 
+/* ps_options.flags: run the mixed form's shape contraction on the SIMT
+ * pipes even where the tensor-core (tcgen05) contraction applies. */
+#define PS_FLAG_NO_TENSOR 1
+
 typedef struct ps_options {
     int32_t device;        /* CUDA device ordinal */
     int32_t form;          /* ps_form */
     int32_t ctas_per_sm;   /* resident fit slots per SM; 0 = tuned default */
-    int32_t flags;         /* reserved, 0 */
+    int32_t flags;         /* PS_FLAG_* bits, 0 for the defaults */
 } ps_options;
 
 /* One output row (period_search_BOINC.cpp:927-931). */
@@ -146,6 +150,8 @@ typedef struct ps_info {
     double freq_start, freq_step;   /* [1/h] */
     int32_t sm_count, slots;        /* device SMs and resident fit slots */
     int64_t h2d_bytes;              /* bytes ps_prepare copied host -> device */
+    int32_t tensor_cores;           /* 1 when the context's form contracts on the tensor cores */
+    int32_t tile_points;            /* observations per tile of the context's form */
 } ps_info;
 
 /* Device timing of the last ps_scan / ps_fit_batch call, measured with CUDA
@@ -305,6 +311,13 @@ typedef struct ps_learned_opts {
  * be NULL. */
 ps_status ps_scan_learned(ps_ctx *ctx, double conw_r, int64_t n_lo, int64_t n_hi, const float *weights,
                           const ps_learned_opts *opts, ps_row *out, ps_learned_stats *stats);
+
+/* Self-test of the tensor-core primitives of the mixed form (tcgen05 TF32
+ * MMA with A in Tensor Memory and B in shared memory): D = A * B^T for A
+ * 128 x K and B 32 x K (row-major FP32, rounded to TF32 on the device),
+ * D 128 x 32, K a multiple of 8 up to 480.  PS_ERR_TIMEOUT when the MMA
+ * completion was not observed within the wait limit. */
+ps_status ps_tc_selftest(int32_t device, const float *A, const float *B, int32_t K, float *D);
 
 /* ---- replica validator ---- */
 

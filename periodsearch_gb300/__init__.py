@@ -139,11 +139,12 @@ def run_files(in_path: str, out_path: str, state_path: Optional[str] = None, dev
 class Engine:
     """One object prepared on one GPU (ps_prepare .. ps_destroy)."""
 
-    def __init__(self, data: InputData, device: int = 0, form: int = PS_FORM_FP64, ctas_per_sm: int = 0):
+    def __init__(self, data: InputData, device: int = 0, form: int = PS_FORM_FP64, ctas_per_sm: int = 0,
+                 tensor_cores: bool = True):
         self._L = _abi.lib()
         self._prob = data.to_problem()
         self._data = data
-        opt = _abi.Options(device, form, ctas_per_sm, 0)
+        opt = _abi.Options(device, form, ctas_per_sm, 0 if tensor_cores else _abi.PS_FLAG_NO_TENSOR)
         ctx = C.c_void_p()
         _abi.check(self._L.ps_prepare(C.byref(self._prob), C.byref(opt), C.byref(ctx)), "ps_prepare")
         self._ctx = ctx

@@ -16,6 +16,7 @@ PS_ERR_ARG = 1
 PS_ERR_LIMIT = 2
 PS_ERR_SINGULAR = 4
 PS_ERR_IO = 5
+PS_FLAG_NO_TENSOR = 1
 PS_ERR_CUDA = 10
 PS_ERR_NO_DEVICE = 11
 PS_ERR_TIMEOUT = 12
@@ -65,7 +66,8 @@ class Info(C.Structure):
     _fields_ = [("ndata", C.c_int32), ("n_lc", C.c_int32), ("ncoef", C.c_int32), ("ma", C.c_int32),
                 ("mfit", C.c_int32), ("nfac", C.c_int32), ("n_max", C.c_int64), ("escl", C.c_double),
                 ("conw_r0", C.c_double), ("freq_start", C.c_double), ("freq_step", C.c_double),
-                ("sm_count", C.c_int32), ("slots", C.c_int32), ("h2d_bytes", C.c_int64)]
+                ("sm_count", C.c_int32), ("slots", C.c_int32), ("h2d_bytes", C.c_int64),
+                ("tensor_cores", C.c_int32), ("tile_points", C.c_int32)]
 
 
 class LearnedStats(C.Structure):
@@ -124,6 +126,8 @@ SIGNATURES = {
     "ps_mlp_grad": (C.c_int, [C.c_int32, C.POINTER(C.c_float), C.POINTER(C.c_float), C.POINTER(C.c_float),
                               C.c_int64, C.POINTER(C.c_float), C.POINTER(C.c_float)]),
     "ps_screen": (C.c_int, [_CTX, C.c_double, C.c_int64, C.c_int64, C.POINTER(C.c_float), C.POINTER(Fit)]),
+    "ps_tc_selftest": (C.c_int, [C.c_int32, C.POINTER(C.c_float), C.POINTER(C.c_float), C.c_int32,
+                                 C.POINTER(C.c_float)]),
     "ps_validate_rows": (C.c_int, [C.POINTER(Row), C.c_int64, C.POINTER(Row), C.c_int64, C.POINTER(C.c_double),
                                    C.POINTER(ValidateReport)]),
     "ps_validate_files": (C.c_int, [C.c_char_p, C.c_char_p, C.POINTER(C.c_double), C.POINTER(ValidateReport)]),

@@ -136,13 +136,16 @@ ps_status make_plan(ps_ctx *c, int form)
     cudaDeviceProp prop;
     PSG_CUDA(c, cudaGetDeviceProperties(&prop, c->opt.device));
     size_t smem_max = static_cast<size_t>(prop.sharedMemPerBlockOptin);
-    // Mixed form: 32-point tiles (the register tile of the contraction) and
-    // the FP32 basis in shared memory when it fits; FP64 form: 16-point tiles.
+    // Mixed form: 32-point tiles with the tensor-core contraction where the
+    // shape tables allow it, else the SIMT contraction with the FP32 basis in
+    // shared memory when it fits; FP64 form: 16-point tiles.
     const bool mixed = form == PS_FORM_MIXED;
-    int P = mixed ? 32 : 16, dsph_smem = mixed ? 1 : 0;
+    int P = mixed ? 32 : 16, dsph_smem = mixed ? psg::kBasisSmem : psg::kBasisGlobal;
+    if (mixed && !(c->opt.flags & PS_FLAG_NO_TENSOR) && psg::tensor_basis_ok(F, o.ncoef, P))
+        dsph_smem = psg::kBasisTensor;
     psg::SlotLayout L = psg::make_layout(form, o.ma, o.mfit, F, o.ncoef, P, dsph_smem);
-    if (L.bytes > smem_max && dsph_smem) {
-        dsph_smem = 0;
+    if (L.bytes > smem_max && dsph_smem != psg::kBasisGlobal) {
+        dsph_smem = psg::kBasisGlobal;
         L = psg::make_layout(form, o.ma, o.mfit, F, o.ncoef, P, dsph_smem);
     }
     while (L.bytes > smem_max && P > 2) {
@@ -153,19 +156,28 @@ ps_status make_plan(ps_ctx *c, int form)
         c->err = "shared-memory plan of a fit slot exceeds the device limit";
         return PS_ERR_LIMIT;
     }
-    int e = psg::set_kernel_smem(form, L.bytes, o.ncoef);
+    // A tensor-core slot holds up to 512 Tensor Memory columns for its whole
+    // life: request enough shared memory that only one slot fits on an SM.
+    size_t bytes = L.bytes;
+    if (dsph_smem == psg::kBasisTensor)
+        bytes = std::min(smem_max, std::max(bytes, static_cast<size_t>(prop.sharedMemPerMultiprocessor) / 2 + 1024));
+    int e = psg::set_kernel_smem(form, bytes, o.ncoef, dsph_smem);
     if (e != 0) return cuda_fail(c, static_cast<cudaError_t>(e), "cudaFuncSetAttribute");
     int per_sm = 0;
-    e = psg::occupancy_slots(form, L.bytes, o.ncoef, &per_sm);
+    e = psg::occupancy_slots(form, bytes, o.ncoef, dsph_smem, &per_sm);
     if (e != 0) return cuda_fail(c, static_cast<cudaError_t>(e), "occupancy");
     if (per_sm < 1) {
         c->err = "fit slot does not fit on an SM";
         return PS_ERR_LIMIT;
     }
     if (c->opt.ctas_per_sm > 0) per_sm = std::min(per_sm, c->opt.ctas_per_sm);
+    if (dsph_smem == psg::kBasisTensor && per_sm > 1) {
+        c->err = "tensor-core fit slots would share an SM";
+        return PS_ERR_LIMIT;
+    }
     pl.P = P;
     pl.dsph_smem = dsph_smem;
-    pl.smem = L.bytes;
+    pl.smem = bytes;
     pl.slots = per_sm * c->sm_count;
     pl.ready = true;
     return PS_OK;
@@ -214,6 +226,11 @@ ps_status run_fits(ps_ctx *c, double conw_r, psg::FitWork w, int form)
     c->timing.evals = evals;
     c->timing.launches = 1;
     c->launch_total++;
+    for (const ps_fit &f : c->h_fits)
+        if (f.err_code == 16) {
+            c->err = "a tensor-core wait gave up: fit results are incomplete";
+            return PS_ERR_TIMEOUT;
+        }
     return PS_OK;
 }
 
@@ -542,6 +559,9 @@ ps_status ps_get_info(const ps_ctx *c, ps_info *out)
     out->sm_count = c->sm_count;
     out->slots = c->slots;
     out->h2d_bytes = c->h2d_bytes;
+    const FormPlan &pl = c->plan[c->opt.form];
+    out->tensor_cores = pl.ready && pl.dsph_smem == psg::kBasisTensor ? 1 : 0;
+    out->tile_points = pl.ready ? pl.P : 0;
     return PS_OK;
 }
 

@@ -23,6 +23,13 @@
 //      parameters, each alpha element summed over points in data order.
 // The three convexity rows (conv.c) are three more rows of the same
 // contraction with W[c][i] = Darea_i * g_i * n_i[c].
+//
+// The mixed form runs the contraction on the tensor cores when the shape
+// tables allow it (tensor_basis_ok): tcgen05 TF32 MMAs with the basis split
+// into high and low TF32 parts resident in Tensor Memory for the CTA's
+// lifetime (A = [Dsph_hi^T; Dsph_lo^T], 128 lanes x F columns) and W split
+// the same way in shared memory (B), so that the four partial products give
+// the contraction to FP32 accuracy; otherwise on the SIMT pipes.
 #include <cuda_runtime.h>
 
 #include <cmath>
@@ -31,6 +38,7 @@
 #include <type_traits>
 
 #include "ps_engine.h"
+#include "ps_tc.cuh"
 
 namespace psg {
 
@@ -59,8 +67,16 @@ struct Smem {
     using R = typename RealOf<FORM>::T;
     double *cg, *atry, *beta, *da, *alpha, *covar, *area, *gv, *ym, *red, *dave, *col, *misc;
     R *areaR, *gvR, *W, *J, *pt;
+    R *pt2;       // the other point set-up buffer (== pt unless set-up runs one tile ahead)
+    float *accs;  // mixed form: per-point FP32 weights and residuals of a tile
     int *ipiv;
     float *dsph;  // FP32 basis in shared memory (mixed form), or nullptr
+    // tensor-core contraction: operand tiles, MMA-completion barrier, Tensor
+    // Memory address slot and the abort flag set when a wait gives up
+    unsigned char *bhi, *blo;
+    uint64_t *mbar;
+    uint32_t *tslot;
+    int *abort;
 };
 
 template <int FORM>
@@ -81,13 +97,27 @@ __device__ inline Smem<FORM> carve(char *base, const SlotLayout &L)
     s.W = reinterpret_cast<R *>(base + L.W);
     s.J = reinterpret_cast<R *>(base + L.J);
     s.pt = reinterpret_cast<R *>(base + L.pt);
+    s.pt2 = reinterpret_cast<R *>(base + L.pt2);
+    s.accs = reinterpret_cast<float *>(base + L.accs);
     s.ym = reinterpret_cast<double *>(base + L.ym);
     s.red = reinterpret_cast<double *>(base + L.red);
     s.dave = reinterpret_cast<double *>(base + L.dave);
     s.col = reinterpret_cast<double *>(base + L.col);
     s.misc = reinterpret_cast<double *>(base + L.misc);
     s.ipiv = reinterpret_cast<int *>(base + L.ipiv);
-    s.dsph = L.dsph_smem ? reinterpret_cast<float *>(base + L.dsph) : nullptr;
+    s.dsph = L.dsph_smem == kBasisSmem ? reinterpret_cast<float *>(base + L.dsph) : nullptr;
+    if (L.dsph_smem == kBasisTensor) {
+        s.bhi = reinterpret_cast<unsigned char *>(base + L.bhi);
+        s.blo = reinterpret_cast<unsigned char *>(base + L.blo);
+        s.mbar = reinterpret_cast<uint64_t *>(base + L.tcm);
+        s.tslot = reinterpret_cast<uint32_t *>(base + L.tcm + 8);
+        s.abort = reinterpret_cast<int *>(base + L.tcm + 12);
+    } else {
+        s.bhi = s.blo = nullptr;
+        s.mbar = nullptr;
+        s.tslot = nullptr;
+        s.abort = nullptr;
+    }
     return s;
 }
 
@@ -238,7 +268,7 @@ __device__ void accumulate_tile(const DevObject &ob, Smem<FORM> &s, double *M, d
     } else {
         // per point: FP32 weight sig2i*w and residual; chi^2 of the tile
         // summed over one warp in FP64
-        float *dyv = reinterpret_cast<float *>(s.pt);
+        float *dyv = s.accs;
         float *wtp = dyv + 32;
         if (tid < 32) {
             double c2 = 0;
@@ -280,7 +310,7 @@ __device__ void accumulate_tile(const DevObject &ob, Smem<FORM> &s, double *M, d
             bv[j] = acc;
         }
     } else {
-        const float *dyv = reinterpret_cast<const float *>(s.pt);
+        const float *dyv = s.accs;
 #pragma unroll
         for (int u = 0; u < kAccPerThread; u++) {
             const int e = tid + u * NT;
@@ -393,6 +423,230 @@ __device__ void contract_mixed(Smem<PS_FORM_MIXED> &s, const float *dsph, int np
     }
 }
 
+// Point set-up of observation q (bright.c:27-57, phasec.c, matrix.c): the
+// rotated Earth and Sun directions with their beta/lambda/omega derivatives,
+// the phase function and its derivatives, into pt[0..27].
+template <int FORM>
+__device__ inline void setup_point(const DevObject &ob, const FitConfig &cfg, int q, double omg,
+                                   const typename RealOf<FORM>::T (&B)[9], const typename RealOf<FORM>::T (&DB0)[9],
+                                   const typename RealOf<FORM>::T (&DB1)[9], typename RealOf<FORM>::T php0,
+                                   typename RealOf<FORM>::T php1, typename RealOf<FORM>::T php2,
+                                   typename RealOf<FORM>::T *pt)
+{
+    using R = typename RealOf<FORM>::T;
+    constexpr bool kFP64 = FORM == PS_FORM_FP64;
+    const R ee[3] = {R(ob.eex[q]), R(ob.eey[q]), R(ob.eez[q])};
+    const R e0v[3] = {R(ob.e0x[q]), R(ob.e0y[q]), R(ob.e0z[q])};
+    const double td = ob.tim[q];
+    const R t = R(td);
+    const R alpha = R(ob.alpha_pt[q]);
+    R ex;
+    if constexpr (kFP64) ex = exp(-alpha / php1);
+    else ex = expf(-alpha / php1);
+    const R scale = 1 + php0 * ex + php2 * alpha;
+    const double f = rotation_phase<FORM>(omg, td, cfg.phi0);
+    R cf, sf;
+    if constexpr (kFP64) {
+        cf = cos(f);
+        sf = sin(f);
+    } else {
+        sincosf(static_cast<float>(f), &sf, &cf);
+    }
+    const R fm[9] = {cf, sf, R(0), -sf, cf, R(0), R(0), R(0), R(1)};
+    const R dfm[9] = {-t * sf, t * cf, R(0), -t * cf, -t * sf, R(0), R(0), R(0), R(0)};
+    R tm[9], d0[9], d1[9], d2[9];
+#pragma unroll
+    for (int i = 0; i < 3; i++)
+#pragma unroll
+        for (int j = 0; j < 3; j++) {
+            R x = 0, y0 = 0, y1 = 0, y2 = 0;
+#pragma unroll
+            for (int k = 0; k < 3; k++) {
+                x = x + fm[i * 3 + k] * B[k * 3 + j];
+                y0 = y0 + fm[i * 3 + k] * DB0[k * 3 + j];
+                y1 = y1 + fm[i * 3 + k] * DB1[k * 3 + j];
+                y2 = y2 + dfm[i * 3 + k] * B[k * 3 + j];
+            }
+            tm[i * 3 + j] = x;
+            d0[i * 3 + j] = y0;
+            d1[i * 3 + j] = y1;
+            d2[i * 3 + j] = y2;
+        }
+#pragma unroll
+    for (int i = 0; i < 3; i++) {
+        R x = 0, y = 0;
+#pragma unroll
+        for (int j = 0; j < 3; j++) {
+            x = x + tm[i * 3 + j] * ee[j];
+            y = y + tm[i * 3 + j] * e0v[j];
+        }
+        pt[i] = x;
+        pt[3 + i] = y;
+    }
+    // de[i][j] = sum_k dtm[j][i][k] ee[k]; stored de[i*3+j] (j = derivative)
+    const R *dd[3] = {d0, d1, d2};
+#pragma unroll
+    for (int i = 0; i < 3; i++)
+#pragma unroll
+        for (int j = 0; j < 3; j++) {
+            R x = 0, y = 0;
+#pragma unroll
+            for (int k = 0; k < 3; k++) {
+                x = x + dd[j][i * 3 + k] * ee[k];
+                y = y + dd[j][i * 3 + k] * e0v[k];
+            }
+            pt[6 + i * 3 + j] = x;
+            pt[15 + i * 3 + j] = y;
+        }
+    pt[24] = scale;
+    pt[25] = ex;
+    pt[26] = php0 * ex * alpha / (php1 * php1);
+    pt[27] = alpha;
+}
+
+// ---------------------------------------------------------------------------
+// Tensor-core contraction of the mixed form (kBasisTensor).
+// ---------------------------------------------------------------------------
+constexpr uint32_t kTcWaitTries = 1u << 22;   // mbarrier polls before a wait gives up
+constexpr int kErrTcTimeout = 16;             // ps_fit.err_code of a fit cut short by a failed wait
+
+// Accumulator columns [tc_dcol, tc_dcol + 64) follow the basis columns [0, F):
+// column p holds A W_hi^T for point p, column 32 + p holds A W_lo^T.
+__device__ inline uint32_t tc_dcol(int F) { return static_cast<uint32_t>((F + 31) & ~31); }
+
+__device__ inline uint32_t tc_cols(int F)
+{
+    uint32_t n = 32;
+    while (n < tc_dcol(F) + 64) n <<= 1;
+    return n;
+}
+
+// Allocates the CTA's Tensor Memory and loads A = [Dsph_hi^T; Dsph_lo^T]:
+// lane m < 64 holds the TF32 rounding of coefficient m's basis column, lane
+// 64 + m the TF32 rounding of what remains of it (taken from the FP64 basis);
+// column i is facet i.  Returns the Tensor Memory base address.
+template <int NT>
+__device__ uint32_t tc_setup(const DevObject &ob, Smem<PS_FORM_MIXED> &s)
+{
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int F = ob.nfac, C = ob.ncoef;
+    if (warp == 0) tc::tmem_alloc(s.tslot, tc_cols(F));
+    if (tid == 0) {
+        tc::mbar_init(s.mbar, 1);
+        *s.abort = 0;
+    }
+    tc::fence_before_sync();
+    __syncthreads();
+    tc::fence_after_sync();
+    const uint32_t tbase = *s.tslot;
+    if (warp < 4) {
+        const int m = warp * 32 + lane, c = m & 63;
+        const bool low = m >= 64;
+        const uint32_t row = tbase + (static_cast<uint32_t>(warp * 32) << 16);
+        for (int k0 = 0; k0 < F; k0 += 8) {
+            uint32_t v[8];
+#pragma unroll
+            for (int j = 0; j < 8; j++) {
+                const double d = c < C ? ob.dsph[static_cast<size_t>(k0 + j) * C + c] : 0.0;
+                const uint32_t hi = tc::to_tf32(static_cast<float>(d));
+                v[j] = low ? tc::to_tf32(static_cast<float>(d - static_cast<double>(__uint_as_float(hi)))) : hi;
+            }
+            tc::tmem_st8(row + static_cast<uint32_t>(k0), v);
+        }
+        tc::tmem_wait_st();
+    }
+    tc::fence_before_sync();
+    __syncthreads();
+    tc::fence_after_sync();
+    return tbase;
+}
+
+// Releases the Tensor Memory.  After an abandoned wait the MMAs of that
+// phase get one more bounded wait first.
+__device__ void tc_teardown(Smem<PS_FORM_MIXED> &s, uint32_t tbase, int F, uint32_t phase)
+{
+    if (*s.abort && threadIdx.x == 0) tc::mbar_wait(s.mbar, phase, kTcWaitTries);
+    tc::fence_before_sync();
+    __syncthreads();
+    if ((threadIdx.x >> 5) == 0) tc::tmem_dealloc(tbase, tc_cols(F));
+}
+
+// Splits the tile's W rows (row-major FP32, stride wcols) into TF32 high and
+// low parts in the canonical K-major layout -- one 8-row x 4-facet core
+// matrix per warp step, 128 contiguous bytes -- with the low parts as rows
+// 32..63 of the same operand, and issues D = A [W_hi; W_lo]^T as F/8 MMAs of
+// 128 x 64 x 8 (one MMA costs the issuing thread about the same for N = 32
+// and N = 64) followed by a commit to the barrier.
+template <int NT>
+__device__ void contract_tc_issue(Smem<PS_FORM_MIXED> &s, int F, int wcols, uint32_t tbase)
+{
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int kcs = F >> 2;
+    for (int cm = warp; cm < 4 * kcs; cm += NT / 32) {
+        const int pg = cm / kcs, kc = cm - pg * kcs;
+        const float w = s.W[(pg * 8 + (lane >> 2)) * wcols + kc * 4 + (lane & 3)];
+        const uint32_t hi = tc::to_tf32(w);
+        const uint32_t lo = tc::to_tf32(w - __uint_as_float(hi));
+        reinterpret_cast<uint32_t *>(s.bhi + cm * 128)[lane] = hi;
+        reinterpret_cast<uint32_t *>(s.blo + cm * 128)[lane] = lo;
+    }
+    tc::fence_proxy_async();
+    tc::fence_before_sync();
+    __syncthreads();
+    if (tid == 0 && !*s.abort) {
+        tc::fence_after_sync();
+        const uint32_t idesc = tc::idesc_tf32(128, 64);
+        const uint32_t sbo = static_cast<uint32_t>(kcs) * 128;
+        const uint32_t bh = tc::smem_u32(s.bhi), d = tbase + tc_dcol(F);
+        for (int k8 = 0; k8 < F / 8; k8++) {
+            const uint32_t a = tbase + static_cast<uint32_t>(k8) * 8, off = static_cast<uint32_t>(k8) * 256;
+            tc::mma_tf32_ts(d, a, tc::smem_desc(bh + off, 128, sbo), idesc, k8 > 0);
+        }
+        tc::mma_commit(s.mbar);
+    }
+}
+
+// Waits for the tile's MMAs, stages the accumulator (lane m = row m) in
+// shared memory and writes J[p][k] = Scale_p (D[k][p] + D[k][32 + p] +
+// D[64 + k][p] + D[64 + k][32 + p]): basis high and low parts times W high
+// and low parts.  A wait that gives up sets the abort flag; the caller ends
+// the fit.
+template <int NT>
+__device__ void contract_tc_finish(Smem<PS_FORM_MIXED> &s, int np, int F, int C, int ma, bool conv, uint32_t tbase,
+                                   uint32_t &phase)
+{
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    if (*s.abort) return;
+    const bool ok = __syncthreads_and(tc::mbar_wait(s.mbar, phase, kTcWaitTries));
+    if (!ok) {
+        if (tid == 0) *s.abort = 1;
+        __syncthreads();
+        return;
+    }
+    phase ^= 1u;
+    tc::fence_after_sync();
+    float *X = reinterpret_cast<float *>(s.bhi);
+    if (warp < 4) {
+        const uint32_t taddr = tbase + (static_cast<uint32_t>(warp * 32) << 16) + tc_dcol(F);
+        float *xr = X + (warp * 32 + lane) * 65;
+#pragma unroll 1
+        for (int q = 0; q < 8; q++) {
+            uint32_t v[8];
+            tc::tmem_ld8(taddr + 8 * q, v);
+            tc::tmem_wait_ld();
+#pragma unroll
+            for (int j = 0; j < 8; j++) xr[8 * q + j] = __uint_as_float(v[j]);
+        }
+    }
+    __syncthreads();
+    for (int e = tid; e < np * C; e += NT) {
+        const int p = e / C, k = e - p * C;
+        const float sc = conv ? 1.f : s.pt[p * kPointStride + 24];
+        const float *xh = X + k * 65, *xl = X + (64 + k) * 65;
+        s.J[p * ma + k] = sc * ((xh[p] + xh[32 + p]) + (xl[p] + xl[32 + p]));
+    }
+}
+
 // ---------------------------------------------------------------------------
 // Model evaluation (mrqcof) at parameters a[] into matrix M (mfit x mfit,
 // lower triangle accumulated then mirrored) and vector bv.  Leaves chi^2,
@@ -400,10 +654,14 @@ __device__ void contract_mixed(Smem<PS_FORM_MIXED> &s, const float *dsph, int np
 // ---------------------------------------------------------------------------
 template <int FORM, int KU>
 __device__ void evaluate(const DevObject &ob, const FitConfig &cfg, const SlotLayout &L, Smem<FORM> &s,
-                         const double *a, double *M, double *bv, typename RealOf<FORM>::T *scratch)
+                         const double *a, double *M, double *bv, typename RealOf<FORM>::T *scratch, uint32_t tbase,
+                         uint32_t &tc_phase)
 {
     using R = typename RealOf<FORM>::T;
     constexpr bool kFP64 = FORM == PS_FORM_FP64;
+    // tensor-core path: the point set-up of the next tile runs on warps 1..15
+    // while thread 0 issues the current tile's MMAs
+    constexpr bool kPipe = !kFP64 && KU == 0;
     constexpr int NT = threads_of<FORM>();
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int F = ob.nfac, C = ob.ncoef, ma = ob.ma, mf = ob.mfit, P = L.P;
@@ -478,6 +736,13 @@ __device__ void evaluate(const DevObject &ob, const FitConfig &cfg, const SlotLa
     int tiles_since_flush = 0;
     const float *dsphF = nullptr;
     if constexpr (!kFP64) dsphF = s.dsph ? s.dsph : ob.dsph_f;
+    // thread of point sp of a set-up that runs beside the MMA issue (warps 1..15)
+    const int pipe_sp = lane * (NT / 32 - 1) + (warp - 1);
+    if constexpr (kPipe) {
+        if (ob.n_lc > 1 && warp > 0 && pipe_sp < min(P, ob.lc_npts[0]))
+            setup_point<FORM>(ob, cfg, ob.lc_start[0] + pipe_sp, omg, B, DB0, DB1, php0, php1, php2,
+                              s.pt + pipe_sp * kPointStride);
+    }
 
     for (int lc = 0; lc < ob.n_lc; lc++) {
         const int start = ob.lc_start[lc], npts = ob.lc_npts[lc];
@@ -491,79 +756,14 @@ __device__ void evaluate(const DevObject &ob, const FitConfig &cfg, const SlotLa
         for (int t0 = 0; t0 < npts; t0 += P) {
             const int np = min(P, npts - t0);
             if (!conv) {
-                // 1. point set-up (bright.c:27-57, phasec.c, matrix.c)
-                // point sp is set up by thread setup_thread(sp) == tid
-                const int sp = (tid % 32) * (NT / 32) + tid / 32;
-                if (sp < np) {
-                    const int q = start + t0 + sp;
-                    const R ee[3] = {R(ob.eex[q]), R(ob.eey[q]), R(ob.eez[q])};
-                    const R e0v[3] = {R(ob.e0x[q]), R(ob.e0y[q]), R(ob.e0z[q])};
-                    const double td = ob.tim[q];
-                    const R t = R(td);
-                    const R alpha = R(ob.alpha_pt[q]);
-                    R ex;
-                    if constexpr (kFP64) ex = exp(-alpha / php1);
-                    else ex = expf(-alpha / php1);
-                    const R scale = 1 + php0 * ex + php2 * alpha;
-                    const double f = rotation_phase<FORM>(omg, td, cfg.phi0);
-                    R cf, sf;
-                    if constexpr (kFP64) {
-                        cf = cos(f);
-                        sf = sin(f);
-                    } else {
-                        sincosf(static_cast<float>(f), &sf, &cf);
-                    }
-                    const R fm[9] = {cf, sf, R(0), -sf, cf, R(0), R(0), R(0), R(1)};
-                    const R dfm[9] = {-t * sf, t * cf, R(0), -t * cf, -t * sf, R(0), R(0), R(0), R(0)};
-                    R tm[9], d0[9], d1[9], d2[9];
-#pragma unroll
-                    for (int i = 0; i < 3; i++)
-#pragma unroll
-                        for (int j = 0; j < 3; j++) {
-                            R x = 0, y0 = 0, y1 = 0, y2 = 0;
-#pragma unroll
-                            for (int k = 0; k < 3; k++) {
-                                x = x + fm[i * 3 + k] * B[k * 3 + j];
-                                y0 = y0 + fm[i * 3 + k] * DB0[k * 3 + j];
-                                y1 = y1 + fm[i * 3 + k] * DB1[k * 3 + j];
-                                y2 = y2 + dfm[i * 3 + k] * B[k * 3 + j];
-                            }
-                            tm[i * 3 + j] = x;
-                            d0[i * 3 + j] = y0;
-                            d1[i * 3 + j] = y1;
-                            d2[i * 3 + j] = y2;
-                        }
-                    R *pt = s.pt + sp * kPointStride;
-#pragma unroll
-                    for (int i = 0; i < 3; i++) {
-                        R x = 0, y = 0;
-#pragma unroll
-                        for (int j = 0; j < 3; j++) {
-                            x = x + tm[i * 3 + j] * ee[j];
-                            y = y + tm[i * 3 + j] * e0v[j];
-                        }
-                        pt[i] = x;
-                        pt[3 + i] = y;
-                    }
-                    // de[i][j] = sum_k dtm[j][i][k] ee[k]; stored de[i*3+j] (j = derivative)
-                    const R *dd[3] = {d0, d1, d2};
-#pragma unroll
-                    for (int i = 0; i < 3; i++)
-#pragma unroll
-                        for (int j = 0; j < 3; j++) {
-                            R x = 0, y = 0;
-#pragma unroll
-                            for (int k = 0; k < 3; k++) {
-                                x = x + dd[j][i * 3 + k] * ee[k];
-                                y = y + dd[j][i * 3 + k] * e0v[k];
-                            }
-                            pt[6 + i * 3 + j] = x;
-                            pt[15 + i * 3 + j] = y;
-                        }
-                    pt[24] = scale;
-                    pt[25] = ex;
-                    pt[26] = php0 * ex * alpha / (php1 * php1);
-                    pt[27] = alpha;
+                // 1. point set-up (bright.c:27-57, phasec.c, matrix.c), one
+                // thread per point spread over the warps; with the tensor
+                // cores it was done during the previous tile's MMAs
+                if constexpr (!kPipe) {
+                    const int sp = (tid % 32) * (NT / 32) + tid / 32;
+                    if (sp < np)
+                        setup_point<FORM>(ob, cfg, start + t0 + sp, omg, B, DB0, DB1, php0, php1, php2,
+                                          s.pt + sp * kPointStride);
                 }
                 __syncthreads();
                 // 2. facet stage (bright.c:59-120), one warp per point
@@ -645,14 +845,19 @@ __device__ void evaluate(const DevObject &ob, const FitConfig &cfg, const SlotLa
                     for (int i = 0; i < F; i++) acc = acc + Wp[i] * ds[static_cast<size_t>(i) * C];
                     s.J[p * ma + k] = conv ? acc : s.pt[p * kPointStride + 24] * acc;
                 }
+            } else if constexpr (KU == 0) {
+                contract_tc_issue<NT>(s, F, wcols, tbase);   // the work below overlaps the MMAs
             } else {
                 if (s.dsph)
                     contract_mixed<NT, KU, true>(s, dsphF, np, F, C, ma, wcols, conv);
                 else
                     contract_mixed<NT, KU, false>(s, dsphF, np, F, C, ma, wcols, conv);
             }
-            if (tid < np) {
-                const int p = tid;
+            // remaining columns of J: one thread per point (not thread 0 on the
+            // tensor-core path: it issues the MMAs)
+            const int jp = kPipe ? (tid + 32) % NT : tid;
+            if (jp < np) {
+                const int p = jp;
                 R *Jp = s.J + p * ma;
                 const double *rd = s.red + p * kRedStride;
                 if (!conv) {
@@ -674,7 +879,22 @@ __device__ void evaluate(const DevObject &ob, const FitConfig &cfg, const SlotLa
                     s.misc[M_CHK + p] = rd[0];
                 }
             }
+            bool next_setup = false;
+            if constexpr (kPipe) {
+                // point set-up of the next tile into the other buffer
+                const int nlc = t0 + P < npts ? lc : lc + 1, nt0 = t0 + P < npts ? t0 + P : 0;
+                next_setup = nlc < ob.n_lc - 1;   // the last lightcurve is the convexity rows
+                if (next_setup && warp > 0 && pipe_sp < min(P, ob.lc_npts[nlc] - nt0))
+                    setup_point<FORM>(ob, cfg, ob.lc_start[nlc] + nt0 + pipe_sp, omg, B, DB0, DB1, php0, php1, php2,
+                                      s.pt2 + pipe_sp * kPointStride);
+                contract_tc_finish<NT>(s, np, F, C, ma, conv, tbase, tc_phase);
+            }
             __syncthreads();
+            if (next_setup) {
+                R *t = s.pt;
+                s.pt = s.pt2;
+                s.pt2 = t;
+            }
             if (rel) {
                 // 4a. lightcurve sums and a copy of the rows (mrqcof.c:51-88)
                 R *dst = scratch + static_cast<size_t>(t0) * (ma + 1);
@@ -957,8 +1177,9 @@ __device__ float mlp_predict_warp(const float *W, const float *f, float *sh)
 template <int FORM, int KU>
 __device__ void run_fit(const DevObject &ob, const FitConfig &cfg, const SlotLayout &L, Smem<FORM> &s,
                         typename RealOf<FORM>::T *scratch, int64_t n, int pole, ps_fit *out, const FitWork &w,
-                        long long fidx)
+                        long long fidx, uint32_t tbase, uint32_t &tc_phase)
 {
+    constexpr bool kTensor = FORM == PS_FORM_MIXED && KU == 0;
     constexpr int NT = threads_of<FORM>();
     const int tid = threadIdx.x;
     const int C = ob.ncoef, ma = ob.ma, mf = ob.mfit;
@@ -993,7 +1214,13 @@ __device__ void run_fit(const DevObject &ob, const FitConfig &cfg, const SlotLay
         bool accepted = false;
         if (alamda < 0) {
             alamda = cfg.alamda_start;
-            evaluate<FORM, KU>(ob, cfg, L, s, s.cg, s.alpha, s.beta, scratch);
+            evaluate<FORM, KU>(ob, cfg, L, s, s.cg, s.alpha, s.beta, scratch, tbase, tc_phase);
+            if constexpr (kTensor) {
+                if (*s.abort) {
+                    last_err = kErrTcTimeout;
+                    break;
+                }
+            }
             ochisq = s.misc[M_CHISQ];
             hist[0] = ochisq;
             area_first = s.misc[M_AREA];
@@ -1031,7 +1258,13 @@ __device__ void run_fit(const DevObject &ob, const FitConfig &cfg, const SlotLay
                 s.atry[l] = s.cg[l] + s.da[j];
             }
             __syncthreads();
-            evaluate<FORM, KU>(ob, cfg, L, s, s.atry, s.covar, s.da, scratch);
+            evaluate<FORM, KU>(ob, cfg, L, s, s.atry, s.covar, s.da, scratch, tbase, tc_phase);
+            if constexpr (kTensor) {
+                if (*s.abort) {
+                    last_err = kErrTcTimeout;
+                    break;
+                }
+            }
             chisq = s.misc[M_CHISQ];
             area_trial = s.misc[M_AREA];
             for (int c = 0; c < 3; c++) chk_trial[c] = s.misc[M_CHK + c];
@@ -1132,8 +1365,11 @@ __global__ void __launch_bounds__(threads_of<FORM>(), 1)
     extern __shared__ __align__(16) char smem[];
     const SlotLayout L = make_layout(FORM, ob.ma, ob.mfit, ob.nfac, ob.ncoef, P, dsph_smem);
     Smem<FORM> s = carve<FORM>(smem, L);
+    constexpr bool kTensor = FORM == PS_FORM_MIXED && KU == 0;
     if (s.dsph)
         for (int e = threadIdx.x; e < ob.nfac * ob.ncoef; e += NT) s.dsph[e] = ob.dsph_f[e];
+    uint32_t tbase = 0, tc_phase = 0;
+    if constexpr (kTensor) tbase = tc_setup<NT>(ob, s);
     R *scratch = reinterpret_cast<R *>(w.scratch + static_cast<size_t>(blockIdx.x) * w.scratch_stride);
     __shared__ long long next;
     for (;;) {
@@ -1142,6 +1378,9 @@ __global__ void __launch_bounds__(threads_of<FORM>(), 1)
         const long long f = next;
         __syncthreads();
         if (f >= w.nfits) break;
+        if constexpr (kTensor) {
+            if (*s.abort) break;
+        }
         int64_t n;
         int pole;
         if (w.period_index) {
@@ -1151,8 +1390,9 @@ __global__ void __launch_bounds__(threads_of<FORM>(), 1)
             n = w.n_lo + f / PS_N_POLES;
             pole = static_cast<int>(f % PS_N_POLES) + 1;
         }
-        run_fit<FORM, KU>(ob, cfg, L, s, scratch, n, pole, w.out + f, w, f);
+        run_fit<FORM, KU>(ob, cfg, L, s, scratch, n, pole, w.out + f, w, f, tbase, tc_phase);
     }
+    if constexpr (kTensor) tc_teardown(s, tbase, ob.nfac, tc_phase);
 }
 
 template <int FORM, int KU>
@@ -1165,11 +1405,22 @@ __global__ void __launch_bounds__(threads_of<FORM>(), 1) eval_kernel(DevObject o
     extern __shared__ __align__(16) char smem[];
     const SlotLayout L = make_layout(FORM, ob.ma, ob.mfit, ob.nfac, ob.ncoef, P, dsph_smem);
     Smem<FORM> s = carve<FORM>(smem, L);
+    constexpr bool kTensor = FORM == PS_FORM_MIXED && KU == 0;
     if (s.dsph)
         for (int e = threadIdx.x; e < ob.nfac * ob.ncoef; e += NT) s.dsph[e] = ob.dsph_f[e];
+    uint32_t tbase = 0, tc_phase = 0;
+    if constexpr (kTensor) tbase = tc_setup<NT>(ob, s);
     for (int i = threadIdx.x; i < ob.ma; i += NT) s.cg[i] = cg[i];
     __syncthreads();
-    evaluate<FORM, KU>(ob, cfg, L, s, s.cg, s.alpha, s.beta, reinterpret_cast<R *>(scratch));
+    evaluate<FORM, KU>(ob, cfg, L, s, s.cg, s.alpha, s.beta, reinterpret_cast<R *>(scratch), tbase, tc_phase);
+    if constexpr (kTensor) {
+        const bool aborted = *s.abort != 0;
+        tc_teardown(s, tbase, ob.nfac, tc_phase);
+        if (aborted) {
+            if (threadIdx.x == 0) *chisq = NAN;
+            return;
+        }
+    }
     const int mf = ob.mfit;
     for (int e = threadIdx.x; e < mf * mf; e += NT) alpha[e] = s.alpha[e];
     for (int j = threadIdx.x; j < mf; j += NT) beta[j] = s.beta[j];
@@ -1297,19 +1548,28 @@ int launch_fits_noalloc(int form, const DevObject &ob, const FitConfig &cfg, Fit
 
 namespace {
 
-// Coefficient slots per lane of the mixed contraction: 1 for C <= 64, 2 up
-// to 128 (the largest Laplace series, L = 10, has 121 coefficients).
-inline int ku_of(int ncoef) { return ncoef <= 64 ? 1 : 2; }
+// Mixed-form kernel variant: 0 = tensor-core contraction; otherwise the
+// SIMT contraction's coefficient slots per lane, 1 for C <= 64 and 2 up to
+// 128 (the largest Laplace series, L = 10, has 121 coefficients).
+inline int ku_of(int ncoef, int dsph_smem)
+{
+    if (dsph_smem == kBasisTensor) return 0;
+    return ncoef <= 64 ? 1 : 2;
+}
 
 template <class Fn>
-cudaError_t for_mixed(int ncoef, Fn fn)
+cudaError_t for_mixed(int ncoef, int dsph_smem, Fn fn)
 {
-    return ku_of(ncoef) == 1 ? fn(std::integral_constant<int, 1>{}) : fn(std::integral_constant<int, 2>{});
+    switch (ku_of(ncoef, dsph_smem)) {
+    case 0: return fn(std::integral_constant<int, 0>{});
+    case 1: return fn(std::integral_constant<int, 1>{});
+    default: return fn(std::integral_constant<int, 2>{});
+    }
 }
 
 }  // namespace
 
-int set_kernel_smem(int form, size_t smem, int ncoef)
+int set_kernel_smem(int form, size_t smem, int ncoef, int dsph_smem)
 {
     cudaError_t e;
     const int bytes = static_cast<int>(smem);
@@ -1318,7 +1578,7 @@ int set_kernel_smem(int form, size_t smem, int ncoef)
         if (e == cudaSuccess)
             e = cudaFuncSetAttribute(eval_kernel<PS_FORM_FP64, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
     } else if (form == PS_FORM_MIXED) {
-        e = for_mixed(ncoef, [&](auto ku) {
+        e = for_mixed(ncoef, dsph_smem, [&](auto ku) {
             constexpr int KU = decltype(ku)::value;
             cudaError_t r = cudaFuncSetAttribute(fit_kernel<PS_FORM_MIXED, KU>,
                                                  cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
@@ -1333,13 +1593,13 @@ int set_kernel_smem(int form, size_t smem, int ncoef)
     return static_cast<int>(e);
 }
 
-int occupancy_slots(int form, size_t smem, int ncoef, int *per_sm)
+int occupancy_slots(int form, size_t smem, int ncoef, int dsph_smem, int *per_sm)
 {
     if (form == PS_FORM_FP64)
         return static_cast<int>(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
             per_sm, fit_kernel<PS_FORM_FP64, 1>, threads_of<PS_FORM_FP64>(), smem));
     if (form == PS_FORM_MIXED)
-        return static_cast<int>(for_mixed(ncoef, [&](auto ku) {
+        return static_cast<int>(for_mixed(ncoef, dsph_smem, [&](auto ku) {
             constexpr int KU = decltype(ku)::value;
             return cudaOccupancyMaxActiveBlocksPerMultiprocessor(per_sm, fit_kernel<PS_FORM_MIXED, KU>,
                                                                  threads_of<PS_FORM_MIXED>(), smem);
@@ -1354,7 +1614,7 @@ int launch_fits(int form, const DevObject &ob, const FitConfig &cfg, const FitWo
     if (form == PS_FORM_FP64) {
         fit_kernel<PS_FORM_FP64, 1><<<grid, threads_of<PS_FORM_FP64>(), smem, st>>>(ob, cfg, w, P, 0);
     } else if (form == PS_FORM_MIXED) {
-        for_mixed(ob.ncoef, [&](auto ku) {
+        for_mixed(ob.ncoef, dsph_smem, [&](auto ku) {
             constexpr int KU = decltype(ku)::value;
             fit_kernel<PS_FORM_MIXED, KU><<<grid, threads_of<PS_FORM_MIXED>(), smem, st>>>(ob, cfg, w, P, dsph_smem);
             return cudaSuccess;
@@ -1373,7 +1633,7 @@ int launch_eval(int form, const DevObject &ob, const FitConfig &cfg, const doubl
         eval_kernel<PS_FORM_FP64, 1><<<1, threads_of<PS_FORM_FP64>(), smem, st>>>(ob, cfg, cg, alpha, beta, chisq,
                                                                                    area, scratch, P, 0);
     } else if (form == PS_FORM_MIXED) {
-        for_mixed(ob.ncoef, [&](auto ku) {
+        for_mixed(ob.ncoef, dsph_smem, [&](auto ku) {
             constexpr int KU = decltype(ku)::value;
             eval_kernel<PS_FORM_MIXED, KU><<<1, threads_of<PS_FORM_MIXED>(), smem, st>>>(
                 ob, cfg, cg, alpha, beta, chisq, area, scratch, P, dsph_smem);

@@ -67,9 +67,17 @@ constexpr int kMlpMu = 0, kMlpSd = kFeat, kMlpW1 = 2 * kFeat, kMlpB1 = kMlpW1 + 
 // Shared-memory plan of a fit slot; identical on host and device.  Offsets
 // are in bytes; every block starts on a 16-byte boundary.  Blocks of type
 // "real" hold doubles in the FP64 form and floats in the mixed form.
+// Where the mixed form's shape contraction takes the basis Dsph from
+// (SlotLayout::dsph_smem): global memory, shared memory (both with the SIMT
+// contraction), or Tensor Memory with the tcgen05 contraction.
+enum BasisMode : int { kBasisGlobal = 0, kBasisSmem = 1, kBasisTensor = 2 };
+
 struct SlotLayout {
     int form, ma, mfit, nfac, ncoef, P, wcols, dsph_smem;
     size_t cg, atry, beta, da, alpha, covar, area, gv, areaR, gvR, W, J, pt, ym, red, dave, col, misc, ipiv, dsph;
+    size_t bhi, blo, tcm;   // tensor-core operand tiles (TF32 high/low parts) and barrier/TMEM slot
+    size_t pt2;             // second point set-up buffer (tensor-core path: next tile's set-up)
+    size_t accs;            // per-point weights and residuals of the accumulation (mixed form)
     size_t bytes;
 };
 
@@ -105,6 +113,9 @@ PSG_HD inline SlotLayout make_layout(int form, int ma, int mfit, int nfac, int n
     L.P = P;
     L.dsph_smem = dsph_smem;
     L.wcols = ((nfac > mfit ? nfac : mfit) + 3) & ~3;
+    // the tensor-core path reads W in 8-row x 4-column blocks: rows 4 banks apart
+    if (dsph_smem == kBasisTensor)
+        while (L.wcols % 32 != 4) L.wcols += 4;
     const size_t rs = form == PS_FORM_MIXED ? sizeof(float) : sizeof(double);
     size_t o = 0;
     auto take = [&o](size_t bytes) {
@@ -132,7 +143,22 @@ PSG_HD inline SlotLayout make_layout(int form, int ma, int mfit, int nfac, int n
     L.col = take((mfit + 1) * d);
     L.misc = take(kMisc * d);
     L.ipiv = take(sizeof(int) * static_cast<size_t>(mfit + 2 + 16));
-    L.dsph = dsph_smem ? take(static_cast<size_t>(nfac) * ncoef * sizeof(float)) : 0;
+    L.dsph = dsph_smem == kBasisSmem ? take(static_cast<size_t>(nfac) * ncoef * sizeof(float)) : 0;
+    if (dsph_smem == kBasisTensor) {
+        // B = [W_hi; W_lo]: 2P rows, the low parts right after the high parts
+        // (8-row groups stride-byte-offset apart); the accumulator rows are
+        // staged over it for the epilogue
+        const size_t tile = static_cast<size_t>(P) * nfac * sizeof(float);
+        const size_t readback = 128 * 65 * sizeof(float);
+        L.bhi = take(2 * tile > readback ? 2 * tile : readback);
+        L.blo = L.bhi + tile;
+        L.tcm = take(16);
+        L.pt2 = take(static_cast<size_t>(P) * kPointStride * rs);
+    } else {
+        L.bhi = L.blo = L.tcm = 0;
+        L.pt2 = L.pt;
+    }
+    L.accs = form == PS_FORM_MIXED ? take(2 * static_cast<size_t>(P) * sizeof(float)) : 0;
     L.bytes = o;
     return L;
 }
@@ -143,8 +169,16 @@ int launch_fits(int form, const DevObject &ob, const FitConfig &cfg, const FitWo
 int launch_eval(int form, const DevObject &ob, const FitConfig &cfg, const double *cg, double *alpha,
                 double *beta, double *chisq, double *area, double *scratch, int P, size_t smem,
                 int dsph_smem, void *stream);
-int set_kernel_smem(int form, size_t smem, int ncoef);
-int occupancy_slots(int form, size_t smem, int ncoef, int *per_sm);
+int set_kernel_smem(int form, size_t smem, int ncoef, int dsph_smem);
+int occupancy_slots(int form, size_t smem, int ncoef, int dsph_smem, int *per_sm);
+// Whether the tcgen05 contraction supports an object's shape tables: at most
+// 64 coefficients (the high and low TF32 parts of the basis fill 128 Tensor
+// Memory lanes), a facet count that is a multiple of 8 and leaves 64
+// accumulator columns within 512, and 32-point tiles.
+PSG_HD inline bool tensor_basis_ok(int nfac, int ncoef, int P)
+{
+    return ncoef <= 64 && nfac % 8 == 0 && ((nfac + 31) & ~31) + 64 <= 512 && P == 32;
+}
 int measure_fma_peaks(double *fp64_tflops, double *fp32_tflops, void *stream);
 // Learned early stop (ps_mlp.cu).
 int mlp_train(float *h_P, const float *h_x, const float *h_y, int n, int epochs, int batch, float lr, uint64_t seed,

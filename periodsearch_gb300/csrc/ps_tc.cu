@@ -1,0 +1,123 @@
+// ps_tc.cu -- self-test of the tcgen05 primitives that the mixed form's
+// shape contraction uses: one CTA stages A (128 x K) in Tensor Memory and B
+// (32 x K) in shared memory in the canonical layout, runs K/8 TF32 MMAs of
+// shape 128 x 32 x 8 into a Tensor Memory accumulator and reads D = A B^T
+// back.  Exposed through the C ABI so that tests can check the operand and
+// accumulator layouts against exact integer products.
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "ps_gb300.h"
+#include "ps_tc.cuh"
+
+namespace psg {
+namespace {
+
+constexpr uint32_t kTmemCols = 512;
+constexpr uint32_t kDCol = 480;             // accumulator columns [480, 512)
+constexpr uint32_t kWaitTries = 1u << 22;   // mbarrier polls before giving up
+
+__global__ void __launch_bounds__(128, 1)
+tc_selftest_kernel(const float *A, const float *B, int K, float *D, int *status)
+{
+    extern __shared__ __align__(1024) unsigned char sm[];
+    uint64_t *mbar = reinterpret_cast<uint64_t *>(sm);
+    uint32_t *slot = reinterpret_cast<uint32_t *>(sm + 8);
+    unsigned char *bs = sm + 1024;
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    if (warp == 0) tc::tmem_alloc(slot, kTmemCols);
+    if (tid == 0) tc::mbar_init(mbar, 1);
+    for (int e = tid; e < 32 * K; e += 128) {
+        const int r = e / K, k = e - r * K;
+        *reinterpret_cast<uint32_t *>(bs + tc::canon_offset(r, k, K)) = tc::to_tf32(B[e]);
+    }
+    tc::fence_proxy_async();
+    tc::fence_before_sync();
+    __syncthreads();
+    tc::fence_after_sync();
+    const uint32_t tbase = *slot;
+    const uint32_t lane_base = static_cast<uint32_t>(warp * 32) << 16;
+    const int m = warp * 32 + lane;
+    for (int k0 = 0; k0 < K; k0 += 8) {
+        uint32_t v[8];
+#pragma unroll
+        for (int j = 0; j < 8; j++) v[j] = tc::to_tf32(A[static_cast<size_t>(m) * K + k0 + j]);
+        tc::tmem_st8(tbase + lane_base + static_cast<uint32_t>(k0), v);
+    }
+    tc::tmem_wait_st();
+    tc::fence_before_sync();
+    __syncthreads();
+    tc::fence_after_sync();
+    if (tid == 0) {
+        const uint32_t idesc = tc::idesc_tf32(128, 32);
+        const uint32_t b0 = tc::smem_u32(bs);
+        for (int k8 = 0; k8 < K / 8; k8++) {
+            const uint64_t bd = tc::smem_desc(b0 + static_cast<uint32_t>(k8) * 256, 128, static_cast<uint32_t>(K / 4) * 128);
+            tc::mma_tf32_ts(tbase + kDCol, tbase + static_cast<uint32_t>(k8) * 8, bd, idesc, k8 > 0);
+        }
+        tc::mma_commit(mbar);
+    }
+    const bool ok = __syncthreads_and(tc::mbar_wait(mbar, 0, kWaitTries));
+    tc::fence_after_sync();
+    if (ok) {
+#pragma unroll
+        for (int c0 = 0; c0 < 32; c0 += 8) {
+            uint32_t v[8];
+            tc::tmem_ld8(tbase + lane_base + kDCol + c0, v);
+            tc::tmem_wait_ld();
+#pragma unroll
+            for (int j = 0; j < 8; j++) D[m * 32 + c0 + j] = __uint_as_float(v[j]);
+        }
+    } else if (tid == 0) {
+        atomicOr(status, 1);
+        // the MMAs may still be in flight: give them another bounded wait
+        // before the columns are released
+        tc::mbar_wait(mbar, 0, kWaitTries);
+    }
+    tc::fence_before_sync();
+    __syncthreads();
+    if (warp == 0) tc::tmem_dealloc(tbase, kTmemCols);
+}
+
+}  // namespace
+}  // namespace psg
+
+extern "C" ps_status ps_tc_selftest(int32_t device, const float *A, const float *B, int32_t K, float *D)
+{
+    if (!A || !B || !D || K < 8 || K > 480 || K % 8) return PS_ERR_ARG;
+    if (cudaSetDevice(device) != cudaSuccess) return PS_ERR_NO_DEVICE;
+    float *dA = nullptr, *dB = nullptr, *dD = nullptr;
+    int *dS = nullptr;
+    ps_status st = PS_OK;
+    const size_t smem = 1024 + static_cast<size_t>(32) * K * 4;
+    int hs = 0;
+    if (cudaMalloc(&dA, sizeof(float) * 128 * K) != cudaSuccess || cudaMalloc(&dB, sizeof(float) * 32 * K) != cudaSuccess ||
+        cudaMalloc(&dD, sizeof(float) * 128 * 32) != cudaSuccess || cudaMalloc(&dS, sizeof(int)) != cudaSuccess) {
+        st = PS_ERR_CUDA;
+        goto done;
+    }
+    cudaMemcpy(dA, A, sizeof(float) * 128 * K, cudaMemcpyHostToDevice);
+    cudaMemcpy(dB, B, sizeof(float) * 32 * K, cudaMemcpyHostToDevice);
+    cudaMemset(dD, 0, sizeof(float) * 128 * 32);
+    cudaMemset(dS, 0, sizeof(int));
+    if (cudaFuncSetAttribute(psg::tc_selftest_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             static_cast<int>(smem)) != cudaSuccess) {
+        st = PS_ERR_CUDA;
+        goto done;
+    }
+    psg::tc_selftest_kernel<<<1, 128, smem>>>(dA, dB, K, dD, dS);
+    if (cudaDeviceSynchronize() != cudaSuccess) {
+        st = PS_ERR_CUDA;
+        goto done;
+    }
+    cudaMemcpy(D, dD, sizeof(float) * 128 * 32, cudaMemcpyDeviceToHost);
+    cudaMemcpy(&hs, dS, sizeof(int), cudaMemcpyDeviceToHost);
+    if (hs) st = PS_ERR_TIMEOUT;
+done:
+    cudaFree(dA);
+    cudaFree(dB);
+    cudaFree(dD);
+    cudaFree(dS);
+    return st;
+}

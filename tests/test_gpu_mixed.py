@@ -80,22 +80,28 @@ def test_mixed_scan_matches_reference(mixed, case):
 
 
 def test_mixed_finds_truth_period(engine_lib, tmp_path):
-    """On a synthetic object (seeded c0 generator) both forms put the best
-    period of a window around the true period on the same index."""
+    """On a synthetic object (seeded c0 generator, a window of 25 periods
+    around the true period) the refined mixed scan puts the best period on
+    the FP64 scan's index; the plain mixed scan's best is that one or a near
+    tie (its FP64 rms within 1 % of the minimum: 200 sparse points leave the
+    rms landscape flat to a few 1e-3)."""
     from periodsearch_gb300 import Engine, PS_FORM_FP64, PS_FORM_MIXED, read_input, synth
 
     obj = synth.write_object(tmp_path / "period_search_in", "c0")
     data = read_input(tmp_path / "period_search_in")
-    best = {}
-    for form in (PS_FORM_FP64, PS_FORM_MIXED):
-        with Engine(data, form=form) as eng:
-            conw_r, _ = eng.precalc_conw()
-            # trial period closest to the truth: freq = freq_start - (n-1) step
-            n_truth = int(round((eng.info.freq_start - 1 / obj.truth["period_h"]) / eng.info.freq_step)) + 1
-            lo = max(1, n_truth - 12)
-            rows = eng.scan(conw_r, lo, min(int(eng.info.n_max), n_truth + 12))
-            best[form] = lo + int(np.argmin(rows["rms"]))
-    assert best[PS_FORM_FP64] == best[PS_FORM_MIXED]
+    with Engine(data, form=PS_FORM_FP64) as e64:
+        conw_r, _ = e64.precalc_conw()
+        # trial period closest to the truth: freq = freq_start - (n-1) step
+        n_truth = int(round((e64.info.freq_start - 1 / obj.truth["period_h"]) / e64.info.freq_step)) + 1
+        lo, hi = max(1, n_truth - 12), min(int(e64.info.n_max), n_truth + 12)
+        full = e64.scan(conw_r, lo, hi)
+    with Engine(data, form=PS_FORM_MIXED) as eng:
+        assert eng.precalc_conw()[0] == conw_r
+        mixed = eng.scan(conw_r, lo, hi)
+        refined, st = eng.scan_refined(conw_r, lo, hi)
+    b64 = int(np.argmin(full["rms"]))
+    assert int(st["best_index"]) == lo + b64 and int(np.argmin(refined["rms"])) == b64
+    assert full["rms"][int(np.argmin(mixed["rms"]))] <= full["rms"][b64] * (1 + 1e-2)
 
 
 def test_refined_golden134(mixed):

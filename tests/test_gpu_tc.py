@@ -1,0 +1,60 @@
+"""The tensor-core primitives of the mixed form (tcgen05 TF32 MMA, A in
+Tensor Memory, B in shared memory in the canonical no-swizzle layout, FP32
+accumulator in Tensor Memory): exact integer products pin the operand and
+accumulator layouts; random operands match a TF32-rounded FP64 product."""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def _tc(A, B):
+    from periodsearch_gb300 import _abi
+
+    A = np.ascontiguousarray(A, np.float32)
+    B = np.ascontiguousarray(B, np.float32)
+    D = np.zeros((128, 32), np.float32)
+    fp = lambda a: a.ctypes.data_as(C.POINTER(C.c_float))   # noqa: E731
+    _abi.check(_abi.lib().ps_tc_selftest(0, fp(A), fp(B), A.shape[1], fp(D)), "ps_tc_selftest")
+    return D
+
+
+def _tf32(x):
+    """Round to TF32 (10 explicit mantissa bits), nearest, ties away from zero."""
+    b = np.ascontiguousarray(x, np.float32).view(np.uint32).astype(np.uint64)
+    b = (b + 0x1000) & 0xFFFFE000
+    return b.astype(np.uint32).view(np.float32)
+
+
+@pytest.mark.parametrize("K", [8, 288, 480])
+def test_tc_integer_products_exact(engine_lib, K):
+    rng = np.random.default_rng(K)
+    A = rng.integers(-8, 9, (128, K)).astype(np.float32)
+    B = rng.integers(-8, 9, (32, K)).astype(np.float32)
+    np.testing.assert_array_equal(_tc(A, B), A.astype(np.float64) @ B.T.astype(np.float64))
+
+
+def test_tc_rows_and_columns_land_in_place(engine_lib):
+    """One-hot operands: D[m][n] = A[m][k] B[n][k] for a single k, so every
+    element of D identifies its row and column."""
+    K = 64
+    A = np.zeros((128, K), np.float32)
+    B = np.zeros((32, K), np.float32)
+    A[:, 5] = np.arange(128) + 1
+    B[:, 5] = 256 * (np.arange(32) + 1)        # exact in TF32 (11 significant bits)
+    D = _tc(A, B)
+    np.testing.assert_array_equal(D, np.outer(np.arange(128) + 1, 256 * (np.arange(32) + 1)))
+
+
+def test_tc_random_matches_tf32_reference(engine_lib):
+    rng = np.random.default_rng(7)
+    A = rng.normal(size=(128, 288)).astype(np.float32)
+    B = rng.normal(size=(32, 288)).astype(np.float32)
+    ref = _tf32(A).astype(np.float64) @ _tf32(B).T.astype(np.float64)
+    got = _tc(A, B)
+    scale = np.abs(A).astype(np.float64) @ np.abs(B).T.astype(np.float64)
+    assert np.max(np.abs(got - ref) / scale) < 1e-5
