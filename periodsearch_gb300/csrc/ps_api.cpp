@@ -141,7 +141,7 @@ ps_status make_plan(ps_ctx *c, int form)
     // shared memory when it fits; FP64 form: 16-point tiles.
     const bool mixed = form == PS_FORM_MIXED;
     int P = mixed ? 32 : 16, dsph_smem = mixed ? psg::kBasisSmem : psg::kBasisGlobal;
-    if (mixed && !(c->opt.flags & PS_FLAG_NO_TENSOR) && psg::tensor_basis_ok(F, o.ncoef, P))
+    if (mixed && !(c->opt.flags & PS_FLAG_NO_TENSOR) && psg::tensor_basis_ok(F, o.ncoef, o.mfit, P))
         dsph_smem = psg::kBasisTensor;
     psg::SlotLayout L = psg::make_layout(form, o.ma, o.mfit, F, o.ncoef, P, dsph_smem);
     if (L.bytes > smem_max && dsph_smem != psg::kBasisGlobal) {

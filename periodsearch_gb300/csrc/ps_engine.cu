@@ -74,7 +74,7 @@ struct Smem {
     // tensor-core contraction: operand tiles, MMA-completion barrier, Tensor
     // Memory address slot and the abort flag set when a wait gives up
     unsigned char *bhi, *blo;
-    uint64_t *mbar;
+    uint64_t *mbar, *mbar2;   // completion of the contraction MMAs / of the alpha MMAs
     uint32_t *tslot;
     int *abort;
 };
@@ -112,9 +112,10 @@ __device__ inline Smem<FORM> carve(char *base, const SlotLayout &L)
         s.mbar = reinterpret_cast<uint64_t *>(base + L.tcm);
         s.tslot = reinterpret_cast<uint32_t *>(base + L.tcm + 8);
         s.abort = reinterpret_cast<int *>(base + L.tcm + 12);
+        s.mbar2 = reinterpret_cast<uint64_t *>(base + L.tcm + 16);
     } else {
         s.bhi = s.blo = nullptr;
-        s.mbar = nullptr;
+        s.mbar = s.mbar2 = nullptr;
         s.tslot = nullptr;
         s.abort = nullptr;
     }
@@ -510,15 +511,43 @@ __device__ inline void setup_point(const DevObject &ob, const FitConfig &cfg, in
 constexpr uint32_t kTcWaitTries = 1u << 22;   // mbarrier polls before a wait gives up
 constexpr int kErrTcTimeout = 16;             // ps_fit.err_code of a fit cut short by a failed wait
 
-// Accumulator columns [tc_dcol, tc_dcol + 64) follow the basis columns [0, F):
-// column p holds A W_hi^T for point p, column 32 + p holds A W_lo^T.
+// Tensor Memory columns: the basis [0, F), the contraction accumulator
+// [tc_dcol, tc_dcol + 64) (column p: A W_hi^T for point p, 32 + p: A W_lo^T)
+// and the alpha accumulator [tc_acol, tc_acol + 128).
 __device__ inline uint32_t tc_dcol(int F) { return static_cast<uint32_t>((F + 31) & ~31); }
+__device__ inline uint32_t tc_acol(int F) { return tc_dcol(F) + 64; }
 
 __device__ inline uint32_t tc_cols(int F)
 {
     uint32_t n = 32;
-    while (n < tc_dcol(F) + 64) n <<= 1;
+    while (n < tc_acol(F) + 128) n <<= 1;
     return n;
+}
+
+// Per-thread view of the CTA's tensor-core state (every thread keeps the
+// same values).
+struct TcState {
+    uint32_t tbase = 0;     // Tensor Memory base address
+    uint32_t phase = 0;     // parity of the contraction barrier's next phase
+    uint32_t aphase = 0;    // parity of the alpha barrier's next phase
+    bool apending = false;  // alpha MMAs committed and not waited for
+    bool afresh = true;     // the alpha accumulator holds nothing since the last flush
+};
+
+// Waits for the committed alpha MMAs (their operands' shared memory is then
+// free); a wait that gives up sets the abort flag.
+__device__ inline void tc_alpha_wait(Smem<PS_FORM_MIXED> &s, TcState &t)
+{
+    if (!t.apending || *s.abort) return;
+    const bool ok = __syncthreads_and(tc::mbar_wait(s.mbar2, t.aphase, kTcWaitTries));
+    t.apending = false;
+    if (!ok) {
+        if (threadIdx.x == 0) *s.abort = 1;
+        __syncthreads();
+        return;
+    }
+    t.aphase ^= 1u;
+    tc::fence_after_sync();
 }
 
 // Allocates the CTA's Tensor Memory and loads A = [Dsph_hi^T; Dsph_lo^T]:
@@ -533,6 +562,7 @@ __device__ uint32_t tc_setup(const DevObject &ob, Smem<PS_FORM_MIXED> &s)
     if (warp == 0) tc::tmem_alloc(s.tslot, tc_cols(F));
     if (tid == 0) {
         tc::mbar_init(s.mbar, 1);
+        tc::mbar_init(s.mbar2, 1);
         *s.abort = 0;
     }
     tc::fence_before_sync();
@@ -561,14 +591,17 @@ __device__ uint32_t tc_setup(const DevObject &ob, Smem<PS_FORM_MIXED> &s)
     return tbase;
 }
 
-// Releases the Tensor Memory.  After an abandoned wait the MMAs of that
-// phase get one more bounded wait first.
-__device__ void tc_teardown(Smem<PS_FORM_MIXED> &s, uint32_t tbase, int F, uint32_t phase)
+// Releases the Tensor Memory.  After an abandoned wait the MMAs in flight
+// get one more bounded wait first.
+__device__ void tc_teardown(Smem<PS_FORM_MIXED> &s, const TcState &t, int F)
 {
-    if (*s.abort && threadIdx.x == 0) tc::mbar_wait(s.mbar, phase, kTcWaitTries);
+    if (*s.abort && threadIdx.x == 0) {
+        tc::mbar_wait(s.mbar, t.phase, kTcWaitTries);
+        if (t.apending) tc::mbar_wait(s.mbar2, t.aphase, kTcWaitTries);
+    }
     tc::fence_before_sync();
     __syncthreads();
-    if ((threadIdx.x >> 5) == 0) tc::tmem_dealloc(tbase, tc_cols(F));
+    if ((threadIdx.x >> 5) == 0) tc::tmem_dealloc(t.tbase, tc_cols(F));
 }
 
 // Splits the tile's W rows (row-major FP32, stride wcols) into TF32 high and
@@ -578,10 +611,12 @@ __device__ void tc_teardown(Smem<PS_FORM_MIXED> &s, uint32_t tbase, int F, uint3
 // 128 x 64 x 8 (one MMA costs the issuing thread about the same for N = 32
 // and N = 64) followed by a commit to the barrier.
 template <int NT>
-__device__ void contract_tc_issue(Smem<PS_FORM_MIXED> &s, int F, int wcols, uint32_t tbase)
+__device__ void contract_tc_issue(Smem<PS_FORM_MIXED> &s, int F, int wcols, TcState &t)
 {
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int kcs = F >> 2;
+    const uint32_t tbase = t.tbase;
+    tc_alpha_wait(s, t);   // the operand region still holds the alpha operands
     for (int cm = warp; cm < 4 * kcs; cm += NT / 32) {
         const int pg = cm / kcs, kc = cm - pg * kcs;
         const float w = s.W[(pg * 8 + (lane >> 2)) * wcols + kc * 4 + (lane & 3)];
@@ -612,18 +647,18 @@ __device__ void contract_tc_issue(Smem<PS_FORM_MIXED> &s, int F, int wcols, uint
 // and low parts.  A wait that gives up sets the abort flag; the caller ends
 // the fit.
 template <int NT>
-__device__ void contract_tc_finish(Smem<PS_FORM_MIXED> &s, int np, int F, int C, int ma, bool conv, uint32_t tbase,
-                                   uint32_t &phase)
+__device__ void contract_tc_finish(Smem<PS_FORM_MIXED> &s, int np, int F, int C, int ma, bool conv, TcState &t)
 {
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const uint32_t tbase = t.tbase;
     if (*s.abort) return;
-    const bool ok = __syncthreads_and(tc::mbar_wait(s.mbar, phase, kTcWaitTries));
+    const bool ok = __syncthreads_and(tc::mbar_wait(s.mbar, t.phase, kTcWaitTries));
     if (!ok) {
         if (tid == 0) *s.abort = 1;
         __syncthreads();
         return;
     }
-    phase ^= 1u;
+    t.phase ^= 1u;
     tc::fence_after_sync();
     float *X = reinterpret_cast<float *>(s.bhi);
     if (warp < 4) {
@@ -647,6 +682,118 @@ __device__ void contract_tc_finish(Smem<PS_FORM_MIXED> &s, int np, int F, int C,
     }
 }
 
+// alpha/beta accumulation of one tile on the tensor cores (mrqcof.c:106-136):
+// D += A B^T over the tile's points with A = [Wt_hi; Wt_lo] (row j: the
+// weighted column J[.][l_j] sig^-2 w of free parameter j, 128 x 32) and B =
+// [Jt_hi; Jt_lo] (row k < mfit: column J[.][l_k]; row mfit: the residuals
+// dy), both split into TF32 high and low parts, so that the four quadrants
+// of the 128 x 128 FP32 accumulator sum to alpha (and beta in column mfit)
+// at FP32 accuracy.  The accumulator stays in Tensor Memory across tiles
+// until tc_alpha_flush.  chi^2 is summed in FP64 by warp 0.
+template <int NT>
+__device__ void accumulate_tile_tc(const DevObject &ob, Smem<PS_FORM_MIXED> &s, int np, int q0pt, bool conv,
+                                   double conv_sig, TcState &t)
+{
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int ma = ob.ma, mf = ob.mfit;
+    float *dyv = s.accs;
+    float *wtp = dyv + 32;
+    if (tid < 32) {
+        double c2 = 0;
+        if (tid < np) {
+            const int q = q0pt + tid;
+            const double sig2i = conv ? 1 / (conv_sig * conv_sig) : ob.sig2i[q];
+            const double wg = ob.weight[q];
+            const double dy = (conv ? 0.0 : ob.bright[q]) - s.ym[tid];
+            dyv[tid] = static_cast<float>(dy);
+            wtp[tid] = static_cast<float>(sig2i * wg);
+            c2 = dy * dy * sig2i * wg;
+        }
+        c2 = warp_sum(c2);
+        if (tid == 0) s.misc[M_CHISQ] += c2;
+    }
+    tc_alpha_wait(s, t);
+    __syncthreads();
+    // operands in the canonical K-major layout, K = the tile's 32 points
+    // (zero beyond np): 8-row x 4-point core matrices, K-adjacent ones 128
+    // bytes apart, 8-row groups 1024 bytes apart; high parts in rows 0..63,
+    // low parts in rows 64..127
+    unsigned char *Ab = s.bhi, *Bb = s.bhi + 16384;
+    for (int cm = warp; cm < 128; cm += NT / 32) {
+        const bool isB = cm >= 64;
+        const int c = cm & 63, rg = c >> 3, kc = c & 7;
+        const int row = rg * 8 + (lane >> 2), p = kc * 4 + (lane & 3);
+        float v = 0.f;
+        if (p < np) {
+            if (row < mf) {
+                v = s.J[p * ma + ob.free_list[row]];
+                if (!isB) v *= wtp[p];
+            } else if (isB && row == mf) {
+                v = dyv[p];
+            }
+        }
+        const uint32_t hi = tc::to_tf32(v);
+        const uint32_t lo = tc::to_tf32(v - __uint_as_float(hi));
+        unsigned char *base = isB ? Bb : Ab;
+        reinterpret_cast<uint32_t *>(base + (rg * 8 + kc) * 128)[lane] = hi;
+        reinterpret_cast<uint32_t *>(base + ((rg + 8) * 8 + kc) * 128)[lane] = lo;
+    }
+    tc::fence_proxy_async();
+    tc::fence_before_sync();
+    __syncthreads();
+    if (tid == 0 && !*s.abort) {
+        tc::fence_after_sync();
+        const uint32_t idesc = tc::idesc_tf32(128, 128);
+        const uint32_t a0 = tc::smem_u32(Ab), b0 = tc::smem_u32(Bb), d = t.tbase + tc_acol(ob.nfac);
+        for (int kk = 0; kk < 4; kk++) {
+            const uint32_t off = static_cast<uint32_t>(kk) * 256;
+            tc::mma_tf32_ss(d, tc::smem_desc(a0 + off, 128, 1024), tc::smem_desc(b0 + off, 128, 1024), idesc,
+                            (t.afresh && kk == 0) ? 0u : 1u);
+        }
+        tc::mma_commit(s.mbar2);
+    }
+    t.apending = true;
+    t.afresh = false;
+}
+
+// Adds the alpha accumulator to the FP64 normal matrix M (lower triangle)
+// and bv, and marks it empty: each quadrant pair is summed on the way out of
+// Tensor Memory (rows m and 64 + m, columns k and 64 + k).
+template <int NT>
+__device__ void tc_alpha_flush(const DevObject &ob, Smem<PS_FORM_MIXED> &s, double *M, double *bv, TcState &t)
+{
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int mf = ob.mfit;
+    if (t.afresh) return;
+    tc_alpha_wait(s, t);
+    if (*s.abort) return;
+    float *S = reinterpret_cast<float *>(s.bhi + kTcAlphaStage);   // [128][65]
+    if (warp < 4) {
+        const uint32_t taddr = t.tbase + (static_cast<uint32_t>(warp * 32) << 16) + tc_acol(ob.nfac);
+        float *sr = S + (warp * 32 + lane) * 65;
+#pragma unroll 1
+        for (int q = 0; q < 8; q++) {
+            uint32_t vh[8], vl[8];
+            tc::tmem_ld8(taddr + 8 * q, vh);
+            tc::tmem_ld8(taddr + 64 + 8 * q, vl);
+            tc::tmem_wait_ld();
+#pragma unroll
+            for (int j = 0; j < 8; j++) sr[8 * q + j] = __uint_as_float(vh[j]) + __uint_as_float(vl[j]);
+        }
+    }
+    __syncthreads();
+    const int ntri = mf * (mf + 1) / 2;
+    for (int e = tid; e < ntri; e += NT) {
+        const int j = tri_row(e);
+        const int k = e - j * (j + 1) / 2;
+        M[j * mf + k] += static_cast<double>(S[j * 65 + k] + S[(64 + j) * 65 + k]);
+    }
+    for (int j = tid; j < mf; j += NT) bv[j] += static_cast<double>(S[j * 65 + mf] + S[(64 + j) * 65 + mf]);
+    t.afresh = true;
+    tc::fence_before_sync();
+    __syncthreads();
+}
+
 // ---------------------------------------------------------------------------
 // Model evaluation (mrqcof) at parameters a[] into matrix M (mfit x mfit,
 // lower triangle accumulated then mirrored) and vector bv.  Leaves chi^2,
@@ -654,8 +801,7 @@ __device__ void contract_tc_finish(Smem<PS_FORM_MIXED> &s, int np, int F, int C,
 // ---------------------------------------------------------------------------
 template <int FORM, int KU>
 __device__ void evaluate(const DevObject &ob, const FitConfig &cfg, const SlotLayout &L, Smem<FORM> &s,
-                         const double *a, double *M, double *bv, typename RealOf<FORM>::T *scratch, uint32_t tbase,
-                         uint32_t &tc_phase)
+                         const double *a, double *M, double *bv, typename RealOf<FORM>::T *scratch, TcState &tcs)
 {
     using R = typename RealOf<FORM>::T;
     constexpr bool kFP64 = FORM == PS_FORM_FP64;
@@ -846,7 +992,7 @@ __device__ void evaluate(const DevObject &ob, const FitConfig &cfg, const SlotLa
                     s.J[p * ma + k] = conv ? acc : s.pt[p * kPointStride + 24] * acc;
                 }
             } else if constexpr (KU == 0) {
-                contract_tc_issue<NT>(s, F, wcols, tbase);   // the work below overlaps the MMAs
+                contract_tc_issue<NT>(s, F, wcols, tcs);   // the work below overlaps the MMAs
             } else {
                 if (s.dsph)
                     contract_mixed<NT, KU, true>(s, dsphF, np, F, C, ma, wcols, conv);
@@ -887,7 +1033,7 @@ __device__ void evaluate(const DevObject &ob, const FitConfig &cfg, const SlotLa
                 if (next_setup && warp > 0 && pipe_sp < min(P, ob.lc_npts[nlc] - nt0))
                     setup_point<FORM>(ob, cfg, ob.lc_start[nlc] + nt0 + pipe_sp, omg, B, DB0, DB1, php0, php1, php2,
                                       s.pt2 + pipe_sp * kPointStride);
-                contract_tc_finish<NT>(s, np, F, C, ma, conv, tbase, tc_phase);
+                contract_tc_finish<NT>(s, np, F, C, ma, conv, tcs);
             }
             __syncthreads();
             if (next_setup) {
@@ -923,11 +1069,19 @@ __device__ void evaluate(const DevObject &ob, const FitConfig &cfg, const SlotLa
                 continue;
             }
             // 5. accumulate (mrqcof.c:106-136)
-            accumulate_tile<FORM>(ob, s, M, bv, np, start + t0, conv, conv_sig, accA, accB);
-            if constexpr (!kFP64) {
+            if constexpr (kPipe) {
+                accumulate_tile_tc<NT>(ob, s, np, start + t0, conv, conv_sig, tcs);
                 if (++tiles_since_flush == kTilesPerFlush) {
-                    flush_partials<FORM>(M, bv, mf, accA, accB);
+                    tc_alpha_flush<NT>(ob, s, M, bv, tcs);
                     tiles_since_flush = 0;
+                }
+            } else {
+                accumulate_tile<FORM>(ob, s, M, bv, np, start + t0, conv, conv_sig, accA, accB);
+                if constexpr (!kFP64) {
+                    if (++tiles_since_flush == kTilesPerFlush) {
+                        flush_partials<FORM>(M, bv, mf, accA, accB);
+                        tiles_since_flush = 0;
+                    }
                 }
             }
         }
@@ -964,16 +1118,25 @@ __device__ void evaluate(const DevObject &ob, const FitConfig &cfg, const SlotLa
                 s.J[e] = (l == 0) ? R(0) : out;
             }
             __syncthreads();
-            accumulate_tile<FORM>(ob, s, M, bv, np, start + t0, false, conv_sig, accA, accB);
-            if constexpr (!kFP64) {
+            if constexpr (kPipe) {
+                accumulate_tile_tc<NT>(ob, s, np, start + t0, false, conv_sig, tcs);
                 if (++tiles_since_flush == kTilesPerFlush) {
-                    flush_partials<FORM>(M, bv, mf, accA, accB);
+                    tc_alpha_flush<NT>(ob, s, M, bv, tcs);
                     tiles_since_flush = 0;
+                }
+            } else {
+                accumulate_tile<FORM>(ob, s, M, bv, np, start + t0, false, conv_sig, accA, accB);
+                if constexpr (!kFP64) {
+                    if (++tiles_since_flush == kTilesPerFlush) {
+                        flush_partials<FORM>(M, bv, mf, accA, accB);
+                        tiles_since_flush = 0;
+                    }
                 }
             }
         }
     }
-    if constexpr (!kFP64) flush_partials<FORM>(M, bv, mf, accA, accB);
+    if constexpr (kPipe) tc_alpha_flush<NT>(ob, s, M, bv, tcs);
+    else if constexpr (!kFP64) flush_partials<FORM>(M, bv, mf, accA, accB);
     __syncthreads();
     // mirror the lower triangle (mrqcof.c:139-141)
     for (int e = tid; e < mf * mf; e += NT) {
@@ -1078,52 +1241,56 @@ __device__ int gauss_jordan(double *A, double *b, int n, double *col, int *ipiv,
 }
 
 // Cholesky factorisation A = L L^T of the damped normal matrix (symmetric
-// positive definite; lower triangle used, overwritten by L) and the two
-// triangular solves for b, in FP64.  Returns 2 when a pivot is not positive.
+// positive definite; lower triangle used, overwritten by L) and the solve of
+// L L^T x = b, in FP64.  The forward substitution runs inside the
+// factorisation (b is the bordering column: y_j = b_j / L_jj, then b_i -=
+// L_ij y_j with the trailing update), so a step costs two CTA barriers: warp
+// 0 takes the pivot's reciprocal square root and scales column j and y_j,
+// then all threads update the trailing block.  The back substitution uses
+// the stored reciprocals.  Returns 2 when a pivot is not positive.
 template <int NT>
-__device__ int cholesky_solve(double *A, double *b, int n, double *col)
+__device__ int cholesky_solve(double *A, double *b, int n, double *col, double *flag)
 {
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     __syncthreads();
     for (int j = 0; j < n; j++) {
-        if (tid == 0) {
-            const double d = A[j * n + j];
-            const double ljj = sqrt(d);
-            col[0] = d > 0.0 ? 1.0 : 0.0;
-            col[1] = ljj;
-            col[2] = 1.0 / ljj;
+        if (warp == 0) {
+            double inv = 0;
+            if (lane == 0) {
+                const double d = A[j * n + j];
+                const bool ok = d > 0.0;
+                inv = ok ? rsqrt(d) : 0.0;
+                *flag = ok ? 1.0 : 0.0;
+                A[j * n + j] = d * inv;      // L_jj = sqrt(d)
+                col[j] = inv;
+                b[j] *= inv;                 // y_j
+            }
+            inv = __shfl_sync(0xffffffffu, inv, 0);
+            for (int i = j + 1 + lane; i < n; i += 32) A[i * n + j] *= inv;
         }
         __syncthreads();
-        if (col[0] == 0.0) return 2;
-        const double ljj = col[1], inv = col[2];
-        for (int i = j + 1 + tid; i < n; i += NT) A[i * n + j] *= inv;
-        __syncthreads();
-        if (tid == 0) A[j * n + j] = ljj;
+        if (*flag == 0.0) return 2;
         const int m = n - j - 1;
         const int ntri = m * (m + 1) / 2;
-        for (int e = tid; e < ntri; e += NT) {
-            const int r = tri_row(e);
-            const int c = e - r * (r + 1) / 2;
-            const int i = j + 1 + r, k = j + 1 + c;
-            A[i * n + k] -= A[i * n + j] * A[k * n + j];
+        const double yj = b[j];
+        for (int e = tid; e < ntri + m; e += NT) {
+            if (e < ntri) {
+                const int r = tri_row(e);
+                const int c = e - r * (r + 1) / 2;
+                const int i = j + 1 + r, k = j + 1 + c;
+                A[i * n + k] -= A[i * n + j] * A[k * n + j];
+            } else {
+                const int i = j + 1 + (e - ntri);
+                b[i] -= A[i * n + j] * yj;
+            }
         }
         __syncthreads();
     }
     if (warp == 0) {
-        for (int j = 0; j < n; j++) {
-            double y = 0;
-            if (lane == 0) {
-                y = b[j] / A[j * n + j];
-                b[j] = y;
-            }
-            y = __shfl_sync(0xffffffffu, y, 0);
-            for (int i = j + 1 + lane; i < n; i += 32) b[i] -= A[i * n + j] * y;
-            __syncwarp();
-        }
         for (int j = n - 1; j >= 0; j--) {
             double x = 0;
             if (lane == 0) {
-                x = b[j] / A[j * n + j];
+                x = b[j] * col[j];
                 b[j] = x;
             }
             x = __shfl_sync(0xffffffffu, x, 0);
@@ -1177,7 +1344,7 @@ __device__ float mlp_predict_warp(const float *W, const float *f, float *sh)
 template <int FORM, int KU>
 __device__ void run_fit(const DevObject &ob, const FitConfig &cfg, const SlotLayout &L, Smem<FORM> &s,
                         typename RealOf<FORM>::T *scratch, int64_t n, int pole, ps_fit *out, const FitWork &w,
-                        long long fidx, uint32_t tbase, uint32_t &tc_phase)
+                        long long fidx, TcState &tcs)
 {
     constexpr bool kTensor = FORM == PS_FORM_MIXED && KU == 0;
     constexpr int NT = threads_of<FORM>();
@@ -1214,7 +1381,7 @@ __device__ void run_fit(const DevObject &ob, const FitConfig &cfg, const SlotLay
         bool accepted = false;
         if (alamda < 0) {
             alamda = cfg.alamda_start;
-            evaluate<FORM, KU>(ob, cfg, L, s, s.cg, s.alpha, s.beta, scratch, tbase, tc_phase);
+            evaluate<FORM, KU>(ob, cfg, L, s, s.cg, s.alpha, s.beta, scratch, tcs);
             if constexpr (kTensor) {
                 if (*s.abort) {
                     last_err = kErrTcTimeout;
@@ -1240,7 +1407,7 @@ __device__ void run_fit(const DevObject &ob, const FitConfig &cfg, const SlotLay
             // The damped normal matrix is symmetric positive definite: solve
             // it by Cholesky in FP64; if a pivot is not positive (rounding on
             // a nearly singular alpha), redo the step with Gauss-Jordan.
-            err = cholesky_solve<NT>(s.covar, s.da, mf, s.col);
+            err = cholesky_solve<NT>(s.covar, s.da, mf, s.col, s.misc + M_PIV);
             if (err) {
                 for (int e = tid; e < mf * mf; e += NT) {
                     const int j = e / mf, k = e - j * mf;
@@ -1258,7 +1425,7 @@ __device__ void run_fit(const DevObject &ob, const FitConfig &cfg, const SlotLay
                 s.atry[l] = s.cg[l] + s.da[j];
             }
             __syncthreads();
-            evaluate<FORM, KU>(ob, cfg, L, s, s.atry, s.covar, s.da, scratch, tbase, tc_phase);
+            evaluate<FORM, KU>(ob, cfg, L, s, s.atry, s.covar, s.da, scratch, tcs);
             if constexpr (kTensor) {
                 if (*s.abort) {
                     last_err = kErrTcTimeout;
@@ -1368,8 +1535,8 @@ __global__ void __launch_bounds__(threads_of<FORM>(), 1)
     constexpr bool kTensor = FORM == PS_FORM_MIXED && KU == 0;
     if (s.dsph)
         for (int e = threadIdx.x; e < ob.nfac * ob.ncoef; e += NT) s.dsph[e] = ob.dsph_f[e];
-    uint32_t tbase = 0, tc_phase = 0;
-    if constexpr (kTensor) tbase = tc_setup<NT>(ob, s);
+    TcState tcs;
+    if constexpr (kTensor) tcs.tbase = tc_setup<NT>(ob, s);
     R *scratch = reinterpret_cast<R *>(w.scratch + static_cast<size_t>(blockIdx.x) * w.scratch_stride);
     __shared__ long long next;
     for (;;) {
@@ -1390,9 +1557,9 @@ __global__ void __launch_bounds__(threads_of<FORM>(), 1)
             n = w.n_lo + f / PS_N_POLES;
             pole = static_cast<int>(f % PS_N_POLES) + 1;
         }
-        run_fit<FORM, KU>(ob, cfg, L, s, scratch, n, pole, w.out + f, w, f, tbase, tc_phase);
+        run_fit<FORM, KU>(ob, cfg, L, s, scratch, n, pole, w.out + f, w, f, tcs);
     }
-    if constexpr (kTensor) tc_teardown(s, tbase, ob.nfac, tc_phase);
+    if constexpr (kTensor) tc_teardown(s, tcs, ob.nfac);
 }
 
 template <int FORM, int KU>
@@ -1408,14 +1575,14 @@ __global__ void __launch_bounds__(threads_of<FORM>(), 1) eval_kernel(DevObject o
     constexpr bool kTensor = FORM == PS_FORM_MIXED && KU == 0;
     if (s.dsph)
         for (int e = threadIdx.x; e < ob.nfac * ob.ncoef; e += NT) s.dsph[e] = ob.dsph_f[e];
-    uint32_t tbase = 0, tc_phase = 0;
-    if constexpr (kTensor) tbase = tc_setup<NT>(ob, s);
+    TcState tcs;
+    if constexpr (kTensor) tcs.tbase = tc_setup<NT>(ob, s);
     for (int i = threadIdx.x; i < ob.ma; i += NT) s.cg[i] = cg[i];
     __syncthreads();
-    evaluate<FORM, KU>(ob, cfg, L, s, s.cg, s.alpha, s.beta, reinterpret_cast<R *>(scratch), tbase, tc_phase);
+    evaluate<FORM, KU>(ob, cfg, L, s, s.cg, s.alpha, s.beta, reinterpret_cast<R *>(scratch), tcs);
     if constexpr (kTensor) {
         const bool aborted = *s.abort != 0;
-        tc_teardown(s, tbase, ob.nfac, tc_phase);
+        tc_teardown(s, tcs, ob.nfac);
         if (aborted) {
             if (threadIdx.x == 0) *chisq = NAN;
             return;

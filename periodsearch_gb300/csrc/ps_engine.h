@@ -98,6 +98,7 @@ PSG_HD constexpr int threads_of()
 constexpr int kPointStride = 32;   // reals of per-point set-up
 constexpr int kRedStride = 8;      // doubles of per-point facet sums
 constexpr int kMisc = 32;
+constexpr size_t kTcAlphaStage = 32768;   // tensor-core alpha/beta operands, then accumulator staging
 
 
 // dsph_smem: the mixed form keeps the FP32 basis Dsph[F][C] in shared memory
@@ -148,11 +149,15 @@ PSG_HD inline SlotLayout make_layout(int form, int ma, int mfit, int nfac, int n
         // B = [W_hi; W_lo]: 2P rows, the low parts right after the high parts
         // (8-row groups stride-byte-offset apart); the accumulator rows are
         // staged over it for the epilogue
+        // The same region then holds the alpha/beta operands (two 128 x 32
+        // TF32 tiles, 32 KB) and the staging of the alpha accumulator.
         const size_t tile = static_cast<size_t>(P) * nfac * sizeof(float);
         const size_t readback = 128 * 65 * sizeof(float);
-        L.bhi = take(2 * tile > readback ? 2 * tile : readback);
+        size_t region = 2 * tile > readback ? 2 * tile : readback;
+        if (region < kTcAlphaStage + readback) region = kTcAlphaStage + readback;
+        L.bhi = take(region);
         L.blo = L.bhi + tile;
-        L.tcm = take(16);
+        L.tcm = take(32);
         L.pt2 = take(static_cast<size_t>(P) * kPointStride * rs);
     } else {
         L.bhi = L.blo = L.tcm = 0;
@@ -171,13 +176,14 @@ int launch_eval(int form, const DevObject &ob, const FitConfig &cfg, const doubl
                 int dsph_smem, void *stream);
 int set_kernel_smem(int form, size_t smem, int ncoef, int dsph_smem);
 int occupancy_slots(int form, size_t smem, int ncoef, int dsph_smem, int *per_sm);
-// Whether the tcgen05 contraction supports an object's shape tables: at most
-// 64 coefficients (the high and low TF32 parts of the basis fill 128 Tensor
-// Memory lanes), a facet count that is a multiple of 8 and leaves 64
+// Whether the tensor-core path supports an object: at most 64 coefficients
+// (the high and low TF32 parts of the basis fill 128 Tensor Memory lanes),
+// at most 63 free parameters (alpha and the beta column in 64 rows), a facet
+// count that is a multiple of 8 and leaves the 64 contraction and 128 alpha
 // accumulator columns within 512, and 32-point tiles.
-PSG_HD inline bool tensor_basis_ok(int nfac, int ncoef, int P)
+PSG_HD inline bool tensor_basis_ok(int nfac, int ncoef, int mfit, int P)
 {
-    return ncoef <= 64 && nfac % 8 == 0 && ((nfac + 31) & ~31) + 64 <= 512 && P == 32;
+    return ncoef <= 64 && mfit <= 63 && nfac % 8 == 0 && ((nfac + 31) & ~31) + 64 + 128 <= 512 && P == 32;
 }
 int measure_fma_peaks(double *fp64_tflops, double *fp32_tflops, void *stream);
 // Learned early stop (ps_mlp.cu).

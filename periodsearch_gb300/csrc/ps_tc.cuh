@@ -97,6 +97,18 @@ __device__ inline void mma_tf32_ts(uint32_t d_taddr, uint32_t a_taddr, uint64_t 
         : "memory");
 }
 
+// ---- MMA: D[tmem] (+)= A[smem] * B[smem]^T, issued by one thread ----
+__device__ inline void mma_tf32_ss(uint32_t d_taddr, uint64_t a_desc, uint64_t b_desc, uint32_t idesc,
+                                   uint32_t accumulate)
+{
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "setp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n\t}" ::"r"(d_taddr),
+        "l"(a_desc), "l"(b_desc), "r"(idesc), "r"(accumulate)
+        : "memory");
+}
+
 // Arrives once on the mbarrier when every MMA issued before by this thread
 // has completed.
 __device__ inline void mma_commit(uint64_t *mbar)
