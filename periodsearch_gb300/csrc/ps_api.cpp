@@ -460,6 +460,20 @@ ps_status ps_prepare(const ps_problem *prob, const ps_options *opt, ps_ctx **out
         sz[q] = o.ee0[3 * q + 2];
         alpha_pt[q] = std::acos(ex[q] * sx[q] + ey[q] * sy[q] + ez[q] * sz[q]);
     }
+    // FP32 point geometry of the mixed form, two float4 per point: Earth
+    // direction and phase angle, Sun direction
+    std::vector<float> geo_f(static_cast<size_t>(o.ndata) * 8);
+    for (int q = 0; q < o.ndata; q++) {
+        float *g = &geo_f[static_cast<size_t>(q) * 8];
+        g[0] = static_cast<float>(ex[q]);
+        g[1] = static_cast<float>(ey[q]);
+        g[2] = static_cast<float>(ez[q]);
+        g[3] = static_cast<float>(alpha_pt[q]);
+        g[4] = static_cast<float>(sx[q]);
+        g[5] = static_cast<float>(sy[q]);
+        g[6] = static_cast<float>(sz[q]);
+        g[7] = 0.f;
+    }
     std::vector<double> sig2i(o.ndata);
     for (int q = 0; q < o.ndata; q++) sig2i[q] = 1 / (o.sig[q] * o.sig[q]);
     std::vector<float> dsph_f(s.dsph.begin(), s.dsph.end());
@@ -473,7 +487,7 @@ ps_status ps_prepare(const ps_problem *prob, const ps_options *opt, ps_ctx **out
            o_sx = pk.add(sx), o_sy = pk.add(sy), o_sz = pk.add(sz), o_ls = pk.add(o.lc_start),
            o_ln = pk.add(o.lc_points), o_lr = pk.add(o.lc_rel), o_fl = pk.add(o.free_list),
            o_cgf = pk.add(o.cg_first), o_dsf = pk.add(dsph_f), o_alp = pk.add(alpha_pt), o_nxf = pk.add(nx_f),
-           o_nyf = pk.add(ny_f), o_nzf = pk.add(nz_f), o_daf = pk.add(darea_f), o_s2i = pk.add(sig2i);
+           o_nyf = pk.add(ny_f), o_nzf = pk.add(nz_f), o_daf = pk.add(darea_f), o_s2i = pk.add(sig2i), o_geo = pk.add(geo_f);
     c->h2d_bytes = static_cast<int64_t>(pk.bytes.size());
     PSG_CUDA(cp, cudaMalloc(&c->d_tables, pk.bytes.size()));
     PSG_CUDA(cp, cudaMemcpyAsync(c->d_tables, pk.bytes.data(), pk.bytes.size(), cudaMemcpyHostToDevice, c->stream));
@@ -520,6 +534,7 @@ ps_status ps_prepare(const ps_problem *prob, const ps_options *opt, ps_ctx **out
     d.nz_f = reinterpret_cast<const float *>(b + o_nzf);
     d.darea_f = reinterpret_cast<const float *>(b + o_daf);
     d.sig2i = reinterpret_cast<const double *>(b + o_s2i);
+    d.geo_f = reinterpret_cast<const float4 *>(b + o_geo);
 
     ps_status pst = make_plan(cp, c->opt.form);
     if (pst != PS_OK) {

@@ -75,6 +75,10 @@ struct Smem {
     // Memory address slot and the abort flag set when a wait gives up
     unsigned char *bhi, *blo;
     uint64_t *mbar, *mbar2;   // completion of the contraction MMAs / of the alpha MMAs
+    float4 *fac;              // per facet: nx, ny, nz, Darea
+    float2 *ag;               // per facet and evaluation: Area, Darea g
+    float *fpart;             // [4][P][9] facet-sum partials of the four facet quarters
+    unsigned char *aop;       // alpha/beta MMA operands
     uint32_t *tslot;
     int *abort;
 };
@@ -113,10 +117,18 @@ __device__ inline Smem<FORM> carve(char *base, const SlotLayout &L)
         s.tslot = reinterpret_cast<uint32_t *>(base + L.tcm + 8);
         s.abort = reinterpret_cast<int *>(base + L.tcm + 12);
         s.mbar2 = reinterpret_cast<uint64_t *>(base + L.tcm + 16);
+        s.fac = reinterpret_cast<float4 *>(base + L.fac);
+        s.ag = reinterpret_cast<float2 *>(base + L.ag);
+        s.fpart = reinterpret_cast<float *>(base + L.fpart);
+        s.aop = reinterpret_cast<unsigned char *>(base + L.aop);
     } else {
         s.bhi = s.blo = nullptr;
         s.mbar = s.mbar2 = nullptr;
         s.tslot = nullptr;
+        s.fac = nullptr;
+        s.ag = nullptr;
+        s.fpart = nullptr;
+        s.aop = nullptr;
         s.abort = nullptr;
     }
     return s;
@@ -436,11 +448,27 @@ __device__ inline void setup_point(const DevObject &ob, const FitConfig &cfg, in
 {
     using R = typename RealOf<FORM>::T;
     constexpr bool kFP64 = FORM == PS_FORM_FP64;
-    const R ee[3] = {R(ob.eex[q]), R(ob.eey[q]), R(ob.eez[q])};
-    const R e0v[3] = {R(ob.e0x[q]), R(ob.e0y[q]), R(ob.e0z[q])};
+    R ee[3], e0v[3], alpha;
+    if constexpr (kFP64) {
+        ee[0] = ob.eex[q];
+        ee[1] = ob.eey[q];
+        ee[2] = ob.eez[q];
+        e0v[0] = ob.e0x[q];
+        e0v[1] = ob.e0y[q];
+        e0v[2] = ob.e0z[q];
+        alpha = ob.alpha_pt[q];
+    } else {
+        const float4 g0 = ob.geo_f[2 * q], g1 = ob.geo_f[2 * q + 1];
+        ee[0] = g0.x;
+        ee[1] = g0.y;
+        ee[2] = g0.z;
+        alpha = g0.w;
+        e0v[0] = g1.x;
+        e0v[1] = g1.y;
+        e0v[2] = g1.z;
+    }
     const double td = ob.tim[q];
     const R t = R(td);
-    const R alpha = R(ob.alpha_pt[q]);
     R ex;
     if constexpr (kFP64) ex = exp(-alpha / php1);
     else ex = expf(-alpha / php1);
@@ -569,6 +597,7 @@ __device__ uint32_t tc_setup(const DevObject &ob, Smem<PS_FORM_MIXED> &s)
     __syncthreads();
     tc::fence_after_sync();
     const uint32_t tbase = *s.tslot;
+    for (int i = tid; i < F; i += NT) s.fac[i] = make_float4(ob.nx_f[i], ob.ny_f[i], ob.nz_f[i], ob.darea_f[i]);
     if (warp < 4) {
         const int m = warp * 32 + lane, c = m & 63;
         const bool low = m >= 64;
@@ -604,27 +633,17 @@ __device__ void tc_teardown(Smem<PS_FORM_MIXED> &s, const TcState &t, int F)
     if ((threadIdx.x >> 5) == 0) tc::tmem_dealloc(t.tbase, tc_cols(F));
 }
 
-// Splits the tile's W rows (row-major FP32, stride wcols) into TF32 high and
-// low parts in the canonical K-major layout -- one 8-row x 4-facet core
-// matrix per warp step, 128 contiguous bytes -- with the low parts as rows
-// 32..63 of the same operand, and issues D = A [W_hi; W_lo]^T as F/8 MMAs of
-// 128 x 64 x 8 (one MMA costs the issuing thread about the same for N = 32
-// and N = 64) followed by a commit to the barrier.
+// Issues D = A [W_hi; W_lo]^T for the tile as F/8 MMAs of 128 x 64 x 8 (one
+// MMA costs the issuing thread about the same for N = 32 and N = 64) and a
+// commit to the barrier.  The facet stage has written the operand: TF32
+// high parts of W in rows 0..31, low parts in rows 32..63, canonical K-major
+// layout (8-row x 4-facet core matrices, K-adjacent ones 128 bytes apart).
 template <int NT>
-__device__ void contract_tc_issue(Smem<PS_FORM_MIXED> &s, int F, int wcols, TcState &t)
+__device__ void contract_tc_issue(Smem<PS_FORM_MIXED> &s, int F, TcState &t)
 {
-    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int tid = threadIdx.x;
     const int kcs = F >> 2;
     const uint32_t tbase = t.tbase;
-    tc_alpha_wait(s, t);   // the operand region still holds the alpha operands
-    for (int cm = warp; cm < 4 * kcs; cm += NT / 32) {
-        const int pg = cm / kcs, kc = cm - pg * kcs;
-        const float w = s.W[(pg * 8 + (lane >> 2)) * wcols + kc * 4 + (lane & 3)];
-        const uint32_t hi = tc::to_tf32(w);
-        const uint32_t lo = tc::to_tf32(w - __uint_as_float(hi));
-        reinterpret_cast<uint32_t *>(s.bhi + cm * 128)[lane] = hi;
-        reinterpret_cast<uint32_t *>(s.blo + cm * 128)[lane] = lo;
-    }
     tc::fence_proxy_async();
     tc::fence_before_sync();
     __syncthreads();
@@ -638,6 +657,130 @@ __device__ void contract_tc_issue(Smem<PS_FORM_MIXED> &s, int F, int wcols, TcSt
             tc::mma_tf32_ts(d, a, tc::smem_desc(bh + off, 128, sbo), idesc, k8 > 0);
         }
         tc::mma_commit(s.mbar);
+    }
+}
+
+// Facet stage of the tensor-core path (bright.c:59-120).  Warp w takes
+// points 8 (w % 4) .. +7 (lane / 4) and the facet quarter w / 4, lanes of a
+// point stepping through the quarter four facets apart (lane % 4), so that
+// one warp store covers a whole 8-point x 4-facet core matrix of the MMA
+// operand [W_hi; W_lo].  The per-point sums (brightness, rotation and
+// scattering derivatives) are reduced over the four lanes and then over the
+// quarters into s.red.  The tile's operand region must be free (previous
+// MMAs waited for).
+template <int NT>
+__device__ void facet_stage_tc(const DevObject &ob, Smem<PS_FORM_MIXED> &s, int np, float cl, float cls)
+{
+    static_assert(NT == 512, "16 warps: 4 point groups x 4 facet quarters");
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int F = ob.nfac, kcs = F >> 2;
+    const int quarter = warp >> 2, p = (warp & 3) * 8 + (lane >> 2), fl = lane & 3;
+    const int fq = (kcs + 3) & ~3;     // facets per quarter, a multiple of 4
+    float e1 = 0, e2 = 0, e3 = 0, f1 = 0, f2 = 0, f3 = 0;
+    if (p < np) {
+        const float *pt = s.pt + p * kPointStride;
+        e1 = pt[0];
+        e2 = pt[1];
+        e3 = pt[2];
+        f1 = pt[3];
+        f2 = pt[4];
+        f3 = pt[5];
+    }
+    // The rotation derivatives sum_i Area_i (dsmu (n_i . D_k) + dsmu0 (n_i .
+    // E_k)) over the lit facets are D_k . U + E_k . V with U = sum Area dsmu
+    // n and V = sum Area dsmu0 n (D_k, E_k: the derivative directions of the
+    // Earth and Sun vectors), so the facet loop accumulates U and V.
+    float br = 0, dcl = 0, dcls = 0, ux = 0, uy = 0, uz = 0, vx = 0, vy = 0, vz = 0;
+    uint32_t *bh = reinterpret_cast<uint32_t *>(s.bhi), *bl = reinterpret_cast<uint32_t *>(s.blo);
+    const int i_end = min(F, (quarter + 1) * fq);
+#pragma unroll 2
+    for (int i0 = quarter * fq; i0 < i_end; i0 += 4) {
+        const int i = i0 + fl;
+        const float4 n = s.fac[i];
+        const float mu = e1 * n.x + e2 * n.y + e3 * n.z;
+        const float mu0 = f1 * n.x + f2 * n.y + f3 * n.z;
+        float w = 0.f;
+        if (mu > float(kTinyMu) && mu0 > float(kTinyMu)) {
+            const float2 a = s.ag[i];
+            const LitTerms<float, PS_FORM_MIXED> lt(mu, mu0, cl, cls);
+            br = br + a.x * lt.sv;
+            w = a.y * lt.sv;
+            const float cu = a.x * lt.dsmu, cv = a.x * lt.dsmu0;
+            ux = fmaf(cu, n.x, ux);
+            uy = fmaf(cu, n.y, uy);
+            uz = fmaf(cu, n.z, uz);
+            vx = fmaf(cv, n.x, vx);
+            vy = fmaf(cv, n.y, vy);
+            vz = fmaf(cv, n.z, vz);
+            dcl = dcl + mu * mu0 * a.x;
+            dcls = dcls + a.x * lt.dcls_w;
+        }
+        const uint32_t hi = tc::to_tf32(w);
+        const uint32_t lo = tc::to_tf32(w - __uint_as_float(hi));
+        const int cm = (warp & 3) * kcs + (i0 >> 2);    // core matrix (8-point group, 4-facet group)
+        bh[cm * 32 + lane] = hi;
+        bl[cm * 32 + lane] = lo;
+    }
+    float v[9] = {br, dcl, dcls, ux, uy, uz, vx, vy, vz};
+#pragma unroll
+    for (int k = 0; k < 9; k++) {
+        v[k] += __shfl_xor_sync(0xffffffffu, v[k], 1);
+        v[k] += __shfl_xor_sync(0xffffffffu, v[k], 2);
+    }
+    if (fl == 0) {
+        float *fp = s.fpart + (quarter * 32 + p) * 9;
+#pragma unroll
+        for (int k = 0; k < 9; k++) fp[k] = v[k];
+    }
+    __syncthreads();
+    if (tid < np) {
+        float t[9];
+#pragma unroll
+        for (int k = 0; k < 9; k++) {
+            float a = 0.f;
+#pragma unroll
+            for (int q = 0; q < 4; q++) a += s.fpart[(q * 32 + tid) * 9 + k];
+            t[k] = a;
+        }
+        const float *pt = s.pt + tid * kPointStride;
+        double *rd = s.red + tid * kRedStride;
+        rd[0] = t[0];
+#pragma unroll
+        for (int k = 0; k < 3; k++) {
+            // D_k = (de[k], de[3 + k], de[6 + k]), E_k likewise from de0
+            const float r = pt[6 + k] * t[3] + pt[9 + k] * t[4] + pt[12 + k] * t[5] + pt[15 + k] * t[6] +
+                            pt[18 + k] * t[7] + pt[21 + k] * t[8];
+            rd[1 + k] = r;
+        }
+        rd[4] = t[1];
+        rd[5] = t[2];
+    }
+}
+
+// Convexity rows (conv.c:12-29) on the tensor-core path: rows 0..2 of the
+// MMA operand hold Darea g n_c split into TF32 high and low parts; the
+// residuals sum Area n_c in FP64.
+template <int NT>
+__device__ void conv_rows_tc(const DevObject &ob, Smem<PS_FORM_MIXED> &s)
+{
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int F = ob.nfac;
+    uint32_t *bh = reinterpret_cast<uint32_t *>(s.bhi), *bl = reinterpret_cast<uint32_t *>(s.blo);
+    for (int e = tid; e < 3 * F; e += NT) {
+        const int c = e / F, i = e - c * F;
+        const double *nc = (c == 0) ? ob.nx : (c == 1) ? ob.ny : ob.nz;
+        const float w = static_cast<float>(ob.darea[i] * s.gv[i] * nc[i]);
+        const uint32_t hi = tc::to_tf32(w);
+        const int off = (i >> 2) * 32 + c * 4 + (i & 3);
+        bh[off] = hi;
+        bl[off] = tc::to_tf32(w - __uint_as_float(hi));
+    }
+    if (warp < 3) {
+        const double *nc = (warp == 0) ? ob.nx : (warp == 1) ? ob.ny : ob.nz;
+        double res = 0;
+        for (int i = lane; i < F; i += 32) res = res + s.area[i] * nc[i];
+        res = warp_sum(res);
+        if (lane == 0) s.red[warp * kRedStride] = res;
     }
 }
 
@@ -718,7 +861,7 @@ __device__ void accumulate_tile_tc(const DevObject &ob, Smem<PS_FORM_MIXED> &s, 
     // (zero beyond np): 8-row x 4-point core matrices, K-adjacent ones 128
     // bytes apart, 8-row groups 1024 bytes apart; high parts in rows 0..63,
     // low parts in rows 64..127
-    unsigned char *Ab = s.bhi, *Bb = s.bhi + 16384;
+    unsigned char *Ab = s.aop, *Bb = s.aop + 16384;
     for (int cm = warp; cm < 128; cm += NT / 32) {
         const bool isB = cm >= 64;
         const int c = cm & 63, rg = c >> 3, kc = c & 7;
@@ -767,7 +910,7 @@ __device__ void tc_alpha_flush(const DevObject &ob, Smem<PS_FORM_MIXED> &s, doub
     if (t.afresh) return;
     tc_alpha_wait(s, t);
     if (*s.abort) return;
-    float *S = reinterpret_cast<float *>(s.bhi + kTcAlphaStage);   // [128][65]
+    float *S = reinterpret_cast<float *>(s.bhi);   // [128][65], after the tile's contraction
     if (warp < 4) {
         const uint32_t taddr = t.tbase + (static_cast<uint32_t>(warp * 32) << 16) + tc_acol(ob.nfac);
         float *sr = S + (warp * 32 + lane) * 65;
@@ -845,6 +988,7 @@ __device__ void evaluate(const DevObject &ob, const FitConfig &cfg, const SlotLa
         if constexpr (!kFP64) {
             s.areaR[i] = static_cast<R>(ar);
             s.gvR[i] = static_cast<R>(g);
+            if constexpr (KU == 0) s.ag[i] = make_float2(static_cast<float>(ar), static_cast<float>(ob.darea[i] * g));
         }
         asum += ar;
     }
@@ -913,6 +1057,8 @@ __device__ void evaluate(const DevObject &ob, const FitConfig &cfg, const SlotLa
                 }
                 __syncthreads();
                 // 2. facet stage (bright.c:59-120), one warp per point
+                if constexpr (kPipe) facet_stage_tc<NT>(ob, s, np, cl, cls);
+                else
                 for (int p = warp; p < np; p += NT / 32) {
                     const R *pt = s.pt + p * kPointStride;
                     const R e1 = pt[0], e2 = pt[1], e3 = pt[2];
@@ -965,6 +1111,8 @@ __device__ void evaluate(const DevObject &ob, const FitConfig &cfg, const SlotLa
                         rd[5] = dcls;
                     }
                 }
+            } else if constexpr (kPipe) {
+                conv_rows_tc<NT>(ob, s);
             } else {
                 // convexity rows (conv.c:12-29): W = Darea g n_c, residual =
                 // sum Area n_c (the residual in FP64 in both forms)
@@ -992,7 +1140,7 @@ __device__ void evaluate(const DevObject &ob, const FitConfig &cfg, const SlotLa
                     s.J[p * ma + k] = conv ? acc : s.pt[p * kPointStride + 24] * acc;
                 }
             } else if constexpr (KU == 0) {
-                contract_tc_issue<NT>(s, F, wcols, tcs);   // the work below overlaps the MMAs
+                contract_tc_issue<NT>(s, F, tcs);   // the work below overlaps the MMAs
             } else {
                 if (s.dsph)
                     contract_mixed<NT, KU, true>(s, dsphF, np, F, C, ma, wcols, conv);

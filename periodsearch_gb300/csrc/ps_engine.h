@@ -28,6 +28,7 @@ struct DevObject {
     const int *free_list;                // [mfit]
     const double *cg_first;              // [ncoef]
     const float *dsph_f;                 // [nfac][ncoef] FP32 copy for the mixed form
+    const float4 *geo_f;                 // [ndata][2] FP32 (ee, alpha), (ee0, 0) for the mixed form
 };
 
 // Constants of one scan (period_search_BOINC.cpp:817-868).
@@ -77,6 +78,8 @@ struct SlotLayout {
     size_t cg, atry, beta, da, alpha, covar, area, gv, areaR, gvR, W, J, pt, ym, red, dave, col, misc, ipiv, dsph;
     size_t bhi, blo, tcm;   // tensor-core operand tiles (TF32 high/low parts) and barrier/TMEM slot
     size_t pt2;             // second point set-up buffer (tensor-core path: next tile's set-up)
+    size_t fac, ag, fpart;  // tensor-core path: packed facet constants, per-evaluation (area, Darea g), facet-sum partials
+    size_t aop;             // tensor-core path: alpha/beta MMA operands
     size_t accs;            // per-point weights and residuals of the accumulation (mixed form)
     size_t bytes;
 };
@@ -98,7 +101,7 @@ PSG_HD constexpr int threads_of()
 constexpr int kPointStride = 32;   // reals of per-point set-up
 constexpr int kRedStride = 8;      // doubles of per-point facet sums
 constexpr int kMisc = 32;
-constexpr size_t kTcAlphaStage = 32768;   // tensor-core alpha/beta operands, then accumulator staging
+constexpr size_t kTcAlphaOperands = 32768;   // tensor-core alpha/beta operands: two 128 x 32 TF32 tiles
 
 
 // dsph_smem: the mixed form keeps the FP32 basis Dsph[F][C] in shared memory
@@ -114,9 +117,6 @@ PSG_HD inline SlotLayout make_layout(int form, int ma, int mfit, int nfac, int n
     L.P = P;
     L.dsph_smem = dsph_smem;
     L.wcols = ((nfac > mfit ? nfac : mfit) + 3) & ~3;
-    // the tensor-core path reads W in 8-row x 4-column blocks: rows 4 banks apart
-    if (dsph_smem == kBasisTensor)
-        while (L.wcols % 32 != 4) L.wcols += 4;
     const size_t rs = form == PS_FORM_MIXED ? sizeof(float) : sizeof(double);
     size_t o = 0;
     auto take = [&o](size_t bytes) {
@@ -135,7 +135,8 @@ PSG_HD inline SlotLayout make_layout(int form, int ma, int mfit, int nfac, int n
     L.gv = take(nfac * d);
     L.areaR = form == PS_FORM_MIXED ? take(nfac * rs) : L.area;
     L.gvR = form == PS_FORM_MIXED ? take(nfac * rs) : L.gv;
-    L.W = take(static_cast<size_t>(P) * L.wcols * rs);
+    // the tensor-core path writes W straight into the MMA operand
+    L.W = take(dsph_smem == kBasisTensor ? 0 : static_cast<size_t>(P) * L.wcols * rs);
     L.J = take(static_cast<size_t>(P) * ma * rs);
     L.pt = take(static_cast<size_t>(P) * kPointStride * rs);
     L.ym = take(P * d);
@@ -149,19 +150,23 @@ PSG_HD inline SlotLayout make_layout(int form, int ma, int mfit, int nfac, int n
         // B = [W_hi; W_lo]: 2P rows, the low parts right after the high parts
         // (8-row groups stride-byte-offset apart); the accumulator rows are
         // staged over it for the epilogue
-        // The same region then holds the alpha/beta operands (two 128 x 32
-        // TF32 tiles, 32 KB) and the staging of the alpha accumulator.
+        // The same region then stages the alpha accumulator; the alpha/beta
+        // operands (two 128 x 32 TF32 tiles) have their own region, so that
+        // their MMAs overlap the next tile's facet stage.
         const size_t tile = static_cast<size_t>(P) * nfac * sizeof(float);
         const size_t readback = 128 * 65 * sizeof(float);
-        size_t region = 2 * tile > readback ? 2 * tile : readback;
-        if (region < kTcAlphaStage + readback) region = kTcAlphaStage + readback;
-        L.bhi = take(region);
+        L.bhi = take(2 * tile > readback ? 2 * tile : readback);
         L.blo = L.bhi + tile;
+        L.aop = take(kTcAlphaOperands);
         L.tcm = take(32);
         L.pt2 = take(static_cast<size_t>(P) * kPointStride * rs);
+        L.fac = take(static_cast<size_t>(nfac) * 4 * sizeof(float));
+        L.ag = take(static_cast<size_t>(nfac) * 2 * sizeof(float));
+        L.fpart = take(4 * static_cast<size_t>(P) * 9 * sizeof(float));
     } else {
         L.bhi = L.blo = L.tcm = 0;
         L.pt2 = L.pt;
+        L.fac = L.ag = L.fpart = L.aop = 0;
     }
     L.accs = form == PS_FORM_MIXED ? take(2 * static_cast<size_t>(P) * sizeof(float)) : 0;
     L.bytes = o;
