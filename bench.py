@@ -9,17 +9,23 @@ contiguous chunk of the period scan (all 10 poles of each period), fitted by
 one launch of the persistent fit kernel; successive steps take chunks spread
 over the whole 2-50 h range.  Seeded synthetic data (no external dataset).
 
-value      fits/s of the chosen form (--form, default mixed) with the object
-           resident in HBM, from CUDA events around the fit kernel on its own
-           stream (sum over steps); the plain FP64 form is timed on the same
-           chunks (plain_fp64), and both forms fit a window around the true
-           period (validation: same best period, chi^2 difference);
+value      fits/s of the chosen form (--form, default mixed: FP32 facet stage,
+           shape contraction and alpha/beta on the tensor cores, FP64 phase,
+           chi^2, solve) with the object resident in HBM, from CUDA events
+           around the fit kernel on its own stream (sum over steps); the plain
+           FP64 form is timed on the same chunks (plain_fp64), and both forms
+           fit a window around the true period (validation: same best period,
+           chi^2 difference; the refined scan -- mixed scan plus FP64 refit of
+           the minimum region -- against the full FP64 scan);
 e2e        the same through the C ABI with host buffers: ps_prepare (host ->
            device copy of the tables), ps_scan (rows back to the host) and
            ps_destroy per step, wall clock;
 roofline   algorithmic FLOP of the fits (2 N F C + 60 N F + N m(m+1) + 9 F C
            per evaluation, 2 m^3 per solve) per launch over the launch time,
-           against the FP64 FMA ceiling measured live on the device;
+           against the FP32 (mixed) or FP64 FMA ceiling measured live on the
+           device; for the mixed form also the two contractions' share
+           (2 N F C + N m(m+1)) against the TF32 tensor peak (half the
+           measured dense BF16 figure);
 cpu_baseline  the CPU oracle (a restatement of the reference's FP64 path)
            on all host cores, one fit per thread, on a bounded sample.
 
@@ -56,6 +62,8 @@ def _args():
     ap.add_argument("--impl", default="engine", choices=["engine", "reference"])
     ap.add_argument("--form", default="mixed", choices=["fp64", "mixed"])
     ap.add_argument("--no-fp64-compare", action="store_true", help="skip timing the plain FP64 form")
+    ap.add_argument("--simt-compare", action="store_true",
+                    help="also time the mixed form with its contractions on the SIMT pipes")
     ap.add_argument("--periods-per-step", type=int, default=64)
     ap.add_argument("--cpu-sample-fits", type=int, default=0, help="fits in the CPU baseline sample (0: 2 per core)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -207,6 +215,11 @@ def run_reference_arm(args):
         print(json.dumps(line))
 
 
+def _measured_peaks() -> dict:
+    p = ROOT / "MEASURED_PEAKS.json"
+    return json.loads(p.read_text()) if p.exists() else {}
+
+
 def _profile_traffic(mixed: bool):
     """DRAM bytes per fit from the committed ncu summary of that form, if present."""
     prof = PROFILES[mixed]
@@ -221,11 +234,11 @@ def _profile_traffic(mixed: bool):
     return None
 
 
-def _time_form(Engine, data, form, local, starts, chunk, warmup, steps, flush, sampler=None):
+def _time_form(Engine, data, form, local, starts, chunk, warmup, steps, flush, sampler=None, tensor_cores=True):
     """Warm-up and timed steps of one form on the given chunk starts."""
     import torch
 
-    eng = Engine(data, device=local, form=form)
+    eng = Engine(data, device=local, form=form, tensor_cores=tensor_cores)
     info = eng.info
     conw_r, _ = eng.precalc_conw()
     fe = flops_per_eval(info.ndata, info.nfac, info.ncoef, info.mfit)
@@ -235,7 +248,7 @@ def _time_form(Engine, data, form, local, starts, chunk, warmup, steps, flush, s
         torch.cuda.synchronize()
         eng.scan(conw_r, starts[k], starts[k] + chunk - 1)
     torch.cuda.synchronize()
-    kernel_ms, fits, flops, launches, rows = 0.0, 0, 0.0, 0, []
+    kernel_ms, fits, flops, launches, rows, evals = 0.0, 0, 0.0, 0, [], 0
     if sampler:
         sampler.__enter__()
     try:
@@ -248,12 +261,13 @@ def _time_form(Engine, data, form, local, starts, chunk, warmup, steps, flush, s
             fits += t["fits"]
             launches += t["launches"]
             flops += t["evals"] * fe + (t["evals"] - t["fits"]) * fs
+            evals += t["evals"]
             rows.append(r)
     finally:
         if sampler:
             sampler.__exit__(None, None, None)
     torch.cuda.synchronize()
-    return {"engine": eng, "conw_r": conw_r, "kernel_ms": kernel_ms, "fits": fits, "flops": flops,
+    return {"engine": eng, "conw_r": conw_r, "kernel_ms": kernel_ms, "fits": fits, "flops": flops, "evals": evals,
             "launches": launches, "rows": rows}
 
 
@@ -301,6 +315,10 @@ def run_engine_arm(args):
         plain = None
         if chosen != PS_FORM_FP64 and not args.no_fp64_compare:
             plain = _time_form(Engine, data, PS_FORM_FP64, local, starts, chunk, 1, args.steps, flush)
+        simt = None
+        if chosen == PS_FORM_MIXED and args.simt_compare:
+            simt = _time_form(Engine, data, chosen, local, starts, chunk, 1, args.steps, flush, tensor_cores=False)
+            simt["engine"].close()
 
         # e2e: the whole C-ABI path with host buffers, per step
         e2e_t, e2e_fits, h2d, d2h = 0.0, 0, 0, 0
@@ -328,7 +346,11 @@ def run_engine_arm(args):
             rel_w = np.abs(w_main["rms"] - w_plain["rms"]) / w_plain["rms"]
             rel_c = np.concatenate([np.abs(a["rms"] - b["rms"]) / b["rms"] for a, b in zip(main["rows"], plain["rows"])])
             bm, bp = int(np.argmin(w_main["rms"])), int(np.argmin(w_plain["rms"]))
+            w_ref, st_ref = main["engine"].scan_refined(main["conw_r"], lo, hi)
             valid = {"window": [lo, hi], "truth_period_h": obj.truth["period_h"],
+                     "refined_best_index": int(st_ref["best_index"]),
+                     "refined_same_best_period": int(st_ref["best_index"]) == lo + int(np.argmin(w_plain["rms"])),
+                     "refined_fp64_refits": int(st_ref["fits_refit"]),
                      "best_index_chosen": lo + bm, "best_index_fp64": lo + bp, "same_best_period": bm == bp,
                      "best_period_h_chosen": float(w_main["period_h"][bm]),
                      "best_period_h_fp64": float(w_plain["period_h"][bp]),
@@ -361,9 +383,21 @@ def run_engine_arm(args):
                     "traffic": traffic_fit * chunk * 10 if traffic_fit else None,
                     "peak_source": ("FP32" if mixed else "FP64") + " FMA ceiling measured live on this device by "
                                    "ps_device_fma_peaks (MEASURED_PEAKS.json has no FP32/FP64 SIMT figure)",
-                    "kernel": "fit_kernel<mixed>" if mixed else "fit_kernel<fp64>",
+                    "kernel": ("fit_kernel<mixed,tensor>" if info.tensor_cores else "fit_kernel<mixed>")
+                    if mixed else "fit_kernel<fp64>",
                     "algorithmic_flop_per_launch": main["flops"] / max(launches, 1),
                     "fp64_fma_peak_tflops": p64.value, "fp32_fma_peak_tflops": p32.value}
+            if mixed and info.tensor_cores:
+                peaks = _measured_peaks()
+                tf32 = peaks["bf16_tflops"] / 2 if peaks.get("bf16_tflops") else None
+                tensor_flops = main["evals"] * (2.0 * info.ndata * info.nfac * info.ncoef
+                                                + info.ndata * info.mfit * (info.mfit + 1))
+                ta = tensor_flops / max(launches, 1) / per_launch_s / 1e12
+                roof["tensor_contractions"] = {
+                    "achieved": ta, "peak": tf32, "unit": "TFLOP/s", "frac": ta / tf32 if tf32 else None,
+                    "peak_source": "half the measured dense BF16 figure of MEASURED_PEAKS.json (TF32 rate)",
+                    "what": "algorithmic FLOP of the shape contraction and alpha/beta (2 N F C + N m(m+1) per "
+                            "evaluation), run as TF32 high/low-split MMAs"}
             fp64 = None
             if plain is not None:
                 pv = plain["fits"] / (plain["kernel_ms"] / 1e3)
@@ -373,6 +407,9 @@ def run_engine_arm(args):
                         "roofline": {"bound": "fp64", "achieved": pa, "peak": p64.value, "unit": "TFLOP/s",
                                      "frac": pa / p64.value,
                                      "traffic": (_profile_traffic(False) or 0) * chunk * 10 or None}}
+            if simt is not None:
+                sv = simt["fits"] / (simt["kernel_ms"] / 1e3)
+                roof["mixed_simt_contractions"] = {"value": sv, "unit": "fits/s", "tensor_speedup": value / sv}
             cb = None
             if not args.no_cpu_baseline:
                 periods = [n for st in starts[args.warmup:] for n in range(st, st + chunk)]
@@ -384,7 +421,8 @@ def run_engine_arm(args):
                     "config": {"workload": WORKLOAD, "form": args.form, "periods_per_step": chunk,
                                "fits_per_step": chunk * 10, "ndata": info.ndata, "nfac": info.nfac,
                                "ncoef": info.ncoef, "mfit": info.mfit, "n_max": n_max, "conw_r": main["conw_r"],
-                               "slots": info.slots, "l2": "flushed between steps (256 MiB rewrite)",
+                               "slots": info.slots, "tensor_cores": bool(info.tensor_cores),
+                               "tile_points": info.tile_points, "l2": "flushed between steps (256 MiB rewrite)",
                                "truth": obj.truth},
                     "e2e": {"value": e2e_fits_all / e2e_s, "unit": "fits/s", "h2d_bytes_per_step": h2d,
                             "d2h_bytes_per_step": d2h},
