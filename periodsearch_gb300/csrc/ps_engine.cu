@@ -207,7 +207,7 @@ __device__ inline double rotation_phase(double omg, double t, double phi0)
 
 // Lit-facet terms of the Lommel-Seeliger + Lambert law (bright.c:65-74,
 // 116-117).  The FP64 form divides as the reference does; the mixed form
-// multiplies by one reciprocal.
+// multiplies by one approximate reciprocal.
 template <class R, int FORM>
 struct LitTerms {
     R sv, dsmu, dsmu0, dcls_w;  // s, ds/dmu, ds/dmu0, mu*mu0/(mu+mu0)
@@ -221,7 +221,8 @@ struct LitTerms {
             dsmu0 = cls * (q1 * q1) + cl * mu;
             dcls_w = mu * mu0 / dnom;
         } else {
-            const R r = __frcp_rn(dnom);
+            R r;
+            asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(dnom));   // ~1 ulp: the mixed form's budget
             sv = mu * mu0 * (cl + cls * r);
             const R q0 = mu0 * r, q1 = mu * r;
             dsmu = cls * (q0 * q0) + cl * mu0;
@@ -470,8 +471,13 @@ __device__ inline void setup_point(const DevObject &ob, const FitConfig &cfg, in
     const double td = ob.tim[q];
     const R t = R(td);
     R ex;
-    if constexpr (kFP64) ex = exp(-alpha / php1);
-    else ex = expf(-alpha / php1);
+    R inv_w = 0;
+    if constexpr (kFP64) {
+        ex = exp(-alpha / php1);
+    } else {
+        inv_w = 1.f / php1;
+        ex = expf(-alpha * inv_w);
+    }
     const R scale = 1 + php0 * ex + php2 * alpha;
     const double f = rotation_phase<FORM>(omg, td, cfg.phi0);
     R cf, sf;
@@ -529,7 +535,8 @@ __device__ inline void setup_point(const DevObject &ob, const FitConfig &cfg, in
         }
     pt[24] = scale;
     pt[25] = ex;
-    pt[26] = php0 * ex * alpha / (php1 * php1);
+    if constexpr (kFP64) pt[26] = php0 * ex * alpha / (php1 * php1);
+    else pt[26] = php0 * ex * alpha * (inv_w * inv_w);
     pt[27] = alpha;
 }
 
@@ -1392,44 +1399,69 @@ __device__ int gauss_jordan(double *A, double *b, int n, double *col, int *ipiv,
 // positive definite; lower triangle used, overwritten by L) and the solve of
 // L L^T x = b, in FP64.  The forward substitution runs inside the
 // factorisation (b is the bordering column: y_j = b_j / L_jj, then b_i -=
-// L_ij y_j with the trailing update), so a step costs two CTA barriers: warp
-// 0 takes the pivot's reciprocal square root and scales column j and y_j,
-// then all threads update the trailing block.  The back substitution uses
-// the stored reciprocals.  Returns 2 when a pivot is not positive.
+// L_ij y_j with the trailing update).  Columns are taken two at a time: warp
+// 0 factors the 2 x 2 pivot block and scales both columns and y, then all
+// threads apply the rank-2 update to the trailing block -- two CTA barriers
+// per pair of columns.  The back substitution uses the stored reciprocals.
+// Returns 2 when a pivot is not positive.
 template <int NT>
 __device__ int cholesky_solve(double *A, double *b, int n, double *col, double *flag)
 {
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     __syncthreads();
-    for (int j = 0; j < n; j++) {
+    for (int j = 0; j < n; j += 2) {
+        const bool two = j + 1 < n;
         if (warp == 0) {
-            double inv = 0;
+            double i0 = 0, l10 = 0, i1 = 0;
             if (lane == 0) {
-                const double d = A[j * n + j];
-                const bool ok = d > 0.0;
-                inv = ok ? rsqrt(d) : 0.0;
+                const double d0 = A[j * n + j];
+                bool ok = d0 > 0.0;
+                i0 = ok ? rsqrt(d0) : 0.0;
+                A[j * n + j] = d0 * i0;
+                col[j] = i0;
+                const double y0 = b[j] * i0;
+                b[j] = y0;
+                if (two && ok) {
+                    l10 = A[(j + 1) * n + j] * i0;
+                    const double d1 = A[(j + 1) * n + j + 1] - l10 * l10;
+                    ok = d1 > 0.0;
+                    i1 = ok ? rsqrt(d1) : 0.0;
+                    A[(j + 1) * n + j] = l10;
+                    A[(j + 1) * n + j + 1] = d1 * i1;
+                    col[j + 1] = i1;
+                    b[j + 1] = (b[j + 1] - l10 * y0) * i1;
+                }
                 *flag = ok ? 1.0 : 0.0;
-                A[j * n + j] = d * inv;      // L_jj = sqrt(d)
-                col[j] = inv;
-                b[j] *= inv;                 // y_j
             }
-            inv = __shfl_sync(0xffffffffu, inv, 0);
-            for (int i = j + 1 + lane; i < n; i += 32) A[i * n + j] *= inv;
+            i0 = __shfl_sync(0xffffffffu, i0, 0);
+            l10 = __shfl_sync(0xffffffffu, l10, 0);
+            i1 = __shfl_sync(0xffffffffu, i1, 0);
+            const int r0 = j + (two ? 2 : 1);
+            for (int i = r0 + lane; i < n; i += 32) {
+                const double a0 = A[i * n + j] * i0;
+                A[i * n + j] = a0;
+                if (two) A[i * n + j + 1] = (A[i * n + j + 1] - a0 * l10) * i1;
+            }
         }
         __syncthreads();
         if (*flag == 0.0) return 2;
-        const int m = n - j - 1;
+        const int j2 = j + (two ? 2 : 1);
+        const int m = n - j2;
         const int ntri = m * (m + 1) / 2;
-        const double yj = b[j];
+        const double y0 = b[j], y1 = two ? b[j + 1] : 0.0;
         for (int e = tid; e < ntri + m; e += NT) {
             if (e < ntri) {
                 const int r = tri_row(e);
                 const int c = e - r * (r + 1) / 2;
-                const int i = j + 1 + r, k = j + 1 + c;
-                A[i * n + k] -= A[i * n + j] * A[k * n + j];
+                const int i = j2 + r, k = j2 + c;
+                double v = A[i * n + k] - A[i * n + j] * A[k * n + j];
+                if (two) v -= A[i * n + j + 1] * A[k * n + j + 1];
+                A[i * n + k] = v;
             } else {
-                const int i = j + 1 + (e - ntri);
-                b[i] -= A[i * n + j] * yj;
+                const int i = j2 + (e - ntri);
+                double v = b[i] - A[i * n + j] * y0;
+                if (two) v -= A[i * n + j + 1] * y1;
+                b[i] = v;
             }
         }
         __syncthreads();
