@@ -64,6 +64,9 @@ def _args():
     ap.add_argument("--no-fp64-compare", action="store_true", help="skip timing the plain FP64 form")
     ap.add_argument("--simt-compare", action="store_true",
                     help="also time the mixed form with its contractions on the SIMT pipes")
+    ap.add_argument("--multi-object", type=int, default=0,
+                    help="also time K small objects (Ndata logU[100, 2000]) packed into one launch against one "
+                         "launch per object")
     ap.add_argument("--periods-per-step", type=int, default=64)
     ap.add_argument("--cpu-sample-fits", type=int, default=0, help="fits in the CPU baseline sample (0: 2 per core)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -213,6 +216,50 @@ def run_reference_arm(args):
                 "cpu_baseline": cb, "e2e": {"value": v, "unit": "fits/s", "h2d_bytes_per_step": 0,
                                             "d2h_bytes_per_step": 0}}
         print(json.dumps(line))
+
+
+def multi_object(K: int, form: int, local: int, units_per_object: int = 8) -> dict:
+    """Packed launch of K objects (sparse calibrated data, Ndata log-uniform
+    in [100, 2000], seeded) against one launch per object, on the same
+    random (object, period, pole) units."""
+    import numpy as np
+
+    from periodsearch_gb300 import Engine, Pack, read_input, synth
+
+    rng = np.random.default_rng(2024)
+    engines = []
+    with tempfile.TemporaryDirectory() as td:
+        for k in range(K):
+            nd = int(round(math.exp(rng.uniform(math.log(100), math.log(2000)))))
+            cfg = synth.SynthConfig(name=f"mo{k}", n_sparse=nd, sparse_block=1000)
+            path = Path(td) / f"o{k}"
+            synth.write_object(path, cfg, seed=7000 + k)
+            engines.append(Engine(read_input(path), device=local, form=form))
+    try:
+        conw = [e.precalc_conw()[0] for e in engines]
+        obj, per, pole = [], [], []
+        for o, e in enumerate(engines):
+            for p in rng.choice(int(e.info.n_max), size=units_per_object, replace=False) + 1:
+                obj += [o] * 10
+                per += [int(p)] * 10
+                pole += list(range(1, 11))
+        obj, per, pole = np.array(obj), np.array(per), np.array(pole)
+        seq_ms = 0.0
+        for o, e in enumerate(engines):
+            sel = obj == o
+            e.fit_batch(conw[o], per[sel], pole[sel])
+            seq_ms += e.timing()["kernel_ms"]
+        with Pack(engines, form=form) as pk:
+            pk.fit(conw, obj, per, pole)   # warm-up
+            pk.fit(conw, obj, per, pole)
+            pms = pk.timing()["kernel_ms"]
+        nd = [e.info.ndata for e in engines]
+        return {"objects": K, "fits": int(len(obj)), "ndata_min": min(nd), "ndata_max": max(nd),
+                "packed_fits_per_s": len(obj) / (pms / 1e3), "one_launch_per_object_fits_per_s": len(obj) / (seq_ms / 1e3),
+                "speedup": seq_ms / pms}
+    finally:
+        for e in engines:
+            e.close()
 
 
 def _measured_peaks() -> dict:
@@ -410,6 +457,7 @@ def run_engine_arm(args):
             if simt is not None:
                 sv = simt["fits"] / (simt["kernel_ms"] / 1e3)
                 roof["mixed_simt_contractions"] = {"value": sv, "unit": "fits/s", "tensor_speedup": value / sv}
+            mo = multi_object(args.multi_object, chosen, local) if args.multi_object > 0 else None
             cb = None
             if not args.no_cpu_baseline:
                 periods = [n for st in starts[args.warmup:] for n in range(st, st + chunk)]
@@ -427,6 +475,7 @@ def run_engine_arm(args):
                     "e2e": {"value": e2e_fits_all / e2e_s, "unit": "fits/s", "h2d_bytes_per_step": h2d,
                             "d2h_bytes_per_step": d2h},
                     "gpu_launches": launches, "roofline": roof, "plain_fp64": fp64, "validation": valid,
+                    "multi_object": mo,
                     "cpu_baseline": cb, "clocks": sampler.summary() if sampler else None, "wall_s": wall}
             print(json.dumps(line))
         main["engine"].close()

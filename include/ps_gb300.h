@@ -319,6 +319,30 @@ ps_status ps_scan_learned(ps_ctx *ctx, double conw_r, int64_t n_lo, int64_t n_hi
  * completion was not observed within the wait limit. */
 ps_status ps_tc_selftest(int32_t device, const float *A, const float *B, int32_t K, float *D);
 
+/* ---- multi-object packing ---- */
+
+/* Many small objects (work units of a multi-object run) fitted by one
+ * persistent launch with one device work queue.  The contexts must be
+ * prepared on the same device with identical shape tables (nrows, Lmax,
+ * Mmax) and free-parameter layout; each keeps its own photometry, period
+ * grid and convexity weight.  The pack borrows the contexts' device tables:
+ * destroy it before them. */
+typedef struct ps_pack ps_pack;
+
+ps_status ps_pack_create(ps_ctx *const *ctxs, int32_t n_objects, int32_t form, ps_pack **out);
+
+/* Fits n_fits units (object index into the create-time list, 1-based period
+ * index of that object's grid, pole 1..10) with conw_r[object] as each
+ * object's convexity weight.  Units are dispatched largest object first
+ * (Ndata) for load balance; out[] is in the caller's order. */
+ps_status ps_pack_fit(ps_pack *pack, const double *conw_r, int64_t n_fits, const int32_t *object,
+                      const int64_t *period_index, const int32_t *pole, ps_fit *out);
+
+/* Device timing of the last ps_pack_fit. */
+ps_status ps_pack_timing(const ps_pack *pack, ps_timing *out);
+const char *ps_pack_last_error(const ps_pack *pack);
+void ps_pack_destroy(ps_pack *pack);
+
 /* ---- replica validator ---- */
 
 /* Agreement of two replicas of one work unit under the project's validator

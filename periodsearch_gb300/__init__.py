@@ -25,7 +25,7 @@ import numpy as np
 from . import _abi
 from ._abi import EngineError, N_POLES, PS_FORM_FP64, PS_FORM_MIXED
 
-__all__ = ["Engine", "InputData", "read_input", "run_files", "format_row", "shape_tables", "ROW_DTYPE",
+__all__ = ["Engine", "Pack", "InputData", "read_input", "run_files", "format_row", "shape_tables", "ROW_DTYPE",
            "FIT_DTYPE", "EngineError", "PS_FORM_FP64", "PS_FORM_MIXED", "N_POLES"]
 
 ROW_DTYPE = np.dtype([(n, "f8") for n in ("period_h", "rms", "chi2", "dark_or_conw", "lambda_deg", "beta_deg")])
@@ -83,6 +83,49 @@ class InputData:
     def nbytes(self) -> int:
         return sum(a.nbytes for a in (self.lc_points, self.lc_calibrated, self.lc_weight, self.jd, self.brightness,
                                       self.sun, self.earth))
+
+
+class Pack:
+    """Several objects fitted by one packed launch (ps_pack_create ..
+    ps_pack_destroy).  The engines must share the shape tables and stay open
+    while the pack lives."""
+
+    def __init__(self, engines, form: int = PS_FORM_FP64):
+        self._L = _abi.lib()
+        self._engines = list(engines)
+        arr = (C.c_void_p * len(self._engines))(*[e._ctx.value for e in self._engines])
+        h = C.c_void_p()
+        _abi.check(self._L.ps_pack_create(arr, len(self._engines), form, C.byref(h)), "ps_pack_create")
+        self._h = h
+
+    def fit(self, conw_r, object_index, period_index, pole) -> np.ndarray:
+        cw = np.ascontiguousarray(conw_r, np.float64)
+        ob = np.ascontiguousarray(object_index, np.int32)
+        pi = np.ascontiguousarray(period_index, np.int64)
+        po = np.ascontiguousarray(pole, np.int32)
+        out = np.zeros(len(pi), FIT_DTYPE)
+        st = self._L.ps_pack_fit(self._h, cw.ctypes.data_as(C.POINTER(C.c_double)), len(pi),
+                                 ob.ctypes.data_as(C.POINTER(C.c_int32)), pi.ctypes.data_as(C.POINTER(C.c_int64)),
+                                 po.ctypes.data_as(C.POINTER(C.c_int32)), out.ctypes.data_as(C.POINTER(_abi.Fit)))
+        if st != _abi.PS_OK:
+            raise EngineError(st, "ps_pack_fit", self._L.ps_pack_last_error(self._h).decode())
+        return out
+
+    def timing(self) -> dict:
+        t = _abi.Timing()
+        _abi.check(self._L.ps_pack_timing(self._h, C.byref(t)), "ps_pack_timing")
+        return {k: getattr(t, k) for k, _ in _abi.Timing._fields_}
+
+    def close(self) -> None:
+        if self._h:
+            self._L.ps_pack_destroy(self._h)
+            self._h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
 
 
 def read_input(path: str) -> InputData:

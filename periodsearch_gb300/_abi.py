@@ -128,6 +128,12 @@ SIGNATURES = {
     "ps_screen": (C.c_int, [_CTX, C.c_double, C.c_int64, C.c_int64, C.POINTER(C.c_float), C.POINTER(Fit)]),
     "ps_tc_selftest": (C.c_int, [C.c_int32, C.POINTER(C.c_float), C.POINTER(C.c_float), C.c_int32,
                                  C.POINTER(C.c_float)]),
+    "ps_pack_create": (C.c_int, [C.POINTER(C.c_void_p), C.c_int32, C.c_int32, C.POINTER(C.c_void_p)]),
+    "ps_pack_fit": (C.c_int, [C.c_void_p, C.POINTER(C.c_double), C.c_int64, C.POINTER(C.c_int32),
+                              C.POINTER(C.c_int64), C.POINTER(C.c_int32), C.POINTER(Fit)]),
+    "ps_pack_timing": (C.c_int, [C.c_void_p, C.POINTER(Timing)]),
+    "ps_pack_last_error": (C.c_char_p, [C.c_void_p]),
+    "ps_pack_destroy": (None, [C.c_void_p]),
     "ps_validate_rows": (C.c_int, [C.POINTER(Row), C.c_int64, C.POINTER(Row), C.c_int64, C.POINTER(C.c_double),
                                    C.POINTER(ValidateReport)]),
     "ps_validate_files": (C.c_int, [C.c_char_p, C.c_char_p, C.POINTER(C.c_double), C.POINTER(ValidateReport)]),

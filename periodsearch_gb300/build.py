@@ -49,7 +49,7 @@ def build(force: bool = False, verbose: bool = False) -> Path:
     nvcc = str(cuda / "bin" / "nvcc")
     inc = ["-I", str(ROOT / "include"), "-I", str(CSRC)]
     BUILD.mkdir(exist_ok=True)
-    headers = sorted(CSRC.glob("*.h")) + [ROOT / "include" / "ps_gb300.h"]
+    headers = sorted(CSRC.glob("*.h")) + sorted(CSRC.glob("*.cuh")) + [ROOT / "include" / "ps_gb300.h"]
     units = {
         "ps_engine.o": [nvcc, *ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
                         "-Xptxas", "-v" if verbose else "-O3", *inc,
@@ -58,6 +58,8 @@ def build(force: bool = False, verbose: bool = False) -> Path:
                      "-c", str(CSRC / "ps_mlp.cu"), "-o", str(BUILD / "ps_mlp.o")],
         "ps_tc.o": [nvcc, *ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", *inc,
                     "-c", str(CSRC / "ps_tc.cu"), "-o", str(BUILD / "ps_tc.o")],
+        "ps_pack.o": [nvcc, *ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", *inc,
+                      "-c", str(CSRC / "ps_pack.cu"), "-o", str(BUILD / "ps_pack.o")],
         "ps_api.o": ["g++", "-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", *inc,
                      "-I", str(cuda / "include"), "-c", str(CSRC / "ps_api.cpp"), "-o", str(BUILD / "ps_api.o")],
         "ps_setup.o": ["g++", "-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", *inc,
@@ -66,9 +68,10 @@ def build(force: bool = False, verbose: bool = False) -> Path:
                           "-c", str(CSRC / "ps_validate.cpp"), "-o", str(BUILD / "ps_validate.o")],
     }
     srcs = {"ps_engine.o": CSRC / "ps_engine.cu", "ps_mlp.o": CSRC / "ps_mlp.cu", "ps_api.o": CSRC / "ps_api.cpp",
-            "ps_setup.o": CSRC / "ps_setup.cpp", "ps_validate.o": CSRC / "ps_validate.cpp", "ps_tc.o": CSRC / "ps_tc.cu"}
+            "ps_setup.o": CSRC / "ps_setup.cpp", "ps_validate.o": CSRC / "ps_validate.cpp", "ps_tc.o": CSRC / "ps_tc.cu",
+            "ps_pack.o": CSRC / "ps_pack.cu"}
     todo = [cmd for obj, cmd in units.items() if force or _stale(BUILD / obj, [srcs[obj], *headers])]
-    with ThreadPoolExecutor(max_workers=6) as ex:
+    with ThreadPoolExecutor(max_workers=8) as ex:
         list(ex.map(_run, todo))
     objs = [str(BUILD / o) for o in units]
     if force or todo or _stale(LIB, [Path(o) for o in objs]):

@@ -917,6 +917,221 @@ ps_status ps_scan_refined(ps_ctx *c, double conw_r, int64_t n_lo, int64_t n_hi, 
     return PS_OK;
 }
 
+}  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Multi-object packing
+// ---------------------------------------------------------------------------
+struct ps_pack {
+    std::vector<ps_ctx *> ctx;
+    int form = PS_FORM_FP64;
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t ev[2] = {nullptr, nullptr};
+    psg::DevObject *d_objs = nullptr;
+    psg::FitConfig *d_cfgs = nullptr;
+    double *d_scratch = nullptr;
+    size_t scratch_stride = 0;
+    int slots = 0, P = 0, dsph_smem = 0;
+    size_t smem = 0;
+    unsigned long long *d_queue = nullptr;
+    int *d_obj = nullptr, *d_pole = nullptr;
+    int64_t *d_pidx = nullptr;
+    ps_fit *d_out = nullptr;
+    size_t cap = 0;
+    ps_timing timing{};
+    std::string err;
+};
+
+namespace {
+
+ps_status pack_fail(ps_pack *k, cudaError_t e, const char *what)
+{
+    k->err = std::string(what) + ": " + cudaGetErrorString(e);
+    return PS_ERR_CUDA;
+}
+
+#define PSG_PACK_CUDA(pk, call)                                    \
+    do {                                                           \
+        cudaError_t e_ = (call);                                   \
+        if (e_ != cudaSuccess) return pack_fail((pk), e_, #call);  \
+    } while (0)
+
+bool same_shape(const psg::HostObject &a, const psg::HostObject &b)
+{
+    return a.shape.nfac == b.shape.nfac && a.ncoef == b.ncoef && a.ma == b.ma && a.mfit == b.mfit &&
+           a.shape.npairs == b.shape.npairs && a.shape.mmax == b.shape.mmax && a.free_list == b.free_list &&
+           a.shape.dsph == b.shape.dsph && a.shape.nor == b.shape.nor;
+}
+
+}  // namespace
+
+extern "C" {
+
+ps_status ps_pack_create(ps_ctx *const *ctxs, int32_t n, int32_t form, ps_pack **out)
+{
+    if (!ctxs || n < 1 || !out || (form != PS_FORM_FP64 && form != PS_FORM_MIXED)) return PS_ERR_ARG;
+    *out = nullptr;
+    for (int32_t i = 0; i < n; i++) {
+        if (!ctxs[i]) return PS_ERR_ARG;
+        if (ctxs[i]->opt.device != ctxs[0]->opt.device || !same_shape(ctxs[i]->obj, ctxs[0]->obj)) return PS_ERR_ARG;
+    }
+    std::unique_ptr<ps_pack> k(new ps_pack());
+    k->ctx.assign(ctxs, ctxs + n);
+    k->form = form;
+    k->device = ctxs[0]->opt.device;
+    ps_ctx *c0 = ctxs[0];
+    PSG_PACK_CUDA(k.get(), cudaSetDevice(k->device));
+    ps_status st = make_plan(c0, form);
+    if (st != PS_OK) {
+        k->err = c0->err;
+        return st;
+    }
+    const FormPlan &pl = c0->plan[form];
+    k->P = pl.P;
+    k->dsph_smem = pl.dsph_smem;
+    k->smem = pl.smem;
+    k->slots = pl.slots;
+    int e = psg::set_pack_smem(form, k->smem, c0->obj.ncoef, k->dsph_smem);
+    if (e != 0) return pack_fail(k.get(), static_cast<cudaError_t>(e), "cudaFuncSetAttribute");
+    for (ps_ctx *c : k->ctx) k->scratch_stride = std::max(k->scratch_stride, c->scratch_stride);
+    PSG_PACK_CUDA(k.get(), cudaStreamCreateWithFlags(&k->stream, cudaStreamNonBlocking));
+    PSG_PACK_CUDA(k.get(), cudaEventCreate(&k->ev[0]));
+    PSG_PACK_CUDA(k.get(), cudaEventCreate(&k->ev[1]));
+    PSG_PACK_CUDA(k.get(), cudaMalloc(&k->d_objs, sizeof(psg::DevObject) * n));
+    PSG_PACK_CUDA(k.get(), cudaMalloc(&k->d_cfgs, sizeof(psg::FitConfig) * n));
+    PSG_PACK_CUDA(k.get(), cudaMalloc(&k->d_scratch, k->scratch_stride * k->slots * sizeof(double)));
+    PSG_PACK_CUDA(k.get(), cudaMalloc(&k->d_queue, sizeof(unsigned long long)));
+    std::vector<psg::DevObject> objs(static_cast<size_t>(n));
+    for (int32_t i = 0; i < n; i++) objs[static_cast<size_t>(i)] = ctxs[i]->dob;
+    PSG_PACK_CUDA(k.get(), cudaMemcpy(k->d_objs, objs.data(), sizeof(psg::DevObject) * n, cudaMemcpyHostToDevice));
+    *out = k.release();
+    return PS_OK;
+}
+
+ps_status ps_pack_fit(ps_pack *k, const double *conw_r, int64_t n_fits, const int32_t *object,
+                      const int64_t *period_index, const int32_t *pole, ps_fit *out)
+{
+    if (!k || !conw_r || n_fits < 1 || !object || !period_index || !pole || !out) return PS_ERR_ARG;
+    const int32_t nobj = static_cast<int32_t>(k->ctx.size());
+    for (int32_t o = 0; o < nobj; o++)
+        if (!(conw_r[o] > 0)) return PS_ERR_ARG;
+    for (int64_t i = 0; i < n_fits; i++)
+        if (object[i] < 0 || object[i] >= nobj || period_index[i] < 1 || pole[i] < 1 || pole[i] > PS_N_POLES)
+            return PS_ERR_ARG;
+    PSG_PACK_CUDA(k, cudaSetDevice(k->device));
+    // largest objects first: the queue then ends on short fits
+    std::vector<int64_t> order(static_cast<size_t>(n_fits));
+    for (int64_t i = 0; i < n_fits; i++) order[static_cast<size_t>(i)] = i;
+    std::stable_sort(order.begin(), order.end(), [&](int64_t a, int64_t b) {
+        return k->ctx[static_cast<size_t>(object[a])]->obj.ndata > k->ctx[static_cast<size_t>(object[b])]->obj.ndata;
+    });
+    std::vector<int> h_obj(static_cast<size_t>(n_fits)), h_pole(static_cast<size_t>(n_fits));
+    std::vector<int64_t> h_pidx(static_cast<size_t>(n_fits));
+    for (int64_t i = 0; i < n_fits; i++) {
+        const int64_t u = order[static_cast<size_t>(i)];
+        h_obj[static_cast<size_t>(i)] = object[u];
+        h_pidx[static_cast<size_t>(i)] = period_index[u];
+        h_pole[static_cast<size_t>(i)] = pole[u];
+    }
+    std::vector<psg::FitConfig> cfgs(static_cast<size_t>(nobj));
+    for (int32_t o = 0; o < nobj; o++) cfgs[static_cast<size_t>(o)] = make_config(k->ctx[static_cast<size_t>(o)], conw_r[o]);
+    if (static_cast<size_t>(n_fits) > k->cap) {
+        cudaFree(k->d_obj);
+        cudaFree(k->d_pole);
+        cudaFree(k->d_pidx);
+        cudaFree(k->d_out);
+        k->d_obj = k->d_pole = nullptr;
+        k->d_pidx = nullptr;
+        k->d_out = nullptr;
+        k->cap = 0;
+        PSG_PACK_CUDA(k, cudaMalloc(&k->d_obj, sizeof(int) * n_fits));
+        PSG_PACK_CUDA(k, cudaMalloc(&k->d_pole, sizeof(int) * n_fits));
+        PSG_PACK_CUDA(k, cudaMalloc(&k->d_pidx, sizeof(int64_t) * n_fits));
+        PSG_PACK_CUDA(k, cudaMalloc(&k->d_out, sizeof(ps_fit) * n_fits));
+        k->cap = static_cast<size_t>(n_fits);
+    }
+    PSG_PACK_CUDA(k, cudaMemcpyAsync(k->d_cfgs, cfgs.data(), sizeof(psg::FitConfig) * nobj, cudaMemcpyHostToDevice,
+                                     k->stream));
+    PSG_PACK_CUDA(k, cudaMemcpyAsync(k->d_obj, h_obj.data(), sizeof(int) * n_fits, cudaMemcpyHostToDevice, k->stream));
+    PSG_PACK_CUDA(k, cudaMemcpyAsync(k->d_pole, h_pole.data(), sizeof(int) * n_fits, cudaMemcpyHostToDevice, k->stream));
+    PSG_PACK_CUDA(k, cudaMemcpyAsync(k->d_pidx, h_pidx.data(), sizeof(int64_t) * n_fits, cudaMemcpyHostToDevice,
+                                     k->stream));
+    PSG_PACK_CUDA(k, cudaMemsetAsync(k->d_queue, 0, sizeof(unsigned long long), k->stream));
+    psg::FitWork w{};
+    w.n_lo = 1;
+    w.nfits = n_fits;
+    w.period_index = k->d_pidx;
+    w.pole = k->d_pole;
+    w.queue = k->d_queue;
+    w.scratch = k->d_scratch;
+    w.scratch_stride = k->scratch_stride;
+    w.out = k->d_out;
+    w.objs = k->d_objs;
+    w.cfgs = k->d_cfgs;
+    w.object = k->d_obj;
+    const int grid = static_cast<int>(std::min<int64_t>(k->slots, n_fits));
+    PSG_PACK_CUDA(k, cudaEventRecord(k->ev[0], k->stream));
+    int e = psg::launch_pack(k->form, w, k->ctx[0]->obj.ncoef, grid, k->P, k->smem, k->dsph_smem, k->stream);
+    if (e != 0) return pack_fail(k, static_cast<cudaError_t>(e), "packed fit kernel launch");
+    PSG_PACK_CUDA(k, cudaEventRecord(k->ev[1], k->stream));
+    std::vector<ps_fit> sorted(static_cast<size_t>(n_fits));
+    PSG_PACK_CUDA(k, cudaMemcpyAsync(sorted.data(), k->d_out, sizeof(ps_fit) * n_fits, cudaMemcpyDeviceToHost,
+                                     k->stream));
+    PSG_PACK_CUDA(k, cudaStreamSynchronize(k->stream));
+    float ms = 0;
+    cudaEventElapsedTime(&ms, k->ev[0], k->ev[1]);
+    int64_t evals = 0;
+    for (int64_t i = 0; i < n_fits; i++) {
+        const ps_fit &f = sorted[static_cast<size_t>(i)];
+        out[order[static_cast<size_t>(i)]] = f;
+        evals += f.niter + 1;
+        if (f.err_code == 16) {
+            k->err = "a tensor-core wait gave up: fit results are incomplete";
+            return PS_ERR_TIMEOUT;
+        }
+    }
+    k->timing = ps_timing{};
+    k->timing.kernel_ms = ms;
+    k->timing.total_ms = ms;
+    k->timing.fits = n_fits;
+    k->timing.evals = evals;
+    k->timing.launches = 1;
+    return PS_OK;
+}
+
+ps_status ps_pack_timing(const ps_pack *k, ps_timing *out)
+{
+    if (!k || !out) return PS_ERR_ARG;
+    *out = k->timing;
+    return PS_OK;
+}
+
+const char *ps_pack_last_error(const ps_pack *k) { return k ? k->err.c_str() : "null pack"; }
+
+void ps_pack_destroy(ps_pack *k)
+{
+    if (!k) return;
+    cudaSetDevice(k->device);
+    if (k->stream) cudaStreamSynchronize(k->stream);
+    cudaFree(k->d_objs);
+    cudaFree(k->d_cfgs);
+    cudaFree(k->d_scratch);
+    cudaFree(k->d_queue);
+    cudaFree(k->d_obj);
+    cudaFree(k->d_pole);
+    cudaFree(k->d_pidx);
+    cudaFree(k->d_out);
+    if (k->ev[0]) cudaEventDestroy(k->ev[0]);
+    if (k->ev[1]) cudaEventDestroy(k->ev[1]);
+    if (k->stream) cudaStreamDestroy(k->stream);
+    delete k;
+}
+
+}  // extern "C"
+
+extern "C" {
+
 ps_status ps_last_timing(const ps_ctx *c, ps_timing *out)
 {
     if (!c || !out) return PS_ERR_ARG;

@@ -1,1780 +1,9 @@
-// ps_engine.cu -- fit kernels of the GB300 period-search engine (sm_103a).
-//
-// One CTA is one fit slot.  A slot pulls fits (period index, initial pole)
-// from a device work counter and runs the whole Levenberg-Marquardt fit on
-// the device: model evaluation (the reference's mrqcof with curv, blmatrix,
-// bright and conv), the damped normal-equation solve (gauss_errc), the
-// accept/reject and lambda update (mrqmin) and the stop rule of the driver
-// loop (period_search_BOINC.cpp:868-893).  Nothing returns to the host until
-// every fit of the launch is done.
-//
-// Evaluation of one parameter vector, per tile of P observations:
-//   1. point set-up (one thread per point, FP64): solar phase angle, phase
-//      function, body rotation f = fmod(omega*t + phi0, 2*pi) and the rotated
-//      Earth/Sun directions with their beta/lambda/omega derivatives;
-//   2. facet stage (one warp per point, lanes over facets): mu, mu0, the
-//      Lommel-Seeliger + Lambert law, brightness, rotation and scattering
-//      derivatives; lit facets write W[p][i] = Darea_i * s_pi * g_i;
-//   3. shape contraction J[p][k] = Scale_p * sum_i W[p][i] * Dsph[i][k]
-//      (the reference's sum over lit facets of dbr * Dg);
-//   4. relative lightcurves: per-lightcurve sums, then the renormalisation of
-//      mrqcof.c:90-104 from a per-slot scratch copy of the lightcurve's rows;
-//   5. normal-matrix accumulation alpha = J^T W J, beta, chi^2 over the free
-//      parameters, each alpha element summed over points in data order.
-// The three convexity rows (conv.c) are three more rows of the same
-// contraction with W[c][i] = Darea_i * g_i * n_i[c].
-//
-// The mixed form runs the contraction on the tensor cores when the shape
-// tables allow it (tensor_basis_ok): tcgen05 TF32 MMAs with the basis split
-// into high and low TF32 parts resident in Tensor Memory for the CTA's
-// lifetime (A = [Dsph_hi^T; Dsph_lo^T], 128 lanes x F columns) and W split
-// the same way in shared memory (B), so that the four partial products give
-// the contraction to FP32 accuracy; otherwise on the SIMT pipes.
-#include <cuda_runtime.h>
-
-#include <cmath>
-#include <cstdint>
-#include <mutex>
-#include <type_traits>
-
-#include "ps_engine.h"
-#include "ps_tc.cuh"
+// ps_engine.cu -- single-object launchers of the fit kernels (ps_fit.cuh),
+// the FMA peak probe and the allocation-free launch.
+#include "ps_fit.cuh"
 
 namespace psg {
-
 namespace {
-
-constexpr double kPi = 3.14159265358979323846;
-constexpr double kTwoPi = 2 * kPi;
-constexpr double kRad2Deg = 180 / kPi;
-constexpr double kDeg2Rad = kPi / 180;
-constexpr double kTinyMu = 1e-8;
-// 2*pi split for the mixed form's phase reduction: hi = 2*pi rounded to
-// double, lo = 2*pi - hi.
-constexpr double kTwoPiHi = 6.283185307179586;
-constexpr double kTwoPiLo = 2.4492935982947064e-16;
-constexpr double kInvTwoPi = 0.15915494309189535;
-
-__constant__ double c_beta_pole[PS_N_POLES] = {0, 0, 0, 0, 60, 60, 60, -60, -60, -60};
-__constant__ double c_lambda_pole[PS_N_POLES] = {0, 90, 180, 270, 60, 180, 300, 60, 180, 300};
-
-// Arithmetic type of the facet stage, the contraction and the model rows.
-template <int FORM> struct RealOf { using T = double; };
-template <> struct RealOf<PS_FORM_MIXED> { using T = float; };
-
-template <int FORM>
-struct Smem {
-    using R = typename RealOf<FORM>::T;
-    double *cg, *atry, *beta, *da, *alpha, *covar, *area, *gv, *ym, *red, *dave, *col, *misc;
-    R *areaR, *gvR, *W, *J, *pt;
-    R *pt2;       // the other point set-up buffer (== pt unless set-up runs one tile ahead)
-    float *accs;  // mixed form: per-point FP32 weights and residuals of a tile
-    int *ipiv;
-    float *dsph;  // FP32 basis in shared memory (mixed form), or nullptr
-    // tensor-core contraction: operand tiles, MMA-completion barrier, Tensor
-    // Memory address slot and the abort flag set when a wait gives up
-    unsigned char *bhi, *blo;
-    uint64_t *mbar, *mbar2;   // completion of the contraction MMAs / of the alpha MMAs
-    float4 *fac;              // per facet: nx, ny, nz, Darea
-    float2 *ag;               // per facet and evaluation: Area, Darea g
-    float *fpart;             // [4][P][9] facet-sum partials of the four facet quarters
-    unsigned char *aop;       // alpha/beta MMA operands
-    uint32_t *tslot;
-    int *abort;
-};
-
-template <int FORM>
-__device__ inline Smem<FORM> carve(char *base, const SlotLayout &L)
-{
-    using R = typename RealOf<FORM>::T;
-    Smem<FORM> s;
-    s.cg = reinterpret_cast<double *>(base + L.cg);
-    s.atry = reinterpret_cast<double *>(base + L.atry);
-    s.beta = reinterpret_cast<double *>(base + L.beta);
-    s.da = reinterpret_cast<double *>(base + L.da);
-    s.alpha = reinterpret_cast<double *>(base + L.alpha);
-    s.covar = reinterpret_cast<double *>(base + L.covar);
-    s.area = reinterpret_cast<double *>(base + L.area);
-    s.gv = reinterpret_cast<double *>(base + L.gv);
-    s.areaR = reinterpret_cast<R *>(base + L.areaR);
-    s.gvR = reinterpret_cast<R *>(base + L.gvR);
-    s.W = reinterpret_cast<R *>(base + L.W);
-    s.J = reinterpret_cast<R *>(base + L.J);
-    s.pt = reinterpret_cast<R *>(base + L.pt);
-    s.pt2 = reinterpret_cast<R *>(base + L.pt2);
-    s.accs = reinterpret_cast<float *>(base + L.accs);
-    s.ym = reinterpret_cast<double *>(base + L.ym);
-    s.red = reinterpret_cast<double *>(base + L.red);
-    s.dave = reinterpret_cast<double *>(base + L.dave);
-    s.col = reinterpret_cast<double *>(base + L.col);
-    s.misc = reinterpret_cast<double *>(base + L.misc);
-    s.ipiv = reinterpret_cast<int *>(base + L.ipiv);
-    s.dsph = L.dsph_smem == kBasisSmem ? reinterpret_cast<float *>(base + L.dsph) : nullptr;
-    if (L.dsph_smem == kBasisTensor) {
-        s.bhi = reinterpret_cast<unsigned char *>(base + L.bhi);
-        s.blo = reinterpret_cast<unsigned char *>(base + L.blo);
-        s.mbar = reinterpret_cast<uint64_t *>(base + L.tcm);
-        s.tslot = reinterpret_cast<uint32_t *>(base + L.tcm + 8);
-        s.abort = reinterpret_cast<int *>(base + L.tcm + 12);
-        s.mbar2 = reinterpret_cast<uint64_t *>(base + L.tcm + 16);
-        s.fac = reinterpret_cast<float4 *>(base + L.fac);
-        s.ag = reinterpret_cast<float2 *>(base + L.ag);
-        s.fpart = reinterpret_cast<float *>(base + L.fpart);
-        s.aop = reinterpret_cast<unsigned char *>(base + L.aop);
-    } else {
-        s.bhi = s.blo = nullptr;
-        s.mbar = s.mbar2 = nullptr;
-        s.tslot = nullptr;
-        s.fac = nullptr;
-        s.ag = nullptr;
-        s.fpart = nullptr;
-        s.aop = nullptr;
-        s.abort = nullptr;
-    }
-    return s;
-}
-
-// misc slots
-enum : int {
-    M_CHISQ = 0,   // chi^2 accumulator of the current evaluation
-    M_AVE = 1,     // relative-lightcurve model sum
-    M_AREA = 2,    // sum of facet areas of the current evaluation
-    M_CHK = 3,     // 3 convexity residuals (sum Area*n) of the current evaluation
-    M_CL = 7,      // exp(log cl)
-    M_TRIG = 8,    // cos/sin of the pole angles beta, lambda (4 doubles)
-    M_PIV = 12,    // pivot broadcast of the solvers (2 doubles + status)
-    M_RED = 16     // 16 doubles of block-reduction scratch
-};
-
-// Row j of packed lower-triangle element e (j*(j+1)/2 <= e < (j+1)*(j+2)/2),
-// from an FP32 square root corrected in integers.
-__device__ inline int tri_row(int e)
-{
-    int j = static_cast<int>((sqrtf(8.0f * static_cast<float>(e) + 1.0f) - 1.0f) * 0.5f);
-    while (j * (j + 1) / 2 > e) j--;
-    while ((j + 1) * (j + 2) / 2 <= e) j++;
-    return j;
-}
-
-// Thread that sets up point p of a tile: points are spread over the warps
-// (p % 8 -> warp, p / 8 -> lane) so that all four SM sub-partitions work.
-template <int NT>
-__device__ inline int setup_thread(int p) { return (p % (NT / 32)) * 32 + p / (NT / 32); }
-
-template <class T>
-__device__ inline T warp_sum(T v)
-{
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-    return v;
-}
-
-// Sum over the block; every thread gets the result.  red holds >= NT/32 doubles.
-template <int NT>
-__device__ inline double block_sum(double v, double *red)
-{
-    v = warp_sum(v);
-    int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    __syncthreads();
-    if (lane == 0) red[w] = v;
-    __syncthreads();
-    double t = 0;
-#pragma unroll
-    for (int i = 0; i < NT / 32; i++) t += red[i];
-    __syncthreads();
-    return t;
-}
-
-// Rotation phase omega*t + phi0 reduced to [0, 2*pi).  The FP64 form rounds
-// the product and the sum separately and reduces with fmod, as the
-// reference does (matrix.c:21-22); the mixed form reduces with a two-part
-// 2*pi (the product rounded once), which is exact to ~1e-16 rad.
-template <int FORM>
-__device__ inline double rotation_phase(double omg, double t, double phi0)
-{
-    if constexpr (FORM == PS_FORM_FP64) {
-        return fmod(__dadd_rn(__dmul_rn(omg, t), phi0), kTwoPi);
-    } else {
-        const double x = fma(omg, t, phi0);
-        const double q = floor(x * kInvTwoPi);
-        double f = fma(-q, kTwoPiHi, x);
-        f = fma(-q, kTwoPiLo, f);
-        if (f < 0) f += kTwoPi;
-        if (f >= kTwoPi) f -= kTwoPi;
-        return f;
-    }
-}
-
-// Lit-facet terms of the Lommel-Seeliger + Lambert law (bright.c:65-74,
-// 116-117).  The FP64 form divides as the reference does; the mixed form
-// multiplies by one approximate reciprocal.
-template <class R, int FORM>
-struct LitTerms {
-    R sv, dsmu, dsmu0, dcls_w;  // s, ds/dmu, ds/dmu0, mu*mu0/(mu+mu0)
-    __device__ inline LitTerms(R mu, R mu0, R cl, R cls)
-    {
-        const R dnom = mu + mu0;
-        if constexpr (FORM == PS_FORM_FP64) {
-            sv = mu * mu0 * (cl + cls / dnom);
-            const R q0 = mu0 / dnom, q1 = mu / dnom;
-            dsmu = cls * (q0 * q0) + cl * mu0;
-            dsmu0 = cls * (q1 * q1) + cl * mu;
-            dcls_w = mu * mu0 / dnom;
-        } else {
-            R r;
-            asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(dnom));   // ~1 ulp: the mixed form's budget
-            sv = mu * mu0 * (cl + cls * r);
-            const R q0 = mu0 * r, q1 = mu * r;
-            dsmu = cls * (q0 * q0) + cl * mu0;
-            dsmu0 = cls * (q1 * q1) + cl * mu;
-            dcls_w = mu * mu0 * r;
-        }
-    }
-};
-
-// Accumulates the rows J[0..np) (model values in ym) of one tile into the
-// normal matrix M (lower triangle), bv and chi^2 (mrqcof.c:106-136).  The
-// FP64 form sums every alpha element over points in data order in FP64; the
-// mixed form sums the tile in FP32 and adds the tile sum to the FP64 total.
-// Mixed form: every thread keeps its share of the alpha lower triangle
-// (elements tid + u*256) and of beta (element tid) as FP32 partial sums in
-// registers and adds them to the FP64 totals every few tiles.
-constexpr int kAccPerThread = 8;    // with 512 threads: mfit <= 90
-constexpr int kTilesPerFlush = 8;
-
-template <int FORM>
-__device__ inline void flush_partials(double *M, double *bv, int mf, float (&accA)[kAccPerThread], float &accB)
-{
-    constexpr int NT = threads_of<FORM>();
-    const int tid = threadIdx.x;
-    const int ntri = mf * (mf + 1) / 2;
-#pragma unroll
-    for (int u = 0; u < kAccPerThread; u++) {
-        const int e = tid + u * NT;
-        if (e < ntri) {
-            const int j = tri_row(e);
-            const int k = e - j * (j + 1) / 2;
-            M[j * mf + k] += static_cast<double>(accA[u]);
-        }
-        accA[u] = 0.f;
-    }
-    if (tid < mf) bv[tid] += static_cast<double>(accB);
-    accB = 0.f;
-}
-
-template <int FORM>
-__device__ void accumulate_tile(const DevObject &ob, Smem<FORM> &s, double *M, double *bv, int np, int q0pt,
-                                bool conv, double conv_sig, float (&accA)[kAccPerThread], float &accB)
-{
-    using R = typename RealOf<FORM>::T;
-    constexpr int NT = threads_of<FORM>();
-    const int tid = threadIdx.x;
-    const int ma = ob.ma, mf = ob.mfit;
-    R *wt = s.W;  // [np][mf], reuses the facet-weight tile
-    if constexpr (FORM == PS_FORM_FP64) {
-        for (int e = tid; e < np * mf; e += NT) {
-            const int p = e / mf, j = e - p * mf;
-            const int q = q0pt + p;
-            const double sig2i = conv ? 1 / (conv_sig * conv_sig) : ob.sig2i[q];
-            const double wg = ob.weight[q];
-            wt[p * mf + j] = s.J[p * ma + ob.free_list[j]] * sig2i * wg;
-        }
-    } else {
-        // per point: FP32 weight sig2i*w and residual; chi^2 of the tile
-        // summed over one warp in FP64
-        float *dyv = s.accs;
-        float *wtp = dyv + 32;
-        if (tid < 32) {
-            double c2 = 0;
-            if (tid < np) {
-                const int q = q0pt + tid;
-                const double sig2i = conv ? 1 / (conv_sig * conv_sig) : ob.sig2i[q];
-                const double wg = ob.weight[q];
-                const double dy = (conv ? 0.0 : ob.bright[q]) - s.ym[tid];
-                dyv[tid] = static_cast<float>(dy);
-                wtp[tid] = static_cast<float>(sig2i * wg);
-                c2 = dy * dy * sig2i * wg;
-            }
-            c2 = warp_sum(c2);
-            if (tid == 0) s.misc[M_CHISQ] += c2;
-        }
-        __syncthreads();
-        for (int e = tid; e < np * mf; e += NT) {
-            const int p = e / mf, j = e - p * mf;
-            wt[p * mf + j] = s.J[p * ma + ob.free_list[j]] * wtp[p];
-        }
-    }
-    __syncthreads();
-    const int ntri = mf * (mf + 1) / 2;
-    if constexpr (FORM == PS_FORM_FP64) {
-        for (int e = tid; e < ntri; e += NT) {
-            const int j = tri_row(e);
-            const int k = e - j * (j + 1) / 2;
-            const int lk = ob.free_list[k];
-            double acc = M[j * mf + k];
-            for (int p = 0; p < np; p++) acc = acc + wt[p * mf + j] * s.J[p * ma + lk];
-            M[j * mf + k] = acc;
-        }
-        for (int j = tid; j < mf; j += NT) {
-            double acc = bv[j];
-            for (int p = 0; p < np; p++) {
-                const double y = conv ? 0.0 : ob.bright[q0pt + p];
-                acc = acc + (y - s.ym[p]) * wt[p * mf + j];
-            }
-            bv[j] = acc;
-        }
-    } else {
-        const float *dyv = s.accs;
-#pragma unroll
-        for (int u = 0; u < kAccPerThread; u++) {
-            const int e = tid + u * NT;
-            if (e < ntri) {
-                const int j = tri_row(e);
-                const int k = e - j * (j + 1) / 2;
-                const int lk = ob.free_list[k];
-                float acc = accA[u];
-                for (int p = 0; p < np; p++) acc = fmaf(wt[p * mf + j], s.J[p * ma + lk], acc);
-                accA[u] = acc;
-            }
-        }
-        if (tid < mf) {
-            float acc = accB;
-            for (int p = 0; p < np; p++) acc = fmaf(dyv[p], wt[p * mf + tid], acc);
-            accB = acc;
-        }
-    }
-    if (FORM == PS_FORM_FP64 && tid == NT - 1) {
-        double c2 = s.misc[M_CHISQ];
-        for (int p = 0; p < np; p++) {
-            const int q = q0pt + p;
-            const double sig2i = conv ? 1 / (conv_sig * conv_sig) : ob.sig2i[q];
-            const double y = conv ? 0.0 : ob.bright[q];
-            const double dy = y - s.ym[p];
-            c2 = c2 + dy * dy * sig2i * ob.weight[q];
-        }
-        s.misc[M_CHISQ] = c2;
-    }
-    __syncthreads();
-}
-
-// Basis element Dsph[i][k] of the mixed form: from shared memory with an
-// explicit shared-space load, or from global memory through the read-only
-// path.
-template <bool SMEM_D>
-__device__ inline float load_basis(const float *d, int idx)
-{
-    if constexpr (SMEM_D) {
-        float v;
-        const unsigned addr = static_cast<unsigned>(__cvta_generic_to_shared(d + idx));
-        asm("ld.shared.f32 %0, [%1];" : "=f"(v) : "r"(addr));
-        return v;
-    } else {
-        return __ldg(d + idx);
-    }
-}
-
-// Mixed-form shape contraction J[p][k] = Scale_p * sum_i W[p][i] Dsph[i][k]
-// of one tile, FP32 on the SIMT pipes.  Register tile: warp w owns points
-// (w % 8) + 8 r (r < 4) and coefficients lane + 32 ((w / 8) + 2 u) (u < KU);
-// W is read four facets at a time (float4 broadcast), Dsph one coalesced row
-// per facet.
-template <int NT, int KU, bool SMEM_D>
-__device__ void contract_mixed(Smem<PS_FORM_MIXED> &s, const float *dsph, int np, int F, int C, int ma, int wcols,
-                               bool conv)
-{
-    static_assert(NT == 512, "the register tile assumes 16 warps");
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const int g = warp & 7, half = warp >> 3;
-    constexpr int kPW = 4;
-    float acc[kPW][KU];
-#pragma unroll
-    for (int r = 0; r < kPW; r++)
-#pragma unroll
-        for (int u = 0; u < KU; u++) acc[r][u] = 0.f;
-    int kk[KU];
-    bool kv[KU];
-#pragma unroll
-    for (int u = 0; u < KU; u++) {
-        kk[u] = lane + 32 * (half + 2 * u);
-        kv[u] = kk[u] < C;
-    }
-    bool any = false;
-#pragma unroll
-    for (int u = 0; u < KU; u++) any |= kv[u];
-    const float *Wf = s.W;
-    if (any) {
-        for (int i = 0; i < F; i += 4) {
-            float4 w4[kPW];
-#pragma unroll
-            for (int r = 0; r < kPW; r++) {
-                const int p = g + 8 * r;
-                w4[r] = (p < np) ? *reinterpret_cast<const float4 *>(Wf + static_cast<size_t>(p) * wcols + i)
-                                 : make_float4(0.f, 0.f, 0.f, 0.f);
-            }
-#pragma unroll
-            for (int ii = 0; ii < 4; ii++) {
-                float d[KU];
-#pragma unroll
-                for (int u = 0; u < KU; u++) d[u] = kv[u] ? load_basis<SMEM_D>(dsph, (i + ii) * C + kk[u]) : 0.f;
-#pragma unroll
-                for (int r = 0; r < kPW; r++) {
-                    const float wv = ii == 0 ? w4[r].x : ii == 1 ? w4[r].y : ii == 2 ? w4[r].z : w4[r].w;
-#pragma unroll
-                    for (int u = 0; u < KU; u++) acc[r][u] = fmaf(wv, d[u], acc[r][u]);
-                }
-            }
-        }
-    }
-#pragma unroll
-    for (int r = 0; r < kPW; r++) {
-        const int p = g + 8 * r;
-        if (p < np) {
-            const float sc = conv ? 1.f : s.pt[p * kPointStride + 24];
-#pragma unroll
-            for (int u = 0; u < KU; u++)
-                if (kv[u]) s.J[p * ma + kk[u]] = sc * acc[r][u];
-        }
-    }
-}
-
-// Point set-up of observation q (bright.c:27-57, phasec.c, matrix.c): the
-// rotated Earth and Sun directions with their beta/lambda/omega derivatives,
-// the phase function and its derivatives, into pt[0..27].
-template <int FORM>
-__device__ inline void setup_point(const DevObject &ob, const FitConfig &cfg, int q, double omg,
-                                   const typename RealOf<FORM>::T (&B)[9], const typename RealOf<FORM>::T (&DB0)[9],
-                                   const typename RealOf<FORM>::T (&DB1)[9], typename RealOf<FORM>::T php0,
-                                   typename RealOf<FORM>::T php1, typename RealOf<FORM>::T php2,
-                                   typename RealOf<FORM>::T *pt)
-{
-    using R = typename RealOf<FORM>::T;
-    constexpr bool kFP64 = FORM == PS_FORM_FP64;
-    R ee[3], e0v[3], alpha;
-    if constexpr (kFP64) {
-        ee[0] = ob.eex[q];
-        ee[1] = ob.eey[q];
-        ee[2] = ob.eez[q];
-        e0v[0] = ob.e0x[q];
-        e0v[1] = ob.e0y[q];
-        e0v[2] = ob.e0z[q];
-        alpha = ob.alpha_pt[q];
-    } else {
-        const float4 g0 = ob.geo_f[2 * q], g1 = ob.geo_f[2 * q + 1];
-        ee[0] = g0.x;
-        ee[1] = g0.y;
-        ee[2] = g0.z;
-        alpha = g0.w;
-        e0v[0] = g1.x;
-        e0v[1] = g1.y;
-        e0v[2] = g1.z;
-    }
-    const double td = ob.tim[q];
-    const R t = R(td);
-    R ex;
-    R inv_w = 0;
-    if constexpr (kFP64) {
-        ex = exp(-alpha / php1);
-    } else {
-        inv_w = 1.f / php1;
-        ex = expf(-alpha * inv_w);
-    }
-    const R scale = 1 + php0 * ex + php2 * alpha;
-    const double f = rotation_phase<FORM>(omg, td, cfg.phi0);
-    R cf, sf;
-    if constexpr (kFP64) {
-        cf = cos(f);
-        sf = sin(f);
-    } else {
-        sincosf(static_cast<float>(f), &sf, &cf);
-    }
-    const R fm[9] = {cf, sf, R(0), -sf, cf, R(0), R(0), R(0), R(1)};
-    const R dfm[9] = {-t * sf, t * cf, R(0), -t * cf, -t * sf, R(0), R(0), R(0), R(0)};
-    R tm[9], d0[9], d1[9], d2[9];
-#pragma unroll
-    for (int i = 0; i < 3; i++)
-#pragma unroll
-        for (int j = 0; j < 3; j++) {
-            R x = 0, y0 = 0, y1 = 0, y2 = 0;
-#pragma unroll
-            for (int k = 0; k < 3; k++) {
-                x = x + fm[i * 3 + k] * B[k * 3 + j];
-                y0 = y0 + fm[i * 3 + k] * DB0[k * 3 + j];
-                y1 = y1 + fm[i * 3 + k] * DB1[k * 3 + j];
-                y2 = y2 + dfm[i * 3 + k] * B[k * 3 + j];
-            }
-            tm[i * 3 + j] = x;
-            d0[i * 3 + j] = y0;
-            d1[i * 3 + j] = y1;
-            d2[i * 3 + j] = y2;
-        }
-#pragma unroll
-    for (int i = 0; i < 3; i++) {
-        R x = 0, y = 0;
-#pragma unroll
-        for (int j = 0; j < 3; j++) {
-            x = x + tm[i * 3 + j] * ee[j];
-            y = y + tm[i * 3 + j] * e0v[j];
-        }
-        pt[i] = x;
-        pt[3 + i] = y;
-    }
-    // de[i][j] = sum_k dtm[j][i][k] ee[k]; stored de[i*3+j] (j = derivative)
-    const R *dd[3] = {d0, d1, d2};
-#pragma unroll
-    for (int i = 0; i < 3; i++)
-#pragma unroll
-        for (int j = 0; j < 3; j++) {
-            R x = 0, y = 0;
-#pragma unroll
-            for (int k = 0; k < 3; k++) {
-                x = x + dd[j][i * 3 + k] * ee[k];
-                y = y + dd[j][i * 3 + k] * e0v[k];
-            }
-            pt[6 + i * 3 + j] = x;
-            pt[15 + i * 3 + j] = y;
-        }
-    pt[24] = scale;
-    pt[25] = ex;
-    if constexpr (kFP64) pt[26] = php0 * ex * alpha / (php1 * php1);
-    else pt[26] = php0 * ex * alpha * (inv_w * inv_w);
-    pt[27] = alpha;
-}
-
-// ---------------------------------------------------------------------------
-// Tensor-core contraction of the mixed form (kBasisTensor).
-// ---------------------------------------------------------------------------
-constexpr uint32_t kTcWaitTries = 1u << 22;   // mbarrier polls before a wait gives up
-constexpr int kErrTcTimeout = 16;             // ps_fit.err_code of a fit cut short by a failed wait
-
-// Tensor Memory columns: the basis [0, F), the contraction accumulator
-// [tc_dcol, tc_dcol + 64) (column p: A W_hi^T for point p, 32 + p: A W_lo^T)
-// and the alpha accumulator [tc_acol, tc_acol + 128).
-__device__ inline uint32_t tc_dcol(int F) { return static_cast<uint32_t>((F + 31) & ~31); }
-__device__ inline uint32_t tc_acol(int F) { return tc_dcol(F) + 64; }
-
-__device__ inline uint32_t tc_cols(int F)
-{
-    uint32_t n = 32;
-    while (n < tc_acol(F) + 128) n <<= 1;
-    return n;
-}
-
-// Per-thread view of the CTA's tensor-core state (every thread keeps the
-// same values).
-struct TcState {
-    uint32_t tbase = 0;     // Tensor Memory base address
-    uint32_t phase = 0;     // parity of the contraction barrier's next phase
-    uint32_t aphase = 0;    // parity of the alpha barrier's next phase
-    bool apending = false;  // alpha MMAs committed and not waited for
-    bool afresh = true;     // the alpha accumulator holds nothing since the last flush
-};
-
-// Waits for the committed alpha MMAs (their operands' shared memory is then
-// free); a wait that gives up sets the abort flag.
-__device__ inline void tc_alpha_wait(Smem<PS_FORM_MIXED> &s, TcState &t)
-{
-    if (!t.apending || *s.abort) return;
-    const bool ok = __syncthreads_and(tc::mbar_wait(s.mbar2, t.aphase, kTcWaitTries));
-    t.apending = false;
-    if (!ok) {
-        if (threadIdx.x == 0) *s.abort = 1;
-        __syncthreads();
-        return;
-    }
-    t.aphase ^= 1u;
-    tc::fence_after_sync();
-}
-
-// Allocates the CTA's Tensor Memory and loads A = [Dsph_hi^T; Dsph_lo^T]:
-// lane m < 64 holds the TF32 rounding of coefficient m's basis column, lane
-// 64 + m the TF32 rounding of what remains of it (taken from the FP64 basis);
-// column i is facet i.  Returns the Tensor Memory base address.
-template <int NT>
-__device__ uint32_t tc_setup(const DevObject &ob, Smem<PS_FORM_MIXED> &s)
-{
-    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    const int F = ob.nfac, C = ob.ncoef;
-    if (warp == 0) tc::tmem_alloc(s.tslot, tc_cols(F));
-    if (tid == 0) {
-        tc::mbar_init(s.mbar, 1);
-        tc::mbar_init(s.mbar2, 1);
-        *s.abort = 0;
-    }
-    tc::fence_before_sync();
-    __syncthreads();
-    tc::fence_after_sync();
-    const uint32_t tbase = *s.tslot;
-    for (int i = tid; i < F; i += NT) s.fac[i] = make_float4(ob.nx_f[i], ob.ny_f[i], ob.nz_f[i], ob.darea_f[i]);
-    if (warp < 4) {
-        const int m = warp * 32 + lane, c = m & 63;
-        const bool low = m >= 64;
-        const uint32_t row = tbase + (static_cast<uint32_t>(warp * 32) << 16);
-        for (int k0 = 0; k0 < F; k0 += 8) {
-            uint32_t v[8];
-#pragma unroll
-            for (int j = 0; j < 8; j++) {
-                const double d = c < C ? ob.dsph[static_cast<size_t>(k0 + j) * C + c] : 0.0;
-                const uint32_t hi = tc::to_tf32(static_cast<float>(d));
-                v[j] = low ? tc::to_tf32(static_cast<float>(d - static_cast<double>(__uint_as_float(hi)))) : hi;
-            }
-            tc::tmem_st8(row + static_cast<uint32_t>(k0), v);
-        }
-        tc::tmem_wait_st();
-    }
-    tc::fence_before_sync();
-    __syncthreads();
-    tc::fence_after_sync();
-    return tbase;
-}
-
-// Releases the Tensor Memory.  After an abandoned wait the MMAs in flight
-// get one more bounded wait first.
-__device__ void tc_teardown(Smem<PS_FORM_MIXED> &s, const TcState &t, int F)
-{
-    if (*s.abort && threadIdx.x == 0) {
-        tc::mbar_wait(s.mbar, t.phase, kTcWaitTries);
-        if (t.apending) tc::mbar_wait(s.mbar2, t.aphase, kTcWaitTries);
-    }
-    tc::fence_before_sync();
-    __syncthreads();
-    if ((threadIdx.x >> 5) == 0) tc::tmem_dealloc(t.tbase, tc_cols(F));
-}
-
-// Issues D = A [W_hi; W_lo]^T for the tile as F/8 MMAs of 128 x 64 x 8 (one
-// MMA costs the issuing thread about the same for N = 32 and N = 64) and a
-// commit to the barrier.  The facet stage has written the operand: TF32
-// high parts of W in rows 0..31, low parts in rows 32..63, canonical K-major
-// layout (8-row x 4-facet core matrices, K-adjacent ones 128 bytes apart).
-template <int NT>
-__device__ void contract_tc_issue(Smem<PS_FORM_MIXED> &s, int F, TcState &t)
-{
-    const int tid = threadIdx.x;
-    const int kcs = F >> 2;
-    const uint32_t tbase = t.tbase;
-    tc::fence_proxy_async();
-    tc::fence_before_sync();
-    __syncthreads();
-    if (tid == 0 && !*s.abort) {
-        tc::fence_after_sync();
-        const uint32_t idesc = tc::idesc_tf32(128, 64);
-        const uint32_t sbo = static_cast<uint32_t>(kcs) * 128;
-        const uint32_t bh = tc::smem_u32(s.bhi), d = tbase + tc_dcol(F);
-        for (int k8 = 0; k8 < F / 8; k8++) {
-            const uint32_t a = tbase + static_cast<uint32_t>(k8) * 8, off = static_cast<uint32_t>(k8) * 256;
-            tc::mma_tf32_ts(d, a, tc::smem_desc(bh + off, 128, sbo), idesc, k8 > 0);
-        }
-        tc::mma_commit(s.mbar);
-    }
-}
-
-// Facet stage of the tensor-core path (bright.c:59-120).  Warp w takes
-// points 8 (w % 4) .. +7 (lane / 4) and the facet quarter w / 4, lanes of a
-// point stepping through the quarter four facets apart (lane % 4), so that
-// one warp store covers a whole 8-point x 4-facet core matrix of the MMA
-// operand [W_hi; W_lo].  The per-point sums (brightness, rotation and
-// scattering derivatives) are reduced over the four lanes and then over the
-// quarters into s.red.  The tile's operand region must be free (previous
-// MMAs waited for).
-template <int NT>
-__device__ void facet_stage_tc(const DevObject &ob, Smem<PS_FORM_MIXED> &s, int np, float cl, float cls)
-{
-    static_assert(NT == 512, "16 warps: 4 point groups x 4 facet quarters");
-    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    const int F = ob.nfac, kcs = F >> 2;
-    const int quarter = warp >> 2, p = (warp & 3) * 8 + (lane >> 2), fl = lane & 3;
-    const int fq = (kcs + 3) & ~3;     // facets per quarter, a multiple of 4
-    float e1 = 0, e2 = 0, e3 = 0, f1 = 0, f2 = 0, f3 = 0;
-    if (p < np) {
-        const float *pt = s.pt + p * kPointStride;
-        e1 = pt[0];
-        e2 = pt[1];
-        e3 = pt[2];
-        f1 = pt[3];
-        f2 = pt[4];
-        f3 = pt[5];
-    }
-    // The rotation derivatives sum_i Area_i (dsmu (n_i . D_k) + dsmu0 (n_i .
-    // E_k)) over the lit facets are D_k . U + E_k . V with U = sum Area dsmu
-    // n and V = sum Area dsmu0 n (D_k, E_k: the derivative directions of the
-    // Earth and Sun vectors), so the facet loop accumulates U and V.
-    float br = 0, dcl = 0, dcls = 0, ux = 0, uy = 0, uz = 0, vx = 0, vy = 0, vz = 0;
-    uint32_t *bh = reinterpret_cast<uint32_t *>(s.bhi), *bl = reinterpret_cast<uint32_t *>(s.blo);
-    const int i_end = min(F, (quarter + 1) * fq);
-#pragma unroll 2
-    for (int i0 = quarter * fq; i0 < i_end; i0 += 4) {
-        const int i = i0 + fl;
-        const float4 n = s.fac[i];
-        const float mu = e1 * n.x + e2 * n.y + e3 * n.z;
-        const float mu0 = f1 * n.x + f2 * n.y + f3 * n.z;
-        float w = 0.f;
-        if (mu > float(kTinyMu) && mu0 > float(kTinyMu)) {
-            const float2 a = s.ag[i];
-            const LitTerms<float, PS_FORM_MIXED> lt(mu, mu0, cl, cls);
-            br = br + a.x * lt.sv;
-            w = a.y * lt.sv;
-            const float cu = a.x * lt.dsmu, cv = a.x * lt.dsmu0;
-            ux = fmaf(cu, n.x, ux);
-            uy = fmaf(cu, n.y, uy);
-            uz = fmaf(cu, n.z, uz);
-            vx = fmaf(cv, n.x, vx);
-            vy = fmaf(cv, n.y, vy);
-            vz = fmaf(cv, n.z, vz);
-            dcl = dcl + mu * mu0 * a.x;
-            dcls = dcls + a.x * lt.dcls_w;
-        }
-        const uint32_t hi = tc::to_tf32(w);
-        const uint32_t lo = tc::to_tf32(w - __uint_as_float(hi));
-        const int cm = (warp & 3) * kcs + (i0 >> 2);    // core matrix (8-point group, 4-facet group)
-        bh[cm * 32 + lane] = hi;
-        bl[cm * 32 + lane] = lo;
-    }
-    float v[9] = {br, dcl, dcls, ux, uy, uz, vx, vy, vz};
-#pragma unroll
-    for (int k = 0; k < 9; k++) {
-        v[k] += __shfl_xor_sync(0xffffffffu, v[k], 1);
-        v[k] += __shfl_xor_sync(0xffffffffu, v[k], 2);
-    }
-    if (fl == 0) {
-        float *fp = s.fpart + (quarter * 32 + p) * 9;
-#pragma unroll
-        for (int k = 0; k < 9; k++) fp[k] = v[k];
-    }
-    __syncthreads();
-    if (tid < np) {
-        float t[9];
-#pragma unroll
-        for (int k = 0; k < 9; k++) {
-            float a = 0.f;
-#pragma unroll
-            for (int q = 0; q < 4; q++) a += s.fpart[(q * 32 + tid) * 9 + k];
-            t[k] = a;
-        }
-        const float *pt = s.pt + tid * kPointStride;
-        double *rd = s.red + tid * kRedStride;
-        rd[0] = t[0];
-#pragma unroll
-        for (int k = 0; k < 3; k++) {
-            // D_k = (de[k], de[3 + k], de[6 + k]), E_k likewise from de0
-            const float r = pt[6 + k] * t[3] + pt[9 + k] * t[4] + pt[12 + k] * t[5] + pt[15 + k] * t[6] +
-                            pt[18 + k] * t[7] + pt[21 + k] * t[8];
-            rd[1 + k] = r;
-        }
-        rd[4] = t[1];
-        rd[5] = t[2];
-    }
-}
-
-// Convexity rows (conv.c:12-29) on the tensor-core path: rows 0..2 of the
-// MMA operand hold Darea g n_c split into TF32 high and low parts; the
-// residuals sum Area n_c in FP64.
-template <int NT>
-__device__ void conv_rows_tc(const DevObject &ob, Smem<PS_FORM_MIXED> &s)
-{
-    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    const int F = ob.nfac;
-    uint32_t *bh = reinterpret_cast<uint32_t *>(s.bhi), *bl = reinterpret_cast<uint32_t *>(s.blo);
-    for (int e = tid; e < 3 * F; e += NT) {
-        const int c = e / F, i = e - c * F;
-        const double *nc = (c == 0) ? ob.nx : (c == 1) ? ob.ny : ob.nz;
-        const float w = static_cast<float>(ob.darea[i] * s.gv[i] * nc[i]);
-        const uint32_t hi = tc::to_tf32(w);
-        const int off = (i >> 2) * 32 + c * 4 + (i & 3);
-        bh[off] = hi;
-        bl[off] = tc::to_tf32(w - __uint_as_float(hi));
-    }
-    if (warp < 3) {
-        const double *nc = (warp == 0) ? ob.nx : (warp == 1) ? ob.ny : ob.nz;
-        double res = 0;
-        for (int i = lane; i < F; i += 32) res = res + s.area[i] * nc[i];
-        res = warp_sum(res);
-        if (lane == 0) s.red[warp * kRedStride] = res;
-    }
-}
-
-// Waits for the tile's MMAs, stages the accumulator (lane m = row m) in
-// shared memory and writes J[p][k] = Scale_p (D[k][p] + D[k][32 + p] +
-// D[64 + k][p] + D[64 + k][32 + p]): basis high and low parts times W high
-// and low parts.  A wait that gives up sets the abort flag; the caller ends
-// the fit.
-template <int NT>
-__device__ void contract_tc_finish(Smem<PS_FORM_MIXED> &s, int np, int F, int C, int ma, bool conv, TcState &t)
-{
-    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    const uint32_t tbase = t.tbase;
-    if (*s.abort) return;
-    const bool ok = __syncthreads_and(tc::mbar_wait(s.mbar, t.phase, kTcWaitTries));
-    if (!ok) {
-        if (tid == 0) *s.abort = 1;
-        __syncthreads();
-        return;
-    }
-    t.phase ^= 1u;
-    tc::fence_after_sync();
-    float *X = reinterpret_cast<float *>(s.bhi);
-    if (warp < 4) {
-        const uint32_t taddr = tbase + (static_cast<uint32_t>(warp * 32) << 16) + tc_dcol(F);
-        float *xr = X + (warp * 32 + lane) * 65;
-#pragma unroll 1
-        for (int q = 0; q < 8; q++) {
-            uint32_t v[8];
-            tc::tmem_ld8(taddr + 8 * q, v);
-            tc::tmem_wait_ld();
-#pragma unroll
-            for (int j = 0; j < 8; j++) xr[8 * q + j] = __uint_as_float(v[j]);
-        }
-    }
-    __syncthreads();
-    for (int e = tid; e < np * C; e += NT) {
-        const int p = e / C, k = e - p * C;
-        const float sc = conv ? 1.f : s.pt[p * kPointStride + 24];
-        const float *xh = X + k * 65, *xl = X + (64 + k) * 65;
-        s.J[p * ma + k] = sc * ((xh[p] + xh[32 + p]) + (xl[p] + xl[32 + p]));
-    }
-}
-
-// alpha/beta accumulation of one tile on the tensor cores (mrqcof.c:106-136):
-// D += A B^T over the tile's points with A = [Wt_hi; Wt_lo] (row j: the
-// weighted column J[.][l_j] sig^-2 w of free parameter j, 128 x 32) and B =
-// [Jt_hi; Jt_lo] (row k < mfit: column J[.][l_k]; row mfit: the residuals
-// dy), both split into TF32 high and low parts, so that the four quadrants
-// of the 128 x 128 FP32 accumulator sum to alpha (and beta in column mfit)
-// at FP32 accuracy.  The accumulator stays in Tensor Memory across tiles
-// until tc_alpha_flush.  chi^2 is summed in FP64 by warp 0.
-template <int NT>
-__device__ void accumulate_tile_tc(const DevObject &ob, Smem<PS_FORM_MIXED> &s, int np, int q0pt, bool conv,
-                                   double conv_sig, TcState &t)
-{
-    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    const int ma = ob.ma, mf = ob.mfit;
-    float *dyv = s.accs;
-    float *wtp = dyv + 32;
-    if (tid < 32) {
-        double c2 = 0;
-        if (tid < np) {
-            const int q = q0pt + tid;
-            const double sig2i = conv ? 1 / (conv_sig * conv_sig) : ob.sig2i[q];
-            const double wg = ob.weight[q];
-            const double dy = (conv ? 0.0 : ob.bright[q]) - s.ym[tid];
-            dyv[tid] = static_cast<float>(dy);
-            wtp[tid] = static_cast<float>(sig2i * wg);
-            c2 = dy * dy * sig2i * wg;
-        }
-        c2 = warp_sum(c2);
-        if (tid == 0) s.misc[M_CHISQ] += c2;
-    }
-    tc_alpha_wait(s, t);
-    __syncthreads();
-    // operands in the canonical K-major layout, K = the tile's 32 points
-    // (zero beyond np): 8-row x 4-point core matrices, K-adjacent ones 128
-    // bytes apart, 8-row groups 1024 bytes apart; high parts in rows 0..63,
-    // low parts in rows 64..127
-    unsigned char *Ab = s.aop, *Bb = s.aop + 16384;
-    for (int cm = warp; cm < 128; cm += NT / 32) {
-        const bool isB = cm >= 64;
-        const int c = cm & 63, rg = c >> 3, kc = c & 7;
-        const int row = rg * 8 + (lane >> 2), p = kc * 4 + (lane & 3);
-        float v = 0.f;
-        if (p < np) {
-            if (row < mf) {
-                v = s.J[p * ma + ob.free_list[row]];
-                if (!isB) v *= wtp[p];
-            } else if (isB && row == mf) {
-                v = dyv[p];
-            }
-        }
-        const uint32_t hi = tc::to_tf32(v);
-        const uint32_t lo = tc::to_tf32(v - __uint_as_float(hi));
-        unsigned char *base = isB ? Bb : Ab;
-        reinterpret_cast<uint32_t *>(base + (rg * 8 + kc) * 128)[lane] = hi;
-        reinterpret_cast<uint32_t *>(base + ((rg + 8) * 8 + kc) * 128)[lane] = lo;
-    }
-    tc::fence_proxy_async();
-    tc::fence_before_sync();
-    __syncthreads();
-    if (tid == 0 && !*s.abort) {
-        tc::fence_after_sync();
-        const uint32_t idesc = tc::idesc_tf32(128, 128);
-        const uint32_t a0 = tc::smem_u32(Ab), b0 = tc::smem_u32(Bb), d = t.tbase + tc_acol(ob.nfac);
-        for (int kk = 0; kk < 4; kk++) {
-            const uint32_t off = static_cast<uint32_t>(kk) * 256;
-            tc::mma_tf32_ss(d, tc::smem_desc(a0 + off, 128, 1024), tc::smem_desc(b0 + off, 128, 1024), idesc,
-                            (t.afresh && kk == 0) ? 0u : 1u);
-        }
-        tc::mma_commit(s.mbar2);
-    }
-    t.apending = true;
-    t.afresh = false;
-}
-
-// Adds the alpha accumulator to the FP64 normal matrix M (lower triangle)
-// and bv, and marks it empty: each quadrant pair is summed on the way out of
-// Tensor Memory (rows m and 64 + m, columns k and 64 + k).
-template <int NT>
-__device__ void tc_alpha_flush(const DevObject &ob, Smem<PS_FORM_MIXED> &s, double *M, double *bv, TcState &t)
-{
-    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    const int mf = ob.mfit;
-    if (t.afresh) return;
-    tc_alpha_wait(s, t);
-    if (*s.abort) return;
-    float *S = reinterpret_cast<float *>(s.bhi);   // [128][65], after the tile's contraction
-    if (warp < 4) {
-        const uint32_t taddr = t.tbase + (static_cast<uint32_t>(warp * 32) << 16) + tc_acol(ob.nfac);
-        float *sr = S + (warp * 32 + lane) * 65;
-#pragma unroll 1
-        for (int q = 0; q < 8; q++) {
-            uint32_t vh[8], vl[8];
-            tc::tmem_ld8(taddr + 8 * q, vh);
-            tc::tmem_ld8(taddr + 64 + 8 * q, vl);
-            tc::tmem_wait_ld();
-#pragma unroll
-            for (int j = 0; j < 8; j++) sr[8 * q + j] = __uint_as_float(vh[j]) + __uint_as_float(vl[j]);
-        }
-    }
-    __syncthreads();
-    const int ntri = mf * (mf + 1) / 2;
-    for (int e = tid; e < ntri; e += NT) {
-        const int j = tri_row(e);
-        const int k = e - j * (j + 1) / 2;
-        M[j * mf + k] += static_cast<double>(S[j * 65 + k] + S[(64 + j) * 65 + k]);
-    }
-    for (int j = tid; j < mf; j += NT) bv[j] += static_cast<double>(S[j * 65 + mf] + S[(64 + j) * 65 + mf]);
-    t.afresh = true;
-    tc::fence_before_sync();
-    __syncthreads();
-}
-
-// ---------------------------------------------------------------------------
-// Model evaluation (mrqcof) at parameters a[] into matrix M (mfit x mfit,
-// lower triangle accumulated then mirrored) and vector bv.  Leaves chi^2,
-// the facet-area sum and the convexity residuals in misc.
-// ---------------------------------------------------------------------------
-template <int FORM, int KU>
-__device__ void evaluate(const DevObject &ob, const FitConfig &cfg, const SlotLayout &L, Smem<FORM> &s,
-                         const double *a, double *M, double *bv, typename RealOf<FORM>::T *scratch, TcState &tcs)
-{
-    using R = typename RealOf<FORM>::T;
-    constexpr bool kFP64 = FORM == PS_FORM_FP64;
-    // tensor-core path: the point set-up of the next tile runs on warps 1..15
-    // while thread 0 issues the current tile's MMAs
-    constexpr bool kPipe = !kFP64 && KU == 0;
-    constexpr int NT = threads_of<FORM>();
-    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    const int F = ob.nfac, C = ob.ncoef, ma = ob.ma, mf = ob.mfit, P = L.P;
-    const int wcols = L.wcols;
-    const R *nxR, *nyR, *nzR, *dareaR;
-    const R *dsphR;
-    if constexpr (kFP64) {
-        nxR = ob.nx;
-        nyR = ob.ny;
-        nzR = ob.nz;
-        dareaR = ob.darea;
-        dsphR = ob.dsph;
-    } else {
-        nxR = ob.nx_f;
-        nyR = ob.ny_f;
-        nzR = ob.nz_f;
-        dareaR = ob.darea_f;
-        dsphR = ob.dsph_f;
-    }
-
-    // curv.c:10-39 -- g_i = exp(sum over (m,l) of P_l^m (c cos + c' sin)), FP64.
-    double asum = 0;
-    for (int i = tid; i < F; i += NT) {
-        double g = 0;
-        for (int q = 0; q < ob.npairs; q++) {
-            int m = ob.pair_m[q], n = ob.pair_n[q];
-            double fsum = a[n] * ob.fc[m * F + i];
-            if (m != 0) fsum = fsum + a[n + 1] * ob.fs[m * F + i];
-            g = g + ob.pleg[q * F + i] * fsum;
-        }
-        g = exp(g);
-        double ar = ob.darea[i] * g;
-        s.area[i] = ar;
-        s.gv[i] = g;
-        if constexpr (!kFP64) {
-            s.areaR[i] = static_cast<R>(ar);
-            s.gvR[i] = static_cast<R>(g);
-            if constexpr (KU == 0) s.ag[i] = make_float2(static_cast<float>(ar), static_cast<float>(ob.darea[i] * g));
-        }
-        asum += ar;
-    }
-    double tot = block_sum<NT>(asum, s.misc + M_RED);
-    if (tid == 0) {
-        s.misc[M_AREA] = tot;
-        s.misc[M_CHISQ] = 0;
-        s.misc[M_CL] = exp(a[ma - 2]);
-        s.misc[M_TRIG] = cos(a[C]);
-        s.misc[M_TRIG + 1] = sin(a[C]);
-        s.misc[M_TRIG + 2] = cos(a[C + 1]);
-        s.misc[M_TRIG + 3] = sin(a[C + 1]);
-    }
-    for (int e = tid; e < mf * mf; e += NT) M[e] = 0;
-    for (int j = tid; j < mf; j += NT) bv[j] = 0;
-
-    // blmatrix.c:9-46 in FP64 (angles' cos/sin from thread 0), then in the
-    // facet-stage type.
-    __syncthreads();
-    const double cb = s.misc[M_TRIG], sb = s.misc[M_TRIG + 1], clm = s.misc[M_TRIG + 2], slm = s.misc[M_TRIG + 3];
-    const R B[9] = {R(cb * clm), R(cb * slm), R(-sb), R(-slm), R(clm), R(0), R(sb * clm), R(sb * slm), R(cb)};
-    const R DB0[9] = {R(-sb * clm), R(-sb * slm), R(-cb), R(0), R(0), R(0), R(cb * clm), R(cb * slm), R(-sb)};
-    const R DB1[9] = {R(-cb * slm), R(cb * clm), R(0), R(-clm), R(-slm), R(0), R(-sb * slm), R(sb * clm), R(0)};
-    const double omg = a[C + 2];
-    const R php0 = R(a[C + 3]), php1 = R(a[C + 4]), php2 = R(a[C + 5]);
-    const R cls = R(a[C + 7]);
-    __syncthreads();
-    const R cl = R(s.misc[M_CL]);
-
-    const double conv_sig = 1 / cfg.conw_r;
-    float accA[kAccPerThread];
-    float accB = 0.f;
-#pragma unroll
-    for (int u = 0; u < kAccPerThread; u++) accA[u] = 0.f;
-    int tiles_since_flush = 0;
-    const float *dsphF = nullptr;
-    if constexpr (!kFP64) dsphF = s.dsph ? s.dsph : ob.dsph_f;
-    // thread of point sp of a set-up that runs beside the MMA issue (warps 1..15)
-    const int pipe_sp = lane * (NT / 32 - 1) + (warp - 1);
-    if constexpr (kPipe) {
-        if (ob.n_lc > 1 && warp > 0 && pipe_sp < min(P, ob.lc_npts[0]))
-            setup_point<FORM>(ob, cfg, ob.lc_start[0] + pipe_sp, omg, B, DB0, DB1, php0, php1, php2,
-                              s.pt + pipe_sp * kPointStride);
-    }
-
-    for (int lc = 0; lc < ob.n_lc; lc++) {
-        const int start = ob.lc_start[lc], npts = ob.lc_npts[lc];
-        const bool rel = ob.lc_rel[lc] != 0;
-        const bool conv = (lc == ob.n_lc - 1);
-        if (rel) {
-            for (int l = tid; l < ma; l += NT) s.dave[l] = 0;
-            if (tid == 0) s.misc[M_AVE] = 0;
-        }
-        // ---- pass 1: model rows of this lightcurve, tile by tile ----
-        for (int t0 = 0; t0 < npts; t0 += P) {
-            const int np = min(P, npts - t0);
-            if (!conv) {
-                // 1. point set-up (bright.c:27-57, phasec.c, matrix.c), one
-                // thread per point spread over the warps; with the tensor
-                // cores it was done during the previous tile's MMAs
-                if constexpr (!kPipe) {
-                    const int sp = (tid % 32) * (NT / 32) + tid / 32;
-                    if (sp < np)
-                        setup_point<FORM>(ob, cfg, start + t0 + sp, omg, B, DB0, DB1, php0, php1, php2,
-                                          s.pt + sp * kPointStride);
-                }
-                __syncthreads();
-                // 2. facet stage (bright.c:59-120), one warp per point
-                if constexpr (kPipe) facet_stage_tc<NT>(ob, s, np, cl, cls);
-                else
-                for (int p = warp; p < np; p += NT / 32) {
-                    const R *pt = s.pt + p * kPointStride;
-                    const R e1 = pt[0], e2 = pt[1], e3 = pt[2];
-                    const R f1 = pt[3], f2 = pt[4], f3 = pt[5];
-                    R de[9], de0[9];
-#pragma unroll
-                    for (int k = 0; k < 9; k++) {
-                        de[k] = pt[6 + k];
-                        de0[k] = pt[15 + k];
-                    }
-                    R br = 0, r0 = 0, r1 = 0, r2 = 0, dcl = 0, dcls = 0;
-                    R *Wp = s.W + static_cast<size_t>(p) * wcols;
-                    for (int i = lane; i < F; i += 32) {
-                        const R nx = nxR[i], ny = nyR[i], nz = nzR[i];
-                        const R mu = e1 * nx + e2 * ny + e3 * nz;
-                        const R mu0 = f1 * nx + f2 * ny + f3 * nz;
-                        R w = 0;
-                        if (mu > R(kTinyMu) && mu0 > R(kTinyMu)) {
-                            const R ar = s.areaR[i];
-                            const LitTerms<R, FORM> lt(mu, mu0, cl, cls);
-                            br = br + ar * lt.sv;
-                            w = dareaR[i] * lt.sv * s.gvR[i];
-                            const R s0 = nx * de[0] + ny * de[3] + nz * de[6];
-                            const R s1 = nx * de[1] + ny * de[4] + nz * de[7];
-                            const R s2 = nx * de[2] + ny * de[5] + nz * de[8];
-                            const R t0v = nx * de0[0] + ny * de0[3] + nz * de0[6];
-                            const R t1v = nx * de0[1] + ny * de0[4] + nz * de0[7];
-                            const R t2v = nx * de0[2] + ny * de0[5] + nz * de0[8];
-                            r0 = r0 + ar * (lt.dsmu * s0 + lt.dsmu0 * t0v);
-                            r1 = r1 + ar * (lt.dsmu * s1 + lt.dsmu0 * t1v);
-                            r2 = r2 + ar * (lt.dsmu * s2 + lt.dsmu0 * t2v);
-                            dcl = dcl + mu * mu0 * ar;
-                            dcls = dcls + ar * lt.dcls_w;
-                        }
-                        Wp[i] = w;
-                    }
-                    br = warp_sum(br);
-                    r0 = warp_sum(r0);
-                    r1 = warp_sum(r1);
-                    r2 = warp_sum(r2);
-                    dcl = warp_sum(dcl);
-                    dcls = warp_sum(dcls);
-                    if (lane == 0) {
-                        double *rd = s.red + p * kRedStride;
-                        rd[0] = br;
-                        rd[1] = r0;
-                        rd[2] = r1;
-                        rd[3] = r2;
-                        rd[4] = dcl;
-                        rd[5] = dcls;
-                    }
-                }
-            } else if constexpr (kPipe) {
-                conv_rows_tc<NT>(ob, s);
-            } else {
-                // convexity rows (conv.c:12-29): W = Darea g n_c, residual =
-                // sum Area n_c (the residual in FP64 in both forms)
-                for (int p = warp; p < np; p += NT / 32) {
-                    const double *nc = (p == 0) ? ob.nx : (p == 1) ? ob.ny : ob.nz;
-                    double res = 0;
-                    R *Wp = s.W + static_cast<size_t>(p) * wcols;
-                    for (int i = lane; i < F; i += 32) {
-                        res = res + s.area[i] * nc[i];
-                        Wp[i] = R(ob.darea[i] * s.gv[i] * nc[i]);
-                    }
-                    res = warp_sum(res);
-                    if (lane == 0) s.red[p * kRedStride] = res;
-                }
-            }
-            __syncthreads();
-            // 3. shape contraction and the remaining columns of J
-            if constexpr (kFP64) {
-                for (int o = tid; o < np * C; o += NT) {
-                    const int p = o / C, k = o - p * C;
-                    const R *Wp = s.W + static_cast<size_t>(p) * wcols;
-                    const R *ds = dsphR + k;
-                    R acc = 0;
-                    for (int i = 0; i < F; i++) acc = acc + Wp[i] * ds[static_cast<size_t>(i) * C];
-                    s.J[p * ma + k] = conv ? acc : s.pt[p * kPointStride + 24] * acc;
-                }
-            } else if constexpr (KU == 0) {
-                contract_tc_issue<NT>(s, F, tcs);   // the work below overlaps the MMAs
-            } else {
-                if (s.dsph)
-                    contract_mixed<NT, KU, true>(s, dsphF, np, F, C, ma, wcols, conv);
-                else
-                    contract_mixed<NT, KU, false>(s, dsphF, np, F, C, ma, wcols, conv);
-            }
-            // remaining columns of J: one thread per point (not thread 0 on the
-            // tensor-core path: it issues the MMAs)
-            const int jp = kPipe ? (tid + 32) % NT : tid;
-            if (jp < np) {
-                const int p = jp;
-                R *Jp = s.J + p * ma;
-                const double *rd = s.red + p * kRedStride;
-                if (!conv) {
-                    const R *pt = s.pt + p * kPointStride;
-                    const R scale = pt[24];
-                    const R br = R(rd[0]);
-                    Jp[C] = scale * R(rd[1]);
-                    Jp[C + 1] = scale * R(rd[2]);
-                    Jp[C + 2] = scale * R(rd[3]);
-                    Jp[C + 3] = br * pt[25];
-                    Jp[C + 4] = br * pt[26];
-                    Jp[C + 5] = br * pt[27];
-                    Jp[C + 6] = scale * R(rd[4]) * cl;
-                    Jp[C + 7] = scale * R(rd[5]);
-                    s.ym[p] = static_cast<double>(br * scale);
-                } else {
-                    for (int k = C; k < ma; k++) Jp[k] = 0;
-                    s.ym[p] = rd[0];
-                    s.misc[M_CHK + p] = rd[0];
-                }
-            }
-            bool next_setup = false;
-            if constexpr (kPipe) {
-                // point set-up of the next tile into the other buffer
-                const int nlc = t0 + P < npts ? lc : lc + 1, nt0 = t0 + P < npts ? t0 + P : 0;
-                next_setup = nlc < ob.n_lc - 1;   // the last lightcurve is the convexity rows
-                if (next_setup && warp > 0 && pipe_sp < min(P, ob.lc_npts[nlc] - nt0))
-                    setup_point<FORM>(ob, cfg, ob.lc_start[nlc] + nt0 + pipe_sp, omg, B, DB0, DB1, php0, php1, php2,
-                                      s.pt2 + pipe_sp * kPointStride);
-                contract_tc_finish<NT>(s, np, F, C, ma, conv, tcs);
-            }
-            __syncthreads();
-            if (next_setup) {
-                R *t = s.pt;
-                s.pt = s.pt2;
-                s.pt2 = t;
-            }
-            if (rel) {
-                // 4a. lightcurve sums and a copy of the rows (mrqcof.c:51-88)
-                R *dst = scratch + static_cast<size_t>(t0) * (ma + 1);
-                for (int e = tid; e < np * ma; e += NT) {
-                    int p = e / ma, l = e - p * ma;
-                    dst[static_cast<size_t>(p) * (ma + 1) + l] = s.J[e];
-                }
-                if (tid < np) dst[static_cast<size_t>(tid) * (ma + 1) + ma] = R(s.ym[tid]);
-                for (int l = tid; l < ma; l += NT) {
-                    if constexpr (kFP64) {
-                        double d = s.dave[l];
-                        for (int p = 0; p < np; p++) d = d + s.J[p * ma + l];
-                        s.dave[l] = d;
-                    } else {
-                        float d = 0.f;
-                        for (int p = 0; p < np; p++) d += s.J[p * ma + l];
-                        s.dave[l] += static_cast<double>(d);
-                    }
-                }
-                if (tid == 0) {
-                    double av = s.misc[M_AVE];
-                    for (int p = 0; p < np; p++) av = av + s.ym[p];
-                    s.misc[M_AVE] = av;
-                }
-                __syncthreads();
-                continue;
-            }
-            // 5. accumulate (mrqcof.c:106-136)
-            if constexpr (kPipe) {
-                accumulate_tile_tc<NT>(ob, s, np, start + t0, conv, conv_sig, tcs);
-                if (++tiles_since_flush == kTilesPerFlush) {
-                    tc_alpha_flush<NT>(ob, s, M, bv, tcs);
-                    tiles_since_flush = 0;
-                }
-            } else {
-                accumulate_tile<FORM>(ob, s, M, bv, np, start + t0, conv, conv_sig, accA, accB);
-                if constexpr (!kFP64) {
-                    if (++tiles_since_flush == kTilesPerFlush) {
-                        flush_partials<FORM>(M, bv, mf, accA, accB);
-                        tiles_since_flush = 0;
-                    }
-                }
-            }
-        }
-        if (!rel) continue;
-        // ---- pass 2: renormalise and accumulate (mrqcof.c:90-136) ----
-        const double ave = s.misc[M_AVE];
-        for (int t0 = 0; t0 < npts; t0 += P) {
-            const int np = min(P, npts - t0);
-            const R *src = scratch + static_cast<size_t>(t0) * (ma + 1);
-            // model values of the tile in FP64 (the FP64 form keeps its own
-            // values; the mixed form parks them as FP32)
-            if (tid < np) {
-                const int q = start + t0 + tid;
-                const double coef = ob.sig[q] * npts / ave;
-                const double yt = static_cast<double>(src[static_cast<size_t>(tid) * (ma + 1) + ma]);
-                s.ym[tid] = coef * yt;
-                s.red[tid * kRedStride + 6] = coef;
-                s.red[tid * kRedStride + 7] = yt / ave;
-            }
-            __syncthreads();
-            for (int e = tid; e < np * ma; e += NT) {
-                const int p = e / ma, l = e - p * ma;
-                const R v = src[static_cast<size_t>(p) * (ma + 1) + l];
-                R out;
-                if constexpr (kFP64) {
-                    const int q = start + t0 + p;
-                    const double coef = ob.sig[q] * npts / ave;
-                    const double yt = src[static_cast<size_t>(p) * (ma + 1) + ma];
-                    out = coef * (v - yt * s.dave[l] / ave);
-                } else {
-                    out = float(s.red[p * kRedStride + 6]) *
-                          (v - float(s.red[p * kRedStride + 7]) * float(s.dave[l]));
-                }
-                s.J[e] = (l == 0) ? R(0) : out;
-            }
-            __syncthreads();
-            if constexpr (kPipe) {
-                accumulate_tile_tc<NT>(ob, s, np, start + t0, false, conv_sig, tcs);
-                if (++tiles_since_flush == kTilesPerFlush) {
-                    tc_alpha_flush<NT>(ob, s, M, bv, tcs);
-                    tiles_since_flush = 0;
-                }
-            } else {
-                accumulate_tile<FORM>(ob, s, M, bv, np, start + t0, false, conv_sig, accA, accB);
-                if constexpr (!kFP64) {
-                    if (++tiles_since_flush == kTilesPerFlush) {
-                        flush_partials<FORM>(M, bv, mf, accA, accB);
-                        tiles_since_flush = 0;
-                    }
-                }
-            }
-        }
-    }
-    if constexpr (kPipe) tc_alpha_flush<NT>(ob, s, M, bv, tcs);
-    else if constexpr (!kFP64) flush_partials<FORM>(M, bv, mf, accA, accB);
-    __syncthreads();
-    // mirror the lower triangle (mrqcof.c:139-141)
-    for (int e = tid; e < mf * mf; e += NT) {
-        const int j = e / mf, k = e - j * mf;
-        if (k > j) M[e] = M[k * mf + j];
-    }
-    __syncthreads();
-}
-
-// Gauss-Jordan elimination with full pivoting on A (n x n, row-major in
-// shared memory) and right-hand side b (gauss_errc.c:9-73).  Only the
-// solution is needed by the LM step, so the columns that already hold the
-// inverse are not updated and the final column unscrambling is skipped; the
-// pivot choices and the solution are those of the full algorithm.
-// Returns 0, 1 (no usable pivot: NaN entries) or 2 (zero pivot).
-template <int NT>
-__device__ int gauss_jordan(double *A, double *b, int n, double *col, int *ipiv, double *red)
-{
-    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    for (int k = tid; k < n; k += NT) ipiv[k] = 0;
-    __syncthreads();
-    for (int step = 0; step < n; step++) {
-        // pivot search: largest |a| over unpivoted rows and columns; ties go
-        // to the last element in row-major order (the reference's >=).
-        double bv = -1.0;
-        int bi = -1;
-        for (int e = tid; e < n * n; e += NT) {
-            const int j = e / n, k = e - j * n;
-            if (ipiv[j] != 1 && ipiv[k] == 0) {
-                const double v = fabs(A[e]);
-                if (v >= 0.0 && (v > bv || (v == bv && e > bi))) {
-                    bv = v;
-                    bi = e;
-                }
-            }
-        }
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) {
-            const double ov = __shfl_xor_sync(0xffffffffu, bv, o);
-            const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
-            if (ov > bv || (ov == bv && oi > bi)) {
-                bv = ov;
-                bi = oi;
-            }
-        }
-        if (lane == 0) {
-            red[warp] = bv;
-            ipiv[n + 2 + warp] = bi;
-        }
-        __syncthreads();
-        if (tid == 0) {
-            double v = red[0];
-            int idx = ipiv[n + 2];
-            for (int w = 1; w < NT / 32; w++) {
-                const double ov = red[w];
-                const int oi = ipiv[n + 2 + w];
-                if (ov > v || (ov == v && oi > idx)) {
-                    v = ov;
-                    idx = oi;
-                }
-            }
-            ipiv[n] = idx;
-            if (idx >= 0) ipiv[idx - (idx / n) * n] += 1;
-        }
-        __syncthreads();
-        const int idx = ipiv[n];
-        if (idx < 0) return 1;
-        const int irow = idx / n, icol = idx - irow * n;
-        if (irow != icol) {
-            for (int l = tid; l < n; l += NT) {
-                const double t = A[irow * n + l];
-                A[irow * n + l] = A[icol * n + l];
-                A[icol * n + l] = t;
-            }
-            if (tid == 0) {
-                const double t = b[irow];
-                b[irow] = b[icol];
-                b[icol] = t;
-            }
-            __syncthreads();
-        }
-        const double piv = A[icol * n + icol];
-        if (piv == 0.0) return 2;
-        if (tid == 0) red[0] = 1.0 / piv;
-        __syncthreads();
-        const double pivinv = red[0];
-        // scale the pivot row over the columns not yet pivoted
-        for (int l = tid; l < n; l += NT)
-            if (ipiv[l] == 0) A[icol * n + l] *= pivinv;
-        if (tid == 0) b[icol] *= pivinv;
-        for (int r = tid; r < n; r += NT) col[r] = A[r * n + icol];
-        __syncthreads();
-        for (int e = tid; e < n * n; e += NT) {
-            const int r = e / n, l = e - r * n;
-            if (r != icol && ipiv[l] == 0) A[e] -= A[icol * n + l] * col[r];
-        }
-        for (int r = tid; r < n; r += NT)
-            if (r != icol) b[r] -= b[icol] * col[r];
-        __syncthreads();
-    }
-    return 0;
-}
-
-// Cholesky factorisation A = L L^T of the damped normal matrix (symmetric
-// positive definite; lower triangle used, overwritten by L) and the solve of
-// L L^T x = b, in FP64.  The forward substitution runs inside the
-// factorisation (b is the bordering column: y_j = b_j / L_jj, then b_i -=
-// L_ij y_j with the trailing update).  Columns are taken two at a time: warp
-// 0 factors the 2 x 2 pivot block and scales both columns and y, then all
-// threads apply the rank-2 update to the trailing block -- two CTA barriers
-// per pair of columns.  The back substitution uses the stored reciprocals.
-// Returns 2 when a pivot is not positive.
-template <int NT>
-__device__ int cholesky_solve(double *A, double *b, int n, double *col, double *flag)
-{
-    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    __syncthreads();
-    for (int j = 0; j < n; j += 2) {
-        const bool two = j + 1 < n;
-        if (warp == 0) {
-            double i0 = 0, l10 = 0, i1 = 0;
-            if (lane == 0) {
-                const double d0 = A[j * n + j];
-                bool ok = d0 > 0.0;
-                i0 = ok ? rsqrt(d0) : 0.0;
-                A[j * n + j] = d0 * i0;
-                col[j] = i0;
-                const double y0 = b[j] * i0;
-                b[j] = y0;
-                if (two && ok) {
-                    l10 = A[(j + 1) * n + j] * i0;
-                    const double d1 = A[(j + 1) * n + j + 1] - l10 * l10;
-                    ok = d1 > 0.0;
-                    i1 = ok ? rsqrt(d1) : 0.0;
-                    A[(j + 1) * n + j] = l10;
-                    A[(j + 1) * n + j + 1] = d1 * i1;
-                    col[j + 1] = i1;
-                    b[j + 1] = (b[j + 1] - l10 * y0) * i1;
-                }
-                *flag = ok ? 1.0 : 0.0;
-            }
-            i0 = __shfl_sync(0xffffffffu, i0, 0);
-            l10 = __shfl_sync(0xffffffffu, l10, 0);
-            i1 = __shfl_sync(0xffffffffu, i1, 0);
-            const int r0 = j + (two ? 2 : 1);
-            for (int i = r0 + lane; i < n; i += 32) {
-                const double a0 = A[i * n + j] * i0;
-                A[i * n + j] = a0;
-                if (two) A[i * n + j + 1] = (A[i * n + j + 1] - a0 * l10) * i1;
-            }
-        }
-        __syncthreads();
-        if (*flag == 0.0) return 2;
-        const int j2 = j + (two ? 2 : 1);
-        const int m = n - j2;
-        const int ntri = m * (m + 1) / 2;
-        const double y0 = b[j], y1 = two ? b[j + 1] : 0.0;
-        for (int e = tid; e < ntri + m; e += NT) {
-            if (e < ntri) {
-                const int r = tri_row(e);
-                const int c = e - r * (r + 1) / 2;
-                const int i = j2 + r, k = j2 + c;
-                double v = A[i * n + k] - A[i * n + j] * A[k * n + j];
-                if (two) v -= A[i * n + j + 1] * A[k * n + j + 1];
-                A[i * n + k] = v;
-            } else {
-                const int i = j2 + (e - ntri);
-                double v = b[i] - A[i * n + j] * y0;
-                if (two) v -= A[i * n + j + 1] * y1;
-                b[i] = v;
-            }
-        }
-        __syncthreads();
-    }
-    if (warp == 0) {
-        for (int j = n - 1; j >= 0; j--) {
-            double x = 0;
-            if (lane == 0) {
-                x = b[j] * col[j];
-                b[j] = x;
-            }
-            x = __shfl_sync(0xffffffffu, x, 0);
-            for (int i = lane; i < j; i += 32) b[i] -= A[j * n + i] * x;
-            __syncwarp();
-        }
-    }
-    __syncthreads();
-    return 0;
-}
-
-// Learned stop predictor, evaluated by warp 0: standardised features f[10]
-// -> 64 GELU -> 64 GELU -> 1, output de-standardised.  Predicts
-// log(final rms / rms after kScreenIters iterations).  sh: 64 floats.
-__device__ inline float gelu(float x) { return 0.5f * x * (1.f + erff(x * 0.70710678118654752f)); }
-
-__device__ float mlp_predict_warp(const float *W, const float *f, float *sh)
-{
-    const int lane = threadIdx.x & 31;
-    float x[kFeat];
-#pragma unroll
-    for (int i = 0; i < kFeat; i++) x[i] = (f[i] - W[kMlpMu + i]) / W[kMlpSd + i];
-    float h1[2];
-#pragma unroll
-    for (int h = 0; h < 2; h++) {
-        const int u = lane + 32 * h;
-        float z = W[kMlpB1 + u];
-#pragma unroll
-        for (int i = 0; i < kFeat; i++) z = fmaf(W[kMlpW1 + u * kFeat + i], x[i], z);
-        h1[h] = gelu(z);
-    }
-    sh[lane] = h1[0];
-    sh[lane + 32] = h1[1];
-    __syncwarp();
-    float y = 0.f;
-#pragma unroll
-    for (int h = 0; h < 2; h++) {
-        const int u = lane + 32 * h;
-        float z = W[kMlpB2 + u];
-        for (int j = 0; j < kHidden; j++) z = fmaf(W[kMlpW2 + u * kHidden + j], sh[j], z);
-        y = fmaf(W[kMlpW3 + u], gelu(z), y);
-    }
-    y = warp_sum(y) + W[kMlpB3];
-    __syncwarp();
-    return y * W[kMlpYSd] + W[kMlpYMu];
-}
-
-// ---------------------------------------------------------------------------
-// One fit (period_search_BOINC.cpp:817-921 with mrqmin.c:11-110).
-// ---------------------------------------------------------------------------
-template <int FORM, int KU>
-__device__ void run_fit(const DevObject &ob, const FitConfig &cfg, const SlotLayout &L, Smem<FORM> &s,
-                        typename RealOf<FORM>::T *scratch, int64_t n, int pole, ps_fit *out, const FitWork &w,
-                        long long fidx, TcState &tcs)
-{
-    constexpr bool kTensor = FORM == PS_FORM_MIXED && KU == 0;
-    constexpr int NT = threads_of<FORM>();
-    const int tid = threadIdx.x;
-    const int C = ob.ncoef, ma = ob.ma, mf = ob.mfit;
-    const double freq = cfg.freq_start - (n - 1) * cfg.freq_step;
-    const double prd = 1 / freq;
-    for (int i = tid; i < ma; i += NT) {
-        double v;
-        if (i < C) v = ob.cg_first[i];
-        else if (i == C) v = kDeg2Rad * (90 - c_beta_pole[pole - 1]);
-        else if (i == C + 1) v = kDeg2Rad * c_lambda_pole[pole - 1];
-        else if (i == C + 2) v = 24 * 2 * kPi / prd;
-        else if (i == C + 3) v = cfg.par0;
-        else if (i == C + 4) v = cfg.par1;
-        else if (i == C + 5) v = cfg.par2;
-        else if (i == C + 6) v = cfg.log_cl;
-        else v = 1;
-        s.cg[i] = v;
-        s.atry[i] = v;
-    }
-    __syncthreads();
-
-    double alamda = -1, ochisq = 0, chisq = 0, rchisq = -1;
-    double iter_diff = 1e40, dev_old = 1e30, dev_new = 0;
-    double chk_acc[3] = {0, 0, 0}, chk_first[3] = {0, 0, 0}, chk_trial[3] = {0, 0, 0};
-    double area_first = 0, area_trial = 0, totarea = 0;
-    int niter = 0, last_err = 0;
-    // learned early stop: accepted chi^2 and lambda of the first iterations
-    double hist[kScreenIters + 1], lam_hist[kScreenIters];
-    double pred_dev = 0;
-    bool screened = false;
-    while (((niter < cfg.n_iter_max) && (iter_diff > cfg.iter_diff_max)) || (niter < cfg.n_iter_min)) {
-        bool accepted = false;
-        if (alamda < 0) {
-            alamda = cfg.alamda_start;
-            evaluate<FORM, KU>(ob, cfg, L, s, s.cg, s.alpha, s.beta, scratch, tcs);
-            if constexpr (kTensor) {
-                if (*s.abort) {
-                    last_err = kErrTcTimeout;
-                    break;
-                }
-            }
-            ochisq = s.misc[M_CHISQ];
-            hist[0] = ochisq;
-            area_first = s.misc[M_AREA];
-            for (int c = 0; c < 3; c++) chk_first[c] = s.misc[M_CHK + c];
-            totarea = area_first;
-        }
-        for (int e = tid; e < mf * mf; e += NT) {
-            const int j = e / mf, k = e - j * mf;
-            s.covar[e] = (j == k) ? s.alpha[e] * (1 + alamda) : s.alpha[e];
-        }
-        for (int j = tid; j < mf; j += NT) s.da[j] = s.beta[j];
-        __syncthreads();
-        int err;
-        if constexpr (FORM == PS_FORM_FP64) {
-            err = gauss_jordan<NT>(s.covar, s.da, mf, s.col, s.ipiv, s.misc + M_RED);
-        } else {
-            // The damped normal matrix is symmetric positive definite: solve
-            // it by Cholesky in FP64; if a pivot is not positive (rounding on
-            // a nearly singular alpha), redo the step with Gauss-Jordan.
-            err = cholesky_solve<NT>(s.covar, s.da, mf, s.col, s.misc + M_PIV);
-            if (err) {
-                for (int e = tid; e < mf * mf; e += NT) {
-                    const int j = e / mf, k = e - j * mf;
-                    s.covar[e] = (j == k) ? s.alpha[e] * (1 + alamda) : s.alpha[e];
-                }
-                for (int j = tid; j < mf; j += NT) s.da[j] = s.beta[j];
-                __syncthreads();
-                err = gauss_jordan<NT>(s.covar, s.da, mf, s.col, s.ipiv, s.misc + M_RED);
-            }
-        }
-        __syncthreads();
-        if (err == 0) {
-            for (int j = tid; j < mf; j += NT) {
-                const int l = ob.free_list[j];
-                s.atry[l] = s.cg[l] + s.da[j];
-            }
-            __syncthreads();
-            evaluate<FORM, KU>(ob, cfg, L, s, s.atry, s.covar, s.da, scratch, tcs);
-            if constexpr (kTensor) {
-                if (*s.abort) {
-                    last_err = kErrTcTimeout;
-                    break;
-                }
-            }
-            chisq = s.misc[M_CHISQ];
-            area_trial = s.misc[M_AREA];
-            for (int c = 0; c < 3; c++) chk_trial[c] = s.misc[M_CHK + c];
-            totarea = area_trial;
-            if (chisq < ochisq) {
-                accepted = true;
-                alamda = alamda / cfg.alamda_incr;
-                for (int e = tid; e < mf * mf; e += NT) s.alpha[e] = s.covar[e];
-                for (int j = tid; j < mf; j += NT) s.beta[j] = s.da[j];
-                for (int l = tid; l < ma; l += NT) s.cg[l] = s.atry[l];
-                __syncthreads();
-            } else {
-                alamda = cfg.alamda_incr * alamda;
-                chisq = ochisq;
-            }
-        } else {
-            last_err = err;
-        }
-        niter++;
-        if ((niter == 1) || (chisq < ochisq)) {
-            ochisq = chisq;
-            // curv(cg) of the driver: the accepted shape is the trial one;
-            // otherwise (first iteration, rejected or failed solve) cg is
-            // still the starting vector of the first evaluation.
-            const double *src = accepted ? chk_trial : chk_first;
-            for (int c = 0; c < 3; c++) chk_acc[c] = src[c];
-            totarea = accepted ? area_trial : area_first;
-            rchisq = chisq - (chk_acc[0] * chk_acc[0] + chk_acc[1] * chk_acc[1] + chk_acc[2] * chk_acc[2]) *
-                                 (cfg.conw_r * cfg.conw_r);
-        }
-        dev_new = sqrt(rchisq / ob.ndata);
-        if (dev_old - dev_new > 1e-10) {
-            iter_diff = dev_old - dev_new;
-            dev_old = dev_new;
-        }
-        if (niter <= kScreenIters) {
-            hist[niter] = ochisq;
-            lam_hist[niter - 1] = alamda;
-        }
-        if (niter == kScreenIters && (w.traj || w.mlp)) {
-            float f[kFeat];
-#pragma unroll
-            for (int i = 0; i < kScreenIters; i++) {
-                f[i] = static_cast<float>(log(hist[i + 1] / hist[0]));
-                f[kScreenIters + i] = static_cast<float>(log10(lam_hist[i]));
-            }
-            f[8] = static_cast<float>(log(static_cast<double>(ob.ndata)));
-            f[9] = static_cast<float>(log(prd));
-            if (w.traj && tid == 0) {
-                float *rec = w.traj + static_cast<size_t>(fidx) * kTrajFloats;
-                for (int i = 0; i < kFeat; i++) rec[i] = f[i];
-                rec[10] = static_cast<float>(dev_new);
-            }
-            if (w.mlp && w.iter_limit == kScreenIters) {
-                if (tid < 32) {
-                    const float y = mlp_predict_warp(w.mlp, f, reinterpret_cast<float *>(s.pt));
-                    if (tid == 0) s.misc[M_PIV + 2] = static_cast<double>(y);
-                }
-                __syncthreads();
-                pred_dev = dev_new * exp(s.misc[M_PIV + 2]);
-            }
-        }
-        if (w.iter_limit > 0 && niter >= w.iter_limit) {
-            screened = true;
-            break;
-        }
-    }
-    if (w.traj && tid == 0) {
-        float *rec = w.traj + static_cast<size_t>(fidx) * kTrajFloats;
-        rec[11] = static_cast<float>(dev_new);
-        rec[12] = static_cast<float>(niter);
-    }
-    if (tid == 0) {
-        ps_fit r;
-        r.dev = dev_new;
-        r.dark = sqrt(chk_acc[0] * chk_acc[0] + chk_acc[1] * chk_acc[1] + chk_acc[2] * chk_acc[2]);
-        r.totarea = totarea;
-        r.period_h = 24 * (2 * kPi / s.cg[C + 2]);
-        r.lambda_deg = kRad2Deg * s.cg[C + 1];
-        r.beta_deg = 90 - kRad2Deg * s.cg[C];
-        r.chisq = chisq;
-        r.niter = niter;
-        r.err_code = last_err;
-        r.pred_dev = pred_dev;
-        r.screened = screened ? 1 : 0;
-        r.reserved = 0;
-        *out = r;
-    }
-    __syncthreads();
-}
-
-template <int FORM, int KU>
-__global__ void __launch_bounds__(threads_of<FORM>(), 1)
-    fit_kernel(DevObject ob, FitConfig cfg, FitWork w, int P, int dsph_smem)
-{
-    using R = typename RealOf<FORM>::T;
-    constexpr int NT = threads_of<FORM>();
-    extern __shared__ __align__(16) char smem[];
-    const SlotLayout L = make_layout(FORM, ob.ma, ob.mfit, ob.nfac, ob.ncoef, P, dsph_smem);
-    Smem<FORM> s = carve<FORM>(smem, L);
-    constexpr bool kTensor = FORM == PS_FORM_MIXED && KU == 0;
-    if (s.dsph)
-        for (int e = threadIdx.x; e < ob.nfac * ob.ncoef; e += NT) s.dsph[e] = ob.dsph_f[e];
-    TcState tcs;
-    if constexpr (kTensor) tcs.tbase = tc_setup<NT>(ob, s);
-    R *scratch = reinterpret_cast<R *>(w.scratch + static_cast<size_t>(blockIdx.x) * w.scratch_stride);
-    __shared__ long long next;
-    for (;;) {
-        if (threadIdx.x == 0) next = static_cast<long long>(atomicAdd(w.queue, 1ULL));
-        __syncthreads();
-        const long long f = next;
-        __syncthreads();
-        if (f >= w.nfits) break;
-        if constexpr (kTensor) {
-            if (*s.abort) break;
-        }
-        int64_t n;
-        int pole;
-        if (w.period_index) {
-            n = w.period_index[f];
-            pole = w.pole[f];
-        } else {
-            n = w.n_lo + f / PS_N_POLES;
-            pole = static_cast<int>(f % PS_N_POLES) + 1;
-        }
-        run_fit<FORM, KU>(ob, cfg, L, s, scratch, n, pole, w.out + f, w, f, tcs);
-    }
-    if constexpr (kTensor) tc_teardown(s, tcs, ob.nfac);
-}
-
-template <int FORM, int KU>
-__global__ void __launch_bounds__(threads_of<FORM>(), 1) eval_kernel(DevObject ob, FitConfig cfg, const double *cg, double *alpha,
-                                                        double *beta, double *chisq, double *area, double *scratch,
-                                                        int P, int dsph_smem)
-{
-    using R = typename RealOf<FORM>::T;
-    constexpr int NT = threads_of<FORM>();
-    extern __shared__ __align__(16) char smem[];
-    const SlotLayout L = make_layout(FORM, ob.ma, ob.mfit, ob.nfac, ob.ncoef, P, dsph_smem);
-    Smem<FORM> s = carve<FORM>(smem, L);
-    constexpr bool kTensor = FORM == PS_FORM_MIXED && KU == 0;
-    if (s.dsph)
-        for (int e = threadIdx.x; e < ob.nfac * ob.ncoef; e += NT) s.dsph[e] = ob.dsph_f[e];
-    TcState tcs;
-    if constexpr (kTensor) tcs.tbase = tc_setup<NT>(ob, s);
-    for (int i = threadIdx.x; i < ob.ma; i += NT) s.cg[i] = cg[i];
-    __syncthreads();
-    evaluate<FORM, KU>(ob, cfg, L, s, s.cg, s.alpha, s.beta, reinterpret_cast<R *>(scratch), tcs);
-    if constexpr (kTensor) {
-        const bool aborted = *s.abort != 0;
-        tc_teardown(s, tcs, ob.nfac);
-        if (aborted) {
-            if (threadIdx.x == 0) *chisq = NAN;
-            return;
-        }
-    }
-    const int mf = ob.mfit;
-    for (int e = threadIdx.x; e < mf * mf; e += NT) alpha[e] = s.alpha[e];
-    for (int j = threadIdx.x; j < mf; j += NT) beta[j] = s.beta[j];
-    if (area)
-        for (int i = threadIdx.x; i < ob.nfac; i += NT) area[i] = s.area[i];
-    if (threadIdx.x == 0) *chisq = s.misc[M_CHISQ];
-}
 
 // FMA throughput probe: 8 independent FMA chains per thread.
 template <class T>

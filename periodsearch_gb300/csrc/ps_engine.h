@@ -48,6 +48,11 @@ struct FitWork {
     double *scratch;              // per-slot scratch for relative lightcurves
     size_t scratch_stride;        // doubles per slot
     ps_fit *out;                  // [nfits]
+    // multi-object packed launch (launch_pack): fit f belongs to object
+    // object[f], described by objs[object[f]] and cfgs[object[f]]
+    const struct DevObject *objs;
+    const struct FitConfig *cfgs;
+    const int *object;
     // learned early stop (all optional)
     int iter_limit;               // > 0: stop every fit after this many LM iterations (screening)
     float *traj;                  // [nfits][kTrajFloats] trajectory records, or nullptr
@@ -180,6 +185,12 @@ int launch_eval(int form, const DevObject &ob, const FitConfig &cfg, const doubl
                 double *beta, double *chisq, double *area, double *scratch, int P, size_t smem,
                 int dsph_smem, void *stream);
 int set_kernel_smem(int form, size_t smem, int ncoef, int dsph_smem);
+// Multi-object packed launch (ps_pack.cu): objects with identical shape
+// tables (facet grid, Laplace series, free parameters) share one persistent
+// launch; w.objs / w.cfgs / w.object / w.period_index / w.pole describe the
+// fits.  The basis and facet constants are taken from w.objs[0].
+int launch_pack(int form, const FitWork &w, int ncoef, int grid, int P, size_t smem, int dsph_smem, void *stream);
+int set_pack_smem(int form, size_t smem, int ncoef, int dsph_smem);
 int occupancy_slots(int form, size_t smem, int ncoef, int dsph_smem, int *per_sm);
 // Whether the tensor-core path supports an object: at most 64 coefficients
 // (the high and low TF32 parts of the basis fill 128 Tensor Memory lanes),
