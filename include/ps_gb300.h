@@ -319,6 +319,35 @@ ps_status ps_scan_learned(ps_ctx *ctx, double conw_r, int64_t n_lo, int64_t n_hi
  * completion was not observed within the wait limit. */
 ps_status ps_tc_selftest(int32_t device, const float *A, const float *B, int32_t K, float *D);
 
+/* ---- autotuner ---- */
+
+/* One kernel configuration tried by ps_autotune. */
+typedef struct ps_tune_candidate {
+    int32_t basis;         /* 0: basis in L2, 1: in shared memory (SIMT contraction), 2: tensor cores */
+    int32_t tile_points;   /* observations per tile */
+    int32_t ctas_per_sm;   /* fit slots per SM */
+    int32_t slots;         /* fit slots on the device */
+    double fits_per_s;     /* measured on the sample (fits of sample_iters LM iterations) */
+} ps_tune_candidate;
+
+#define PS_TUNE_MAX 16
+typedef struct ps_tune_report {
+    int32_t n;             /* candidates measured */
+    int32_t chosen;        /* index of the fastest, now the context's plan */
+    int32_t sample_fits, sample_iters;
+    ps_tune_candidate cand[PS_TUNE_MAX];
+} ps_tune_report;
+
+/* Times every kernel configuration that the object admits for the
+ * context's form -- basis placement (tensor cores, shared memory, L2), tile
+ * size and fit slots per SM -- on a sample of fits spread over the scan
+ * (sample_fits, 0: two waves of the default plan; each fit stopped after
+ * sample_iters LM iterations, 0: 6) and keeps the fastest as the context's
+ * plan.  Results of all forms' kernels are valid under every
+ * configuration; the mixed form's values differ between configurations
+ * within its parity tolerance. */
+ps_status ps_autotune(ps_ctx *ctx, double conw_r, int32_t sample_fits, int32_t sample_iters, ps_tune_report *report);
+
 /* ---- multi-object packing ---- */
 
 /* Many small objects (work units of a multi-object run) fitted by one

@@ -259,6 +259,21 @@ class Engine:
         _abi.check(r, "ps_screen", self._ctx)
         return out
 
+    def autotune(self, conw_r: float, sample_fits: int = 0, sample_iters: int = 0) -> dict:
+        """Times the kernel configurations the object admits (ps_autotune)
+        and keeps the fastest; returns the measured candidates."""
+        r = _abi.TuneReport()
+        _abi.check(self._L.ps_autotune(self._ctx, conw_r, sample_fits, sample_iters, C.byref(r)), "ps_autotune",
+                   self._ctx)
+        inf = _abi.Info()
+        _abi.check(self._L.ps_get_info(self._ctx, C.byref(inf)), "ps_get_info", self._ctx)
+        self.info = inf
+        names = {0: "l2", 1: "shared", 2: "tensor"}
+        cands = [{"basis": names.get(c.basis, c.basis), "tile_points": c.tile_points, "ctas_per_sm": c.ctas_per_sm,
+                  "slots": c.slots, "fits_per_s": c.fits_per_s} for c in r.cand[:r.n]]
+        return {"candidates": cands, "chosen": r.chosen, "sample_fits": r.sample_fits,
+                "sample_iters": r.sample_iters}
+
     def scan_refined(self, conw_r: float, n_lo: int, n_hi: int, refit_rel: float = 0.01, refit_halfwidth: int = 2):
         """Scan in the engine's form, then refit the minimum region in full
         with the FP64 form (ps_scan_refined); returns the rows and the

@@ -83,6 +83,19 @@ class ValidateReport(C.Structure):
                 ("argmax_dev", C.c_int64 * 3), ("parse_error_a", C.c_int32), ("parse_error_b", C.c_int32)]
 
 
+class TuneCandidate(C.Structure):
+    _fields_ = [("basis", C.c_int32), ("tile_points", C.c_int32), ("ctas_per_sm", C.c_int32), ("slots", C.c_int32),
+                ("fits_per_s", C.c_double)]
+
+
+TUNE_MAX = 16
+
+
+class TuneReport(C.Structure):
+    _fields_ = [("n", C.c_int32), ("chosen", C.c_int32), ("sample_fits", C.c_int32), ("sample_iters", C.c_int32),
+                ("cand", TuneCandidate * TUNE_MAX)]
+
+
 class LearnedOpts(C.Structure):
     _fields_ = [("top_k", C.c_int32), ("margin", C.c_double), ("region_rel", C.c_double),
                 ("region_halfwidth", C.c_int32), ("refit_rel", C.c_double), ("refit_halfwidth", C.c_int32)]
@@ -128,6 +141,7 @@ SIGNATURES = {
     "ps_screen": (C.c_int, [_CTX, C.c_double, C.c_int64, C.c_int64, C.POINTER(C.c_float), C.POINTER(Fit)]),
     "ps_tc_selftest": (C.c_int, [C.c_int32, C.POINTER(C.c_float), C.POINTER(C.c_float), C.c_int32,
                                  C.POINTER(C.c_float)]),
+    "ps_autotune": (C.c_int, [_CTX, C.c_double, C.c_int32, C.c_int32, C.POINTER(TuneReport)]),
     "ps_pack_create": (C.c_int, [C.POINTER(C.c_void_p), C.c_int32, C.c_int32, C.POINTER(C.c_void_p)]),
     "ps_pack_fit": (C.c_int, [C.c_void_p, C.POINTER(C.c_double), C.c_int64, C.POINTER(C.c_int32),
                               C.POINTER(C.c_int64), C.POINTER(C.c_int32), C.POINTER(Fit)]),

@@ -126,36 +126,19 @@ ps_status ensure_out(ps_ctx *c, size_t nfits)
     return PS_OK;
 }
 
-// Shared-memory plan, kernel attributes and resident slots of one form.
-ps_status make_plan(ps_ctx *c, int form)
+// Plan of one form for a given basis mode and tile size: shared-memory
+// layout, kernel attribute and resident slots (at most per_sm_cap per SM when
+// positive).  PS_ERR_LIMIT when the slot does not fit.
+ps_status build_plan(ps_ctx *c, int form, int dsph_smem, int P, int per_sm_cap, FormPlan *out)
 {
-    FormPlan &pl = c->plan[form];
-    if (pl.ready) return PS_OK;
     const psg::HostObject &o = c->obj;
     const int F = o.shape.nfac;
     cudaDeviceProp prop;
     PSG_CUDA(c, cudaGetDeviceProperties(&prop, c->opt.device));
-    size_t smem_max = static_cast<size_t>(prop.sharedMemPerBlockOptin);
-    // Mixed form: 32-point tiles with the tensor-core contraction where the
-    // shape tables allow it, else the SIMT contraction with the FP32 basis in
-    // shared memory when it fits; FP64 form: 16-point tiles.
-    const bool mixed = form == PS_FORM_MIXED;
-    int P = mixed ? 32 : 16, dsph_smem = mixed ? psg::kBasisSmem : psg::kBasisGlobal;
-    if (mixed && !(c->opt.flags & PS_FLAG_NO_TENSOR) && psg::tensor_basis_ok(F, o.ncoef, o.mfit, P))
-        dsph_smem = psg::kBasisTensor;
-    psg::SlotLayout L = psg::make_layout(form, o.ma, o.mfit, F, o.ncoef, P, dsph_smem);
-    if (L.bytes > smem_max && dsph_smem != psg::kBasisGlobal) {
-        dsph_smem = psg::kBasisGlobal;
-        L = psg::make_layout(form, o.ma, o.mfit, F, o.ncoef, P, dsph_smem);
-    }
-    while (L.bytes > smem_max && P > 2) {
-        P /= 2;
-        L = psg::make_layout(form, o.ma, o.mfit, F, o.ncoef, P, dsph_smem);
-    }
-    if (L.bytes > smem_max) {
-        c->err = "shared-memory plan of a fit slot exceeds the device limit";
-        return PS_ERR_LIMIT;
-    }
+    const size_t smem_max = static_cast<size_t>(prop.sharedMemPerBlockOptin);
+    if (dsph_smem == psg::kBasisTensor && !psg::tensor_basis_ok(F, o.ncoef, o.mfit, P)) return PS_ERR_LIMIT;
+    const psg::SlotLayout L = psg::make_layout(form, o.ma, o.mfit, F, o.ncoef, P, dsph_smem);
+    if (L.bytes > smem_max) return PS_ERR_LIMIT;
     // A tensor-core slot holds up to 512 Tensor Memory columns for its whole
     // life: request enough shared memory that only one slot fits on an SM.
     size_t bytes = L.bytes;
@@ -166,21 +149,50 @@ ps_status make_plan(ps_ctx *c, int form)
     int per_sm = 0;
     e = psg::occupancy_slots(form, bytes, o.ncoef, dsph_smem, &per_sm);
     if (e != 0) return cuda_fail(c, static_cast<cudaError_t>(e), "occupancy");
-    if (per_sm < 1) {
-        c->err = "fit slot does not fit on an SM";
-        return PS_ERR_LIMIT;
-    }
-    if (c->opt.ctas_per_sm > 0) per_sm = std::min(per_sm, c->opt.ctas_per_sm);
+    if (per_sm < 1) return PS_ERR_LIMIT;
+    if (per_sm_cap > 0) per_sm = std::min(per_sm, per_sm_cap);
     if (dsph_smem == psg::kBasisTensor && per_sm > 1) {
         c->err = "tensor-core fit slots would share an SM";
         return PS_ERR_LIMIT;
     }
-    pl.P = P;
-    pl.dsph_smem = dsph_smem;
-    pl.smem = bytes;
-    pl.slots = per_sm * c->sm_count;
-    pl.ready = true;
+    out->P = P;
+    out->dsph_smem = dsph_smem;
+    out->smem = bytes;
+    out->slots = per_sm * c->sm_count;
+    out->ready = true;
     return PS_OK;
+}
+
+// Default plan of one form: 32-point tiles (halved until a slot fits); the
+// mixed form with the tensor-core contraction where the shape tables allow
+// it, else the SIMT contraction with the FP32 basis in shared memory when it
+// fits (else in L2).  The FP64 form's results do not depend on the tile
+// size (its sums run in data order); 32 points measured fastest.
+ps_status make_plan(ps_ctx *c, int form)
+{
+    FormPlan &pl = c->plan[form];
+    if (pl.ready) return PS_OK;
+    const psg::HostObject &o = c->obj;
+    const bool mixed = form == PS_FORM_MIXED;
+    int modes[3], nm = 0;
+    if (mixed) {
+        if (!(c->opt.flags & PS_FLAG_NO_TENSOR) && psg::tensor_basis_ok(o.shape.nfac, o.ncoef, o.mfit, 32))
+            modes[nm++] = psg::kBasisTensor;
+        modes[nm++] = psg::kBasisSmem;
+    }
+    modes[nm++] = psg::kBasisGlobal;
+    for (int P = 32; P >= 2; P /= 2)
+        for (int k = 0; k < nm; k++) {
+            FormPlan cand;
+            const ps_status st = build_plan(c, form, modes[k], P, c->opt.ctas_per_sm, &cand);
+            if (st == PS_OK) {
+                pl = cand;
+                return PS_OK;
+            }
+            if (st != PS_ERR_LIMIT) return st;
+        }
+    c->err = "shared-memory plan of a fit slot exceeds the device limit";
+    return PS_ERR_LIMIT;
 }
 
 // Launches the fits described by w in the given form (queue and outputs
@@ -251,7 +263,8 @@ ps_status scan_rows(ps_ctx *c, double conw_r, int64_t n_lo, int64_t n_hi, ps_row
 
 // Fits given as (period index, pole) lists on the host: copied to the
 // device and launched in the given form; results in c->h_fits.
-ps_status run_list(ps_ctx *c, double conw_r, const int64_t *pidx, const int32_t *pole, int64_t n, int form)
+ps_status run_list(ps_ctx *c, double conw_r, const int64_t *pidx, const int32_t *pole, int64_t n, int form,
+                   int iter_limit = 0)
 {
     if (static_cast<size_t>(n) > c->list_cap) {
         cudaFree(c->d_pidx);
@@ -269,6 +282,7 @@ ps_status run_list(ps_ctx *c, double conw_r, const int64_t *pidx, const int32_t 
     w.nfits = n;
     w.period_index = c->d_pidx;
     w.pole = c->d_pole;
+    w.iter_limit = iter_limit;
     return run_fits(c, conw_r, w, form);
 }
 
@@ -918,6 +932,94 @@ ps_status ps_scan_refined(ps_ctx *c, double conw_r, int64_t n_lo, int64_t n_hi, 
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Autotuner
+// ---------------------------------------------------------------------------
+extern "C" ps_status ps_autotune(ps_ctx *c, double conw_r, int32_t sample_fits, int32_t sample_iters,
+                                 ps_tune_report *rep)
+{
+    if (!c || !rep || !(conw_r > 0) || sample_fits < 0 || sample_iters < 0) return PS_ERR_ARG;
+    PSG_CUDA(c, cudaSetDevice(c->opt.device));
+    const int form = c->opt.form;
+    const bool mixed = form == PS_FORM_MIXED;
+    const psg::HostObject &o = c->obj;
+    ps_status st = make_plan(c, form);
+    if (st != PS_OK) return st;
+    const FormPlan dflt = c->plan[form];
+    *rep = ps_tune_report{};
+    const int64_t nfit = sample_fits > 0 ? sample_fits : 2 * static_cast<int64_t>(dflt.slots);
+    const int iters = sample_iters > 0 ? sample_iters : 6;
+    rep->sample_fits = static_cast<int32_t>(nfit);
+    rep->sample_iters = iters;
+    // sample: periods spread over the scan, all poles in turn
+    std::vector<int64_t> pidx(static_cast<size_t>(nfit));
+    std::vector<int32_t> pole(static_cast<size_t>(nfit));
+    for (int64_t k = 0; k < nfit; k++) {
+        pidx[static_cast<size_t>(k)] = 1 + (k / PS_N_POLES * 7919) % std::max<int64_t>(o.n_max, 1);
+        pole[static_cast<size_t>(k)] = static_cast<int32_t>(k % PS_N_POLES) + 1;
+    }
+    std::vector<int> modes;
+    if (mixed) {
+        if (!(c->opt.flags & PS_FLAG_NO_TENSOR)) modes.push_back(psg::kBasisTensor);
+        modes.push_back(psg::kBasisSmem);
+    }
+    modes.push_back(psg::kBasisGlobal);
+    const int tiles_mixed[] = {32, 16}, tiles_fp64[] = {32, 16, 8};
+    std::vector<FormPlan> plans;
+    double best = -1;
+    int chosen = -1;
+    for (int mode : modes) {
+        const int *tiles = mixed ? tiles_mixed : tiles_fp64;
+        const int ntiles = mixed ? 2 : 3;
+        for (int t = 0; t < ntiles; t++) {
+            for (int cap : {0, 1}) {
+                if (rep->n >= PS_TUNE_MAX) break;
+                FormPlan cand;
+                st = build_plan(c, form, mode, tiles[t], cap, &cand);
+                if (st == PS_ERR_LIMIT) continue;
+                if (st != PS_OK) return st;
+                bool dup = false;
+                for (const FormPlan &q : plans)
+                    dup |= q.P == cand.P && q.dsph_smem == cand.dsph_smem && q.slots == cand.slots;
+                if (dup) continue;
+                c->plan[form] = cand;
+                st = run_list(c, conw_r, pidx.data(), pole.data(), nfit, form, iters);   // warm-up
+                if (st == PS_OK) st = run_list(c, conw_r, pidx.data(), pole.data(), nfit, form, iters);
+                if (st != PS_OK) {
+                    c->plan[form] = dflt;
+                    return st;
+                }
+                ps_tune_candidate &r = rep->cand[rep->n];
+                r.basis = cand.dsph_smem;
+                r.tile_points = cand.P;
+                r.ctas_per_sm = cand.slots / std::max(c->sm_count, 1);
+                r.slots = cand.slots;
+                r.fits_per_s = c->timing.kernel_ms > 0 ? nfit / (c->timing.kernel_ms * 1e-3) : 0;
+                if (r.fits_per_s > best) {
+                    best = r.fits_per_s;
+                    chosen = rep->n;
+                }
+                plans.push_back(cand);
+                rep->n++;
+            }
+        }
+    }
+    if (chosen < 0) {
+        c->plan[form] = dflt;
+        c->err = "no kernel configuration could be measured";
+        return PS_ERR_LIMIT;
+    }
+    c->plan[form] = plans[static_cast<size_t>(chosen)];
+    const FormPlan &pl = c->plan[form];
+    const int e = psg::set_kernel_smem(form, pl.smem, o.ncoef, pl.dsph_smem);
+    if (e != 0) return cuda_fail(c, static_cast<cudaError_t>(e), "cudaFuncSetAttribute");
+    c->P = pl.P;
+    c->dsph_smem = pl.dsph_smem;
+    c->smem = pl.smem;
+    rep->chosen = chosen;
+    return PS_OK;
+}
 
 // ---------------------------------------------------------------------------
 // Multi-object packing

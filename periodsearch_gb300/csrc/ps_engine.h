@@ -173,7 +173,8 @@ PSG_HD inline SlotLayout make_layout(int form, int ma, int mfit, int nfac, int n
         L.pt2 = L.pt;
         L.fac = L.ag = L.fpart = L.aop = 0;
     }
-    L.accs = form == PS_FORM_MIXED ? take(2 * static_cast<size_t>(P) * sizeof(float)) : 0;
+    // 32 residuals then 32 weights, whatever the tile size
+    L.accs = form == PS_FORM_MIXED ? take(64 * sizeof(float)) : 0;
     L.bytes = o;
     return L;
 }
