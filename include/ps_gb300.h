@@ -319,6 +319,42 @@ ps_status ps_scan_learned(ps_ctx *ctx, double conw_r, int64_t n_lo, int64_t n_hi
  * completion was not observed within the wait limit. */
 ps_status ps_tc_selftest(int32_t device, const float *A, const float *B, int32_t K, float *D);
 
+/* ---- the reference's prepared state (CUDA port host calls) ---- */
+
+/* One object as the reference's main() holds it after reading and
+ * preparing period_search_in (period_search_BOINC.cpp:343-600): for callers
+ * that have done that work themselves, such as the drop-in adaptor of the
+ * CUDA port's CUDAPrepare / CUDAPrecalc / CUDAStart.  Arrays are 0-based
+ * and read during the call only. */
+typedef struct ps_state {
+    int32_t lmax, mmax, nrows;        /* Laplace series and facet grid */
+    int32_t n_lc;                     /* real lightcurves */
+    const int32_t *lc_points;         /* [n_lc] */
+    const int32_t *lc_rel;            /* [n_lc] 1 = relative */
+    int32_t ndata;                    /* real points */
+    const double *tim;                /* [ndata] JD minus the epoch */
+    const double *brightness, *sig, *weight;    /* [ndata] */
+    const double *ee, *ee0;           /* [ndata * 3] unit vectors asteroid -> Earth / Sun */
+    double phi0;                      /* initial rotation angle [rad] */
+    double par[3], cl;                /* phase function and Lambert weight start values */
+    double alamda_start, alamda_incr;
+    double stop_condition;
+    int32_t n_iter_min;
+    const int32_t *ia;                /* [ncoef + 8] free flags in the reference's parameter order */
+    const double *cg_first;           /* [ncoef] initial shape coefficients */
+    double escl;                      /* size scale of the initial ellipsoid */
+    double freq_start, freq_end, freq_step;     /* [1/h] */
+    double conw_r;                    /* initial convexity weight / escl^2 */
+} ps_state;
+
+ps_status ps_prepare_state(const ps_state *state, const ps_options *opt, ps_ctx **out);
+
+/* One round of the convexity-weight pre-pass at *conw_r (the CUDA port's
+ * CUDAPrecalc, start_CUDA.cu:248-521): fits the first min(10, n_max)
+ * periods, then sets *new_conw = 1 when their mean dark-facet statistic is
+ * below 1, else doubles *conw_r.  ps_precalc_conw repeats it. */
+ps_status ps_precalc_step(ps_ctx *ctx, double *conw_r, int32_t *new_conw);
+
 /* ---- autotuner ---- */
 
 /* One kernel configuration tried by ps_autotune. */

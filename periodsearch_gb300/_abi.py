@@ -83,6 +83,18 @@ class ValidateReport(C.Structure):
                 ("argmax_dev", C.c_int64 * 3), ("parse_error_a", C.c_int32), ("parse_error_b", C.c_int32)]
 
 
+class State(C.Structure):
+    _fields_ = [("lmax", C.c_int32), ("mmax", C.c_int32), ("nrows", C.c_int32), ("n_lc", C.c_int32),
+                ("lc_points", C.POINTER(C.c_int32)), ("lc_rel", C.POINTER(C.c_int32)), ("ndata", C.c_int32),
+                ("tim", C.POINTER(C.c_double)), ("brightness", C.POINTER(C.c_double)), ("sig", C.POINTER(C.c_double)),
+                ("weight", C.POINTER(C.c_double)), ("ee", C.POINTER(C.c_double)), ("ee0", C.POINTER(C.c_double)),
+                ("phi0", C.c_double), ("par", C.c_double * 3), ("cl", C.c_double), ("alamda_start", C.c_double),
+                ("alamda_incr", C.c_double), ("stop_condition", C.c_double), ("n_iter_min", C.c_int32),
+                ("ia", C.POINTER(C.c_int32)), ("cg_first", C.POINTER(C.c_double)), ("escl", C.c_double),
+                ("freq_start", C.c_double), ("freq_end", C.c_double), ("freq_step", C.c_double),
+                ("conw_r", C.c_double)]
+
+
 class TuneCandidate(C.Structure):
     _fields_ = [("basis", C.c_int32), ("tile_points", C.c_int32), ("ctas_per_sm", C.c_int32), ("slots", C.c_int32),
                 ("fits_per_s", C.c_double)]
@@ -141,6 +153,8 @@ SIGNATURES = {
     "ps_screen": (C.c_int, [_CTX, C.c_double, C.c_int64, C.c_int64, C.POINTER(C.c_float), C.POINTER(Fit)]),
     "ps_tc_selftest": (C.c_int, [C.c_int32, C.POINTER(C.c_float), C.POINTER(C.c_float), C.c_int32,
                                  C.POINTER(C.c_float)]),
+    "ps_prepare_state": (C.c_int, [C.POINTER(State), C.POINTER(Options), C.POINTER(C.c_void_p)]),
+    "ps_precalc_step": (C.c_int, [_CTX, C.POINTER(C.c_double), C.POINTER(C.c_int32)]),
     "ps_autotune": (C.c_int, [_CTX, C.c_double, C.c_int32, C.c_int32, C.POINTER(TuneReport)]),
     "ps_pack_create": (C.c_int, [C.POINTER(C.c_void_p), C.c_int32, C.c_int32, C.POINTER(C.c_void_p)]),
     "ps_pack_fit": (C.c_int, [C.c_void_p, C.POINTER(C.c_double), C.c_int64, C.POINTER(C.c_int32),

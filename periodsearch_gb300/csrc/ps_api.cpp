@@ -417,6 +417,14 @@ ps_status ps_input_problem(const ps_input *in, ps_problem *v)
 
 void ps_input_free(ps_input *in) { delete in; }
 
+}  // extern "C"
+
+namespace {
+ps_status upload_object(std::unique_ptr<ps_ctx> &c, ps_ctx **out);
+}  // namespace
+
+extern "C" {
+
 ps_status ps_prepare(const ps_problem *prob, const ps_options *opt, ps_ctx **out)
 {
     if (!prob || !out) return PS_ERR_ARG;
@@ -430,6 +438,33 @@ ps_status ps_prepare(const ps_problem *prob, const ps_options *opt, ps_ctx **out
         std::fprintf(stderr, "ps_prepare: %s\n", err.c_str());
         return st;
     }
+    return upload_object(c, out);
+}
+
+ps_status ps_prepare_state(const ps_state *state, const ps_options *opt, ps_ctx **out)
+{
+    if (!state || !out) return PS_ERR_ARG;
+    *out = nullptr;
+    auto c = std::make_unique<ps_ctx>();
+    if (opt) c->opt = *opt;
+    if (c->opt.form != PS_FORM_FP64 && c->opt.form != PS_FORM_MIXED) return PS_ERR_ARG;
+    std::string err;
+    ps_status st = psg::prepare_object_state(*state, c->obj, err);
+    if (st != PS_OK) {
+        std::fprintf(stderr, "ps_prepare_state: %s\n", err.c_str());
+        return st;
+    }
+    return upload_object(c, out);
+}
+
+}  // extern "C"
+
+namespace {
+
+// Device side of a prepared object: stream, events, the tables in one
+// allocation, the fit plan and the per-slot scratch.
+ps_status upload_object(std::unique_ptr<ps_ctx> &c, ps_ctx **out)
+{
     int ndev = 0;
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev <= c->opt.device || c->opt.device < 0)
         return PS_ERR_NO_DEVICE;
@@ -570,6 +605,10 @@ ps_status ps_prepare(const ps_problem *prob, const ps_options *opt, ps_ctx **out
     return PS_OK;
 }
 
+}  // namespace
+
+extern "C" {
+
 ps_status ps_get_info(const ps_ctx *c, ps_info *out)
 {
     if (!c || !out) return PS_ERR_ARG;
@@ -594,31 +633,42 @@ ps_status ps_get_info(const ps_ctx *c, ps_info *out)
     return PS_OK;
 }
 
+ps_status ps_precalc_step(ps_ctx *c, double *conw_r, int32_t *new_conw)
+{
+    if (!c || !conw_r || !new_conw || !(*conw_r > 0)) return PS_ERR_ARG;
+    PSG_CUDA(c, cudaSetDevice(c->opt.device));
+    const int64_t ntest = std::min<int64_t>(10, c->obj.n_max);
+    if (ntest < 1) return PS_ERR_ARG;
+    std::vector<ps_row> rows(static_cast<size_t>(ntest));
+    ps_status st = scan_rows(c, *conw_r, 1, ntest, rows.data(), true);
+    if (st != PS_OK) return st;
+    double sum = 0.0;
+    for (int64_t n = 0; n < ntest; n++) sum = sum + rows[static_cast<size_t>(n)].dark_or_conw;
+    const double ave = sum / ntest;
+    if (ave < 1.0) *new_conw = 1;
+    if (ave >= 1.0) *conw_r = *conw_r * 2;
+    return PS_OK;
+}
+
 ps_status ps_precalc_conw(ps_ctx *c, double *conw_r, int32_t *new_conw)
 {
     if (!c || !conw_r || !new_conw) return PS_ERR_ARG;
     PSG_CUDA(c, cudaSetDevice(c->opt.device));
     const psg::HostObject &o = c->obj;
     double cw = o.conw_r0;
-    int nc = 0;
-    int64_t ntest = std::min<int64_t>(10, o.n_max);
-    std::vector<ps_row> rows(static_cast<size_t>(std::max<int64_t>(ntest, 1)));
+    int32_t nc = 0;
+    const int64_t ntest = std::min<int64_t>(10, o.n_max);
     double launches = 0, kms = 0, tms = 0;
     int64_t fits = 0, evals = 0;
     while (nc != 1 && (cw * o.escl * o.escl) < 10.0) {
         if (ntest < 1) break;
-        ps_status st = scan_rows(c, cw, 1, ntest, rows.data(), true);
+        ps_status st = ps_precalc_step(c, &cw, &nc);
         if (st != PS_OK) return st;
         launches += 1;
         kms += c->timing.kernel_ms;
         tms += c->timing.total_ms;
         fits += c->timing.fits;
         evals += c->timing.evals;
-        double sum = 0.0;
-        for (int64_t n = 0; n < ntest; n++) sum = sum + rows[static_cast<size_t>(n)].dark_or_conw;
-        double ave = sum / ntest;
-        if (ave < 1.0) nc = 1;
-        if (ave >= 1.0) cw = cw * 2;
     }
     c->timing.kernel_ms = kms;
     c->timing.total_ms = tms;

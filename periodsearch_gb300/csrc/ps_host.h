@@ -60,6 +60,8 @@ struct HostObject {
 
 // Input preparation of one problem; returns PS_OK or the reference's error.
 ps_status prepare_object(const ps_problem &p, HostObject &o, std::string &err);
+// The same from the reference's prepared state (no input preparation).
+ps_status prepare_object_state(const ps_state &st, HostObject &o, std::string &err);
 // Sets the convexity rows for a given conw_r (brightness 0, sigma 1/conw_r).
 void set_convexity_rows(HostObject &o, double conw_r);
 

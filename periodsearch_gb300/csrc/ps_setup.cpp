@@ -483,6 +483,107 @@ ps_status prepare_object(const ps_problem &p, HostObject &o, std::string &err)
     return PS_OK;
 }
 
+ps_status prepare_object_state(const ps_state &st, HostObject &o, std::string &err)
+{
+    if (st.n_lc < 1 || !st.lc_points || !st.lc_rel || !st.tim || !st.brightness || !st.sig || !st.weight || !st.ee ||
+        !st.ee0 || !st.ia || !st.cg_first) {
+        err = "ps_state: missing arrays or no lightcurves";
+        return PS_ERR_ARG;
+    }
+    if (st.n_lc > PS_MAX_LC) {
+        err = "number of lightcurves exceeds PS_MAX_LC";
+        return PS_ERR_LIMIT;
+    }
+    if (st.lmax < 0 || st.mmax < 0 || st.mmax > st.lmax || st.lmax > PS_MAX_LM || st.nrows < 1) {
+        err = "bad Laplace-series degree/order or nrows";
+        return PS_ERR_ARG;
+    }
+    if (8 * st.nrows * st.nrows > PS_MAX_N_FAC) {
+        err = "number of facets exceeds PS_MAX_N_FAC";
+        return PS_ERR_LIMIT;
+    }
+    if (!(st.freq_step > 0) || !(st.escl > 0) || !(st.conw_r > 0) || !(st.cl > 0)) {
+        err = "ps_state: frequency step, escl, conw_r and cl must be positive";
+        return PS_ERR_ARG;
+    }
+    ps_header h{};
+    h.lmax = st.lmax;
+    h.mmax = st.mmax;
+    h.nrows = st.nrows;
+    for (int k = 0; k < 3; k++) h.par[k] = st.par[k];
+    h.cl = st.cl;
+    h.alamda_start = st.alamda_start;
+    h.alamda_incr = st.alamda_incr;
+    h.stop_condition = st.stop_condition;
+    h.n_iter_min = st.n_iter_min;
+    o.hdr = h;
+    o.n_lc = st.n_lc;
+    o.lc_points.assign(st.n_lc + 1, 0);
+    o.lc_rel.assign(st.n_lc + 1, 0);
+    o.lc_start.assign(st.n_lc + 1, 0);
+    int nd = 0;
+    o.onlyrel = true;
+    o.max_rel_points = 0;
+    for (int i = 0; i < st.n_lc; i++) {
+        const int np = st.lc_points[i];
+        if (np < 1 || np > PS_POINTS_MAX) {
+            err = "lightcurve point count outside 1..PS_POINTS_MAX";
+            return PS_ERR_LIMIT;
+        }
+        o.lc_points[i] = np;
+        o.lc_rel[i] = st.lc_rel[i] ? 1 : 0;
+        o.lc_start[i] = nd;
+        if (!o.lc_rel[i]) o.onlyrel = false;
+        else o.max_rel_points = std::max(o.max_rel_points, np);
+        nd += np;
+    }
+    if (nd != st.ndata || nd > PS_MAX_N_OBS) {
+        err = "ndata differs from the sum of lc_points or exceeds PS_MAX_N_OBS";
+        return PS_ERR_ARG;
+    }
+    o.ndata = nd;
+    o.lc_points[st.n_lc] = 3;
+    o.lc_rel[st.n_lc] = 0;
+    o.lc_start[st.n_lc] = nd;
+    o.tim.assign(st.tim, st.tim + nd);
+    o.bright.assign(st.brightness, st.brightness + nd);
+    o.sig.assign(st.sig, st.sig + nd);
+    o.weight.assign(st.weight, st.weight + nd);
+    for (int j = 0; j < 3; j++) {
+        o.tim.push_back(0.0);
+        o.bright.push_back(0.0);
+        o.sig.push_back(0.0);
+        o.weight.push_back(1.0);
+    }
+    o.ee.assign(st.ee, st.ee + 3 * static_cast<size_t>(nd));
+    o.ee0.assign(st.ee0, st.ee0 + 3 * static_cast<size_t>(nd));
+    o.phi0 = st.phi0;
+    o.escl = st.escl;
+    o.conw_r0 = st.conw_r;
+    o.freq_start = st.freq_start;
+    o.freq_end = st.freq_end;
+    o.freq_step = st.freq_step;
+    o.n_max = static_cast<int64_t>((o.freq_start - o.freq_end) / o.freq_step) + 1;
+    build_shape(o.shape, st.nrows, st.lmax, st.mmax);
+    o.ncoef = o.shape.ncoef;
+    o.ma = o.ncoef + 5 + kNPhPar;
+    if (o.ncoef + 3 + kNPhPar + 1 > PS_MAX_N_PAR) {
+        err = "number of parameters exceeds PS_MAX_N_PAR";
+        return PS_ERR_LIMIT;
+    }
+    o.cg_first.assign(st.cg_first, st.cg_first + o.ncoef);
+    o.ia.assign(st.ia, st.ia + o.ma);
+    o.hdr.ia_prd = o.ia[o.ncoef + 2];
+    for (int i = 0; i < kNPhPar; i++) o.hdr.ia_par[i] = o.ia[o.ncoef + 3 + i];
+    o.hdr.ia_cl = o.ia[o.ncoef + 3 + kNPhPar];
+    o.free_list.clear();
+    for (int l = 0; l < o.ma; l++)
+        if (o.ia[l]) o.free_list.push_back(l);
+    o.mfit = static_cast<int>(o.free_list.size());
+    set_convexity_rows(o, o.conw_r0);
+    return PS_OK;
+}
+
 void set_convexity_rows(HostObject &o, double conw_r)
 {
     for (int j = 0; j < 3; j++) {
