@@ -609,6 +609,7 @@ __device__ uint32_t tc_setup(const DevObject &ob, Smem<PS_FORM_MIXED> &s)
     tc::fence_after_sync();
     const uint32_t tbase = *s.tslot;
     for (int i = tid; i < F; i += NT) s.fac[i] = make_float4(ob.nx_f[i], ob.ny_f[i], ob.nz_f[i], ob.darea_f[i]);
+    for (int i = tid; i < static_cast<int>(kTcAlphaOperands / 4); i += NT) reinterpret_cast<uint32_t *>(s.aop)[i] = 0;
     if (warp < 4) {
         const int m = warp * 32 + lane, c = m & 63;
         const bool low = m >= 64;
@@ -814,17 +815,21 @@ __device__ void contract_tc_finish(Smem<PS_FORM_MIXED> &s, int np, int F, int C,
     }
     t.phase ^= 1u;
     tc::fence_after_sync();
+    // every warp reads 16 of the 64 accumulator columns of its lane quadrant
+    // (warp w may access Tensor Memory lanes 32 (w % 4) .. + 31)
     float *X = reinterpret_cast<float *>(s.bhi);
-    if (warp < 4) {
-        const uint32_t taddr = tbase + (static_cast<uint32_t>(warp * 32) << 16) + tc_dcol(F);
-        float *xr = X + (warp * 32 + lane) * 65;
-#pragma unroll 1
-        for (int q = 0; q < 8; q++) {
-            uint32_t v[8];
-            tc::tmem_ld8(taddr + 8 * q, v);
-            tc::tmem_wait_ld();
+    {
+        const int quad = warp & 3, cgrp = warp >> 2;
+        const uint32_t taddr = tbase + (static_cast<uint32_t>(quad * 32) << 16) + tc_dcol(F) + 16 * cgrp;
+        float *xr = X + (quad * 32 + lane) * 65 + 16 * cgrp;
+        uint32_t v0[8], v1[8];
+        tc::tmem_ld8(taddr, v0);
+        tc::tmem_ld8(taddr + 8, v1);
+        tc::tmem_wait_ld();
 #pragma unroll
-            for (int j = 0; j < 8; j++) xr[8 * q + j] = __uint_as_float(v[j]);
+        for (int j = 0; j < 8; j++) {
+            xr[j] = __uint_as_float(v0[j]);
+            xr[8 + j] = __uint_as_float(v1[j]);
         }
     }
     __syncthreads();
@@ -873,9 +878,11 @@ __device__ void accumulate_tile_tc(const DevObject &ob, Smem<PS_FORM_MIXED> &s, 
     // bytes apart, 8-row groups 1024 bytes apart; high parts in rows 0..63,
     // low parts in rows 64..127
     unsigned char *Ab = s.aop, *Bb = s.aop + 16384;
+    const int rg_end = (mf + 1 + 7) >> 3;   // row groups past it stay zero (cleared at set-up)
     for (int cm = warp; cm < 128; cm += NT / 32) {
         const bool isB = cm >= 64;
         const int c = cm & 63, rg = c >> 3, kc = c & 7;
+        if (rg >= rg_end) continue;
         const int row = rg * 8 + (lane >> 2), p = kc * 4 + (lane & 3);
         float v = 0.f;
         if (p < np) {
@@ -922,11 +929,14 @@ __device__ void tc_alpha_flush(const DevObject &ob, Smem<PS_FORM_MIXED> &s, doub
     tc_alpha_wait(s, t);
     if (*s.abort) return;
     float *S = reinterpret_cast<float *>(s.bhi);   // [128][65], after the tile's contraction
-    if (warp < 4) {
-        const uint32_t taddr = t.tbase + (static_cast<uint32_t>(warp * 32) << 16) + tc_acol(ob.nfac);
-        float *sr = S + (warp * 32 + lane) * 65;
-#pragma unroll 1
-        for (int q = 0; q < 8; q++) {
+    {
+        // every warp: 16 of the 64 column pairs of its lane quadrant
+        const int quad = warp & 3, cgrp = warp >> 2;
+        const uint32_t taddr =
+            t.tbase + (static_cast<uint32_t>(quad * 32) << 16) + tc_acol(ob.nfac) + 16 * cgrp;
+        float *sr = S + (quad * 32 + lane) * 65 + 16 * cgrp;
+#pragma unroll
+        for (int q = 0; q < 2; q++) {
             uint32_t vh[8], vl[8];
             tc::tmem_ld8(taddr + 8 * q, vh);
             tc::tmem_ld8(taddr + 64 + 8 * q, vl);
