@@ -168,3 +168,51 @@ def test_cross_build_agreement_report(mixed, engine_lib):
     for name, pair in rpt["pairs"].items():
         assert pair["validator_match"] and pair["same_best_index"], (name, pair)
     assert rpt["pairs"]["reference|fp64"]["rms_rel_median"] <= 1e-6
+
+
+@pytest.fixture(scope="module")
+def c2_object(tmp_path_factory):
+    """A c2-shaped object: Laplace series L = M = 8 (81 coefficients) on the
+    512-facet grid, 200 sparse points -- beyond the tensor-core path, so the
+    mixed form runs its two-coefficients-per-lane SIMT contraction."""
+    from periodsearch_gb300 import read_input, synth
+
+    cfg = synth.SynthConfig(name="c2s", lmax_truth=8, lmax=8, nrows=8, n_periods=40)
+    path = tmp_path_factory.mktemp("c2") / "period_search_in"
+    synth.write_object(path, cfg, seed=41)
+    return path
+
+
+def test_c2_eval_both_forms_match_oracle(engine_lib, oracle, c2_object):
+    from periodsearch_gb300 import Engine, PS_FORM_FP64, PS_FORM_MIXED, read_input
+
+    ora = oracle.OracleProblem(c2_object)
+    conw_r = ora.info()["conw_r"]
+    data = read_input(c2_object)
+    for form in (PS_FORM_FP64, PS_FORM_MIXED):
+        with Engine(data, form=form) as eng:
+            assert eng.info.ncoef == 81 and eng.info.nfac == 512 and not eng.info.tensor_cores
+            for n, pole in [(1, 2), (5, 8)]:
+                cg = ora.initial_cg(n, pole)
+                a_g, b_g, x_g, _ = eng.eval(conw_r, cg)
+                a_o, b_o, x_o, _ = ora.eval(cg)
+                tol = (1e-10, 1e-10, 1e-10) if form == PS_FORM_FP64 else (1e-5, 1e-4, 1e-3)
+                assert abs(x_g - x_o) <= tol[0] * abs(x_o)
+                assert np.abs(a_g - a_o).max() <= tol[1] * np.abs(a_o).max()
+                assert np.abs(b_g - b_o).max() <= tol[2] * np.abs(b_o).max()
+
+
+def test_c2_mixed_scan_matches_fp64(engine_lib, c2_object):
+    from periodsearch_gb300 import Engine, PS_FORM_FP64, PS_FORM_MIXED, read_input
+
+    data = read_input(c2_object)
+    with Engine(data, form=PS_FORM_FP64) as e64:
+        conw_r, _ = e64.precalc_conw()
+        ref = e64.scan(conw_r, 1, 12)
+    with Engine(data, form=PS_FORM_MIXED) as eng:
+        got = eng.scan(conw_r, 1, 12)
+        refined, _ = eng.scan_refined(conw_r, 1, 12)
+    signed = (got["rms"] - ref["rms"]) / ref["rms"]
+    assert signed.max() <= MAX_REL and signed.min() >= -MAX_REL_BELOW
+    assert np.median(np.abs(signed)) <= MEDIAN_REL
+    assert int(np.argmin(refined["rms"])) == int(np.argmin(ref["rms"]))
