@@ -1053,6 +1053,7 @@ __device__ void evaluate(const DevObject &ob, const FitConfig &cfg, const SlotLa
         if (ob.n_lc > 1 && warp > 0 && pipe_sp < min(P, ob.lc_npts[0]))
             setup_point<FORM>(ob, cfg, ob.lc_start[0] + pipe_sp, omg, B, DB0, DB1, php0, php1, php2,
                               s.pt + pipe_sp * kPointStride);
+        __syncthreads();   // the first tile's facet stage reads it
     }
 
     for (int lc = 0; lc < ob.n_lc; lc++) {
@@ -1076,7 +1077,9 @@ __device__ void evaluate(const DevObject &ob, const FitConfig &cfg, const SlotLa
                         setup_point<FORM>(ob, cfg, start + t0 + sp, omg, B, DB0, DB1, php0, php1, php2,
                                           s.pt + sp * kPointStride);
                 }
-                __syncthreads();
+                // (with the tensor cores the set-up is a tile old: the
+                // barrier after the previous tile's contraction ordered it)
+                if constexpr (!kPipe) __syncthreads();
                 // 2. facet stage (bright.c:59-120), one warp per point
                 if constexpr (kPipe) facet_stage_tc<NT>(ob, s, np, cl, cls);
                 else
@@ -1149,7 +1152,8 @@ __device__ void evaluate(const DevObject &ob, const FitConfig &cfg, const SlotLa
                     if (lane == 0) s.red[p * kRedStride] = res;
                 }
             }
-            __syncthreads();
+            // (the tensor-core issue below begins with a barrier of its own)
+            if constexpr (!kPipe) __syncthreads();
             // 3. shape contraction and the remaining columns of J
             if constexpr (kFP64) {
                 for (int o = tid; o < np * C; o += NT) {
