@@ -1261,6 +1261,9 @@ __device__ void evaluate(const DevObject &ob, const FitConfig &cfg, const SlotLa
         if (!rel) continue;
         // ---- pass 2: renormalise and accumulate (mrqcof.c:90-136) ----
         const double ave = s.misc[M_AVE];
+        // the mixed form multiplies by one reciprocal of the lightcurve sum;
+        // the FP64 form divides as the reference does
+        const double inv_ave = kFP64 ? 0.0 : 1.0 / ave;
         for (int t0 = 0; t0 < npts; t0 += P) {
             const int np = min(P, npts - t0);
             const R *src = scratch + static_cast<size_t>(t0) * (ma + 1);
@@ -1268,11 +1271,18 @@ __device__ void evaluate(const DevObject &ob, const FitConfig &cfg, const SlotLa
             // values; the mixed form parks them as FP32)
             if (tid < np) {
                 const int q = start + t0 + tid;
-                const double coef = ob.sig[q] * npts / ave;
                 const double yt = static_cast<double>(src[static_cast<size_t>(tid) * (ma + 1) + ma]);
+                double coef, ytr;
+                if constexpr (kFP64) {
+                    coef = ob.sig[q] * npts / ave;
+                    ytr = yt / ave;
+                } else {
+                    coef = ob.sig[q] * npts * inv_ave;
+                    ytr = yt * inv_ave;
+                }
                 s.ym[tid] = coef * yt;
                 s.red[tid * kRedStride + 6] = coef;
-                s.red[tid * kRedStride + 7] = yt / ave;
+                s.red[tid * kRedStride + 7] = ytr;
             }
             __syncthreads();
             for (int e = tid; e < np * ma; e += NT) {

@@ -110,7 +110,7 @@ def grad(P: np.ndarray, x: np.ndarray, y: np.ndarray, device: int = 0):
 
 
 def load_default():
-    """Committed weights and calibrated margin, or (None, None)."""
+    """Committed weights and their training record, or (None, None)."""
     if not WEIGHTS.exists():
         return None, None
     meta = json.loads(META.read_text()) if META.exists() else {}
