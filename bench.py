@@ -13,10 +13,13 @@ value      fits/s of the chosen form (--form, default mixed: FP32 facet stage,
            shape contraction and alpha/beta on the tensor cores, FP64 phase,
            chi^2, solve) with the object resident in HBM, from CUDA events
            around the fit kernel on its own stream (sum over steps); the plain
-           FP64 form is timed on the same chunks (plain_fp64), and both forms
-           fit a window around the true period (validation: same best period,
-           chi^2 difference; the refined scan -- mixed scan plus FP64 refit of
-           the minimum region -- against the full FP64 scan);
+           FP64 form is timed on the same chunks (plain_fp64); on a window of
+           --validation-window periods around the true period every scan
+           type -- full FP64, full mixed, refined (mixed scan plus FP64 refit
+           of the minimum region) and the learned early-stop cascade -- is
+           timed and its best period compared with the full FP64 scan's
+           (validation.scans, fits/s = the window's fits over the scan's
+           kernel time);
 e2e        the same through the C ABI with host buffers: ps_prepare (host ->
            device copy of the tables), ps_scan (rows back to the host) and
            ps_destroy per step, wall clock;
@@ -64,6 +67,8 @@ def _args():
     ap.add_argument("--no-fp64-compare", action="store_true", help="skip timing the plain FP64 form")
     ap.add_argument("--simt-compare", action="store_true",
                     help="also time the mixed form with its contractions on the SIMT pipes")
+    ap.add_argument("--validation-window", type=int, default=300,
+                    help="periods of the window around the true period on which every scan type is compared")
     ap.add_argument("--multi-object", type=int, default=0,
                     help="also time K small objects (Ndata logU[100, 2000]) packed into one launch against one "
                          "launch per object")
@@ -387,16 +392,49 @@ def run_engine_arm(args):
         valid = None
         if plain is not None and rank == 0:
             n_truth = int(round((info.freq_start - 1 / obj.truth["period_h"]) / info.freq_step)) + 1
-            lo, hi = max(1, n_truth - 16), min(n_max, n_truth + 15)
-            w_main = main["engine"].scan(main["conw_r"], lo, hi)
-            w_plain = plain["engine"].scan(plain["conw_r"], lo, hi)
+            half = max(args.validation_window // 2, 1)
+            lo, hi = max(1, n_truth - half), min(n_max, n_truth + half - 1)
+            wfits = (hi - lo + 1) * 10
+
+            def _timed(fn):
+                torch.cuda.synchronize()
+                out = fn()
+                torch.cuda.synchronize()
+                return out
+
+            w_main = _timed(lambda: main["engine"].scan(main["conw_r"], lo, hi))
+            t_main = main["engine"].timing()["kernel_ms"]
+            w_plain = _timed(lambda: plain["engine"].scan(plain["conw_r"], lo, hi))
+            t_plain = plain["engine"].timing()["kernel_ms"]
             rel_w = np.abs(w_main["rms"] - w_plain["rms"]) / w_plain["rms"]
             rel_c = np.concatenate([np.abs(a["rms"] - b["rms"]) / b["rms"] for a, b in zip(main["rows"], plain["rows"])])
             bm, bp = int(np.argmin(w_main["rms"])), int(np.argmin(w_plain["rms"]))
             w_ref, st_ref = main["engine"].scan_refined(main["conw_r"], lo, hi)
+            t_ref = st_ref["complete_ms"] + st_ref["refit_ms"]
+            scans = {"fp64": {"fits_per_s": wfits / (t_plain / 1e3)},
+                     "mixed": {"fits_per_s": wfits / (t_main / 1e3)},
+                     "refined": {"fits_per_s": wfits / (t_ref / 1e3), "fp64_refits": int(st_ref["fits_refit"]),
+                                 "best_index": int(st_ref["best_index"])}}
+            try:
+                from periodsearch_gb300 import learned
+
+                _, st_l = main["engine"].scan_learned(main["conw_r"], lo, hi, **learned.CASCADE)
+                scans["learned"] = {"fits_per_s": wfits / ((st_l["screen_ms"] + st_l["complete_ms"] + st_l["refit_ms"])
+                                                           / 1e3),
+                                    "fits_screened_out": int(st_l["fits_screened_out"]),
+                                    "best_index": int(st_l["best_index"])}
+            except Exception as exc:   # no committed predictor
+                scans["learned"] = {"unavailable": str(exc)[:120]}
+            bp_all = lo + int(np.argmin(w_plain["rms"]))
+            scans["fp64"]["best_index"] = bp_all
+            scans["mixed"]["best_index"] = lo + int(np.argmin(w_main["rms"]))
+            for v in scans.values():
+                if "best_index" in v:
+                    v["same_best_period_as_fp64"] = v["best_index"] == bp_all
             valid = {"window": [lo, hi], "truth_period_h": obj.truth["period_h"],
+                     "scans": scans,
                      "refined_best_index": int(st_ref["best_index"]),
-                     "refined_same_best_period": int(st_ref["best_index"]) == lo + int(np.argmin(w_plain["rms"])),
+                     "refined_same_best_period": int(st_ref["best_index"]) == bp_all,
                      "refined_fp64_refits": int(st_ref["fits_refit"]),
                      "best_index_chosen": lo + bm, "best_index_fp64": lo + bp, "same_best_period": bm == bp,
                      "best_period_h_chosen": float(w_main["period_h"][bm]),
