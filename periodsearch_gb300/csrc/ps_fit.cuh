@@ -160,11 +160,6 @@ __device__ inline int tri_row(int e)
     return j;
 }
 
-// Thread that sets up point p of a tile: points are spread over the warps
-// (p % 8 -> warp, p / 8 -> lane) so that all four SM sub-partitions work.
-template <int NT>
-__device__ inline int setup_thread(int p) { return (p % (NT / 32)) * 32 + p / (NT / 32); }
-
 template <class T>
 __device__ inline T warp_sum(T v)
 {
@@ -1047,10 +1042,15 @@ __device__ void evaluate(const DevObject &ob, const FitConfig &cfg, const SlotLa
     int tiles_since_flush = 0;
     const float *dsphF = nullptr;
     if constexpr (!kFP64) dsphF = s.dsph ? s.dsph : ob.dsph_f;
-    // thread of point sp of a set-up that runs beside the MMA issue (warps 1..15)
-    const int pipe_sp = lane * (NT / 32 - 1) + (warp - 1);
+    // Point set-up threads.  An FP64 instruction holds its sub-partition's
+    // FP64 unit for the whole warp however few lanes are active, so the
+    // set-up keeps its points on as few warps as possible: the mixed form
+    // (FP64 only for the rotation phase) on one warp, lane = point -- warp 1
+    // when it runs beside thread 0's MMA issue; the FP64 form on warps 0..3,
+    // one per sub-partition.
+    const int pipe_sp = warp == 1 ? lane : -1;
     if constexpr (kPipe) {
-        if (ob.n_lc > 1 && warp > 0 && pipe_sp < min(P, ob.lc_npts[0]))
+        if (ob.n_lc > 1 && pipe_sp >= 0 && pipe_sp < min(P, ob.lc_npts[0]))
             setup_point<FORM>(ob, cfg, ob.lc_start[0] + pipe_sp, omg, B, DB0, DB1, php0, php1, php2,
                               s.pt + pipe_sp * kPointStride);
         __syncthreads();   // the first tile's facet stage reads it
@@ -1069,11 +1069,12 @@ __device__ void evaluate(const DevObject &ob, const FitConfig &cfg, const SlotLa
             const int np = min(P, npts - t0);
             if (!conv) {
                 // 1. point set-up (bright.c:27-57, phasec.c, matrix.c), one
-                // thread per point spread over the warps; with the tensor
-                // cores it was done during the previous tile's MMAs
+                // thread per point on as few warps as possible; with the
+                // tensor cores it was done during the previous tile's MMAs
                 if constexpr (!kPipe) {
-                    const int sp = (tid % 32) * (NT / 32) + tid / 32;
-                    if (sp < np)
+                    const int ppw = (P + 3) / 4;   // FP64 form: points per warp
+                    const int sp = kFP64 ? (lane < ppw && warp < 4 ? warp * ppw + lane : -1) : (warp == 0 ? lane : -1);
+                    if (sp >= 0 && sp < np)
                         setup_point<FORM>(ob, cfg, start + t0 + sp, omg, B, DB0, DB1, php0, php1, php2,
                                           s.pt + sp * kPointStride);
                 }
@@ -1203,7 +1204,7 @@ __device__ void evaluate(const DevObject &ob, const FitConfig &cfg, const SlotLa
                 // point set-up of the next tile into the other buffer
                 const int nlc = t0 + P < npts ? lc : lc + 1, nt0 = t0 + P < npts ? t0 + P : 0;
                 next_setup = nlc < ob.n_lc - 1;   // the last lightcurve is the convexity rows
-                if (next_setup && warp > 0 && pipe_sp < min(P, ob.lc_npts[nlc] - nt0))
+                if (next_setup && pipe_sp >= 0 && pipe_sp < min(P, ob.lc_npts[nlc] - nt0))
                     setup_point<FORM>(ob, cfg, ob.lc_start[nlc] + nt0 + pipe_sp, omg, B, DB0, DB1, php0, php1, php2,
                                       s.pt2 + pipe_sp * kPointStride);
                 contract_tc_finish<NT>(s, np, F, C, ma, conv, tcs);
@@ -1233,10 +1234,16 @@ __device__ void evaluate(const DevObject &ob, const FitConfig &cfg, const SlotLa
                         s.dave[l] += static_cast<double>(d);
                     }
                 }
-                if (tid == 0) {
-                    double av = s.misc[M_AVE];
-                    for (int p = 0; p < np; p++) av = av + s.ym[p];
-                    s.misc[M_AVE] = av;
+                if constexpr (kFP64) {
+                    // the reference's order
+                    if (tid == 0) {
+                        double av = s.misc[M_AVE];
+                        for (int p = 0; p < np; p++) av = av + s.ym[p];
+                        s.misc[M_AVE] = av;
+                    }
+                } else if (warp == 0) {
+                    const double v = warp_sum(lane < np ? s.ym[lane] : 0.0);
+                    if (lane == 0) s.misc[M_AVE] += v;
                 }
                 __syncthreads();
                 continue;
