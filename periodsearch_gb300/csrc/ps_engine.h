@@ -86,6 +86,7 @@ struct SlotLayout {
     size_t fac, ag, fpart;  // tensor-core path: packed facet constants, per-evaluation (area, Darea g), facet-sum partials
     size_t aop;             // tensor-core path: alpha/beta MMA operands
     size_t accs;            // per-point weights and residuals of the accumulation (mixed form)
+    size_t davef;           // FP32 copy of a relative lightcurve's derivative sums (mixed form)
     size_t bytes;
 };
 
@@ -175,6 +176,7 @@ PSG_HD inline SlotLayout make_layout(int form, int ma, int mfit, int nfac, int n
     }
     // 32 residuals then 32 weights, whatever the tile size
     L.accs = form == PS_FORM_MIXED ? take(64 * sizeof(float)) : 0;
+    L.davef = form == PS_FORM_MIXED ? take(static_cast<size_t>(ma) * sizeof(float)) : 0;
     L.bytes = o;
     return L;
 }

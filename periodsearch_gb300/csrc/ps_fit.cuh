@@ -73,6 +73,7 @@ struct Smem {
     R *areaR, *gvR, *W, *J, *pt;
     R *pt2;       // the other point set-up buffer (== pt unless set-up runs one tile ahead)
     float *accs;  // mixed form: per-point FP32 weights and residuals of a tile
+    float *davef; // mixed form: FP32 copy of a relative lightcurve's derivative sums
     int *ipiv;
     float *dsph;  // FP32 basis in shared memory (mixed form), or nullptr
     // tensor-core contraction: operand tiles, MMA-completion barrier, Tensor
@@ -107,6 +108,7 @@ __device__ inline Smem<FORM> carve(char *base, const SlotLayout &L)
     s.pt = reinterpret_cast<R *>(base + L.pt);
     s.pt2 = reinterpret_cast<R *>(base + L.pt2);
     s.accs = reinterpret_cast<float *>(base + L.accs);
+    s.davef = reinterpret_cast<float *>(base + L.davef);
     s.ym = reinterpret_cast<double *>(base + L.ym);
     s.red = reinterpret_cast<double *>(base + L.red);
     s.dave = reinterpret_cast<double *>(base + L.dave);
@@ -1271,6 +1273,10 @@ __device__ void evaluate(const DevObject &ob, const FitConfig &cfg, const SlotLa
         // the mixed form multiplies by one reciprocal of the lightcurve sum;
         // the FP64 form divides as the reference does
         const double inv_ave = kFP64 ? 0.0 : 1.0 / ave;
+        // the mixed form's renormalisation runs in FP32 on FP32 copies (a
+        // conversion from FP64 would occupy the FP64 unit per element)
+        if constexpr (!kFP64)
+            for (int l = tid; l < ma; l += NT) s.davef[l] = static_cast<float>(s.dave[l]);
         for (int t0 = 0; t0 < npts; t0 += P) {
             const int np = min(P, npts - t0);
             const R *src = scratch + static_cast<size_t>(t0) * (ma + 1);
@@ -1288,8 +1294,10 @@ __device__ void evaluate(const DevObject &ob, const FitConfig &cfg, const SlotLa
                     ytr = yt * inv_ave;
                 }
                 s.ym[tid] = coef * yt;
-                s.red[tid * kRedStride + 6] = coef;
-                s.red[tid * kRedStride + 7] = ytr;
+                if constexpr (!kFP64) {
+                    s.accs[tid] = static_cast<float>(coef);        // consumed before the
+                    s.accs[32 + tid] = static_cast<float>(ytr);    // accumulation reuses it
+                }
             }
             __syncthreads();
             for (int e = tid; e < np * ma; e += NT) {
@@ -1302,8 +1310,7 @@ __device__ void evaluate(const DevObject &ob, const FitConfig &cfg, const SlotLa
                     const double yt = src[static_cast<size_t>(p) * (ma + 1) + ma];
                     out = coef * (v - yt * s.dave[l] / ave);
                 } else {
-                    out = float(s.red[p * kRedStride + 6]) *
-                          (v - float(s.red[p * kRedStride + 7]) * float(s.dave[l]));
+                    out = s.accs[p] * (v - s.accs[32 + p] * s.davef[l]);
                 }
                 s.J[e] = (l == 0) ? R(0) : out;
             }
