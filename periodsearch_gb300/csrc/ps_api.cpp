@@ -93,6 +93,7 @@ psg::FitConfig make_config(const ps_ctx *c, double conw_r)
     f.alamda_start = h.alamda_start;
     f.alamda_incr = h.alamda_incr;
     f.conw_r = conw_r;
+    f.conv_sig = 1 / conw_r;
     f.freq_start = o.freq_start;
     f.freq_step = o.freq_step;
     f.log_cl = std::log(h.cl);

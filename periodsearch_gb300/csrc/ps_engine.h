@@ -34,6 +34,7 @@ struct DevObject {
 // Constants of one scan (period_search_BOINC.cpp:817-868).
 struct FitConfig {
     double phi0, alamda_start, alamda_incr, iter_diff_max, conw_r;
+    double conv_sig;              // 1 / conw_r, the sigma of the convexity rows
     double freq_start, freq_step, log_cl, par0, par1, par2;
     int n_iter_max, n_iter_min;
 };
@@ -87,6 +88,7 @@ struct SlotLayout {
     size_t aop;             // tensor-core path: alpha/beta MMA operands
     size_t accs;            // per-point weights and residuals of the accumulation (mixed form)
     size_t davef;           // FP32 copy of a relative lightcurve's derivative sums (mixed form)
+    size_t bmat;            // rotation matrices and phase/scattering parameters of an evaluation
     size_t bytes;
 };
 
@@ -177,6 +179,7 @@ PSG_HD inline SlotLayout make_layout(int form, int ma, int mfit, int nfac, int n
     // 32 residuals then 32 weights, whatever the tile size
     L.accs = form == PS_FORM_MIXED ? take(64 * sizeof(float)) : 0;
     L.davef = form == PS_FORM_MIXED ? take(static_cast<size_t>(ma) * sizeof(float)) : 0;
+    L.bmat = take(32 * rs);
     L.bytes = o;
     return L;
 }

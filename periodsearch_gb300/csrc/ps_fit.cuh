@@ -60,6 +60,11 @@ constexpr double kTwoPiLo = 2.4492935982947064e-16;
 constexpr double kInvTwoPi = 0.15915494309189535;
 
 __constant__ double c_beta_pole[PS_N_POLES] = {0, 0, 0, 0, 60, 60, 60, -60, -60, -60};
+// blmatrix.c:9-46 entry by entry: factor a (0 zero, 1 cos beta, 2 sin beta,
+// 3 one) | factor b << 2 (0 one, 1 cos lambda, 2 sin lambda) | 16 negated;
+// rows of B, then dB/dbeta, then dB/dlambda
+__constant__ unsigned char c_bl_code[27] = {5,  9,  18, 27, 7, 0, 6,  10, 1,  22, 26, 17, 0, 0,
+                                            0,  5,  9,  18, 25, 5, 0, 23, 27, 0,  26, 6,  0};
 __constant__ double c_lambda_pole[PS_N_POLES] = {0, 90, 180, 270, 60, 180, 300, 60, 180, 300};
 
 // Arithmetic type of the facet stage, the contraction and the model rows.
@@ -74,6 +79,8 @@ struct Smem {
     R *pt2;       // the other point set-up buffer (== pt unless set-up runs one tile ahead)
     float *accs;  // mixed form: per-point FP32 weights and residuals of a tile
     float *davef; // mixed form: FP32 copy of a relative lightcurve's derivative sums
+    R *bmat;      // [27] rotation matrix and its beta/lambda derivatives, [27..29] phase
+                  // function a, d, k, [30] Lommel-Seeliger and [31] Lambert weight
     int *ipiv;
     float *dsph;  // FP32 basis in shared memory (mixed form), or nullptr
     // tensor-core contraction: operand tiles, MMA-completion barrier, Tensor
@@ -109,6 +116,7 @@ __device__ inline Smem<FORM> carve(char *base, const SlotLayout &L)
     s.pt2 = reinterpret_cast<R *>(base + L.pt2);
     s.accs = reinterpret_cast<float *>(base + L.accs);
     s.davef = reinterpret_cast<float *>(base + L.davef);
+    s.bmat = reinterpret_cast<R *>(base + L.bmat);
     s.ym = reinterpret_cast<double *>(base + L.ym);
     s.red = reinterpret_cast<double *>(base + L.red);
     s.dave = reinterpret_cast<double *>(base + L.dave);
@@ -146,6 +154,7 @@ enum : int {
     M_AVE = 1,     // relative-lightcurve model sum
     M_AREA = 2,    // sum of facet areas of the current evaluation
     M_CHK = 3,     // 3 convexity residuals (sum Area*n) of the current evaluation
+    M_INVAVE = 6,  // mixed form: 1 / sum of the current relative lightcurve's model
     M_CL = 7,      // exp(log cl)
     M_TRIG = 8,    // cos/sin of the pole angles beta, lambda (4 doubles)
     M_PIV = 12,    // pivot broadcast of the solvers (2 doubles + status)
@@ -443,11 +452,10 @@ __device__ void contract_mixed(Smem<PS_FORM_MIXED> &s, const float *dsph, int np
 // the phase function and its derivatives, into pt[0..27].
 template <int FORM>
 __device__ inline void setup_point(const DevObject &ob, const FitConfig &cfg, int q, double omg,
-                                   const typename RealOf<FORM>::T (&B)[9], const typename RealOf<FORM>::T (&DB0)[9],
-                                   const typename RealOf<FORM>::T (&DB1)[9], typename RealOf<FORM>::T php0,
-                                   typename RealOf<FORM>::T php1, typename RealOf<FORM>::T php2,
-                                   typename RealOf<FORM>::T *pt)
+                                   const typename RealOf<FORM>::T *bm, typename RealOf<FORM>::T *pt)
 {
+    const typename RealOf<FORM>::T *B = bm, *DB0 = bm + 9, *DB1 = bm + 18;
+    const typename RealOf<FORM>::T php0 = bm[27], php1 = bm[28], php2 = bm[29];
     using R = typename RealOf<FORM>::T;
     constexpr bool kFP64 = FORM == PS_FORM_FP64;
     R ee[3], e0v[3], alpha;
@@ -1023,20 +1031,30 @@ __device__ void evaluate(const DevObject &ob, const FitConfig &cfg, const SlotLa
     for (int e = tid; e < mf * mf; e += NT) M[e] = 0;
     for (int j = tid; j < mf; j += NT) bv[j] = 0;
 
-    // blmatrix.c:9-46 in FP64 (angles' cos/sin from thread 0), then in the
-    // facet-stage type.
+    // blmatrix.c:9-46 in FP64 from the angles' cos/sin of thread 0, one
+    // entry per lane of warp 0 (every FP64 instruction holds the FP64 unit
+    // for the whole warp, so each scalar is computed once), stored in the
+    // facet-stage type with the phase and scattering parameters.
     __syncthreads();
-    const double cb = s.misc[M_TRIG], sb = s.misc[M_TRIG + 1], clm = s.misc[M_TRIG + 2], slm = s.misc[M_TRIG + 3];
-    const R B[9] = {R(cb * clm), R(cb * slm), R(-sb), R(-slm), R(clm), R(0), R(sb * clm), R(sb * slm), R(cb)};
-    const R DB0[9] = {R(-sb * clm), R(-sb * slm), R(-cb), R(0), R(0), R(0), R(cb * clm), R(cb * slm), R(-sb)};
-    const R DB1[9] = {R(-cb * slm), R(cb * clm), R(0), R(-clm), R(-slm), R(0), R(-sb * slm), R(sb * clm), R(0)};
+    if (warp == 0) {
+        R v;
+        if (lane < 27) {
+            const int code = c_bl_code[lane];
+            const int fa = code & 3, fb = (code >> 2) & 3;
+            const double va = fa == 1 ? s.misc[M_TRIG] : fa == 2 ? s.misc[M_TRIG + 1] : fa == 3 ? 1.0 : 0.0;
+            const double vb = fb == 1 ? s.misc[M_TRIG + 2] : fb == 2 ? s.misc[M_TRIG + 3] : 1.0;
+            const double p = va * vb;
+            v = R((code & 16) ? -p : p);
+        } else {
+            v = R(lane == 31 ? s.misc[M_CL] : a[lane == 30 ? C + 7 : C + 3 + (lane - 27)]);
+        }
+        s.bmat[lane] = v;
+    }
     const double omg = a[C + 2];
-    const R php0 = R(a[C + 3]), php1 = R(a[C + 4]), php2 = R(a[C + 5]);
-    const R cls = R(a[C + 7]);
     __syncthreads();
-    const R cl = R(s.misc[M_CL]);
+    const R cls = s.bmat[30], cl = s.bmat[31];
 
-    const double conv_sig = 1 / cfg.conw_r;
+    const double conv_sig = cfg.conv_sig;
     float accA[kAccPerThread];
     float accB = 0.f;
 #pragma unroll
@@ -1053,7 +1071,7 @@ __device__ void evaluate(const DevObject &ob, const FitConfig &cfg, const SlotLa
     const int pipe_sp = warp == 1 ? lane : -1;
     if constexpr (kPipe) {
         if (ob.n_lc > 1 && pipe_sp >= 0 && pipe_sp < min(P, ob.lc_npts[0]))
-            setup_point<FORM>(ob, cfg, ob.lc_start[0] + pipe_sp, omg, B, DB0, DB1, php0, php1, php2,
+            setup_point<FORM>(ob, cfg, ob.lc_start[0] + pipe_sp, omg, s.bmat,
                               s.pt + pipe_sp * kPointStride);
         __syncthreads();   // the first tile's facet stage reads it
     }
@@ -1077,7 +1095,7 @@ __device__ void evaluate(const DevObject &ob, const FitConfig &cfg, const SlotLa
                     const int ppw = (P + 3) / 4;   // FP64 form: points per warp
                     const int sp = kFP64 ? (lane < ppw && warp < 4 ? warp * ppw + lane : -1) : (warp == 0 ? lane : -1);
                     if (sp >= 0 && sp < np)
-                        setup_point<FORM>(ob, cfg, start + t0 + sp, omg, B, DB0, DB1, php0, php1, php2,
+                        setup_point<FORM>(ob, cfg, start + t0 + sp, omg, s.bmat,
                                           s.pt + sp * kPointStride);
                 }
                 // (with the tensor cores the set-up is a tile old: the
@@ -1207,7 +1225,7 @@ __device__ void evaluate(const DevObject &ob, const FitConfig &cfg, const SlotLa
                 const int nlc = t0 + P < npts ? lc : lc + 1, nt0 = t0 + P < npts ? t0 + P : 0;
                 next_setup = nlc < ob.n_lc - 1;   // the last lightcurve is the convexity rows
                 if (next_setup && pipe_sp >= 0 && pipe_sp < min(P, ob.lc_npts[nlc] - nt0))
-                    setup_point<FORM>(ob, cfg, ob.lc_start[nlc] + nt0 + pipe_sp, omg, B, DB0, DB1, php0, php1, php2,
+                    setup_point<FORM>(ob, cfg, ob.lc_start[nlc] + nt0 + pipe_sp, omg, s.bmat,
                                       s.pt2 + pipe_sp * kPointStride);
                 contract_tc_finish<NT>(s, np, F, C, ma, conv, tcs);
             }
@@ -1272,11 +1290,14 @@ __device__ void evaluate(const DevObject &ob, const FitConfig &cfg, const SlotLa
         const double ave = s.misc[M_AVE];
         // the mixed form multiplies by one reciprocal of the lightcurve sum;
         // the FP64 form divides as the reference does
-        const double inv_ave = kFP64 ? 0.0 : 1.0 / ave;
-        // the mixed form's renormalisation runs in FP32 on FP32 copies (a
-        // conversion from FP64 would occupy the FP64 unit per element)
-        if constexpr (!kFP64)
+        // the mixed form's renormalisation runs in FP32 on FP32 copies, with
+        // one reciprocal of the lightcurve sum (computed once, not per warp)
+        if constexpr (!kFP64) {
             for (int l = tid; l < ma; l += NT) s.davef[l] = static_cast<float>(s.dave[l]);
+            if (tid == 0) s.misc[M_INVAVE] = 1.0 / ave;
+            __syncthreads();
+        }
+        const double inv_ave = kFP64 ? 0.0 : s.misc[M_INVAVE];
         for (int t0 = 0; t0 < npts; t0 += P) {
             const int np = min(P, npts - t0);
             const R *src = scratch + static_cast<size_t>(t0) * (ma + 1);
