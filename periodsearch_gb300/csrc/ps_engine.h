@@ -108,7 +108,7 @@ PSG_HD constexpr int threads_of()
 }
 constexpr int kPointStride = 32;   // reals of per-point set-up
 constexpr int kRedStride = 8;      // doubles of per-point facet sums
-constexpr int kMisc = 32;
+constexpr int kMisc = 40;
 constexpr size_t kTcAlphaOperands = 32768;   // tensor-core alpha/beta operands: two 128 x 32 TF32 tiles
 
 

@@ -158,7 +158,8 @@ enum : int {
     M_CL = 7,      // exp(log cl)
     M_TRIG = 8,    // cos/sin of the pole angles beta, lambda (4 doubles)
     M_PIV = 12,    // pivot broadcast of the solvers (2 doubles + status)
-    M_RED = 16     // 16 doubles of block-reduction scratch
+    M_RED = 16,    // 16 doubles of block-reduction scratch
+    M_LM = 32      // 4 doubles: lambda, ochisq, dev, iter_diff of the fit, broadcast from thread 0
 };
 
 // Row j of packed lower-triangle element e (j*(j+1)/2 <= e < (j+1)*(j+2)/2),
@@ -1681,61 +1682,74 @@ __device__ void run_fit(const DevObject &ob, const FitConfig &cfg, const SlotLay
             totarea = area_trial;
             if (chisq < ochisq) {
                 accepted = true;
-                alamda = alamda / cfg.alamda_incr;
                 for (int e = tid; e < mf * mf; e += NT) s.alpha[e] = s.covar[e];
                 for (int j = tid; j < mf; j += NT) s.beta[j] = s.da[j];
                 for (int l = tid; l < ma; l += NT) s.cg[l] = s.atry[l];
-                __syncthreads();
             } else {
-                alamda = cfg.alamda_incr * alamda;
                 chisq = ochisq;
             }
         } else {
             last_err = err;
         }
         niter++;
-        if ((niter == 1) || (chisq < ochisq)) {
-            ochisq = chisq;
-            // curv(cg) of the driver: the accepted shape is the trial one;
-            // otherwise (first iteration, rejected or failed solve) cg is
-            // still the starting vector of the first evaluation.
-            const double *src = accepted ? chk_trial : chk_first;
-            for (int c = 0; c < 3; c++) chk_acc[c] = src[c];
-            totarea = accepted ? area_trial : area_first;
-            rchisq = chisq - (chk_acc[0] * chk_acc[0] + chk_acc[1] * chk_acc[1] + chk_acc[2] * chk_acc[2]) *
-                                 (cfg.conw_r * cfg.conw_r);
+        // The scalar bookkeeping of the step (mrqmin.c:91-107 and
+        // period_search_BOINC.cpp:873-892) runs on thread 0 and is broadcast:
+        // an FP64 instruction holds the FP64 unit for the whole warp, so
+        // every warp computing it would cost 16 times the FP64 time.
+        if (tid == 0) {
+            if (err == 0) alamda = accepted ? alamda / cfg.alamda_incr : cfg.alamda_incr * alamda;
+            if ((niter == 1) || accepted) {
+                ochisq = chisq;
+                // curv(cg) of the driver: the accepted shape is the trial one;
+                // otherwise (first iteration, rejected or failed solve) cg is
+                // still the starting vector of the first evaluation.
+                const double *src = accepted ? chk_trial : chk_first;
+                for (int c = 0; c < 3; c++) chk_acc[c] = src[c];
+                totarea = accepted ? area_trial : area_first;
+                rchisq = chisq - (chk_acc[0] * chk_acc[0] + chk_acc[1] * chk_acc[1] + chk_acc[2] * chk_acc[2]) *
+                                     (cfg.conw_r * cfg.conw_r);
+            }
+            dev_new = sqrt(rchisq / ob.ndata);
+            if (dev_old - dev_new > 1e-10) {
+                iter_diff = dev_old - dev_new;
+                dev_old = dev_new;
+            }
+            s.misc[M_LM] = alamda;
+            s.misc[M_LM + 1] = ochisq;
+            s.misc[M_LM + 2] = dev_new;
+            s.misc[M_LM + 3] = iter_diff;
         }
-        dev_new = sqrt(rchisq / ob.ndata);
-        if (dev_old - dev_new > 1e-10) {
-            iter_diff = dev_old - dev_new;
-            dev_old = dev_new;
-        }
+        __syncthreads();
+        alamda = s.misc[M_LM];
+        ochisq = s.misc[M_LM + 1];
+        dev_new = s.misc[M_LM + 2];
+        iter_diff = s.misc[M_LM + 3];
         if (niter <= kScreenIters) {
             hist[niter] = ochisq;
             lam_hist[niter - 1] = alamda;
         }
         if (niter == kScreenIters && (w.traj || w.mlp)) {
-            float f[kFeat];
+            // features and prediction on warp 0 only (FP64 logarithms)
+            if (tid < 32) {
+                float f[kFeat];
 #pragma unroll
-            for (int i = 0; i < kScreenIters; i++) {
-                f[i] = static_cast<float>(log(hist[i + 1] / hist[0]));
-                f[kScreenIters + i] = static_cast<float>(log10(lam_hist[i]));
-            }
-            f[8] = static_cast<float>(log(static_cast<double>(ob.ndata)));
-            f[9] = static_cast<float>(log(prd));
-            if (w.traj && tid == 0) {
-                float *rec = w.traj + static_cast<size_t>(fidx) * kTrajFloats;
-                for (int i = 0; i < kFeat; i++) rec[i] = f[i];
-                rec[10] = static_cast<float>(dev_new);
-            }
-            if (w.mlp && w.iter_limit == kScreenIters) {
-                if (tid < 32) {
-                    const float y = mlp_predict_warp(w.mlp, f, reinterpret_cast<float *>(s.pt));
-                    if (tid == 0) s.misc[M_PIV + 2] = static_cast<double>(y);
+                for (int i = 0; i < kScreenIters; i++) {
+                    f[i] = static_cast<float>(log(hist[i + 1] / hist[0]));
+                    f[kScreenIters + i] = static_cast<float>(log10(lam_hist[i]));
                 }
-                __syncthreads();
-                pred_dev = dev_new * exp(s.misc[M_PIV + 2]);
+                f[8] = static_cast<float>(log(static_cast<double>(ob.ndata)));
+                f[9] = static_cast<float>(log(prd));
+                if (w.traj && tid == 0) {
+                    float *rec = w.traj + static_cast<size_t>(fidx) * kTrajFloats;
+                    for (int i = 0; i < kFeat; i++) rec[i] = f[i];
+                    rec[10] = static_cast<float>(dev_new);
+                }
+                if (w.mlp && w.iter_limit == kScreenIters) {
+                    const float y = mlp_predict_warp(w.mlp, f, reinterpret_cast<float *>(s.pt));
+                    if (tid == 0) pred_dev = dev_new * exp(static_cast<double>(y));
+                }
             }
+            __syncthreads();
         }
         if (w.iter_limit > 0 && niter >= w.iter_limit) {
             screened = true;
