@@ -717,22 +717,24 @@ __device__ void facet_stage_tc(const DevObject &ob, Smem<PS_FORM_MIXED> &s, int 
         const float4 n = s.fac[i];
         const float mu = e1 * n.x + e2 * n.y + e3 * n.z;
         const float mu0 = f1 * n.x + f2 * n.y + f3 * n.z;
-        float w = 0.f;
-        if (mu > float(kTinyMu) && mu0 > float(kTinyMu)) {
-            const float2 a = s.ag[i];
-            const LitTerms<float, PS_FORM_MIXED> lt(mu, mu0, cl, cls);
-            br = br + a.x * lt.sv;
-            w = a.y * lt.sv;
-            const float cu = a.x * lt.dsmu, cv = a.x * lt.dsmu0;
-            ux = fmaf(cu, n.x, ux);
-            uy = fmaf(cu, n.y, uy);
-            uz = fmaf(cu, n.z, uz);
-            vx = fmaf(cv, n.x, vx);
-            vy = fmaf(cv, n.y, vy);
-            vz = fmaf(cv, n.z, vz);
-            dcl = dcl + mu * mu0 * a.x;
-            dcls = dcls + a.x * lt.dcls_w;
-        }
+        // Branch-free: the 8 points of a warp see different lit facets, so a
+        // branch would diverge on almost every step; unlit facets get zero
+        // area (every term vanishes) and a safe denominator.
+        const bool lit = mu > float(kTinyMu) && mu0 > float(kTinyMu);
+        const float2 ag = s.ag[i];
+        const float ax = lit ? ag.x : 0.f, ay = lit ? ag.y : 0.f;
+        const LitTerms<float, PS_FORM_MIXED> lt(lit ? mu : 1.f, lit ? mu0 : 1.f, cl, cls);
+        br = fmaf(ax, lt.sv, br);
+        const float w = ay * lt.sv;
+        const float cu = ax * lt.dsmu, cv = ax * lt.dsmu0;
+        ux = fmaf(cu, n.x, ux);
+        uy = fmaf(cu, n.y, uy);
+        uz = fmaf(cu, n.z, uz);
+        vx = fmaf(cv, n.x, vx);
+        vy = fmaf(cv, n.y, vy);
+        vz = fmaf(cv, n.z, vz);
+        dcl = fmaf(mu * mu0, ax, dcl);
+        dcls = fmaf(ax, lt.dcls_w, dcls);
         const uint32_t hi = tc::to_tf32(w);
         const uint32_t lo = tc::to_tf32(w - __uint_as_float(hi));
         const int cm = (warp & 3) * kcs + (i0 >> 2);    // core matrix (8-point group, 4-facet group)
