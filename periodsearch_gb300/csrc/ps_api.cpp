@@ -28,6 +28,7 @@ struct ps_input {
 struct FormPlan {
     bool ready = false;
     int P = 16, dsph_smem = 0, slots = 0;
+    int rel_rows = 0;   // relative-lightcurve rows parked in shared memory (0: global scratch)
     size_t smem = 0;
 };
 
@@ -39,7 +40,7 @@ struct ps_ctx {
     cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};
     char *d_tables = nullptr;          // one allocation with every table
     psg::DevObject dob{};
-    int sm_count = 0, slots = 0, P = 16, dsph_smem = 0;
+    int sm_count = 0, slots = 0, P = 16, dsph_smem = 0, rel_rows = 0;
     int64_t h2d_bytes = 0;
     size_t smem = 0;
     double *d_scratch = nullptr;
@@ -129,7 +130,10 @@ ps_status ensure_out(ps_ctx *c, size_t nfits)
 
 // Plan of one form for a given basis mode and tile size: shared-memory
 // layout, kernel attribute and resident slots (at most per_sm_cap per SM when
-// positive).  PS_ERR_LIMIT when the slot does not fit.
+// positive).  PS_ERR_LIMIT when the slot does not fit.  The rows of the
+// relative lightcurves live in shared memory when they fit without costing
+// a resident slot (they are re-read by the second pass over each relative
+// lightcurve), else in the per-slot global scratch.
 ps_status build_plan(ps_ctx *c, int form, int dsph_smem, int P, int per_sm_cap, FormPlan *out)
 {
     const psg::HostObject &o = c->obj;
@@ -142,14 +146,35 @@ ps_status build_plan(ps_ctx *c, int form, int dsph_smem, int P, int per_sm_cap, 
     if (L.bytes > smem_max) return PS_ERR_LIMIT;
     // A tensor-core slot holds up to 512 Tensor Memory columns for its whole
     // life: request enough shared memory that only one slot fits on an SM.
+    const size_t floor_tc = static_cast<size_t>(prop.sharedMemPerMultiprocessor) / 2 + 1024;
     size_t bytes = L.bytes;
-    if (dsph_smem == psg::kBasisTensor)
-        bytes = std::min(smem_max, std::max(bytes, static_cast<size_t>(prop.sharedMemPerMultiprocessor) / 2 + 1024));
+    if (dsph_smem == psg::kBasisTensor) bytes = std::min(smem_max, std::max(bytes, floor_tc));
     int e = psg::set_kernel_smem(form, bytes, o.ncoef, dsph_smem);
     if (e != 0) return cuda_fail(c, static_cast<cudaError_t>(e), "cudaFuncSetAttribute");
     int per_sm = 0;
     e = psg::occupancy_slots(form, bytes, o.ncoef, dsph_smem, &per_sm);
     if (e != 0) return cuda_fail(c, static_cast<cudaError_t>(e), "occupancy");
+    int rel_rows = 0;
+    if (o.max_rel_points > 0) {
+        const psg::SlotLayout Lr = psg::make_layout(form, o.ma, o.mfit, F, o.ncoef, P, dsph_smem, o.max_rel_points);
+        const size_t need = dsph_smem == psg::kBasisTensor ? std::max(Lr.bytes, floor_tc) : Lr.bytes;
+        if (Lr.bytes <= smem_max) {
+            e = psg::set_kernel_smem(form, need, o.ncoef, dsph_smem);
+            if (e != 0) return cuda_fail(c, static_cast<cudaError_t>(e), "cudaFuncSetAttribute");
+            int per_sm_r = 0;
+            e = psg::occupancy_slots(form, need, o.ncoef, dsph_smem, &per_sm_r);
+            if (e != 0) return cuda_fail(c, static_cast<cudaError_t>(e), "occupancy");
+            const int cap = per_sm_cap > 0 ? per_sm_cap : 1 << 20;
+            if (std::min(per_sm_r, cap) >= std::min(per_sm, cap)) {
+                rel_rows = o.max_rel_points;
+                bytes = need;
+                per_sm = per_sm_r;
+            } else {
+                e = psg::set_kernel_smem(form, bytes, o.ncoef, dsph_smem);
+                if (e != 0) return cuda_fail(c, static_cast<cudaError_t>(e), "cudaFuncSetAttribute");
+            }
+        }
+    }
     if (per_sm < 1) return PS_ERR_LIMIT;
     if (per_sm_cap > 0) per_sm = std::min(per_sm, per_sm_cap);
     if (dsph_smem == psg::kBasisTensor && per_sm > 1) {
@@ -158,6 +183,7 @@ ps_status build_plan(ps_ctx *c, int form, int dsph_smem, int P, int per_sm_cap, 
     }
     out->P = P;
     out->dsph_smem = dsph_smem;
+    out->rel_rows = rel_rows;
     out->smem = bytes;
     out->slots = per_sm * c->sm_count;
     out->ready = true;
@@ -216,6 +242,7 @@ ps_status run_fits(ps_ctx *c, double conw_r, psg::FitWork w, int form)
     w.queue = c->d_queue;
     w.scratch = c->d_scratch;
     w.scratch_stride = c->scratch_stride;
+    w.rel_rows = pl.rel_rows;
     w.out = c->d_out;
     int grid = static_cast<int>(std::min<int64_t>(pl.slots, std::max<int64_t>(w.nfits, 1)));
     PSG_CUDA(c, cudaMemsetAsync(c->d_queue, 0, sizeof(unsigned long long), c->stream));
@@ -593,6 +620,7 @@ ps_status upload_object(std::unique_ptr<ps_ctx> &c, ps_ctx **out)
     }
     c->P = c->plan[c->opt.form].P;
     c->dsph_smem = c->plan[c->opt.form].dsph_smem;
+    c->rel_rows = c->plan[c->opt.form].rel_rows;
     c->smem = c->plan[c->opt.form].smem;
     c->slots = c->plan[c->opt.form].slots;
     c->scratch_stride = static_cast<size_t>(std::max(o.max_rel_points, 1)) * (o.ma + 1);
@@ -752,7 +780,7 @@ ps_status ps_eval(ps_ctx *c, double conw_r, const double *cg, double *alpha, dou
     PSG_CUDA(c, cudaMemcpyAsync(d_cg, cg, ma * sizeof(double), cudaMemcpyHostToDevice, c->stream));
     psg::FitConfig cfg = make_config(c, conw_r);
     int e = psg::launch_eval(c->opt.form, c->dob, cfg, d_cg, d_al, d_be, d_c2, d_ar, c->d_scratch, c->P, c->smem,
-                             c->dsph_smem, c->stream);
+                             c->dsph_smem, c->rel_rows, c->stream);
     if (e != 0) return cuda_fail(c, static_cast<cudaError_t>(e), "eval kernel launch");
     PSG_CUDA(c, cudaMemcpyAsync(alpha, d_al, static_cast<size_t>(mf) * mf * sizeof(double), cudaMemcpyDeviceToHost,
                                 c->stream));
@@ -1067,6 +1095,7 @@ extern "C" ps_status ps_autotune(ps_ctx *c, double conw_r, int32_t sample_fits, 
     if (e != 0) return cuda_fail(c, static_cast<cudaError_t>(e), "cudaFuncSetAttribute");
     c->P = pl.P;
     c->dsph_smem = pl.dsph_smem;
+    c->rel_rows = pl.rel_rows;
     c->smem = pl.smem;
     rep->chosen = chosen;
     return PS_OK;

@@ -202,17 +202,18 @@ int launch_fits(int form, const DevObject &ob, const FitConfig &cfg, const FitWo
 }
 
 int launch_eval(int form, const DevObject &ob, const FitConfig &cfg, const double *cg, double *alpha, double *beta,
-                double *chisq, double *area, double *scratch, int P, size_t smem, int dsph_smem, void *stream)
+                double *chisq, double *area, double *scratch, int P, size_t smem, int dsph_smem, int rel_rows,
+                void *stream)
 {
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     if (form == PS_FORM_FP64) {
         eval_kernel<PS_FORM_FP64, 1><<<1, threads_of<PS_FORM_FP64>(), smem, st>>>(ob, cfg, cg, alpha, beta, chisq,
-                                                                                   area, scratch, P, 0);
+                                                                                   area, scratch, P, 0, rel_rows);
     } else if (form == PS_FORM_MIXED) {
         for_mixed(ob.ncoef, dsph_smem, [&](auto ku) {
             constexpr int KU = decltype(ku)::value;
             eval_kernel<PS_FORM_MIXED, KU><<<1, threads_of<PS_FORM_MIXED>(), smem, st>>>(
-                ob, cfg, cg, alpha, beta, chisq, area, scratch, P, dsph_smem);
+                ob, cfg, cg, alpha, beta, chisq, area, scratch, P, dsph_smem, rel_rows);
             return cudaSuccess;
         });
     } else {

@@ -49,6 +49,7 @@ struct FitWork {
     double *scratch;              // per-slot scratch for relative lightcurves
     size_t scratch_stride;        // doubles per slot
     ps_fit *out;                  // [nfits]
+    int rel_rows;                 // > 0: relative-lightcurve rows in shared memory (make_layout)
     // multi-object packed launch (launch_pack): fit f belongs to object
     // object[f], described by objs[object[f]] and cfgs[object[f]]
     const struct DevObject *objs;
@@ -89,6 +90,7 @@ struct SlotLayout {
     size_t accs;            // per-point weights and residuals of the accumulation (mixed form)
     size_t davef;           // FP32 copy of a relative lightcurve's derivative sums (mixed form)
     size_t bmat;            // rotation matrices and phase/scattering parameters of an evaluation
+    size_t rels;            // relative-lightcurve rows in shared memory, or 0 (global scratch)
     size_t bytes;
 };
 
@@ -114,7 +116,10 @@ constexpr size_t kTcAlphaOperands = 32768;   // tensor-core alpha/beta operands:
 
 // dsph_smem: the mixed form keeps the FP32 basis Dsph[F][C] in shared memory
 // for the whole launch (it is read once per point tile by every warp).
-PSG_HD inline SlotLayout make_layout(int form, int ma, int mfit, int nfac, int ncoef, int P, int dsph_smem)
+// rel_rows > 0: the rows of relative lightcurves (up to rel_rows points)
+// are parked in shared memory instead of the per-slot global scratch.
+PSG_HD inline SlotLayout make_layout(int form, int ma, int mfit, int nfac, int ncoef, int P, int dsph_smem,
+                                     int rel_rows = 0)
 {
     SlotLayout L{};
     L.form = form;
@@ -180,6 +185,7 @@ PSG_HD inline SlotLayout make_layout(int form, int ma, int mfit, int nfac, int n
     L.accs = form == PS_FORM_MIXED ? take(64 * sizeof(float)) : 0;
     L.davef = form == PS_FORM_MIXED ? take(static_cast<size_t>(ma) * sizeof(float)) : 0;
     L.bmat = take(32 * rs);
+    L.rels = rel_rows > 0 ? take(static_cast<size_t>(rel_rows) * (ma + 1) * rs) : 0;
     L.bytes = o;
     return L;
 }
@@ -189,7 +195,7 @@ int launch_fits(int form, const DevObject &ob, const FitConfig &cfg, const FitWo
                 int P, size_t smem, int dsph_smem, void *stream);
 int launch_eval(int form, const DevObject &ob, const FitConfig &cfg, const double *cg, double *alpha,
                 double *beta, double *chisq, double *area, double *scratch, int P, size_t smem,
-                int dsph_smem, void *stream);
+                int dsph_smem, int rel_rows, void *stream);
 int set_kernel_smem(int form, size_t smem, int ncoef, int dsph_smem);
 // Multi-object packed launch (ps_pack.cu): objects with identical shape
 // tables (facet grid, Laplace series, free parameters) share one persistent

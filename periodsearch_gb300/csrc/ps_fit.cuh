@@ -1789,14 +1789,15 @@ __global__ void __launch_bounds__(threads_of<FORM>(), 1)
     using R = typename RealOf<FORM>::T;
     constexpr int NT = threads_of<FORM>();
     extern __shared__ __align__(16) char smem[];
-    const SlotLayout L = make_layout(FORM, ob.ma, ob.mfit, ob.nfac, ob.ncoef, P, dsph_smem);
+    const SlotLayout L = make_layout(FORM, ob.ma, ob.mfit, ob.nfac, ob.ncoef, P, dsph_smem, w.rel_rows);
     Smem<FORM> s = carve<FORM>(smem, L);
     constexpr bool kTensor = FORM == PS_FORM_MIXED && KU == 0;
     if (s.dsph)
         for (int e = threadIdx.x; e < ob.nfac * ob.ncoef; e += NT) s.dsph[e] = ob.dsph_f[e];
     TcState tcs;
     if constexpr (kTensor) tcs.tbase = tc_setup<NT>(ob, s);
-    R *scratch = reinterpret_cast<R *>(w.scratch + static_cast<size_t>(blockIdx.x) * w.scratch_stride);
+    R *scratch = L.rels ? reinterpret_cast<R *>(smem + L.rels)
+                        : reinterpret_cast<R *>(w.scratch + static_cast<size_t>(blockIdx.x) * w.scratch_stride);
     __shared__ long long next;
     for (;;) {
         if (threadIdx.x == 0) next = static_cast<long long>(atomicAdd(w.queue, 1ULL));
@@ -1824,12 +1825,12 @@ __global__ void __launch_bounds__(threads_of<FORM>(), 1)
 template <int FORM, int KU>
 __global__ void __launch_bounds__(threads_of<FORM>(), 1) eval_kernel(DevObject ob, FitConfig cfg, const double *cg, double *alpha,
                                                         double *beta, double *chisq, double *area, double *scratch,
-                                                        int P, int dsph_smem)
+                                                        int P, int dsph_smem, int rel_rows)
 {
     using R = typename RealOf<FORM>::T;
     constexpr int NT = threads_of<FORM>();
     extern __shared__ __align__(16) char smem[];
-    const SlotLayout L = make_layout(FORM, ob.ma, ob.mfit, ob.nfac, ob.ncoef, P, dsph_smem);
+    const SlotLayout L = make_layout(FORM, ob.ma, ob.mfit, ob.nfac, ob.ncoef, P, dsph_smem, rel_rows);
     Smem<FORM> s = carve<FORM>(smem, L);
     constexpr bool kTensor = FORM == PS_FORM_MIXED && KU == 0;
     if (s.dsph)
@@ -1838,7 +1839,8 @@ __global__ void __launch_bounds__(threads_of<FORM>(), 1) eval_kernel(DevObject o
     if constexpr (kTensor) tcs.tbase = tc_setup<NT>(ob, s);
     for (int i = threadIdx.x; i < ob.ma; i += NT) s.cg[i] = cg[i];
     __syncthreads();
-    evaluate<FORM, KU>(ob, cfg, L, s, s.cg, s.alpha, s.beta, reinterpret_cast<R *>(scratch), tcs);
+    R *rows = L.rels ? reinterpret_cast<R *>(smem + L.rels) : reinterpret_cast<R *>(scratch);
+    evaluate<FORM, KU>(ob, cfg, L, s, s.cg, s.alpha, s.beta, rows, tcs);
     if constexpr (kTensor) {
         const bool aborted = *s.abort != 0;
         tc_teardown(s, tcs, ob.nfac);
