@@ -497,6 +497,53 @@ __device__ inline void setup_point(const DevObject &ob, const FitConfig &cfg, in
     } else {
         sincosf(static_cast<float>(f), &sf, &cf);
     }
+    if constexpr (!kFP64) {
+        // The rotation fm about the spin axis (matrix.c) commutes out of the
+        // products: with u = B ee, e = fm u, de/dbeta = fm (dB/dbeta ee),
+        // de/dlambda = fm (dB/dlambda ee) and de/domega = (dfm/domega) u =
+        // t (e_y, -e_x, 0); the same for the Sun vector.
+        const R *src[3] = {B, DB0, DB1};
+#pragma unroll
+        for (int m = 0; m < 3; m++) {
+            R u[3], u0[3];
+#pragma unroll
+            for (int k = 0; k < 3; k++) {
+                const R *row = src[m] + 3 * k;
+                u[k] = row[0] * ee[0] + row[1] * ee[1] + row[2] * ee[2];
+                u0[k] = row[0] * e0v[0] + row[1] * e0v[1] + row[2] * e0v[2];
+            }
+            const R r0 = cf * u[0] + sf * u[1], r1 = cf * u[1] - sf * u[0];
+            const R s0 = cf * u0[0] + sf * u0[1], s1 = cf * u0[1] - sf * u0[0];
+            if (m == 0) {
+                pt[0] = r0;
+                pt[1] = r1;
+                pt[2] = u[2];
+                pt[3] = s0;
+                pt[4] = s1;
+                pt[5] = u0[2];
+                // d/domega (column 2 of de and de0)
+                pt[6 + 2] = t * r1;
+                pt[6 + 3 + 2] = -t * r0;
+                pt[6 + 6 + 2] = R(0);
+                pt[15 + 2] = t * s1;
+                pt[15 + 3 + 2] = -t * s0;
+                pt[15 + 6 + 2] = R(0);
+            } else {
+                const int j = m - 1;   // column 0: d/dbeta, 1: d/dlambda
+                pt[6 + j] = r0;
+                pt[6 + 3 + j] = r1;
+                pt[6 + 6 + j] = u[2];
+                pt[15 + j] = s0;
+                pt[15 + 3 + j] = s1;
+                pt[15 + 6 + j] = u0[2];
+            }
+        }
+        pt[24] = scale;
+        pt[25] = ex;
+        pt[26] = php0 * ex * alpha * (inv_w * inv_w);
+        pt[27] = alpha;
+        return;
+    }
     const R fm[9] = {cf, sf, R(0), -sf, cf, R(0), R(0), R(0), R(1)};
     const R dfm[9] = {-t * sf, t * cf, R(0), -t * cf, -t * sf, R(0), R(0), R(0), R(0)};
     R tm[9], d0[9], d1[9], d2[9];
@@ -718,8 +765,10 @@ __device__ void facet_stage_tc(const DevObject &ob, Smem<PS_FORM_MIXED> &s, int 
         const float mu = e1 * n.x + e2 * n.y + e3 * n.z;
         const float mu0 = f1 * n.x + f2 * n.y + f3 * n.z;
         // Branch-free: the 8 points of a warp see different lit facets, so a
-        // branch would diverge on almost every step; unlit facets get zero
-        // area (every term vanishes) and a safe denominator.
+        // branch would diverge on almost every step (and a warp-uniform skip
+        // of groups unlit for all 8 points measured slower: it breaks the
+        // two-step interleave); unlit facets get zero area (every term
+        // vanishes) and a safe denominator.
         const bool lit = mu > float(kTinyMu) && mu0 > float(kTinyMu);
         const float2 ag = s.ag[i];
         const float ax = lit ? ag.x : 0.f, ay = lit ? ag.y : 0.f;
@@ -1465,83 +1514,154 @@ __device__ int gauss_jordan(double *A, double *b, int n, double *col, int *ipiv,
 // positive definite; lower triangle used, overwritten by L) and the solve of
 // L L^T x = b, in FP64.  The forward substitution runs inside the
 // factorisation (b is the bordering column: y_j = b_j / L_jj, then b_i -=
-// L_ij y_j with the trailing update).  Columns are taken two at a time: warp
-// 0 factors the 2 x 2 pivot block and scales both columns and y, then all
-// threads apply the rank-2 update to the trailing block -- two CTA barriers
-// per pair of columns.  The back substitution uses the stored reciprocals.
-// Returns 2 when a pivot is not positive.
+// L_ij y_j with the trailing update).
+//
+// Columns are taken two at a time, with one pair of look-ahead.  Every FP64
+// instruction holds its sub-partition's FP64 unit for the whole warp, so the
+// serial chain of a pivot (warp 0) and the bulk of the trailing update (the
+// warps of sub-partitions 1..3) run on different sub-partitions at the same
+// time: while the workers apply pair j to the columns beyond pair j + 2, warp
+// 0 applies it to pair j + 2 alone and factors that pair -- one CTA barrier
+// per pair.  The 2 x 2 pivot takes its two reciprocal square roots (of the
+// leading element and of the block's determinant) in one lane-parallel
+// sequence.  The back substitution runs on warp 0 with b in registers and
+// the rows of L pre-scaled by their reciprocal diagonal.  Returns 2 when a
+// pivot is not positive.
+__device__ inline void chol_pivot_pair(double *A, double *b, int n, int j, double *col, double *flag, int lane)
+{
+    const bool two = j + 1 < n;
+    const double a = A[j * n + j];
+    const double bq = two ? A[(j + 1) * n + j] : 0.0;
+    const double c = two ? A[(j + 1) * n + j + 1] : 1.0;
+    // lane 0: the leading element, lane 1: the determinant a c - bq^2
+    // (L11 = sqrt(det / a), so 1 / L11 = a rsqrt(a) rsqrt(det))
+    const double x = lane == 1 ? fma(a, c, -(bq * bq)) : a;
+    const bool okx = x > 0.0;
+    const double r = okx ? rsqrt(x) : 0.0;
+    const unsigned okm = __ballot_sync(0xffffffffu, okx);
+    const double i0 = __shfl_sync(0xffffffffu, r, 0);
+    const double rd = __shfl_sync(0xffffffffu, r, 1);
+    // lane 1: l10 = bq / L00, lane 2: y0 = b_j / L00, lane 3: 1 / L11
+    const double u = lane == 1 ? bq : lane == 2 ? b[j] : a;
+    double v = u * i0;
+    if (lane == 3) v *= rd;
+    const double l10 = __shfl_sync(0xffffffffu, v, 1);
+    const double y0 = __shfl_sync(0xffffffffu, v, 2);
+    const double i1 = __shfl_sync(0xffffffffu, v, 3);
+    const bool ok = (okm & 1u) && (!two || (okm & 2u));
+    if (lane == 0) {
+        *flag = ok ? 1.0 : 0.0;
+        col[j] = i0;
+        b[j] = y0;
+        if (two) {
+            col[j + 1] = i1;
+            b[j + 1] = (b[j + 1] - l10 * y0) * i1;
+        }
+    }
+    if (two && lane == 1) A[(j + 1) * n + j] = l10;
+    for (int i = j + (two ? 2 : 1) + lane; i < n; i += 32) {
+        const double a0 = A[i * n + j] * i0;
+        A[i * n + j] = a0;
+        if (two) A[i * n + j + 1] = (A[i * n + j + 1] - a0 * l10) * i1;
+    }
+}
+
 template <int NT>
 __device__ int cholesky_solve(double *A, double *b, int n, double *col, double *flag)
 {
+    static_assert(NT % 128 == 0, "whole warps on every sub-partition");
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    // trailing-update workers: the warps of sub-partitions 1..3
+    constexpr int kWorkers = NT / 128 * 3 * 32;
+    const bool worker = (warp & 3) != 0;
+    const int wtid = ((warp >> 2) * 3 + (warp & 3) - 1) * 32 + lane;
     __syncthreads();
-    for (int j = 0; j < n; j += 2) {
+    if (warp == 0) chol_pivot_pair(A, b, n, 0, col, flag, lane);
+    __syncthreads();
+    if (*flag == 0.0) return 2;
+    for (int j = 0; j + 2 < n; j += 2) {
+        // pair (j, j + 1) is factored; b[j], b[j + 1] hold its y
         const bool two = j + 1 < n;
+        const int jn = j + 2;
         if (warp == 0) {
-            double i0 = 0, l10 = 0, i1 = 0;
-            if (lane == 0) {
-                const double d0 = A[j * n + j];
-                bool ok = d0 > 0.0;
-                i0 = ok ? rsqrt(d0) : 0.0;
-                A[j * n + j] = d0 * i0;
-                col[j] = i0;
-                const double y0 = b[j] * i0;
-                b[j] = y0;
-                if (two && ok) {
-                    l10 = A[(j + 1) * n + j] * i0;
-                    const double d1 = A[(j + 1) * n + j + 1] - l10 * l10;
-                    ok = d1 > 0.0;
-                    i1 = ok ? rsqrt(d1) : 0.0;
-                    A[(j + 1) * n + j] = l10;
-                    A[(j + 1) * n + j + 1] = d1 * i1;
-                    col[j + 1] = i1;
-                    b[j + 1] = (b[j + 1] - l10 * y0) * i1;
-                }
-                *flag = ok ? 1.0 : 0.0;
+            // apply pair j to the next pair's columns and rows of b, then
+            // factor the next pair
+            const bool twon = jn + 1 < n;
+            const double p0 = A[jn * n + j], p1 = two ? A[jn * n + j + 1] : 0.0;
+            const double q0 = twon ? A[(jn + 1) * n + j] : 0.0, q1 = (twon && two) ? A[(jn + 1) * n + j + 1] : 0.0;
+            const double y0 = b[j], y1 = two ? b[j + 1] : 0.0;
+            for (int i = jn + lane; i < n; i += 32) {
+                const double li0 = A[i * n + j], li1 = two ? A[i * n + j + 1] : 0.0;
+                A[i * n + jn] = A[i * n + jn] - li0 * p0 - li1 * p1;
+                if (i > jn) A[i * n + jn + 1] = A[i * n + jn + 1] - li0 * q0 - li1 * q1;
             }
-            i0 = __shfl_sync(0xffffffffu, i0, 0);
-            l10 = __shfl_sync(0xffffffffu, l10, 0);
-            i1 = __shfl_sync(0xffffffffu, i1, 0);
-            const int r0 = j + (two ? 2 : 1);
-            for (int i = r0 + lane; i < n; i += 32) {
-                const double a0 = A[i * n + j] * i0;
-                A[i * n + j] = a0;
-                if (two) A[i * n + j + 1] = (A[i * n + j + 1] - a0 * l10) * i1;
+            if (lane < (twon ? 2 : 1)) {
+                const int i = jn + lane;
+                double vb = b[i] - A[i * n + j] * y0;
+                if (two) vb -= A[i * n + j + 1] * y1;
+                b[i] = vb;
+            }
+            __syncwarp();
+            chol_pivot_pair(A, b, n, jn, col, flag, lane);
+        } else if (worker) {
+            // apply pair j to the columns beyond the next pair
+            const int j2 = j + 4;
+            if (j2 < n) {
+                const int m = n - j2;
+                const int ntri = m * (m + 1) / 2;
+                const double y0 = b[j], y1 = two ? b[j + 1] : 0.0;
+                for (int e = wtid; e < ntri + m; e += kWorkers) {
+                    if (e < ntri) {
+                        const int r = tri_row(e);
+                        const int cc = e - r * (r + 1) / 2;
+                        const int i = j2 + r, k = j2 + cc;
+                        double v = A[i * n + k] - A[i * n + j] * A[k * n + j];
+                        if (two) v -= A[i * n + j + 1] * A[k * n + j + 1];
+                        A[i * n + k] = v;
+                    } else {
+                        const int i = j2 + (e - ntri);
+                        double v = b[i] - A[i * n + j] * y0;
+                        if (two) v -= A[i * n + j + 1] * y1;
+                        b[i] = v;
+                    }
+                }
             }
         }
         __syncthreads();
         if (*flag == 0.0) return 2;
-        const int j2 = j + (two ? 2 : 1);
-        const int m = n - j2;
-        const int ntri = m * (m + 1) / 2;
-        const double y0 = b[j], y1 = two ? b[j + 1] : 0.0;
-        for (int e = tid; e < ntri + m; e += NT) {
-            if (e < ntri) {
-                const int r = tri_row(e);
-                const int c = e - r * (r + 1) / 2;
-                const int i = j2 + r, k = j2 + c;
-                double v = A[i * n + k] - A[i * n + j] * A[k * n + j];
-                if (two) v -= A[i * n + j + 1] * A[k * n + j + 1];
-                A[i * n + k] = v;
-            } else {
-                const int i = j2 + (e - ntri);
-                double v = b[i] - A[i * n + j] * y0;
-                if (two) v -= A[i * n + j + 1] * y1;
-                b[i] = v;
-            }
-        }
-        __syncthreads();
     }
+    // L^T x = y: with the rows of L scaled, L'_jk = L_jk / L_jj (k < j),
+    // x = col .* z where z_j = y_j - sum_{i > j} L'_ij z_i
+    const int nstrict = n * (n - 1) / 2;
+    for (int e = tid; e < nstrict; e += NT) {
+        const int r = tri_row(e) + 1;
+        const int cc = e - r * (r - 1) / 2;
+        A[r * n + cc] *= col[r];
+    }
+    __syncthreads();
     if (warp == 0) {
-        for (int j = n - 1; j >= 0; j--) {
-            double x = 0;
-            if (lane == 0) {
-                x = b[j] * col[j];
-                b[j] = x;
+        if (n <= 96) {
+            double z0 = lane < n ? b[lane] : 0.0, z1 = lane + 32 < n ? b[lane + 32] : 0.0,
+                   z2 = lane + 64 < n ? b[lane + 64] : 0.0;
+            for (int jj = n - 1; jj >= 1; jj--) {
+                const int slot = jj >> 5;
+                const double own = slot == 0 ? z0 : slot == 1 ? z1 : z2;
+                const double zj = __shfl_sync(0xffffffffu, own, jj & 31);
+                const double *row = A + jj * n;
+                if (lane < jj) z0 -= row[lane] * zj;
+                if (lane + 32 < jj) z1 -= row[lane + 32] * zj;
+                if (lane + 64 < jj) z2 -= row[lane + 64] * zj;
             }
-            x = __shfl_sync(0xffffffffu, x, 0);
-            for (int i = lane; i < j; i += 32) b[i] -= A[j * n + i] * x;
-            __syncwarp();
+            if (lane < n) b[lane] = z0 * col[lane];
+            if (lane + 32 < n) b[lane + 32] = z1 * col[lane + 32];
+            if (lane + 64 < n) b[lane + 64] = z2 * col[lane + 64];
+        } else {
+            for (int jj = n - 1; jj >= 1; jj--) {
+                const double zj = b[jj];
+                for (int i = lane; i < jj; i += 32) b[i] -= A[jj * n + i] * zj;
+                __syncwarp();
+            }
+            for (int i = lane; i < n; i += 32) b[i] *= col[i];
         }
     }
     __syncthreads();
