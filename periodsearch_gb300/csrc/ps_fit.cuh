@@ -731,7 +731,7 @@ __device__ void contract_tc_issue(Smem<PS_FORM_MIXED> &s, int F, TcState &t)
 // one warp store covers a whole 8-point x 4-facet core matrix of the MMA
 // operand [W_hi; W_lo].  The per-point sums (brightness, rotation and
 // scattering derivatives) are reduced over the four lanes and then over the
-// quarters into s.red.  The tile's operand region must be free (previous
+// quarters into s.fpart[p * 9 + 0..5] (FP32: the J columns they feed are).  The tile's operand region must be free (previous
 // MMAs waited for).
 template <int NT>
 __device__ void facet_stage_tc(const DevObject &ob, Smem<PS_FORM_MIXED> &s, int np, float cl, float cls)
@@ -811,18 +811,21 @@ __device__ void facet_stage_tc(const DevObject &ob, Smem<PS_FORM_MIXED> &s, int 
             for (int q = 0; q < 4; q++) a += s.fpart[(q * 32 + tid) * 9 + k];
             t[k] = a;
         }
+        // the point's sums in FP32 over its own quarter-0 partials (read
+        // above by this thread only): brightness, the three rotation
+        // derivatives, the Lambert and the scattering-weight derivatives
         const float *pt = s.pt + tid * kPointStride;
-        double *rd = s.red + tid * kRedStride;
-        rd[0] = t[0];
+        float *rf = s.fpart + tid * 9;
+        rf[0] = t[0];
 #pragma unroll
         for (int k = 0; k < 3; k++) {
             // D_k = (de[k], de[3 + k], de[6 + k]), E_k likewise from de0
             const float r = pt[6 + k] * t[3] + pt[9 + k] * t[4] + pt[12 + k] * t[5] + pt[15 + k] * t[6] +
                             pt[18 + k] * t[7] + pt[21 + k] * t[8];
-            rd[1 + k] = r;
+            rf[1 + k] = r;
         }
-        rd[4] = t[1];
-        rd[5] = t[2];
+        rf[4] = t[1];
+        rf[5] = t[2];
     }
 }
 
@@ -905,16 +908,17 @@ __device__ void contract_tc_finish(Smem<PS_FORM_MIXED> &s, int np, int F, int C,
 // dy), both split into TF32 high and low parts, so that the four quadrants
 // of the 128 x 128 FP32 accumulator sum to alpha (and beta in column mfit)
 // at FP32 accuracy.  The accumulator stays in Tensor Memory across tiles
-// until tc_alpha_flush.  chi^2 is summed in FP64 by warp 0.
+// until tc_alpha_flush.  chi^2 is summed in FP64 by warp 0, unless the
+// caller has prepared the weights, residuals and chi^2 (prepared).
 template <int NT>
 __device__ void accumulate_tile_tc(const DevObject &ob, Smem<PS_FORM_MIXED> &s, int np, int q0pt, bool conv,
-                                   double conv_sig, TcState &t)
+                                   double conv_sig, TcState &t, bool prepared)
 {
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int ma = ob.ma, mf = ob.mfit;
     float *dyv = s.accs;
     float *wtp = dyv + 32;
-    if (tid < 32) {
+    if (tid < 32 && !prepared) {
         double c2 = 0;
         if (tid < np) {
             const int q = q0pt + tid;
@@ -1253,22 +1257,51 @@ __device__ void evaluate(const DevObject &ob, const FitConfig &cfg, const SlotLa
                 R *Jp = s.J + p * ma;
                 const double *rd = s.red + p * kRedStride;
                 if (!conv) {
+                    R v[6];
+                    if constexpr (kPipe) {
+#pragma unroll
+                        for (int k = 0; k < 6; k++) v[k] = s.fpart[p * 9 + k];
+                    } else {
+#pragma unroll
+                        for (int k = 0; k < 6; k++) v[k] = R(rd[k]);
+                    }
                     const R *pt = s.pt + p * kPointStride;
                     const R scale = pt[24];
-                    const R br = R(rd[0]);
-                    Jp[C] = scale * R(rd[1]);
-                    Jp[C + 1] = scale * R(rd[2]);
-                    Jp[C + 2] = scale * R(rd[3]);
+                    const R br = v[0];
+                    Jp[C] = scale * v[1];
+                    Jp[C + 1] = scale * v[2];
+                    Jp[C + 2] = scale * v[3];
                     Jp[C + 3] = br * pt[25];
                     Jp[C + 4] = br * pt[26];
                     Jp[C + 5] = br * pt[27];
-                    Jp[C + 6] = scale * R(rd[4]) * cl;
-                    Jp[C + 7] = scale * R(rd[5]);
+                    Jp[C + 6] = scale * v[4] * cl;
+                    Jp[C + 7] = scale * v[5];
                     s.ym[p] = static_cast<double>(br * scale);
                 } else {
                     for (int k = C; k < ma; k++) Jp[k] = 0;
                     s.ym[p] = rd[0];
                     s.misc[M_CHK + p] = rd[0];
+                }
+            }
+            if constexpr (kPipe) {
+                // the accumulation's per-point FP64 work (weights, residuals,
+                // chi^2) of an absolute lightcurve or of the convexity rows,
+                // here on warp 15 while thread 0 issues the contraction
+                // (same per-point values and reduction as in the
+                // accumulation itself)
+                if (!rel && warp == NT / 32 - 1) {
+                    double c2 = 0;
+                    if (jp < np) {
+                        const int q = start + t0 + jp;
+                        const double sig2i = conv ? 1 / (conv_sig * conv_sig) : ob.sig2i[q];
+                        const double wg = ob.weight[q];
+                        const double dy = (conv ? 0.0 : ob.bright[q]) - s.ym[jp];
+                        s.accs[jp] = static_cast<float>(dy);
+                        s.accs[32 + jp] = static_cast<float>(sig2i * wg);
+                        c2 = dy * dy * sig2i * wg;
+                    }
+                    c2 = warp_sum(c2);
+                    if (lane == 0) s.misc[M_CHISQ] += c2;
                 }
             }
             bool next_setup = false;
@@ -1322,7 +1355,7 @@ __device__ void evaluate(const DevObject &ob, const FitConfig &cfg, const SlotLa
             }
             // 5. accumulate (mrqcof.c:106-136)
             if constexpr (kPipe) {
-                accumulate_tile_tc<NT>(ob, s, np, start + t0, conv, conv_sig, tcs);
+                accumulate_tile_tc<NT>(ob, s, np, start + t0, conv, conv_sig, tcs, true);
                 if (++tiles_since_flush == kTilesPerFlush) {
                     tc_alpha_flush<NT>(ob, s, M, bv, tcs);
                     tiles_since_flush = 0;
@@ -1389,7 +1422,7 @@ __device__ void evaluate(const DevObject &ob, const FitConfig &cfg, const SlotLa
             }
             __syncthreads();
             if constexpr (kPipe) {
-                accumulate_tile_tc<NT>(ob, s, np, start + t0, false, conv_sig, tcs);
+                accumulate_tile_tc<NT>(ob, s, np, start + t0, false, conv_sig, tcs, false);
                 if (++tiles_since_flush == kTilesPerFlush) {
                     tc_alpha_flush<NT>(ob, s, M, bv, tcs);
                     tiles_since_flush = 0;
@@ -1518,15 +1551,18 @@ __device__ int gauss_jordan(double *A, double *b, int n, double *col, int *ipiv,
 //
 // Columns are taken two at a time, with one pair of look-ahead.  Every FP64
 // instruction holds its sub-partition's FP64 unit for the whole warp, so the
-// serial chain of a pivot (warp 0) and the bulk of the trailing update (the
-// warps of sub-partitions 1..3) run on different sub-partitions at the same
-// time: while the workers apply pair j to the columns beyond pair j + 2, warp
-// 0 applies it to pair j + 2 alone and factors that pair -- one CTA barrier
-// per pair.  The 2 x 2 pivot takes its two reciprocal square roots (of the
-// leading element and of the block's determinant) in one lane-parallel
-// sequence.  The back substitution runs on warp 0 with b in registers and
-// the rows of L pre-scaled by their reciprocal diagonal.  Returns 2 when a
-// pivot is not positive.
+// serial chain of a pivot and the bulk of the trailing update run on
+// different sub-partitions at the same time.  While pair j is applied to
+// the columns beyond pair j + 2 (the workers: warps of sub-partitions 1..3
+// but warp 1), warp 0 applies it to the 2 x 2 block of pair j + 2 and to
+// its two rows of b and factors the block, and warp 1 applies it to the
+// rest of pair j + 2's columns and scales them once warp 0 has published
+// the pivot (a named barrier of the two warps) -- one CTA barrier per pair.
+// The 2 x 2 pivot takes its two reciprocal square roots (of the leading
+// element and of the block's determinant) in one lane-parallel sequence.
+// The back substitution runs on warp 0 with b in registers and the rows of
+// L pre-scaled by their reciprocal diagonal.  Returns 2 when a pivot is not
+// positive.
 __device__ inline void chol_pivot_pair(double *A, double *b, int n, int j, double *col, double *flag, int lane)
 {
     const bool two = j + 1 < n;
@@ -1566,15 +1602,47 @@ __device__ inline void chol_pivot_pair(double *A, double *b, int n, int j, doubl
     }
 }
 
+// The 2 x 2 block [a bq; bq c] of pair (j, j + 1) and its rows bj, bj1 of
+// b, already updated, in registers of every lane of warp 0: stores 1/L_jj,
+// 1/L_j+1,j+1 (col), L_j+1,j and y (b); the columns below are scaled by the
+// helper warp.
+__device__ inline void chol_pivot_block(double a, double bq, double c, double bj, double bj1, double *A, double *b,
+                                        int n, int j, bool two, double *col, double *flag, int lane)
+{
+    const double x = lane == 1 ? fma(a, c, -(bq * bq)) : a;
+    const bool okx = x > 0.0;
+    const double r = okx ? rsqrt(x) : 0.0;
+    const unsigned okm = __ballot_sync(0xffffffffu, okx);
+    const double i0 = __shfl_sync(0xffffffffu, r, 0);
+    const double rd = __shfl_sync(0xffffffffu, r, 1);
+    const double u = lane == 1 ? bq : lane == 2 ? bj : a;
+    double v = u * i0;
+    if (lane == 3) v *= rd;
+    const double l10 = __shfl_sync(0xffffffffu, v, 1);
+    const double y0 = __shfl_sync(0xffffffffu, v, 2);
+    const double i1 = __shfl_sync(0xffffffffu, v, 3);
+    const bool ok = (okm & 1u) && (!two || (okm & 2u));
+    if (lane == 0) {
+        *flag = ok ? 1.0 : 0.0;
+        col[j] = i0;
+        b[j] = y0;
+        if (two) {
+            col[j + 1] = i1;
+            b[j + 1] = (bj1 - l10 * y0) * i1;
+            A[(j + 1) * n + j] = l10;
+        }
+    }
+}
+
 template <int NT>
 __device__ int cholesky_solve(double *A, double *b, int n, double *col, double *flag)
 {
-    static_assert(NT % 128 == 0, "whole warps on every sub-partition");
+    static_assert(NT % 128 == 0 && NT >= 256, "whole warps on every sub-partition");
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    // trailing-update workers: the warps of sub-partitions 1..3
-    constexpr int kWorkers = NT / 128 * 3 * 32;
-    const bool worker = (warp & 3) != 0;
-    const int wtid = ((warp >> 2) * 3 + (warp & 3) - 1) * 32 + lane;
+    // trailing-update workers: the warps of sub-partitions 1..3 but warp 1
+    constexpr int kWorkers = (NT / 128 * 3 - 1) * 32;
+    const bool worker = (warp & 3) != 0 && warp != 1;
+    const int wtid = ((warp >> 2) * 3 + (warp & 3) - 2) * 32 + lane;
     __syncthreads();
     if (warp == 0) chol_pivot_pair(A, b, n, 0, col, flag, lane);
     __syncthreads();
@@ -1583,26 +1651,63 @@ __device__ int cholesky_solve(double *A, double *b, int n, double *col, double *
         // pair (j, j + 1) is factored; b[j], b[j + 1] hold its y
         const bool two = j + 1 < n;
         const int jn = j + 2;
+        const bool twon = jn + 1 < n;
+        // pair j's L in rows jn, jn + 1 and its y
+        const double p0 = A[jn * n + j], p1 = two ? A[jn * n + j + 1] : 0.0;
+        const double q0 = twon ? A[(jn + 1) * n + j] : 0.0, q1 = (twon && two) ? A[(jn + 1) * n + j + 1] : 0.0;
         if (warp == 0) {
-            // apply pair j to the next pair's columns and rows of b, then
-            // factor the next pair
-            const bool twon = jn + 1 < n;
-            const double p0 = A[jn * n + j], p1 = two ? A[jn * n + j + 1] : 0.0;
-            const double q0 = twon ? A[(jn + 1) * n + j] : 0.0, q1 = (twon && two) ? A[(jn + 1) * n + j + 1] : 0.0;
+            // the next pair's 2 x 2 block and rows of b, one value per lane
+            // (lane 0: a, 1: bq, 2: c, 3: b_jn, 4: b_jn+1), then its pivot
             const double y0 = b[j], y1 = two ? b[j + 1] : 0.0;
-            for (int i = jn + lane; i < n; i += 32) {
+            double xv = 0.0, u1 = 0.0, v1 = 0.0, u2 = 0.0, v2 = 0.0;
+            if (lane == 0) { xv = A[jn * n + jn]; u1 = p0; v1 = p0; u2 = p1; v2 = p1; }
+            if (lane == 1 && twon) { xv = A[(jn + 1) * n + jn]; u1 = q0; v1 = p0; u2 = q1; v2 = p1; }
+            if (lane == 2) { xv = twon ? A[(jn + 1) * n + jn + 1] : 1.0; u1 = q0; v1 = q0; u2 = q1; v2 = q1; }
+            if (lane == 3) { xv = b[jn]; u1 = p0; v1 = y0; u2 = p1; v2 = y1; }
+            if (lane == 4 && twon) { xv = b[jn + 1]; u1 = q0; v1 = y0; u2 = q1; v2 = y1; }
+            const double xu = xv - u1 * v1 - u2 * v2;
+            const double a = __shfl_sync(0xffffffffu, xu, 0);
+            const double bq = __shfl_sync(0xffffffffu, xu, 1);
+            const double cc = __shfl_sync(0xffffffffu, xu, 2);
+            const double bj = __shfl_sync(0xffffffffu, xu, 3);
+            const double bj1 = __shfl_sync(0xffffffffu, xu, 4);
+            chol_pivot_block(a, bq, cc, bj, bj1, A, b, n, jn, twon, col, flag, lane);
+            asm volatile("bar.arrive 1, 64;" ::: "memory");
+        } else if (warp == 1) {
+            // the rest of the next pair's columns: update now, scale once
+            // warp 0 has published the pivot
+            const int i = jn + 2 + lane, i2 = i + 32;
+            double c0 = 0, c1 = 0, d0 = 0, d1 = 0;
+            if (i < n) {
                 const double li0 = A[i * n + j], li1 = two ? A[i * n + j + 1] : 0.0;
-                A[i * n + jn] = A[i * n + jn] - li0 * p0 - li1 * p1;
-                if (i > jn) A[i * n + jn + 1] = A[i * n + jn + 1] - li0 * q0 - li1 * q1;
+                c0 = A[i * n + jn] - li0 * p0 - li1 * p1;
+                if (twon) c1 = A[i * n + jn + 1] - li0 * q0 - li1 * q1;
             }
-            if (lane < (twon ? 2 : 1)) {
-                const int i = jn + lane;
-                double vb = b[i] - A[i * n + j] * y0;
-                if (two) vb -= A[i * n + j + 1] * y1;
-                b[i] = vb;
+            if (i2 < n) {
+                const double li0 = A[i2 * n + j], li1 = two ? A[i2 * n + j + 1] : 0.0;
+                d0 = A[i2 * n + jn] - li0 * p0 - li1 * p1;
+                if (twon) d1 = A[i2 * n + jn + 1] - li0 * q0 - li1 * q1;
             }
-            __syncwarp();
-            chol_pivot_pair(A, b, n, jn, col, flag, lane);
+            asm volatile("bar.sync 1, 64;" ::: "memory");
+            const double i0 = col[jn];
+            const double i1 = twon ? col[jn + 1] : 0.0, l10 = twon ? A[(jn + 1) * n + jn] : 0.0;
+            if (i < n) {
+                const double a0 = c0 * i0;
+                A[i * n + jn] = a0;
+                if (twon) A[i * n + jn + 1] = (c1 - a0 * l10) * i1;
+            }
+            if (i2 < n) {
+                const double a0 = d0 * i0;
+                A[i2 * n + jn] = a0;
+                if (twon) A[i2 * n + jn + 1] = (d1 - a0 * l10) * i1;
+            }
+            for (int r = i2 + 32; r < n; r += 32) {   // n > 66: the remaining rows, unpipelined
+                const double li0 = A[r * n + j], li1 = two ? A[r * n + j + 1] : 0.0;
+                const double e0 = A[r * n + jn] - li0 * p0 - li1 * p1;
+                const double a0 = e0 * i0;
+                A[r * n + jn] = a0;
+                if (twon) A[r * n + jn + 1] = (A[r * n + jn + 1] - li0 * q0 - li1 * q1 - a0 * l10) * i1;
+            }
         } else if (worker) {
             // apply pair j to the columns beyond the next pair
             const int j2 = j + 4;
