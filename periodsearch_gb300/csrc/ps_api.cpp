@@ -623,7 +623,7 @@ ps_status upload_object(std::unique_ptr<ps_ctx> &c, ps_ctx **out)
     c->rel_rows = c->plan[c->opt.form].rel_rows;
     c->smem = c->plan[c->opt.form].smem;
     c->slots = c->plan[c->opt.form].slots;
-    c->scratch_stride = static_cast<size_t>(std::max(o.max_rel_points, 1)) * (o.ma + 1);
+    c->scratch_stride = static_cast<size_t>(std::max(o.max_rel_points, 1)) * psg::rel_row_stride(o.ma);
     c->scratch_stride = (c->scratch_stride + 31) & ~size_t(31);
     PSG_CUDA(cp, cudaMalloc(&c->d_scratch, c->scratch_stride * c->slots * sizeof(double)));
     PSG_CUDA(cp, cudaMalloc(&c->d_queue, 256));

@@ -114,6 +114,10 @@ constexpr int kMisc = 40;
 constexpr size_t kTcAlphaOperands = 32768;   // tensor-core alpha/beta operands: two 128 x 32 TF32 tiles
 
 
+// Parked row of a relative lightcurve's point (scratch): the ma model-row
+// entries, the model value, and two values the second pass prepares.
+PSG_HD constexpr int rel_row_stride(int ma) { return ma + 3; }
+
 // dsph_smem: the mixed form keeps the FP32 basis Dsph[F][C] in shared memory
 // for the whole launch (it is read once per point tile by every warp).
 // rel_rows > 0: the rows of relative lightcurves (up to rel_rows points)
@@ -185,7 +189,7 @@ PSG_HD inline SlotLayout make_layout(int form, int ma, int mfit, int nfac, int n
     L.accs = form == PS_FORM_MIXED ? take(64 * sizeof(float)) : 0;
     L.davef = form == PS_FORM_MIXED ? take(static_cast<size_t>(ma) * sizeof(float)) : 0;
     L.bmat = take(32 * rs);
-    L.rels = rel_rows > 0 ? take(static_cast<size_t>(rel_rows) * (ma + 1) * rs) : 0;
+    L.rels = rel_rows > 0 ? take(static_cast<size_t>(rel_rows) * rel_row_stride(ma) * rs) : 0;
     L.bytes = o;
     return L;
 }

@@ -1037,6 +1037,7 @@ __device__ void evaluate(const DevObject &ob, const FitConfig &cfg, const SlotLa
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int F = ob.nfac, C = ob.ncoef, ma = ob.ma, mf = ob.mfit, P = L.P;
     const int wcols = L.wcols;
+    const int RW = rel_row_stride(ma);   // parked row of a relative lightcurve
     const R *nxR, *nyR, *nzR, *dareaR;
     const R *dsphR;
     if constexpr (kFP64) {
@@ -1289,6 +1290,17 @@ __device__ void evaluate(const DevObject &ob, const FitConfig &cfg, const SlotLa
                 // here on warp 15 while thread 0 issues the contraction
                 // (same per-point values and reduction as in the
                 // accumulation itself)
+                if (rel && warp == NT / 32 - 1) {
+                    // relative lightcurve: park the model value with the
+                    // row and add the tile to the lightcurve sum
+                    double y = 0;
+                    if (jp < np) {
+                        y = s.ym[jp];
+                        scratch[static_cast<size_t>(t0 + jp) * RW + ma] = R(y);
+                    }
+                    y = warp_sum(y);
+                    if (lane == 0) s.misc[M_AVE] += y;
+                }
                 if (!rel && warp == NT / 32 - 1) {
                     double c2 = 0;
                     if (jp < np) {
@@ -1322,13 +1334,17 @@ __device__ void evaluate(const DevObject &ob, const FitConfig &cfg, const SlotLa
             }
             if (rel) {
                 // 4a. lightcurve sums and a copy of the rows (mrqcof.c:51-88)
-                R *dst = scratch + static_cast<size_t>(t0) * (ma + 1);
+                // (on the tensor-core path warp 15 has parked the model
+                // values and summed them during the contraction; the FP64
+                // column sums run on sub-partitions 2 and 3)
+                R *dst = scratch + static_cast<size_t>(t0) * RW;
                 for (int e = tid; e < np * ma; e += NT) {
                     int p = e / ma, l = e - p * ma;
-                    dst[static_cast<size_t>(p) * (ma + 1) + l] = s.J[e];
+                    dst[static_cast<size_t>(p) * RW + l] = s.J[e];
                 }
-                if (tid < np) dst[static_cast<size_t>(tid) * (ma + 1) + ma] = R(s.ym[tid]);
-                for (int l = tid; l < ma; l += NT) {
+                if (!kPipe && tid < np) dst[static_cast<size_t>(tid) * RW + ma] = R(s.ym[tid]);
+                for (int l = kPipe ? tid - 64 : tid; l < ma; l += NT) {
+                    if (l < 0) break;
                     if constexpr (kFP64) {
                         double d = s.dave[l];
                         for (int p = 0; p < np; p++) d = d + s.J[p * ma + l];
@@ -1346,7 +1362,7 @@ __device__ void evaluate(const DevObject &ob, const FitConfig &cfg, const SlotLa
                         for (int p = 0; p < np; p++) av = av + s.ym[p];
                         s.misc[M_AVE] = av;
                     }
-                } else if (warp == 0) {
+                } else if (!kPipe && warp == 0) {
                     const double v = warp_sum(lane < np ? s.ym[lane] : 0.0);
                     if (lane == 0) s.misc[M_AVE] += v;
                 }
@@ -1383,14 +1399,54 @@ __device__ void evaluate(const DevObject &ob, const FitConfig &cfg, const SlotLa
             __syncthreads();
         }
         const double inv_ave = kFP64 ? 0.0 : s.misc[M_INVAVE];
+        if constexpr (kPipe) {
+            // The per-point FP64 work of the whole lightcurve at once, one
+            // tile per warp (the tiles' FP64 chains on different
+            // sub-partitions): renormalisation factor coef and y/ave into
+            // the row's columns 0 (unused by the renormalised row) and ma,
+            // residual and weight into ma + 1 and ma + 2; the tiles' chi^2
+            // sums are added in tile order (16 tiles a round).
+            for (int r0 = 0; r0 * P < npts; r0 += NT / 32) {
+                const int tt = r0 + warp;
+                const int p = tt * P + lane;
+                double c2 = 0;
+                if (lane < P && p < npts) {
+                    const int q = start + p;
+                    R *row = scratch + static_cast<size_t>(p) * RW;
+                    const double yt = static_cast<double>(row[ma]);
+                    const double coef = ob.sig[q] * npts * inv_ave;
+                    const double ym = coef * yt;
+                    const double sig2i = ob.sig2i[q];
+                    const double wg = ob.weight[q];
+                    const double dy = ob.bright[q] - ym;
+                    row[0] = static_cast<float>(coef);
+                    row[ma] = static_cast<float>(yt * inv_ave);
+                    row[ma + 1] = static_cast<float>(dy);
+                    row[ma + 2] = static_cast<float>(sig2i * wg);
+                    c2 = dy * dy * sig2i * wg;
+                }
+                c2 = warp_sum(c2);
+                if (lane == 0) s.red[warp] = c2;
+                __syncthreads();
+                if (tid == 0)
+                    for (int w = 0; w < NT / 32 && (r0 + w) * P < npts; w++) s.misc[M_CHISQ] += s.red[w];
+                if ((r0 + NT / 32) * P < npts) __syncthreads();
+            }
+        }
         for (int t0 = 0; t0 < npts; t0 += P) {
             const int np = min(P, npts - t0);
-            const R *src = scratch + static_cast<size_t>(t0) * (ma + 1);
+            const R *src = scratch + static_cast<size_t>(t0) * RW;
             // model values of the tile in FP64 (the FP64 form keeps its own
-            // values; the mixed form parks them as FP32)
-            if (tid < np) {
+            // values; the mixed form parks them as FP32); on the tensor-core
+            // path they were prepared above, and the tile's residuals and
+            // weights go where the accumulation reads them
+            if (kPipe && tid < np) {
+                s.accs[tid] = static_cast<float>(src[static_cast<size_t>(tid) * RW + ma + 1]);
+                s.accs[32 + tid] = static_cast<float>(src[static_cast<size_t>(tid) * RW + ma + 2]);
+            }
+            if (!kPipe && tid < np) {
                 const int q = start + t0 + tid;
-                const double yt = static_cast<double>(src[static_cast<size_t>(tid) * (ma + 1) + ma]);
+                const double yt = static_cast<double>(src[static_cast<size_t>(tid) * RW + ma]);
                 double coef, ytr;
                 if constexpr (kFP64) {
                     coef = ob.sig[q] * npts / ave;
@@ -1405,16 +1461,19 @@ __device__ void evaluate(const DevObject &ob, const FitConfig &cfg, const SlotLa
                     s.accs[32 + tid] = static_cast<float>(ytr);    // accumulation reuses it
                 }
             }
-            __syncthreads();
+            if constexpr (!kPipe) __syncthreads();
             for (int e = tid; e < np * ma; e += NT) {
                 const int p = e / ma, l = e - p * ma;
-                const R v = src[static_cast<size_t>(p) * (ma + 1) + l];
+                const R v = src[static_cast<size_t>(p) * RW + l];
                 R out;
                 if constexpr (kFP64) {
                     const int q = start + t0 + p;
                     const double coef = ob.sig[q] * npts / ave;
-                    const double yt = src[static_cast<size_t>(p) * (ma + 1) + ma];
+                    const double yt = src[static_cast<size_t>(p) * RW + ma];
                     out = coef * (v - yt * s.dave[l] / ave);
+                } else if constexpr (kPipe) {
+                    const R *row = src + static_cast<size_t>(p) * RW;
+                    out = row[0] * (v - row[ma] * s.davef[l]);
                 } else {
                     out = s.accs[p] * (v - s.accs[32 + p] * s.davef[l]);
                 }
@@ -1422,7 +1481,7 @@ __device__ void evaluate(const DevObject &ob, const FitConfig &cfg, const SlotLa
             }
             __syncthreads();
             if constexpr (kPipe) {
-                accumulate_tile_tc<NT>(ob, s, np, start + t0, false, conv_sig, tcs, false);
+                accumulate_tile_tc<NT>(ob, s, np, start + t0, false, conv_sig, tcs, true);
                 if (++tiles_since_flush == kTilesPerFlush) {
                     tc_alpha_flush<NT>(ob, s, M, bv, tcs);
                     tiles_since_flush = 0;
