@@ -319,6 +319,11 @@ ps_status ps_scan_learned(ps_ctx *ctx, double conw_r, int64_t n_lo, int64_t n_hi
  * completion was not observed within the wait limit. */
 ps_status ps_tc_selftest(int32_t device, const float *A, const float *B, int32_t K, float *D);
 
+/* The same with FP16 operands (tcgen05 kind::f16, two elements per Tensor
+ * Memory column, K = 16 per MMA): A and B rounded to FP16 on the device, K a
+ * multiple of 16 up to 960. */
+ps_status ps_tc_selftest_f16(int32_t device, const float *A, const float *B, int32_t K, float *D);
+
 /* ---- the reference's prepared state (CUDA port host calls) ---- */
 
 /* One object as the reference's main() holds it after reading and

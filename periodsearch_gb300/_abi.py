@@ -153,6 +153,8 @@ SIGNATURES = {
     "ps_screen": (C.c_int, [_CTX, C.c_double, C.c_int64, C.c_int64, C.POINTER(C.c_float), C.POINTER(Fit)]),
     "ps_tc_selftest": (C.c_int, [C.c_int32, C.POINTER(C.c_float), C.POINTER(C.c_float), C.c_int32,
                                  C.POINTER(C.c_float)]),
+    "ps_tc_selftest_f16": (C.c_int, [C.c_int32, C.POINTER(C.c_float), C.POINTER(C.c_float), C.c_int32,
+                                 C.POINTER(C.c_float)]),
     "ps_prepare_state": (C.c_int, [C.POINTER(State), C.POINTER(Options), C.POINTER(C.c_void_p)]),
     "ps_precalc_step": (C.c_int, [_CTX, C.POINTER(C.c_double), C.POINTER(C.c_int32)]),
     "ps_autotune": (C.c_int, [_CTX, C.c_double, C.c_int32, C.c_int32, C.POINTER(TuneReport)]),

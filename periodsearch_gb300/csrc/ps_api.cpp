@@ -538,7 +538,7 @@ ps_status upload_object(std::unique_ptr<ps_ctx> &c, ps_ctx **out)
         alpha_pt[q] = std::acos(ex[q] * sx[q] + ey[q] * sy[q] + ez[q] * sz[q]);
     }
     // FP32 point geometry of the mixed form, two float4 per point: Earth
-    // direction and phase angle, Sun direction
+    // direction and phase angle, Sun direction and time
     std::vector<float> geo_f(static_cast<size_t>(o.ndata) * 8);
     for (int q = 0; q < o.ndata; q++) {
         float *g = &geo_f[static_cast<size_t>(q) * 8];
@@ -549,7 +549,7 @@ ps_status upload_object(std::unique_ptr<ps_ctx> &c, ps_ctx **out)
         g[4] = static_cast<float>(sx[q]);
         g[5] = static_cast<float>(sy[q]);
         g[6] = static_cast<float>(sz[q]);
-        g[7] = 0.f;
+        g[7] = static_cast<float>(o.tim[q]);
     }
     std::vector<double> sig2i(o.ndata);
     for (int q = 0; q < o.ndata; q++) sig2i[q] = 1 / (o.sig[q] * o.sig[q]);

@@ -145,9 +145,21 @@ cudaError_t for_mixed(int ncoef, int dsph_smem, Fn fn)
 
 }  // namespace
 
+// The dynamic shared-memory limit is a property of the kernel function (per
+// device), shared by every context of the process: it is only ever raised,
+// so that a context whose slots need less shared memory does not lower it
+// under another context's launches.
 int set_kernel_smem(int form, size_t smem, int ncoef, int dsph_smem)
 {
-    cudaError_t e;
+    static std::mutex mu;
+    static int raised[64][2][3] = {};
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return static_cast<int>(e);
+    const int ku = form == PS_FORM_FP64 ? 1 : (dsph_smem == kBasisTensor ? 0 : (ncoef <= 64 ? 1 : 2));
+    std::lock_guard<std::mutex> lock(mu);
+    int *cur = (dev >= 0 && dev < 64 && (form == PS_FORM_FP64 || form == PS_FORM_MIXED)) ? &raised[dev][form][ku] : nullptr;
+    if (cur && *cur >= static_cast<int>(smem)) return 0;
     const int bytes = static_cast<int>(smem);
     if (form == PS_FORM_FP64) {
         e = cudaFuncSetAttribute(fit_kernel<PS_FORM_FP64, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
@@ -166,6 +178,7 @@ int set_kernel_smem(int form, size_t smem, int ncoef, int dsph_smem)
     } else {
         return static_cast<int>(cudaErrorInvalidValue);
     }
+    if (e == cudaSuccess && cur) *cur = bytes;
     return static_cast<int>(e);
 }
 

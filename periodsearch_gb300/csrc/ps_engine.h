@@ -108,7 +108,7 @@ PSG_HD constexpr int threads_of()
 {
     return FORM == PS_FORM_MIXED ? 512 : 256;
 }
-constexpr int kPointStride = 32;   // reals of per-point set-up
+constexpr int kPointStride = 33;   // reals of per-point set-up (odd: a warp with one point per lane hits 32 banks)
 constexpr int kRedStride = 8;      // doubles of per-point facet sums
 constexpr int kMisc = 40;
 constexpr size_t kTcAlphaOperands = 32768;   // tensor-core alpha/beta operands: two 128 x 32 TF32 tiles
@@ -117,6 +117,12 @@ constexpr size_t kTcAlphaOperands = 32768;   // tensor-core alpha/beta operands:
 // Parked row of a relative lightcurve's point (scratch): the ma model-row
 // entries, the model value, and two values the second pass prepares.
 PSG_HD constexpr int rel_row_stride(int ma) { return ma + 3; }
+
+// Facets of the tensor-core contraction, padded with empty facets to a
+// multiple of 32 (four facet quarters of whole 8-facet core matrices; a
+// multiple of the 16 facets of one FP16 MMA).
+PSG_HD constexpr int tc_kpad(int nfac) { return (nfac + 31) & ~31; }
+
 
 // dsph_smem: the mixed form keeps the FP32 basis Dsph[F][C] in shared memory
 // for the whole launch (it is read once per point tile by every warp).
@@ -170,15 +176,16 @@ PSG_HD inline SlotLayout make_layout(int form, int ma, int mfit, int nfac, int n
         // The same region then stages the alpha accumulator; the alpha/beta
         // operands (two 128 x 32 TF32 tiles) have their own region, so that
         // their MMAs overlap the next tile's facet stage.
-        const size_t tile = static_cast<size_t>(P) * nfac * sizeof(float);
+        // (FP16 elements, facets padded to tc_kpad)
+        const size_t tile = static_cast<size_t>(P) * tc_kpad(nfac) * 2;
         const size_t readback = 128 * 65 * sizeof(float);
         L.bhi = take(2 * tile > readback ? 2 * tile : readback);
         L.blo = L.bhi + tile;
         L.aop = take(kTcAlphaOperands);
         L.tcm = take(32);
         L.pt2 = take(static_cast<size_t>(P) * kPointStride * rs);
-        L.fac = take(static_cast<size_t>(nfac) * 4 * sizeof(float));
-        L.ag = take(static_cast<size_t>(nfac) * 2 * sizeof(float));
+        L.fac = take(static_cast<size_t>(tc_kpad(nfac)) * 4 * sizeof(float));
+        L.ag = take(static_cast<size_t>(tc_kpad(nfac)) * 2 * sizeof(float));
         L.fpart = take(4 * static_cast<size_t>(P) * 9 * sizeof(float));
     } else {
         L.bhi = L.blo = L.tcm = 0;
@@ -215,7 +222,7 @@ int occupancy_slots(int form, size_t smem, int ncoef, int dsph_smem, int *per_sm
 // accumulator columns within 512, and 32-point tiles.
 PSG_HD inline bool tensor_basis_ok(int nfac, int ncoef, int mfit, int P)
 {
-    return ncoef <= 64 && mfit <= 63 && nfac % 8 == 0 && ((nfac + 31) & ~31) + 64 + 128 <= 512 && P == 32;
+    return ncoef <= 64 && mfit <= 63 && (((tc_kpad(nfac) >> 1) + 31) & ~31) + 64 + 128 <= 512 && P == 32;
 }
 int measure_fma_peaks(double *fp64_tflops, double *fp32_tflops, void *stream);
 // Learned early stop (ps_mlp.cu).

@@ -159,7 +159,8 @@ enum : int {
     M_TRIG = 8,    // cos/sin of the pole angles beta, lambda (4 doubles)
     M_PIV = 12,    // pivot broadcast of the solvers (2 doubles + status)
     M_RED = 16,    // 16 doubles of block-reduction scratch
-    M_LM = 32      // 4 doubles: lambda, ochisq, dev, iter_diff of the fit, broadcast from thread 0
+    M_LM = 32,     // 4 doubles: lambda, ochisq, dev, iter_diff of the fit, broadcast from thread 0
+    M_WEXP = 36    // tensor-core path: exponent of the evaluation's W scale
 };
 
 // Row j of packed lower-triangle element e (j*(j+1)/2 <= e < (j+1)*(j+2)/2),
@@ -198,22 +199,26 @@ __device__ inline double block_sum(double v, double *red)
 
 // Rotation phase omega*t + phi0 reduced to [0, 2*pi).  The FP64 form rounds
 // the product and the sum separately and reduces with fmod, as the
-// reference does (matrix.c:21-22); the mixed form reduces with a two-part
-// 2*pi (the product rounded once), which is exact to ~1e-16 rad.
-template <int FORM>
-__device__ inline double rotation_phase(double omg, double t, double phi0)
+// reference does (matrix.c:21-22).  The mixed form reduces in FP64 with a
+// two-part 2*pi (the product rounded once), exact to ~1e-16 rad, and hands
+// the phase on in FP32 (its only use is the FP32 cos/sin), so the final
+// wrap into [0, 2*pi) runs in FP32.
+__device__ inline double rotation_phase_fp64(double omg, double t, double phi0)
 {
-    if constexpr (FORM == PS_FORM_FP64) {
-        return fmod(__dadd_rn(__dmul_rn(omg, t), phi0), kTwoPi);
-    } else {
-        const double x = fma(omg, t, phi0);
-        const double q = floor(x * kInvTwoPi);
-        double f = fma(-q, kTwoPiHi, x);
-        f = fma(-q, kTwoPiLo, f);
-        if (f < 0) f += kTwoPi;
-        if (f >= kTwoPi) f -= kTwoPi;
-        return f;
-    }
+    return fmod(__dadd_rn(__dmul_rn(omg, t), phi0), kTwoPi);
+}
+
+__device__ inline float rotation_phase_mixed(double omg, double t, double phi0)
+{
+    constexpr float kTwoPiF = 6.28318548f;   // 2*pi rounded to FP32
+    const double x = fma(omg, t, phi0);
+    const double q = floor(x * kInvTwoPi);
+    double f = fma(-q, kTwoPiHi, x);
+    f = fma(-q, kTwoPiLo, f);
+    float ff = static_cast<float>(f);
+    if (ff < 0.f) ff += kTwoPiF;
+    if (ff >= kTwoPiF) ff -= kTwoPiF;
+    return ff;
 }
 
 // Lit-facet terms of the Lommel-Seeliger + Lambert law (bright.c:65-74,
@@ -451,10 +456,97 @@ __device__ void contract_mixed(Smem<PS_FORM_MIXED> &s, const float *dsph, int np
 // Point set-up of observation q (bright.c:27-57, phasec.c, matrix.c): the
 // rotated Earth and Sun directions with their beta/lambda/omega derivatives,
 // the phase function and its derivatives, into pt[0..27].
+// Mixed-form point set-up in three parts, so that the tensor-core path can
+// run the first two on different warps (the FP64 rotation phase holds its
+// sub-partition's FP64 unit for the whole warp): setup_mixed_phase (the
+// rotation phase and its cos and sin into pt[28], pt[29]), setup_mixed_geo
+// (the phase function into pt[24..27], the products of the pole matrix and
+// its beta/lambda derivatives with the Earth and Sun vectors into pt[0..17],
+// the time into pt[30]) and setup_mixed_rotate (the rotation about the spin
+// axis into pt[0..23], by the thread that ran setup_mixed_geo).  The
+// rotation fm commutes out of the products (matrix.c): with u = B ee,
+// e = fm u, de/dbeta = fm (dB/dbeta ee), de/dlambda = fm (dB/dlambda ee) and
+// de/domega = (dfm/domega) u = t (e_y, -e_x, 0); the same for the Sun vector.
+__device__ inline void setup_mixed_phase(const DevObject &ob, const FitConfig &cfg, int q, double omg, float *pt)
+{
+    const float f = rotation_phase_mixed(omg, ob.tim[q], cfg.phi0);
+    float sf, cf;
+    sincosf(f, &sf, &cf);
+    pt[28] = cf;
+    pt[29] = sf;
+}
+
+__device__ inline void setup_mixed_geo(const DevObject &ob, int q, const float *bm, float *pt)
+{
+    const float4 g0 = ob.geo_f[2 * q], g1 = ob.geo_f[2 * q + 1];
+    const float ee[3] = {g0.x, g0.y, g0.z}, e0v[3] = {g1.x, g1.y, g1.z};
+    const float alpha = g0.w;
+    const float php0 = bm[27], php1 = bm[28], php2 = bm[29];
+    const float inv_w = 1.f / php1;
+    const float ex = expf(-alpha * inv_w);
+    pt[24] = 1 + php0 * ex + php2 * alpha;
+    pt[25] = ex;
+    pt[26] = php0 * ex * alpha * (inv_w * inv_w);
+    pt[27] = alpha;
+    pt[30] = g1.w;
+#pragma unroll
+    for (int m = 0; m < 3; m++) {
+#pragma unroll
+        for (int k = 0; k < 3; k++) {
+            const float *row = bm + 9 * m + 3 * k;
+            pt[6 * m + k] = row[0] * ee[0] + row[1] * ee[1] + row[2] * ee[2];
+            pt[6 * m + 3 + k] = row[0] * e0v[0] + row[1] * e0v[1] + row[2] * e0v[2];
+        }
+    }
+}
+
+__device__ inline void setup_mixed_rotate(float *pt)
+{
+    const float cf = pt[28], sf = pt[29], t = pt[30];
+    float u[18];
+#pragma unroll
+    for (int i = 0; i < 18; i++) u[i] = pt[i];
+#pragma unroll
+    for (int m = 0; m < 3; m++) {
+        const float *ue = u + 6 * m, *us = u + 6 * m + 3;
+        const float r0 = cf * ue[0] + sf * ue[1], r1 = cf * ue[1] - sf * ue[0];
+        const float s0 = cf * us[0] + sf * us[1], s1 = cf * us[1] - sf * us[0];
+        if (m == 0) {
+            pt[0] = r0;
+            pt[1] = r1;
+            pt[2] = ue[2];
+            pt[3] = s0;
+            pt[4] = s1;
+            pt[5] = us[2];
+            // d/domega (column 2 of de and de0)
+            pt[6 + 2] = t * r1;
+            pt[6 + 3 + 2] = -t * r0;
+            pt[6 + 6 + 2] = 0.f;
+            pt[15 + 2] = t * s1;
+            pt[15 + 3 + 2] = -t * s0;
+            pt[15 + 6 + 2] = 0.f;
+        } else {
+            const int j = m - 1;   // column 0: d/dbeta, 1: d/dlambda
+            pt[6 + j] = r0;
+            pt[6 + 3 + j] = r1;
+            pt[6 + 6 + j] = ue[2];
+            pt[15 + j] = s0;
+            pt[15 + 3 + j] = s1;
+            pt[15 + 6 + j] = us[2];
+        }
+    }
+}
+
 template <int FORM>
 __device__ inline void setup_point(const DevObject &ob, const FitConfig &cfg, int q, double omg,
                                    const typename RealOf<FORM>::T *bm, typename RealOf<FORM>::T *pt)
 {
+    if constexpr (FORM == PS_FORM_MIXED) {
+        setup_mixed_phase(ob, cfg, q, omg, pt);
+        setup_mixed_geo(ob, q, bm, pt);
+        setup_mixed_rotate(pt);
+        return;
+    }
     const typename RealOf<FORM>::T *B = bm, *DB0 = bm + 9, *DB1 = bm + 18;
     const typename RealOf<FORM>::T php0 = bm[27], php1 = bm[28], php2 = bm[29];
     using R = typename RealOf<FORM>::T;
@@ -489,61 +581,8 @@ __device__ inline void setup_point(const DevObject &ob, const FitConfig &cfg, in
         ex = expf(-alpha * inv_w);
     }
     const R scale = 1 + php0 * ex + php2 * alpha;
-    const double f = rotation_phase<FORM>(omg, td, cfg.phi0);
-    R cf, sf;
-    if constexpr (kFP64) {
-        cf = cos(f);
-        sf = sin(f);
-    } else {
-        sincosf(static_cast<float>(f), &sf, &cf);
-    }
-    if constexpr (!kFP64) {
-        // The rotation fm about the spin axis (matrix.c) commutes out of the
-        // products: with u = B ee, e = fm u, de/dbeta = fm (dB/dbeta ee),
-        // de/dlambda = fm (dB/dlambda ee) and de/domega = (dfm/domega) u =
-        // t (e_y, -e_x, 0); the same for the Sun vector.
-        const R *src[3] = {B, DB0, DB1};
-#pragma unroll
-        for (int m = 0; m < 3; m++) {
-            R u[3], u0[3];
-#pragma unroll
-            for (int k = 0; k < 3; k++) {
-                const R *row = src[m] + 3 * k;
-                u[k] = row[0] * ee[0] + row[1] * ee[1] + row[2] * ee[2];
-                u0[k] = row[0] * e0v[0] + row[1] * e0v[1] + row[2] * e0v[2];
-            }
-            const R r0 = cf * u[0] + sf * u[1], r1 = cf * u[1] - sf * u[0];
-            const R s0 = cf * u0[0] + sf * u0[1], s1 = cf * u0[1] - sf * u0[0];
-            if (m == 0) {
-                pt[0] = r0;
-                pt[1] = r1;
-                pt[2] = u[2];
-                pt[3] = s0;
-                pt[4] = s1;
-                pt[5] = u0[2];
-                // d/domega (column 2 of de and de0)
-                pt[6 + 2] = t * r1;
-                pt[6 + 3 + 2] = -t * r0;
-                pt[6 + 6 + 2] = R(0);
-                pt[15 + 2] = t * s1;
-                pt[15 + 3 + 2] = -t * s0;
-                pt[15 + 6 + 2] = R(0);
-            } else {
-                const int j = m - 1;   // column 0: d/dbeta, 1: d/dlambda
-                pt[6 + j] = r0;
-                pt[6 + 3 + j] = r1;
-                pt[6 + 6 + j] = u[2];
-                pt[15 + j] = s0;
-                pt[15 + 3 + j] = s1;
-                pt[15 + 6 + j] = u0[2];
-            }
-        }
-        pt[24] = scale;
-        pt[25] = ex;
-        pt[26] = php0 * ex * alpha * (inv_w * inv_w);
-        pt[27] = alpha;
-        return;
-    }
+    const double f = rotation_phase_fp64(omg, td, cfg.phi0);
+    const R cf = cos(f), sf = sin(f);
     const R fm[9] = {cf, sf, R(0), -sf, cf, R(0), R(0), R(0), R(1)};
     const R dfm[9] = {-t * sf, t * cf, R(0), -t * cf, -t * sf, R(0), R(0), R(0), R(0)};
     R tm[9], d0[9], d1[9], d2[9];
@@ -603,10 +642,11 @@ __device__ inline void setup_point(const DevObject &ob, const FitConfig &cfg, in
 constexpr uint32_t kTcWaitTries = 1u << 22;   // mbarrier polls before a wait gives up
 constexpr int kErrTcTimeout = 16;             // ps_fit.err_code of a fit cut short by a failed wait
 
-// Tensor Memory columns: the basis [0, F), the contraction accumulator
-// [tc_dcol, tc_dcol + 64) (column p: A W_hi^T for point p, 32 + p: A W_lo^T)
-// and the alpha accumulator [tc_acol, tc_acol + 128).
-__device__ inline uint32_t tc_dcol(int F) { return static_cast<uint32_t>((F + 31) & ~31); }
+// Tensor Memory columns: the basis [0, Fp/2) (FP16 pairs of facets, Fp =
+// tc_kpad(F)), the contraction accumulator [tc_dcol, tc_dcol + 64) (column
+// p: A W_hi^T for point p, 32 + p: A W_lo^T) and the alpha accumulator
+// [tc_acol, tc_acol + 128).
+__device__ inline uint32_t tc_dcol(int F) { return static_cast<uint32_t>(((tc_kpad(F) >> 1) + 31) & ~31); }
 __device__ inline uint32_t tc_acol(int F) { return tc_dcol(F) + 64; }
 
 __device__ inline uint32_t tc_cols(int F)
@@ -620,6 +660,7 @@ __device__ inline uint32_t tc_cols(int F)
 // same values).
 struct TcState {
     uint32_t tbase = 0;     // Tensor Memory base address
+    int basis_exp = 0;      // the basis is held scaled by 2^basis_exp
     uint32_t phase = 0;     // parity of the contraction barrier's next phase
     uint32_t aphase = 0;    // parity of the alpha barrier's next phase
     bool apending = false;  // alpha MMAs committed and not waited for
@@ -642,47 +683,70 @@ __device__ inline void tc_alpha_wait(Smem<PS_FORM_MIXED> &s, TcState &t)
     tc::fence_after_sync();
 }
 
-// Allocates the CTA's Tensor Memory and loads A = [Dsph_hi^T; Dsph_lo^T]:
-// lane m < 64 holds the TF32 rounding of coefficient m's basis column, lane
-// 64 + m the TF32 rounding of what remains of it (taken from the FP64 basis);
-// column i is facet i.  Returns the Tensor Memory base address.
+// Allocates the CTA's Tensor Memory, initialises the barriers, stages the
+// facet constants (zero for the padding facets) and loads the basis into
+// Tensor Memory as A = [Dsph_hi^T; Dsph_lo^T]: lane m < 64 holds coefficient
+// m, lane 64 + m what remains of it, both FP16 and scaled by 2^basis_exp
+// (the largest magnitude just below 2^14, so that the low parts stay normal
+// FP16 numbers for elements down to 2^-3 of it); column j holds facets 2j
+// and 2j + 1.
 template <int NT>
-__device__ uint32_t tc_setup(const DevObject &ob, Smem<PS_FORM_MIXED> &s)
+__device__ void tc_setup(const DevObject &ob, Smem<PS_FORM_MIXED> &s, TcState &t)
 {
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    const int F = ob.nfac, C = ob.ncoef;
+    const int F = ob.nfac, C = ob.ncoef, Fp = tc_kpad(F);
     if (warp == 0) tc::tmem_alloc(s.tslot, tc_cols(F));
     if (tid == 0) {
         tc::mbar_init(s.mbar, 1);
         tc::mbar_init(s.mbar2, 1);
         *s.abort = 0;
     }
+    double mx = 0.0;
+    for (int e = tid; e < F * C; e += NT) mx = fmax(mx, fabs(ob.dsph[e]));
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+    if (lane == 0) s.red[warp] = mx;
     tc::fence_before_sync();
     __syncthreads();
     tc::fence_after_sync();
+    mx = 0.0;
+    for (int w = 0; w < NT / 32; w++) mx = fmax(mx, s.red[w]);
+    const int bexp = (mx > 0.0 && mx < 1e300) ? 13 - ilogb(mx) : 0;
+    const double bscale = ldexp(1.0, bexp);
     const uint32_t tbase = *s.tslot;
-    for (int i = tid; i < F; i += NT) s.fac[i] = make_float4(ob.nx_f[i], ob.ny_f[i], ob.nz_f[i], ob.darea_f[i]);
+    for (int i = tid; i < Fp; i += NT) {
+        s.fac[i] = i < F ? make_float4(ob.nx_f[i], ob.ny_f[i], ob.nz_f[i], ob.darea_f[i])
+                         : make_float4(0.f, 0.f, 0.f, 0.f);
+        if (i >= F) s.ag[i] = make_float2(0.f, 0.f);
+    }
     for (int i = tid; i < static_cast<int>(kTcAlphaOperands / 4); i += NT) reinterpret_cast<uint32_t *>(s.aop)[i] = 0;
     if (warp < 4) {
         const int m = warp * 32 + lane, c = m & 63;
         const bool low = m >= 64;
         const uint32_t row = tbase + (static_cast<uint32_t>(warp * 32) << 16);
-        for (int k0 = 0; k0 < F; k0 += 8) {
+        for (int j0 = 0; j0 < Fp / 2; j0 += 8) {
             uint32_t v[8];
 #pragma unroll
             for (int j = 0; j < 8; j++) {
-                const double d = c < C ? ob.dsph[static_cast<size_t>(k0 + j) * C + c] : 0.0;
-                const uint32_t hi = tc::to_tf32(static_cast<float>(d));
-                v[j] = low ? tc::to_tf32(static_cast<float>(d - static_cast<double>(__uint_as_float(hi)))) : hi;
+                float h[2];
+#pragma unroll
+                for (int u = 0; u < 2; u++) {
+                    const int i = 2 * (j0 + j) + u;
+                    const double d = (c < C && i < F) ? ob.dsph[static_cast<size_t>(i) * C + c] * bscale : 0.0;
+                    const float hi = tc::round_f16(static_cast<float>(d));
+                    h[u] = low ? static_cast<float>(d - static_cast<double>(hi)) : hi;
+                }
+                v[j] = tc::pack_f16x2(h[0], h[1]);
             }
-            tc::tmem_st8(row + static_cast<uint32_t>(k0), v);
+            tc::tmem_st8(row + static_cast<uint32_t>(j0), v);
         }
         tc::tmem_wait_st();
     }
     tc::fence_before_sync();
     __syncthreads();
     tc::fence_after_sync();
-    return tbase;
+    t.tbase = tbase;
+    t.basis_exp = bexp;
 }
 
 // Releases the Tensor Memory.  After an abandoned wait the MMAs in flight
@@ -698,49 +762,52 @@ __device__ void tc_teardown(Smem<PS_FORM_MIXED> &s, const TcState &t, int F)
     if ((threadIdx.x >> 5) == 0) tc::tmem_dealloc(t.tbase, tc_cols(F));
 }
 
-// Issues D = A [W_hi; W_lo]^T for the tile as F/8 MMAs of 128 x 64 x 8 (one
-// MMA costs the issuing thread about the same for N = 32 and N = 64) and a
-// commit to the barrier.  The facet stage has written the operand: TF32
-// high parts of W in rows 0..31, low parts in rows 32..63, canonical K-major
-// layout (8-row x 4-facet core matrices, K-adjacent ones 128 bytes apart).
+// Issues D = A [W_hi; W_lo]^T for the tile as Fp/16 FP16 MMAs of 128 x 64 x
+// 16 (one MMA costs the issuing thread about the same for N = 32 and N = 64,
+// and the same for K = 8 TF32 and K = 16 FP16 elements) and a commit to the
+// barrier.  The facet stage has written the operand: FP16 high parts of W
+// in rows 0..31, low parts in rows 32..63, canonical K-major layout (8-row x
+// 8-facet core matrices, K-adjacent ones 128 bytes apart).
 template <int NT>
 __device__ void contract_tc_issue(Smem<PS_FORM_MIXED> &s, int F, TcState &t)
 {
     const int tid = threadIdx.x;
-    const int kcs = F >> 2;
+    const int Fp = tc_kpad(F), kcs = Fp >> 3;
     const uint32_t tbase = t.tbase;
     tc::fence_proxy_async();
     tc::fence_before_sync();
     __syncthreads();
     if (tid == 0 && !*s.abort) {
         tc::fence_after_sync();
-        const uint32_t idesc = tc::idesc_tf32(128, 64);
+        const uint32_t idesc = tc::idesc_f16(128, 64);
         const uint32_t sbo = static_cast<uint32_t>(kcs) * 128;
         const uint32_t bh = tc::smem_u32(s.bhi), d = tbase + tc_dcol(F);
-        for (int k8 = 0; k8 < F / 8; k8++) {
-            const uint32_t a = tbase + static_cast<uint32_t>(k8) * 8, off = static_cast<uint32_t>(k8) * 256;
-            tc::mma_tf32_ts(d, a, tc::smem_desc(bh + off, 128, sbo), idesc, k8 > 0);
+        for (int ks = 0; ks < Fp / 16; ks++) {
+            const uint32_t a = tbase + static_cast<uint32_t>(ks) * 8, off = static_cast<uint32_t>(ks) * 256;
+            tc::mma_f16_ts(d, a, tc::smem_desc(bh + off, 128, sbo), idesc, ks > 0);
         }
         tc::mma_commit(s.mbar);
     }
 }
 
 // Facet stage of the tensor-core path (bright.c:59-120).  Warp w takes
-// points 8 (w % 4) .. +7 (lane / 4) and the facet quarter w / 4, lanes of a
-// point stepping through the quarter four facets apart (lane % 4), so that
-// one warp store covers a whole 8-point x 4-facet core matrix of the MMA
-// operand [W_hi; W_lo].  The per-point sums (brightness, rotation and
+// points 8 (w % 4) .. +7 (lane / 4) and the facet quarter w / 4, each lane
+// of a point taking two adjacent facets of every 8 (lane % 4), so that one
+// warp store covers a whole 8-point x 8-facet core matrix of the MMA
+// operand [W_hi; W_lo] (FP16 pairs, W scaled by wscale = 2^k so that the
+// evaluation's largest W is just below 2^14).  The per-point sums (brightness, rotation and
 // scattering derivatives) are reduced over the four lanes and then over the
 // quarters into s.fpart[p * 9 + 0..5] (FP32: the J columns they feed are).  The tile's operand region must be free (previous
 // MMAs waited for).
 template <int NT>
-__device__ void facet_stage_tc(const DevObject &ob, Smem<PS_FORM_MIXED> &s, int np, float cl, float cls)
+__device__ void facet_stage_tc(const DevObject &ob, Smem<PS_FORM_MIXED> &s, int np, float cl, float cls,
+                               float wscale)
 {
     static_assert(NT == 512, "16 warps: 4 point groups x 4 facet quarters");
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    const int F = ob.nfac, kcs = F >> 2;
-    const int quarter = warp >> 2, p = (warp & 3) * 8 + (lane >> 2), fl = lane & 3;
-    const int fq = (kcs + 3) & ~3;     // facets per quarter, a multiple of 4
+    const int kcs = tc_kpad(ob.nfac) >> 3;   // 8-facet core matrices per row group
+    const int cq = kcs >> 2;                 // per facet quarter
+    const int quarter = warp >> 2, g = warp & 3, p = g * 8 + (lane >> 2), fl = lane & 3;
     float e1 = 0, e2 = 0, e3 = 0, f1 = 0, f2 = 0, f3 = 0;
     if (p < np) {
         const float *pt = s.pt + p * kPointStride;
@@ -757,38 +824,39 @@ __device__ void facet_stage_tc(const DevObject &ob, Smem<PS_FORM_MIXED> &s, int 
     // Earth and Sun vectors), so the facet loop accumulates U and V.
     float br = 0, dcl = 0, dcls = 0, ux = 0, uy = 0, uz = 0, vx = 0, vy = 0, vz = 0;
     uint32_t *bh = reinterpret_cast<uint32_t *>(s.bhi), *bl = reinterpret_cast<uint32_t *>(s.blo);
-    const int i_end = min(F, (quarter + 1) * fq);
-#pragma unroll 2
-    for (int i0 = quarter * fq; i0 < i_end; i0 += 4) {
-        const int i = i0 + fl;
-        const float4 n = s.fac[i];
-        const float mu = e1 * n.x + e2 * n.y + e3 * n.z;
-        const float mu0 = f1 * n.x + f2 * n.y + f3 * n.z;
-        // Branch-free: the 8 points of a warp see different lit facets, so a
-        // branch would diverge on almost every step (and a warp-uniform skip
-        // of groups unlit for all 8 points measured slower: it breaks the
-        // two-step interleave); unlit facets get zero area (every term
-        // vanishes) and a safe denominator.
-        const bool lit = mu > float(kTinyMu) && mu0 > float(kTinyMu);
-        const float2 ag = s.ag[i];
-        const float ax = lit ? ag.x : 0.f, ay = lit ? ag.y : 0.f;
-        const LitTerms<float, PS_FORM_MIXED> lt(lit ? mu : 1.f, lit ? mu0 : 1.f, cl, cls);
-        br = fmaf(ax, lt.sv, br);
-        const float w = ay * lt.sv;
-        const float cu = ax * lt.dsmu, cv = ax * lt.dsmu0;
-        ux = fmaf(cu, n.x, ux);
-        uy = fmaf(cu, n.y, uy);
-        uz = fmaf(cu, n.z, uz);
-        vx = fmaf(cv, n.x, vx);
-        vy = fmaf(cv, n.y, vy);
-        vz = fmaf(cv, n.z, vz);
-        dcl = fmaf(mu * mu0, ax, dcl);
-        dcls = fmaf(ax, lt.dcls_w, dcls);
-        const uint32_t hi = tc::to_tf32(w);
-        const uint32_t lo = tc::to_tf32(w - __uint_as_float(hi));
-        const int cm = (warp & 3) * kcs + (i0 >> 2);    // core matrix (8-point group, 4-facet group)
-        bh[cm * 32 + lane] = hi;
-        bl[cm * 32 + lane] = lo;
+    for (int kc = quarter * cq; kc < (quarter + 1) * cq; kc++) {
+        const int i = kc * 8 + 2 * fl;
+        float wv[2];
+#pragma unroll
+        for (int u = 0; u < 2; u++) {
+            const float4 n = s.fac[i + u];
+            const float mu = e1 * n.x + e2 * n.y + e3 * n.z;
+            const float mu0 = f1 * n.x + f2 * n.y + f3 * n.z;
+            // Branch-free: the 8 points of a warp see different lit facets,
+            // so a branch would diverge on almost every step (and a
+            // warp-uniform skip of groups unlit for all 8 points measured
+            // slower); unlit and padding facets get zero area (every term
+            // vanishes) and a safe denominator.
+            const bool lit = mu > float(kTinyMu) && mu0 > float(kTinyMu);
+            const float2 ag = s.ag[i + u];
+            const float ax = lit ? ag.x : 0.f, ay = lit ? ag.y : 0.f;
+            const LitTerms<float, PS_FORM_MIXED> lt(lit ? mu : 1.f, lit ? mu0 : 1.f, cl, cls);
+            br = fmaf(ax, lt.sv, br);
+            wv[u] = ay * lt.sv * wscale;
+            const float cu = ax * lt.dsmu, cv = ax * lt.dsmu0;
+            ux = fmaf(cu, n.x, ux);
+            uy = fmaf(cu, n.y, uy);
+            uz = fmaf(cu, n.z, uz);
+            vx = fmaf(cv, n.x, vx);
+            vy = fmaf(cv, n.y, vy);
+            vz = fmaf(cv, n.z, vz);
+            dcl = fmaf(mu * mu0, ax, dcl);
+            dcls = fmaf(ax, lt.dcls_w, dcls);
+        }
+        const float h0 = tc::round_f16(wv[0]), h1 = tc::round_f16(wv[1]);
+        const int cm = g * kcs + kc;    // core matrix (8-point group, 8-facet group)
+        bh[cm * 32 + lane] = tc::pack_f16x2(h0, h1);
+        bl[cm * 32 + lane] = tc::pack_f16x2(wv[0] - h0, wv[1] - h1);
     }
     float v[9] = {br, dcl, dcls, ux, uy, uz, vx, vy, vz};
 #pragma unroll
@@ -830,22 +898,27 @@ __device__ void facet_stage_tc(const DevObject &ob, Smem<PS_FORM_MIXED> &s, int 
 }
 
 // Convexity rows (conv.c:12-29) on the tensor-core path: rows 0..2 of the
-// MMA operand hold Darea g n_c split into TF32 high and low parts; the
-// residuals sum Area n_c in FP64.
+// MMA operand hold Darea g n_c (scaled by wscale) split into FP16 high and
+// low parts; the residuals sum Area n_c in FP64.
 template <int NT>
-__device__ void conv_rows_tc(const DevObject &ob, Smem<PS_FORM_MIXED> &s)
+__device__ void conv_rows_tc(const DevObject &ob, Smem<PS_FORM_MIXED> &s, float wscale)
 {
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    const int F = ob.nfac;
+    const int F = ob.nfac, half = tc_kpad(F) >> 1;
     uint32_t *bh = reinterpret_cast<uint32_t *>(s.bhi), *bl = reinterpret_cast<uint32_t *>(s.blo);
-    for (int e = tid; e < 3 * F; e += NT) {
-        const int c = e / F, i = e - c * F;
+    for (int e = tid; e < 3 * half; e += NT) {
+        const int c = e / half, i = 2 * (e - c * half);
         const double *nc = (c == 0) ? ob.nx : (c == 1) ? ob.ny : ob.nz;
-        const float w = static_cast<float>(ob.darea[i] * s.gv[i] * nc[i]);
-        const uint32_t hi = tc::to_tf32(w);
-        const int off = (i >> 2) * 32 + c * 4 + (i & 3);
-        bh[off] = hi;
-        bl[off] = tc::to_tf32(w - __uint_as_float(hi));
+        float w[2], h[2];
+#pragma unroll
+        for (int u = 0; u < 2; u++) {
+            w[u] = i + u < F ? static_cast<float>(ob.darea[i + u] * s.gv[i + u] * nc[i + u]) * wscale : 0.f;
+            h[u] = tc::round_f16(w[u]);
+        }
+        // row c of the first 8-row group, facets i, i + 1 of core matrix i / 8
+        const int off = (i >> 3) * 32 + c * 4 + ((i & 7) >> 1);
+        bh[off] = tc::pack_f16x2(h[0], h[1]);
+        bl[off] = tc::pack_f16x2(w[0] - h[0], w[1] - h[1]);
     }
     if (warp < 3) {
         const double *nc = (warp == 0) ? ob.nx : (warp == 1) ? ob.ny : ob.nz;
@@ -857,12 +930,13 @@ __device__ void conv_rows_tc(const DevObject &ob, Smem<PS_FORM_MIXED> &s)
 }
 
 // Waits for the tile's MMAs, stages the accumulator (lane m = row m) in
-// shared memory and writes J[p][k] = Scale_p (D[k][p] + D[k][32 + p] +
-// D[64 + k][p] + D[64 + k][32 + p]): basis high and low parts times W high
-// and low parts.  A wait that gives up sets the abort flag; the caller ends
+// shared memory and writes J[p][k] = Scale_p jscale (D[k][p] + D[k][32 + p]
+// + D[64 + k][p] + D[64 + k][32 + p]): basis high and low parts times W high
+// and low parts, jscale undoing the operands' power-of-two scales.  A wait that gives up sets the abort flag; the caller ends
 // the fit.
 template <int NT>
-__device__ void contract_tc_finish(Smem<PS_FORM_MIXED> &s, int np, int F, int C, int ma, bool conv, TcState &t)
+__device__ void contract_tc_finish(Smem<PS_FORM_MIXED> &s, int np, int F, int C, int ma, bool conv, TcState &t,
+                                   float jscale)
 {
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const uint32_t tbase = t.tbase;
@@ -895,7 +969,7 @@ __device__ void contract_tc_finish(Smem<PS_FORM_MIXED> &s, int np, int F, int C,
     __syncthreads();
     for (int e = tid; e < np * C; e += NT) {
         const int p = e / C, k = e - p * C;
-        const float sc = conv ? 1.f : s.pt[p * kPointStride + 24];
+        const float sc = (conv ? 1.f : s.pt[p * kPointStride + 24]) * jscale;
         const float *xh = X + k * 65, *xl = X + (64 + k) * 65;
         s.J[p * ma + k] = sc * ((xh[p] + xh[32 + p]) + (xl[p] + xl[32 + p]));
     }
@@ -1106,10 +1180,26 @@ __device__ void evaluate(const DevObject &ob, const FitConfig &cfg, const SlotLa
             v = R(lane == 31 ? s.misc[M_CL] : a[lane == 30 ? C + 7 : C + 3 + (lane - 27)]);
         }
         s.bmat[lane] = v;
+    } else if (kPipe && warp == 1) {
+        // Scale of the contraction operand W = Darea g s: s <= |cl| +
+        // |cls| / 2 (mu mu0 <= 1, mu mu0 / (mu + mu0) <= 1/2), and the
+        // convexity rows' W <= Darea g, so 2^k puts the evaluation's largest
+        // W just below 2^14.
+        float mx = 0.f;
+        for (int i = lane; i < F; i += 32) mx = fmaxf(mx, s.ag[i].y);
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+        const float wmax =
+            mx * fmaxf(1.f, fabsf(static_cast<float>(s.misc[M_CL])) + 0.5f * fabsf(static_cast<float>(a[C + 7])));
+        if (lane == 0) s.misc[M_WEXP] = (wmax > 0.f && wmax < 1e30f) ? static_cast<double>(13 - ilogbf(wmax)) : 0.0;
     }
     const double omg = a[C + 2];
     __syncthreads();
     const R cls = s.bmat[30], cl = s.bmat[31];
+    // power-of-two scales of the tensor-core contraction's operands
+    const int wexp = kPipe ? static_cast<int>(s.misc[M_WEXP]) : 0;
+    const float wscale = ldexpf(1.f, wexp);
+    const float jscale = ldexpf(1.f, -(wexp + tcs.basis_exp));
 
     const double conv_sig = cfg.conv_sig;
     float accA[kAccPerThread];
@@ -1159,7 +1249,7 @@ __device__ void evaluate(const DevObject &ob, const FitConfig &cfg, const SlotLa
                 // barrier after the previous tile's contraction ordered it)
                 if constexpr (!kPipe) __syncthreads();
                 // 2. facet stage (bright.c:59-120), one warp per point
-                if constexpr (kPipe) facet_stage_tc<NT>(ob, s, np, cl, cls);
+                if constexpr (kPipe) facet_stage_tc<NT>(ob, s, np, cl, cls, wscale);
                 else
                 for (int p = warp; p < np; p += NT / 32) {
                     const R *pt = s.pt + p * kPointStride;
@@ -1214,7 +1304,7 @@ __device__ void evaluate(const DevObject &ob, const FitConfig &cfg, const SlotLa
                     }
                 }
             } else if constexpr (kPipe) {
-                conv_rows_tc<NT>(ob, s);
+                conv_rows_tc<NT>(ob, s, wscale);
             } else {
                 // convexity rows (conv.c:12-29): W = Darea g n_c, residual =
                 // sum Area n_c (the residual in FP64 in both forms)
@@ -1287,8 +1377,9 @@ __device__ void evaluate(const DevObject &ob, const FitConfig &cfg, const SlotLa
             if constexpr (kPipe) {
                 // the accumulation's per-point FP64 work (weights, residuals,
                 // chi^2) of an absolute lightcurve or of the convexity rows,
-                // here on warp 15 while thread 0 issues the contraction
-                // (same per-point values and reduction as in the
+                // here on warp 14 (its own copy of the model value) while
+                // thread 0 issues the contraction and warp 15 writes the J
+                // columns (same per-point values and reduction as in the
                 // accumulation itself)
                 if (rel && warp == NT / 32 - 1) {
                     // relative lightcurve: park the model value with the
@@ -1301,15 +1392,18 @@ __device__ void evaluate(const DevObject &ob, const FitConfig &cfg, const SlotLa
                     y = warp_sum(y);
                     if (lane == 0) s.misc[M_AVE] += y;
                 }
-                if (!rel && warp == NT / 32 - 1) {
+                if (!rel && warp == NT / 32 - 2) {
                     double c2 = 0;
-                    if (jp < np) {
-                        const int q = start + t0 + jp;
+                    if (lane < np) {
+                        const int q = start + t0 + lane;
+                        const double ymv = conv ? s.red[lane * kRedStride]
+                                                : static_cast<double>(s.fpart[lane * 9] *
+                                                                      s.pt[lane * kPointStride + 24]);
                         const double sig2i = conv ? 1 / (conv_sig * conv_sig) : ob.sig2i[q];
                         const double wg = ob.weight[q];
-                        const double dy = (conv ? 0.0 : ob.bright[q]) - s.ym[jp];
-                        s.accs[jp] = static_cast<float>(dy);
-                        s.accs[32 + jp] = static_cast<float>(sig2i * wg);
+                        const double dy = (conv ? 0.0 : ob.bright[q]) - ymv;
+                        s.accs[lane] = static_cast<float>(dy);
+                        s.accs[32 + lane] = static_cast<float>(sig2i * wg);
                         c2 = dy * dy * sig2i * wg;
                     }
                     c2 = warp_sum(c2);
@@ -1318,13 +1412,26 @@ __device__ void evaluate(const DevObject &ob, const FitConfig &cfg, const SlotLa
             }
             bool next_setup = false;
             if constexpr (kPipe) {
-                // point set-up of the next tile into the other buffer
+                // point set-up of the next tile into the other buffer, one
+                // point per lane: the rotation phase on warp 1, the
+                // geometry on warp 2, then the rotation on warp 2 once warp
+                // 1 has published the phase (a named barrier of the two)
                 const int nlc = t0 + P < npts ? lc : lc + 1, nt0 = t0 + P < npts ? t0 + P : 0;
                 next_setup = nlc < ob.n_lc - 1;   // the last lightcurve is the convexity rows
-                if (next_setup && pipe_sp >= 0 && pipe_sp < min(P, ob.lc_npts[nlc] - nt0))
-                    setup_point<FORM>(ob, cfg, ob.lc_start[nlc] + nt0 + pipe_sp, omg, s.bmat,
-                                      s.pt2 + pipe_sp * kPointStride);
-                contract_tc_finish<NT>(s, np, F, C, ma, conv, tcs);
+                if (next_setup && (warp == 1 || warp == 2)) {
+                    const bool have = lane < min(P, ob.lc_npts[nlc] - nt0);
+                    const int q = ob.lc_start[nlc] + nt0 + lane;
+                    float *ptn = s.pt2 + lane * kPointStride;
+                    if (warp == 1) {
+                        if (have) setup_mixed_phase(ob, cfg, q, omg, ptn);
+                        asm volatile("bar.arrive 2, 64;" ::: "memory");
+                    } else {
+                        if (have) setup_mixed_geo(ob, q, s.bmat, ptn);
+                        asm volatile("bar.sync 2, 64;" ::: "memory");
+                        if (have) setup_mixed_rotate(ptn);
+                    }
+                }
+                contract_tc_finish<NT>(s, np, F, C, ma, conv, tcs, jscale);
             }
             __syncthreads();
             if (next_setup) {
@@ -2079,7 +2186,7 @@ __global__ void __launch_bounds__(threads_of<FORM>(), 1)
     if (s.dsph)
         for (int e = threadIdx.x; e < ob.nfac * ob.ncoef; e += NT) s.dsph[e] = ob.dsph_f[e];
     TcState tcs;
-    if constexpr (kTensor) tcs.tbase = tc_setup<NT>(ob, s);
+    if constexpr (kTensor) tc_setup<NT>(ob, s, tcs);
     R *scratch = L.rels ? reinterpret_cast<R *>(smem + L.rels)
                         : reinterpret_cast<R *>(w.scratch + static_cast<size_t>(blockIdx.x) * w.scratch_stride);
     __shared__ long long next;
@@ -2120,7 +2227,7 @@ __global__ void __launch_bounds__(threads_of<FORM>(), 1) eval_kernel(DevObject o
     if (s.dsph)
         for (int e = threadIdx.x; e < ob.nfac * ob.ncoef; e += NT) s.dsph[e] = ob.dsph_f[e];
     TcState tcs;
-    if constexpr (kTensor) tcs.tbase = tc_setup<NT>(ob, s);
+    if constexpr (kTensor) tc_setup<NT>(ob, s, tcs);
     for (int i = threadIdx.x; i < ob.ma; i += NT) s.cg[i] = cg[i];
     __syncthreads();
     R *rows = L.rels ? reinterpret_cast<R *>(smem + L.rels) : reinterpret_cast<R *>(scratch);

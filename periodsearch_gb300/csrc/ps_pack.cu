@@ -28,7 +28,7 @@ __global__ void __launch_bounds__(threads_of<FORM>(), 1) pack_kernel(FitWork w, 
     if (s.dsph)
         for (int e = threadIdx.x; e < s_ob.nfac * s_ob.ncoef; e += NT) s.dsph[e] = s_ob.dsph_f[e];
     TcState tcs;
-    if constexpr (kTensor) tcs.tbase = tc_setup<NT>(s_ob, s);
+    if constexpr (kTensor) tc_setup<NT>(s_ob, s, tcs);
     R *scratch = reinterpret_cast<R *>(w.scratch + static_cast<size_t>(blockIdx.x) * w.scratch_stride);
     for (;;) {
         if (threadIdx.x == 0) next = static_cast<long long>(atomicAdd(w.queue, 1ULL));
@@ -62,14 +62,27 @@ cudaError_t for_pack(int form, int ncoef, int dsph_smem, Fn fn)
 
 }  // namespace
 
+// Raises (never lowers) the kernel's dynamic shared-memory limit on the
+// current device, as set_kernel_smem does.
 int set_pack_smem(int form, size_t smem, int ncoef, int dsph_smem)
 {
     if (form != PS_FORM_FP64 && form != PS_FORM_MIXED) return static_cast<int>(cudaErrorInvalidValue);
-    return static_cast<int>(for_pack(form, ncoef, dsph_smem, [&](auto f, auto ku) {
-        constexpr int FORM = decltype(f)::value, KU = decltype(ku)::value;
+    static std::mutex mu;
+    static int raised[64][2][3] = {};
+    int dev = 0;
+    const cudaError_t de = cudaGetDevice(&dev);
+    if (de != cudaSuccess) return static_cast<int>(de);
+    const int ku = form == PS_FORM_FP64 ? 1 : (dsph_smem == kBasisTensor ? 0 : (ncoef <= 64 ? 1 : 2));
+    std::lock_guard<std::mutex> lock(mu);
+    int *cur = (dev >= 0 && dev < 64) ? &raised[dev][form][ku] : nullptr;
+    if (cur && *cur >= static_cast<int>(smem)) return 0;
+    const cudaError_t e = for_pack(form, ncoef, dsph_smem, [&](auto f, auto kk) {
+        constexpr int FORM = decltype(f)::value, KU = decltype(kk)::value;
         return cudaFuncSetAttribute(pack_kernel<FORM, KU>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                     static_cast<int>(smem));
-    }));
+    });
+    if (e == cudaSuccess && cur) *cur = static_cast<int>(smem);
+    return static_cast<int>(e);
 }
 
 int launch_pack(int form, const FitWork &w, int ncoef, int grid, int P, size_t smem, int dsph_smem, void *stream)

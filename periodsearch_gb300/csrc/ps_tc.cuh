@@ -1,14 +1,17 @@
 // ps_tc.cuh -- Blackwell tensor-core primitives (tcgen05, Tensor Memory,
 // mbarrier) as inline PTX for sm_103a, used by the mixed form's shape
-// contraction.
+// contraction and normal-matrix accumulation.
 //
 // The contraction is J^T[k][p] = sum_i Dsph^T[k][i] W^T[i][p] with A =
 // Dsph^T (coefficients x facets) resident in Tensor Memory and B = W (points
 // x facets, K-major) staged in shared memory in the no-swizzle canonical
 // layout: 8-row x 16-byte core matrices, K-adjacent core matrices 128 bytes
-// apart (leading byte offset), 8-row groups K/4 core matrices apart (stride
-// byte offset).  The accumulator D (M = 128 lanes x N columns, FP32) lives
-// in Tensor Memory and is read back with tcgen05.ld (row m = lane m).
+// apart (leading byte offset), 8-row groups K/e core matrices apart (stride
+// byte offset; e = 4 TF32 or 8 FP16 elements per 16 bytes).  In Tensor
+// Memory a 32-bit column holds one TF32 element or two FP16 elements (the
+// lower K index in the low half).  The accumulator D (M = 128 lanes x N
+// columns, FP32) lives in Tensor Memory and is read back with tcgen05.ld
+// (row m = lane m).
 #pragma once
 
 #include <cstdint>
@@ -27,6 +30,17 @@ __host__ __device__ constexpr uint32_t idesc_tf32(int M, int N)
            | (static_cast<uint32_t>(M >> 4) << 24);   // M / 16
 }
 
+// Instruction descriptor of tcgen05.mma.kind::f16 with FP16 A and B: D
+// FP32, both K-major, dense, shape M x N (K = 16 per MMA).
+__host__ __device__ constexpr uint32_t idesc_f16(int M, int N)
+{
+    return (1u << 4)                                  // D format F32
+           | (0u << 7)                                // A format F16
+           | (0u << 10)                               // B format F16
+           | (static_cast<uint32_t>(N >> 3) << 17)    // N / 8
+           | (static_cast<uint32_t>(M >> 4) << 24);   // M / 16
+}
+
 // Shared-memory matrix descriptor, no swizzle: start address, leading byte
 // offset (K direction) and stride byte offset (M/N direction), all >> 4;
 // bits 46-48 hold the fixed value 0b001.
@@ -41,6 +55,12 @@ __device__ inline uint64_t smem_desc(uint32_t saddr, uint32_t lbo, uint32_t sbo)
 __host__ __device__ inline uint32_t canon_offset(int r, int k, int K)
 {
     return static_cast<uint32_t>(((r >> 3) * (K >> 2) + (k >> 2)) * 128 + (r & 7) * 16 + (k & 3) * 4);
+}
+
+// The same for 16-bit elements (8 per core-matrix row).
+__host__ __device__ inline uint32_t canon_offset16(int r, int k, int K)
+{
+    return static_cast<uint32_t>(((r >> 3) * (K >> 3) + (k >> 3)) * 128 + (r & 7) * 16 + (k & 7) * 2);
 }
 
 __device__ inline uint32_t smem_u32(const void *p) { return static_cast<uint32_t>(__cvta_generic_to_shared(p)); }
@@ -97,6 +117,17 @@ __device__ inline void mma_tf32_ts(uint32_t d_taddr, uint32_t a_taddr, uint64_t 
         : "memory");
 }
 
+__device__ inline void mma_f16_ts(uint32_t d_taddr, uint32_t a_taddr, uint64_t b_desc, uint32_t idesc,
+                                  uint32_t accumulate)
+{
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "setp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::f16 [%0], [%1], %2, %3, p;\n\t}" ::"r"(d_taddr),
+        "r"(a_taddr), "l"(b_desc), "r"(idesc), "r"(accumulate)
+        : "memory");
+}
+
 // ---- MMA: D[tmem] (+)= A[smem] * B[smem]^T, issued by one thread ----
 __device__ inline void mma_tf32_ss(uint32_t d_taddr, uint64_t a_desc, uint64_t b_desc, uint32_t idesc,
                                    uint32_t accumulate)
@@ -141,6 +172,38 @@ __device__ inline bool mbar_wait(uint64_t *mbar, uint32_t parity, uint32_t max_t
         if (done) return true;
     }
     return false;
+}
+
+// FP16 rounding (round to nearest even) of two FP32 values, packed with the
+// first (the lower K index) in the low half: cvt.f16x2 puts its first
+// source in the high half.
+__device__ inline uint32_t pack_f16x2(float k0, float k1)
+{
+    uint32_t r;
+    asm("cvt.rn.f16x2.f32 %0, %1, %2;" : "=r"(r) : "f"(k1), "f"(k0));
+    return r;
+}
+
+// x rounded to FP16 (nearest even), as an FP32 value.
+__device__ inline float round_f16(float x)
+{
+    float r;
+    asm("{\n\t.reg .b16 h;\n\tcvt.rn.f16.f32 h, %1;\n\tcvt.f32.f16 %0, h;\n\t}" : "=f"(r) : "f"(x));
+    return r;
+}
+
+// The FP32 value of the low or high FP16 half of a packed pair.
+__device__ inline float f16_lo(uint32_t v)
+{
+    float f;
+    asm("{\n\t.reg .b16 l, h;\n\tmov.b32 {l, h}, %1;\n\tcvt.f32.f16 %0, l;\n\t}" : "=f"(f) : "r"(v));
+    return f;
+}
+__device__ inline float f16_hi(uint32_t v)
+{
+    float f;
+    asm("{\n\t.reg .b16 l, h;\n\tmov.b32 {l, h}, %1;\n\tcvt.f32.f16 %0, h;\n\t}" : "=f"(f) : "r"(v));
+    return f;
 }
 
 // TF32 rounding (round to nearest, ties away) of an FP32 value, as a bit pattern.
