@@ -91,6 +91,8 @@ struct SlotLayout {
     size_t davef;           // FP32 copy of a relative lightcurve's derivative sums (mixed form)
     size_t bmat;            // rotation matrices and phase/scattering parameters of an evaluation
     size_t rels;            // relative-lightcurve rows in shared memory, or 0 (global scratch)
+    size_t pref;            // tensor-core path: per-point data prefetched for the contraction window
+    size_t flist;           // tensor-core path: the free parameters' columns
     size_t bytes;
 };
 
@@ -111,6 +113,10 @@ PSG_HD constexpr int threads_of()
 constexpr int kPointStride = 33;   // reals of per-point set-up (odd: a warp with one point per lane hits 32 banks)
 constexpr int kRedStride = 8;      // doubles of per-point facet sums
 constexpr int kMisc = 40;
+// Prefetch area of the tensor-core path, for a 32-point tile: times (32
+// doubles), FP32 geometry (32 x 2 float4) and sig^-2, weight, brightness
+// (32 x 3 doubles).
+constexpr size_t kPrefTim = 0, kPrefGeo = 256, kPrefAcc = 1280, kPrefBytes = 2048;
 constexpr size_t kTcAlphaOperands = 32768;   // tensor-core alpha/beta operands: two 128 x 32 TF32 tiles
 
 
@@ -187,10 +193,12 @@ PSG_HD inline SlotLayout make_layout(int form, int ma, int mfit, int nfac, int n
         L.fac = take(static_cast<size_t>(tc_kpad(nfac)) * 4 * sizeof(float));
         L.ag = take(static_cast<size_t>(tc_kpad(nfac)) * 2 * sizeof(float));
         L.fpart = take(4 * static_cast<size_t>(P) * 9 * sizeof(float));
+        L.pref = take(kPrefBytes);
+        L.flist = take(static_cast<size_t>(mfit + 1) * sizeof(int));
     } else {
         L.bhi = L.blo = L.tcm = 0;
         L.pt2 = L.pt;
-        L.fac = L.ag = L.fpart = L.aop = 0;
+        L.fac = L.ag = L.fpart = L.aop = L.pref = L.flist = 0;
     }
     // 32 residuals then 32 weights, whatever the tile size
     L.accs = form == PS_FORM_MIXED ? take(64 * sizeof(float)) : 0;

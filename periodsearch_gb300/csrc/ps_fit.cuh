@@ -91,6 +91,8 @@ struct Smem {
     float2 *ag;               // per facet and evaluation: Area, Darea g
     float *fpart;             // [4][P][9] facet-sum partials of the four facet quarters
     unsigned char *aop;       // alpha/beta MMA operands
+    unsigned char *pref;      // per-point data prefetched for the contraction window
+    int *flist;               // the free parameters' columns (tensor-core path)
     uint32_t *tslot;
     int *abort;
 };
@@ -135,6 +137,8 @@ __device__ inline Smem<FORM> carve(char *base, const SlotLayout &L)
         s.ag = reinterpret_cast<float2 *>(base + L.ag);
         s.fpart = reinterpret_cast<float *>(base + L.fpart);
         s.aop = reinterpret_cast<unsigned char *>(base + L.aop);
+        s.pref = reinterpret_cast<unsigned char *>(base + L.pref);
+        s.flist = reinterpret_cast<int *>(base + L.flist);
     } else {
         s.bhi = s.blo = nullptr;
         s.mbar = s.mbar2 = nullptr;
@@ -143,6 +147,8 @@ __device__ inline Smem<FORM> carve(char *base, const SlotLayout &L)
         s.ag = nullptr;
         s.fpart = nullptr;
         s.aop = nullptr;
+        s.pref = nullptr;
+        s.flist = nullptr;
         s.abort = nullptr;
     }
     return s;
@@ -196,6 +202,24 @@ __device__ inline double block_sum(double v, double *red)
     __syncthreads();
     return t;
 }
+
+// Asynchronous global -> shared copies (cp.async, 8 or 16 bytes, both
+// addresses aligned to the size), completed by cp_async_wait_all of the
+// issuing thread.
+__device__ inline void cp_async8(void *dst_smem, const void *src)
+{
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(static_cast<uint32_t>(__cvta_generic_to_shared(dst_smem))),
+                 "l"(src)
+                 : "memory");
+}
+__device__ inline void cp_async16(void *dst_smem, const void *src)
+{
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 16;" ::"r"(static_cast<uint32_t>(__cvta_generic_to_shared(dst_smem))),
+                 "l"(src)
+                 : "memory");
+}
+__device__ inline void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+__device__ inline void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
 
 // Rotation phase omega*t + phi0 reduced to [0, 2*pi).  The FP64 form rounds
 // the product and the sum separately and reduces with fmod, as the
@@ -257,6 +281,9 @@ struct LitTerms {
 // registers and adds them to the FP64 totals every few tiles.
 constexpr int kAccPerThread = 8;    // with 512 threads: mfit <= 90
 constexpr int kTilesPerFlush = 8;
+// The tensor-core path's FP32 alpha accumulator in Tensor Memory (products
+// of TF32 high/low parts) is added to the FP64 normal matrix every 16 tiles.
+constexpr int kTcTilesPerFlush = 16;
 
 template <int FORM>
 __device__ inline void flush_partials(double *M, double *bv, int mf, float (&accA)[kAccPerThread], float &accB)
@@ -467,18 +494,17 @@ __device__ void contract_mixed(Smem<PS_FORM_MIXED> &s, const float *dsph, int np
 // rotation fm commutes out of the products (matrix.c): with u = B ee,
 // e = fm u, de/dbeta = fm (dB/dbeta ee), de/dlambda = fm (dB/dlambda ee) and
 // de/domega = (dfm/domega) u = t (e_y, -e_x, 0); the same for the Sun vector.
-__device__ inline void setup_mixed_phase(const DevObject &ob, const FitConfig &cfg, int q, double omg, float *pt)
+__device__ inline void setup_mixed_phase(double td, double omg, double phi0, float *pt)
 {
-    const float f = rotation_phase_mixed(omg, ob.tim[q], cfg.phi0);
+    const float f = rotation_phase_mixed(omg, td, phi0);
     float sf, cf;
     sincosf(f, &sf, &cf);
     pt[28] = cf;
     pt[29] = sf;
 }
 
-__device__ inline void setup_mixed_geo(const DevObject &ob, int q, const float *bm, float *pt)
+__device__ inline void setup_mixed_geo(float4 g0, float4 g1, const float *bm, float *pt)
 {
-    const float4 g0 = ob.geo_f[2 * q], g1 = ob.geo_f[2 * q + 1];
     const float ee[3] = {g0.x, g0.y, g0.z}, e0v[3] = {g1.x, g1.y, g1.z};
     const float alpha = g0.w;
     const float php0 = bm[27], php1 = bm[28], php2 = bm[29];
@@ -542,8 +568,8 @@ __device__ inline void setup_point(const DevObject &ob, const FitConfig &cfg, in
                                    const typename RealOf<FORM>::T *bm, typename RealOf<FORM>::T *pt)
 {
     if constexpr (FORM == PS_FORM_MIXED) {
-        setup_mixed_phase(ob, cfg, q, omg, pt);
-        setup_mixed_geo(ob, q, bm, pt);
+        setup_mixed_phase(ob.tim[q], omg, cfg.phi0, pt);
+        setup_mixed_geo(ob.geo_f[2 * q], ob.geo_f[2 * q + 1], bm, pt);
         setup_mixed_rotate(pt);
         return;
     }
@@ -720,6 +746,7 @@ __device__ void tc_setup(const DevObject &ob, Smem<PS_FORM_MIXED> &s, TcState &t
         if (i >= F) s.ag[i] = make_float2(0.f, 0.f);
     }
     for (int i = tid; i < static_cast<int>(kTcAlphaOperands / 4); i += NT) reinterpret_cast<uint32_t *>(s.aop)[i] = 0;
+    for (int j = tid; j < ob.mfit; j += NT) s.flist[j] = ob.free_list[j];
     if (warp < 4) {
         const int m = warp * 32 + lane, c = m & 63;
         const bool low = m >= 64;
@@ -949,29 +976,33 @@ __device__ void contract_tc_finish(Smem<PS_FORM_MIXED> &s, int np, int F, int C,
     }
     t.phase ^= 1u;
     tc::fence_after_sync();
-    // every warp reads 16 of the 64 accumulator columns of its lane quadrant
-    // (warp w may access Tensor Memory lanes 32 (w % 4) .. + 31)
-    float *X = reinterpret_cast<float *>(s.bhi);
+    // every warp reads, for 8 points of its lane quadrant's rows (warp w may
+    // access Tensor Memory lanes 32 (w % 4) .. + 31), the products with W_hi
+    // (column p) and W_lo (column 32 + p) and stages their sum Y[m][p]
+    float *Y = reinterpret_cast<float *>(s.bhi);   // [128][33]
     {
-        const int quad = warp & 3, cgrp = warp >> 2;
-        const uint32_t taddr = tbase + (static_cast<uint32_t>(quad * 32) << 16) + tc_dcol(F) + 16 * cgrp;
-        float *xr = X + (quad * 32 + lane) * 65 + 16 * cgrp;
-        uint32_t v0[8], v1[8];
-        tc::tmem_ld8(taddr, v0);
-        tc::tmem_ld8(taddr + 8, v1);
+        const int quad = warp & 3, pg = warp >> 2;
+        const uint32_t taddr = tbase + (static_cast<uint32_t>(quad * 32) << 16) + tc_dcol(F) + 8 * pg;
+        float *yr = Y + (quad * 32 + lane) * 33 + 8 * pg;
+        uint32_t vh[8], vl[8];
+        tc::tmem_ld8(taddr, vh);
+        tc::tmem_ld8(taddr + 32, vl);
         tc::tmem_wait_ld();
 #pragma unroll
-        for (int j = 0; j < 8; j++) {
-            xr[j] = __uint_as_float(v0[j]);
-            xr[8 + j] = __uint_as_float(v1[j]);
-        }
+        for (int j = 0; j < 8; j++) yr[j] = __uint_as_float(vh[j]) + __uint_as_float(vl[j]);
     }
     __syncthreads();
-    for (int e = tid; e < np * C; e += NT) {
-        const int p = e / C, k = e - p * C;
-        const float sc = (conv ? 1.f : s.pt[p * kPointStride + 24]) * jscale;
-        const float *xh = X + k * 65, *xl = X + (64 + k) * 65;
-        s.J[p * ma + k] = sc * ((xh[p] + xh[32 + p]) + (xl[p] + xl[32 + p]));
+    // J[p][k] = Scale_p jscale (Y[k][p] + Y[64 + k][p]); thread: k = tid % 64,
+    // points tid / 64 + 8 i (C <= 64 on this path)
+    {
+        const int k = tid & 63;
+        if (k < C) {
+            const float *yh = Y + k * 33, *yl = Y + (64 + k) * 33;
+            for (int p = tid >> 6; p < np; p += NT / 64) {
+                const float sc = (conv ? 1.f : s.pt[p * kPointStride + 24]) * jscale;
+                s.J[p * ma + k] = sc * (yh[p] + yl[p]);
+            }
+        }
     }
 }
 
@@ -983,10 +1014,15 @@ __device__ void contract_tc_finish(Smem<PS_FORM_MIXED> &s, int np, int F, int C,
 // of the 128 x 128 FP32 accumulator sum to alpha (and beta in column mfit)
 // at FP32 accuracy.  The accumulator stays in Tensor Memory across tiles
 // until tc_alpha_flush.  chi^2 is summed in FP64 by warp 0, unless the
-// caller has prepared the weights, residuals and chi^2 (prepared).
+// caller has prepared the weights, residuals and chi^2 (prepared).  With
+// rows (a relative lightcurve's second pass) the operands are built straight
+// from the parked rows (stride rw: renormalisation factor in column 0, y/ave
+// in ma, residual in ma + 1, weight in ma + 2), renormalising on the way
+// (mrqcof.c:90-104).
 template <int NT>
 __device__ void accumulate_tile_tc(const DevObject &ob, Smem<PS_FORM_MIXED> &s, int np, int q0pt, bool conv,
-                                   double conv_sig, TcState &t, bool prepared)
+                                   double conv_sig, TcState &t, bool prepared, const float *rows = nullptr,
+                                   int rw = 0)
 {
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int ma = ob.ma, mf = ob.mfit;
@@ -1014,25 +1050,39 @@ __device__ void accumulate_tile_tc(const DevObject &ob, Smem<PS_FORM_MIXED> &s, 
     // low parts in rows 64..127
     unsigned char *Ab = s.aop, *Bb = s.aop + 16384;
     const int rg_end = (mf + 1 + 7) >> 3;   // row groups past it stay zero (cleared at set-up)
-    for (int cm = warp; cm < 128; cm += NT / 32) {
-        const bool isB = cm >= 64;
-        const int c = cm & 63, rg = c >> 3, kc = c & 7;
-        if (rg >= rg_end) continue;
-        const int row = rg * 8 + (lane >> 2), p = kc * 4 + (lane & 3);
-        float v = 0.f;
-        if (p < np) {
-            if (row < mf) {
-                v = s.J[p * ma + ob.free_list[row]];
-                if (!isB) v *= wtp[p];
-            } else if (isB && row == mf) {
-                v = dyv[p];
+    static_assert(NT == 512, "16 warps x 4 core matrices of each operand");
+    // warp w: core matrices c = w + 16 i of both operands (row group c / 8,
+    // points 4 (c % 8) .. + 3), the same J element feeding A and B
+#pragma unroll
+    for (int i = 0; i < 4; i++) {
+        const int c = warp + 16 * i, rg = c >> 3, kc = c & 7;
+        if (rg < rg_end) {
+            const int row = rg * 8 + (lane >> 2), p = kc * 4 + (lane & 3);
+            float va = 0.f, vb = 0.f;
+            if (p < np) {
+                if (rows) {
+                    const float *r = rows + static_cast<size_t>(p) * rw;
+                    if (row < mf) {
+                        const int l = s.flist[row];
+                        vb = l == 0 ? 0.f : r[0] * (r[l] - r[ma] * s.davef[l]);
+                        va = vb * r[ma + 2];
+                    } else if (row == mf) {
+                        vb = r[ma + 1];
+                    }
+                } else if (row < mf) {
+                    vb = s.J[p * ma + s.flist[row]];
+                    va = vb * wtp[p];
+                } else if (row == mf) {
+                    vb = dyv[p];
+                }
             }
+            const uint32_t ah = tc::to_tf32(va), bh = tc::to_tf32(vb);
+            const uint32_t al = tc::to_tf32(va - __uint_as_float(ah)), bl = tc::to_tf32(vb - __uint_as_float(bh));
+            reinterpret_cast<uint32_t *>(Ab + (rg * 8 + kc) * 128)[lane] = ah;
+            reinterpret_cast<uint32_t *>(Ab + ((rg + 8) * 8 + kc) * 128)[lane] = al;
+            reinterpret_cast<uint32_t *>(Bb + (rg * 8 + kc) * 128)[lane] = bh;
+            reinterpret_cast<uint32_t *>(Bb + ((rg + 8) * 8 + kc) * 128)[lane] = bl;
         }
-        const uint32_t hi = tc::to_tf32(v);
-        const uint32_t lo = tc::to_tf32(v - __uint_as_float(hi));
-        unsigned char *base = isB ? Bb : Ab;
-        reinterpret_cast<uint32_t *>(base + (rg * 8 + kc) * 128)[lane] = hi;
-        reinterpret_cast<uint32_t *>(base + ((rg + 8) * 8 + kc) * 128)[lane] = lo;
     }
     tc::fence_proxy_async();
     tc::fence_before_sync();
@@ -1249,7 +1299,35 @@ __device__ void evaluate(const DevObject &ob, const FitConfig &cfg, const SlotLa
                 // barrier after the previous tile's contraction ordered it)
                 if constexpr (!kPipe) __syncthreads();
                 // 2. facet stage (bright.c:59-120), one warp per point
-                if constexpr (kPipe) facet_stage_tc<NT>(ob, s, np, cl, cls, wscale);
+                if constexpr (kPipe) {
+                    // prefetch for the contraction window: the next tile's
+                    // times (warp 1) and geometry (warp 2), this tile's
+                    // accumulation data (warp 14)
+                    if (warp == 14) {
+                        if (!rel && lane < np) {
+                            const int q = start + t0 + lane;
+                            double *d = reinterpret_cast<double *>(s.pref + kPrefAcc) + 3 * lane;
+                            cp_async8(d, ob.sig2i + q);
+                            cp_async8(d + 1, ob.weight + q);
+                            cp_async8(d + 2, ob.bright + q);
+                        }
+                        cp_async_commit();
+                    } else if (warp == 1 || warp == 2) {
+                        const int nlc = t0 + P < npts ? lc : lc + 1, nt0 = t0 + P < npts ? t0 + P : 0;
+                        if (nlc < ob.n_lc - 1 && lane < min(P, ob.lc_npts[nlc] - nt0)) {
+                            const int q = ob.lc_start[nlc] + nt0 + lane;
+                            if (warp == 1) {
+                                cp_async8(reinterpret_cast<double *>(s.pref + kPrefTim) + lane, ob.tim + q);
+                            } else {
+                                float4 *g = reinterpret_cast<float4 *>(s.pref + kPrefGeo) + 2 * lane;
+                                cp_async16(g, ob.geo_f + 2 * q);
+                                cp_async16(g + 1, ob.geo_f + 2 * q + 1);
+                            }
+                        }
+                        cp_async_commit();
+                    }
+                    facet_stage_tc<NT>(ob, s, np, cl, cls, wscale);
+                }
                 else
                 for (int p = warp; p < np; p += NT / 32) {
                     const R *pt = s.pt + p * kPointStride;
@@ -1394,14 +1472,16 @@ __device__ void evaluate(const DevObject &ob, const FitConfig &cfg, const SlotLa
                 }
                 if (!rel && warp == NT / 32 - 2) {
                     double c2 = 0;
+                    cp_async_wait_all();
                     if (lane < np) {
                         const int q = start + t0 + lane;
+                        const double *pa = reinterpret_cast<const double *>(s.pref + kPrefAcc) + 3 * lane;
                         const double ymv = conv ? s.red[lane * kRedStride]
                                                 : static_cast<double>(s.fpart[lane * 9] *
                                                                       s.pt[lane * kPointStride + 24]);
-                        const double sig2i = conv ? 1 / (conv_sig * conv_sig) : ob.sig2i[q];
-                        const double wg = ob.weight[q];
-                        const double dy = (conv ? 0.0 : ob.bright[q]) - ymv;
+                        const double sig2i = conv ? 1 / (conv_sig * conv_sig) : pa[0];
+                        const double wg = conv ? ob.weight[q] : pa[1];
+                        const double dy = (conv ? 0.0 : pa[2]) - ymv;
                         s.accs[lane] = static_cast<float>(dy);
                         s.accs[32 + lane] = static_cast<float>(sig2i * wg);
                         c2 = dy * dy * sig2i * wg;
@@ -1422,11 +1502,14 @@ __device__ void evaluate(const DevObject &ob, const FitConfig &cfg, const SlotLa
                     const bool have = lane < min(P, ob.lc_npts[nlc] - nt0);
                     const int q = ob.lc_start[nlc] + nt0 + lane;
                     float *ptn = s.pt2 + lane * kPointStride;
+                    cp_async_wait_all();
                     if (warp == 1) {
-                        if (have) setup_mixed_phase(ob, cfg, q, omg, ptn);
+                        if (have) setup_mixed_phase(reinterpret_cast<const double *>(s.pref + kPrefTim)[lane], omg,
+                                                    cfg.phi0, ptn);
                         asm volatile("bar.arrive 2, 64;" ::: "memory");
                     } else {
-                        if (have) setup_mixed_geo(ob, q, s.bmat, ptn);
+                        const float4 *g = reinterpret_cast<const float4 *>(s.pref + kPrefGeo) + 2 * lane;
+                        if (have) setup_mixed_geo(g[0], g[1], s.bmat, ptn);
                         asm volatile("bar.sync 2, 64;" ::: "memory");
                         if (have) setup_mixed_rotate(ptn);
                     }
@@ -1479,7 +1562,7 @@ __device__ void evaluate(const DevObject &ob, const FitConfig &cfg, const SlotLa
             // 5. accumulate (mrqcof.c:106-136)
             if constexpr (kPipe) {
                 accumulate_tile_tc<NT>(ob, s, np, start + t0, conv, conv_sig, tcs, true);
-                if (++tiles_since_flush == kTilesPerFlush) {
+                if (++tiles_since_flush == kTcTilesPerFlush) {
                     tc_alpha_flush<NT>(ob, s, M, bv, tcs);
                     tiles_since_flush = 0;
                 }
@@ -1547,11 +1630,16 @@ __device__ void evaluate(const DevObject &ob, const FitConfig &cfg, const SlotLa
             // values; the mixed form parks them as FP32); on the tensor-core
             // path they were prepared above, and the tile's residuals and
             // weights go where the accumulation reads them
-            if (kPipe && tid < np) {
-                s.accs[tid] = static_cast<float>(src[static_cast<size_t>(tid) * RW + ma + 1]);
-                s.accs[32 + tid] = static_cast<float>(src[static_cast<size_t>(tid) * RW + ma + 2]);
+            if constexpr (kPipe) {
+                // operands built from the parked rows (renormalised on the way)
+                accumulate_tile_tc<NT>(ob, s, np, start + t0, false, conv_sig, tcs, true, src, RW);
+                if (++tiles_since_flush == kTcTilesPerFlush) {
+                    tc_alpha_flush<NT>(ob, s, M, bv, tcs);
+                    tiles_since_flush = 0;
+                }
+                continue;
             }
-            if (!kPipe && tid < np) {
+            if (tid < np) {
                 const int q = start + t0 + tid;
                 const double yt = static_cast<double>(src[static_cast<size_t>(tid) * RW + ma]);
                 double coef, ytr;
@@ -1568,7 +1656,7 @@ __device__ void evaluate(const DevObject &ob, const FitConfig &cfg, const SlotLa
                     s.accs[32 + tid] = static_cast<float>(ytr);    // accumulation reuses it
                 }
             }
-            if constexpr (!kPipe) __syncthreads();
+            __syncthreads();
             for (int e = tid; e < np * ma; e += NT) {
                 const int p = e / ma, l = e - p * ma;
                 const R v = src[static_cast<size_t>(p) * RW + l];
@@ -1578,28 +1666,17 @@ __device__ void evaluate(const DevObject &ob, const FitConfig &cfg, const SlotLa
                     const double coef = ob.sig[q] * npts / ave;
                     const double yt = src[static_cast<size_t>(p) * RW + ma];
                     out = coef * (v - yt * s.dave[l] / ave);
-                } else if constexpr (kPipe) {
-                    const R *row = src + static_cast<size_t>(p) * RW;
-                    out = row[0] * (v - row[ma] * s.davef[l]);
                 } else {
                     out = s.accs[p] * (v - s.accs[32 + p] * s.davef[l]);
                 }
                 s.J[e] = (l == 0) ? R(0) : out;
             }
             __syncthreads();
-            if constexpr (kPipe) {
-                accumulate_tile_tc<NT>(ob, s, np, start + t0, false, conv_sig, tcs, true);
+            accumulate_tile<FORM>(ob, s, M, bv, np, start + t0, false, conv_sig, accA, accB);
+            if constexpr (!kFP64) {
                 if (++tiles_since_flush == kTilesPerFlush) {
-                    tc_alpha_flush<NT>(ob, s, M, bv, tcs);
+                    flush_partials<FORM>(M, bv, mf, accA, accB);
                     tiles_since_flush = 0;
-                }
-            } else {
-                accumulate_tile<FORM>(ob, s, M, bv, np, start + t0, false, conv_sig, accA, accB);
-                if constexpr (!kFP64) {
-                    if (++tiles_since_flush == kTilesPerFlush) {
-                        flush_partials<FORM>(M, bv, mf, accA, accB);
-                        tiles_since_flush = 0;
-                    }
                 }
             }
         }
