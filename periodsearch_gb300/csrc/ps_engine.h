@@ -85,7 +85,7 @@ struct SlotLayout {
     size_t cg, atry, beta, da, alpha, covar, area, gv, areaR, gvR, W, J, pt, ym, red, dave, col, misc, ipiv, dsph;
     size_t bhi, blo, tcm;   // tensor-core operand tiles (TF32 high/low parts) and barrier/TMEM slot
     size_t pt2;             // second point set-up buffer (tensor-core path: next tile's set-up)
-    size_t fac, ag, fpart;  // tensor-core path: packed facet constants, per-evaluation (area, Darea g), facet-sum partials
+    size_t fac, fpart;      // tensor-core path: facet normals and per-evaluation areas, facet-sum partials
     size_t aop;             // tensor-core path: alpha/beta MMA operands
     size_t accs;            // per-point weights and residuals of the accumulation (mixed form)
     size_t davef;           // FP32 copy of a relative lightcurve's derivative sums (mixed form)
@@ -191,14 +191,13 @@ PSG_HD inline SlotLayout make_layout(int form, int ma, int mfit, int nfac, int n
         L.tcm = take(32);
         L.pt2 = take(static_cast<size_t>(P) * kPointStride * rs);
         L.fac = take(static_cast<size_t>(tc_kpad(nfac)) * 4 * sizeof(float));
-        L.ag = take(static_cast<size_t>(tc_kpad(nfac)) * 2 * sizeof(float));
         L.fpart = take(4 * static_cast<size_t>(P) * 9 * sizeof(float));
         L.pref = take(kPrefBytes);
         L.flist = take(static_cast<size_t>(mfit + 1) * sizeof(int));
     } else {
         L.bhi = L.blo = L.tcm = 0;
         L.pt2 = L.pt;
-        L.fac = L.ag = L.fpart = L.aop = L.pref = L.flist = 0;
+        L.fac = L.fpart = L.aop = L.pref = L.flist = 0;
     }
     // 32 residuals then 32 weights, whatever the tile size
     L.accs = form == PS_FORM_MIXED ? take(64 * sizeof(float)) : 0;

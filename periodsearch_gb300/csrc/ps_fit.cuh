@@ -87,8 +87,7 @@ struct Smem {
     // Memory address slot and the abort flag set when a wait gives up
     unsigned char *bhi, *blo;
     uint64_t *mbar, *mbar2;   // completion of the contraction MMAs / of the alpha MMAs
-    float4 *fac;              // per facet: nx, ny, nz, Darea
-    float2 *ag;               // per facet and evaluation: Area, Darea g
+    float4 *fac;              // per facet: nx, ny, nz and the evaluation's Area = Darea g
     float *fpart;             // [4][P][9] facet-sum partials of the four facet quarters
     unsigned char *aop;       // alpha/beta MMA operands
     unsigned char *pref;      // per-point data prefetched for the contraction window
@@ -134,7 +133,6 @@ __device__ inline Smem<FORM> carve(char *base, const SlotLayout &L)
         s.abort = reinterpret_cast<int *>(base + L.tcm + 12);
         s.mbar2 = reinterpret_cast<uint64_t *>(base + L.tcm + 16);
         s.fac = reinterpret_cast<float4 *>(base + L.fac);
-        s.ag = reinterpret_cast<float2 *>(base + L.ag);
         s.fpart = reinterpret_cast<float *>(base + L.fpart);
         s.aop = reinterpret_cast<unsigned char *>(base + L.aop);
         s.pref = reinterpret_cast<unsigned char *>(base + L.pref);
@@ -144,7 +142,6 @@ __device__ inline Smem<FORM> carve(char *base, const SlotLayout &L)
         s.mbar = s.mbar2 = nullptr;
         s.tslot = nullptr;
         s.fac = nullptr;
-        s.ag = nullptr;
         s.fpart = nullptr;
         s.aop = nullptr;
         s.pref = nullptr;
@@ -740,11 +737,8 @@ __device__ void tc_setup(const DevObject &ob, Smem<PS_FORM_MIXED> &s, TcState &t
     const int bexp = (mx > 0.0 && mx < 1e300) ? 13 - ilogb(mx) : 0;
     const double bscale = ldexp(1.0, bexp);
     const uint32_t tbase = *s.tslot;
-    for (int i = tid; i < Fp; i += NT) {
-        s.fac[i] = i < F ? make_float4(ob.nx_f[i], ob.ny_f[i], ob.nz_f[i], ob.darea_f[i])
-                         : make_float4(0.f, 0.f, 0.f, 0.f);
-        if (i >= F) s.ag[i] = make_float2(0.f, 0.f);
-    }
+    for (int i = tid; i < Fp; i += NT)
+        s.fac[i] = i < F ? make_float4(ob.nx_f[i], ob.ny_f[i], ob.nz_f[i], 0.f) : make_float4(0.f, 0.f, 0.f, 0.f);
     for (int i = tid; i < static_cast<int>(kTcAlphaOperands / 4); i += NT) reinterpret_cast<uint32_t *>(s.aop)[i] = 0;
     for (int j = tid; j < ob.mfit; j += NT) s.flist[j] = ob.free_list[j];
     if (warp < 4) {
@@ -865,11 +859,12 @@ __device__ void facet_stage_tc(const DevObject &ob, Smem<PS_FORM_MIXED> &s, int 
             // slower); unlit and padding facets get zero area (every term
             // vanishes) and a safe denominator.
             const bool lit = mu > float(kTinyMu) && mu0 > float(kTinyMu);
-            const float2 ag = s.ag[i + u];
-            const float ax = lit ? ag.x : 0.f, ay = lit ? ag.y : 0.f;
+            // Area (= Darea g, also the weight of W: the Lambert and
+            // Lommel-Seeliger terms share it)
+            const float ax = lit ? n.w : 0.f;
             const LitTerms<float, PS_FORM_MIXED> lt(lit ? mu : 1.f, lit ? mu0 : 1.f, cl, cls);
             br = fmaf(ax, lt.sv, br);
-            wv[u] = ay * lt.sv * wscale;
+            wv[u] = ax * lt.sv * wscale;
             const float cu = ax * lt.dsmu, cv = ax * lt.dsmu0;
             ux = fmaf(cu, n.x, ux);
             uy = fmaf(cu, n.y, uy);
@@ -880,10 +875,10 @@ __device__ void facet_stage_tc(const DevObject &ob, Smem<PS_FORM_MIXED> &s, int 
             dcl = fmaf(mu * mu0, ax, dcl);
             dcls = fmaf(ax, lt.dcls_w, dcls);
         }
-        const float h0 = tc::round_f16(wv[0]), h1 = tc::round_f16(wv[1]);
+        const uint32_t hp = tc::pack_f16x2(wv[0], wv[1]);
         const int cm = g * kcs + kc;    // core matrix (8-point group, 8-facet group)
-        bh[cm * 32 + lane] = tc::pack_f16x2(h0, h1);
-        bl[cm * 32 + lane] = tc::pack_f16x2(wv[0] - h0, wv[1] - h1);
+        bh[cm * 32 + lane] = hp;
+        bl[cm * 32 + lane] = tc::pack_f16x2(wv[0] - tc::f16_lo(hp), wv[1] - tc::f16_hi(hp));
     }
     float v[9] = {br, dcl, dcls, ux, uy, uz, vx, vy, vz};
 #pragma unroll
@@ -959,8 +954,8 @@ __device__ void conv_rows_tc(const DevObject &ob, Smem<PS_FORM_MIXED> &s, float 
 // Waits for the tile's MMAs, stages the accumulator (lane m = row m) in
 // shared memory and writes J[p][k] = Scale_p jscale (D[k][p] + D[k][32 + p]
 // + D[64 + k][p] + D[64 + k][32 + p]): basis high and low parts times W high
-// and low parts, jscale undoing the operands' power-of-two scales.  A wait that gives up sets the abort flag; the caller ends
-// the fit.
+// and low parts, jscale undoing the operands' power-of-two scales.  A wait
+// that gives up sets the abort flag; the caller ends the fit.
 template <int NT>
 __device__ void contract_tc_finish(Smem<PS_FORM_MIXED> &s, int np, int F, int C, int ma, bool conv, TcState &t,
                                    float jscale)
@@ -1195,7 +1190,7 @@ __device__ void evaluate(const DevObject &ob, const FitConfig &cfg, const SlotLa
         if constexpr (!kFP64) {
             s.areaR[i] = static_cast<R>(ar);
             s.gvR[i] = static_cast<R>(g);
-            if constexpr (KU == 0) s.ag[i] = make_float2(static_cast<float>(ar), static_cast<float>(ob.darea[i] * g));
+            if constexpr (KU == 0) s.fac[i].w = static_cast<float>(ar);
         }
         asum += ar;
     }
@@ -1236,7 +1231,7 @@ __device__ void evaluate(const DevObject &ob, const FitConfig &cfg, const SlotLa
         // convexity rows' W <= Darea g, so 2^k puts the evaluation's largest
         // W just below 2^14.
         float mx = 0.f;
-        for (int i = lane; i < F; i += 32) mx = fmaxf(mx, s.ag[i].y);
+        for (int i = lane; i < F; i += 32) mx = fmaxf(mx, s.fac[i].w);
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
         const float wmax =
