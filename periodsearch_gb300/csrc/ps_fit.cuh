@@ -847,6 +847,7 @@ __device__ void facet_stage_tc(const DevObject &ob, Smem<PS_FORM_MIXED> &s, int 
     uint32_t *bh = reinterpret_cast<uint32_t *>(s.bhi), *bl = reinterpret_cast<uint32_t *>(s.blo);
     for (int kc = quarter * cq; kc < (quarter + 1) * cq; kc++) {
         const int i = kc * 8 + 2 * fl;
+        const int cm = g * kcs + kc;    // core matrix (8-point group, 8-facet group)
         float wv[2];
 #pragma unroll
         for (int u = 0; u < 2; u++) {
@@ -856,8 +857,8 @@ __device__ void facet_stage_tc(const DevObject &ob, Smem<PS_FORM_MIXED> &s, int 
             // Branch-free: the 8 points of a warp see different lit facets,
             // so a branch would diverge on almost every step (and a
             // warp-uniform skip of groups unlit for all 8 points measured
-            // slower); unlit and padding facets get zero area (every term
-            // vanishes) and a safe denominator.
+            // slower, twice); unlit and padding facets get zero area (every
+            // term vanishes) and a safe denominator.
             const bool lit = mu > float(kTinyMu) && mu0 > float(kTinyMu);
             // Area (= Darea g, also the weight of W: the Lambert and
             // Lommel-Seeliger terms share it)
@@ -876,7 +877,6 @@ __device__ void facet_stage_tc(const DevObject &ob, Smem<PS_FORM_MIXED> &s, int 
             dcls = fmaf(ax, lt.dcls_w, dcls);
         }
         const uint32_t hp = tc::pack_f16x2(wv[0], wv[1]);
-        const int cm = g * kcs + kc;    // core matrix (8-point group, 8-facet group)
         bh[cm * 32 + lane] = hp;
         bl[cm * 32 + lane] = tc::pack_f16x2(wv[0] - tc::f16_lo(hp), wv[1] - tc::f16_hi(hp));
     }
@@ -1842,8 +1842,8 @@ __device__ inline void chol_pivot_pair(double *A, double *b, int n, int j, doubl
 
 // The 2 x 2 block [a bq; bq c] of pair (j, j + 1) and its rows bj, bj1 of
 // b, already updated, in registers of every lane of warp 0: stores 1/L_jj,
-// 1/L_j+1,j+1 (col), L_j+1,j and y (b); the columns below are scaled by the
-// helper warp.
+// 1/L_j+1,j+1 (col) and L_j+1,j, arrives on the helper warp's named barrier
+// (the helper scales the columns below), then stores y (b).
 __device__ inline void chol_pivot_block(double a, double bq, double c, double bj, double bj1, double *A, double *b,
                                         int n, int j, bool two, double *col, double *flag, int lane)
 {
@@ -1866,10 +1866,12 @@ __device__ inline void chol_pivot_block(double a, double bq, double c, double bj
         b[j] = y0;
         if (two) {
             col[j + 1] = i1;
-            b[j + 1] = (bj1 - l10 * y0) * i1;
             A[(j + 1) * n + j] = l10;
         }
     }
+    // the helper warp may scale the columns now
+    asm volatile("bar.arrive 1, 64;" ::: "memory");
+    if (lane == 0 && two) b[j + 1] = (bj1 - l10 * y0) * i1;
 }
 
 template <int NT>
@@ -1910,7 +1912,6 @@ __device__ int cholesky_solve(double *A, double *b, int n, double *col, double *
             const double bj = __shfl_sync(0xffffffffu, xu, 3);
             const double bj1 = __shfl_sync(0xffffffffu, xu, 4);
             chol_pivot_block(a, bq, cc, bj, bj1, A, b, n, jn, twon, col, flag, lane);
-            asm volatile("bar.arrive 1, 64;" ::: "memory");
         } else if (warp == 1) {
             // the rest of the next pair's columns: update now, scale once
             // warp 0 has published the pivot
