@@ -829,14 +829,18 @@ __device__ void facet_stage_tc(const DevObject &ob, Smem<PS_FORM_MIXED> &s, int 
     const int kcs = tc_kpad(ob.nfac) >> 3;   // 8-facet core matrices per row group
     const int cq = kcs >> 2;                 // per facet quarter
     const int quarter = warp >> 2, g = warp & 3, p = g * 8 + (lane >> 2), fl = lane & 3;
+    // The point records of this path hold the pole products before the
+    // rotation about the spin axis (setup_mixed_geo) and its cos/sin
+    // (setup_mixed_phase): Earth and Sun directions rotated here.
     float e1 = 0, e2 = 0, e3 = 0, f1 = 0, f2 = 0, f3 = 0;
     if (p < np) {
         const float *pt = s.pt + p * kPointStride;
-        e1 = pt[0];
-        e2 = pt[1];
+        const float cf = pt[28], sf = pt[29];
+        e1 = cf * pt[0] + sf * pt[1];
+        e2 = cf * pt[1] - sf * pt[0];
         e3 = pt[2];
-        f1 = pt[3];
-        f2 = pt[4];
+        f1 = cf * pt[3] + sf * pt[4];
+        f2 = cf * pt[4] - sf * pt[3];
         f3 = pt[5];
     }
     // The rotation derivatives sum_i Area_i (dsmu (n_i . D_k) + dsmu0 (n_i .
@@ -904,16 +908,20 @@ __device__ void facet_stage_tc(const DevObject &ob, Smem<PS_FORM_MIXED> &s, int 
         // the point's sums in FP32 over its own quarter-0 partials (read
         // above by this thread only): brightness, the three rotation
         // derivatives, the Lambert and the scattering-weight derivatives
+        // D_k . U with D_k = fm u_k (k: beta, lambda) is u_k . fm^T U; the
+        // omega derivative is D_2 = t (e_y, -e_x, 0), e = fm u_0
         const float *pt = s.pt + tid * kPointStride;
+        const float cf = pt[28], sf = pt[29], tt = pt[30];
+        const float Ux = cf * t[3] - sf * t[4], Uy = sf * t[3] + cf * t[4], Uz = t[5];
+        const float Vx = cf * t[6] - sf * t[7], Vy = sf * t[6] + cf * t[7], Vz = t[8];
         float *rf = s.fpart + tid * 9;
         rf[0] = t[0];
 #pragma unroll
-        for (int k = 0; k < 3; k++) {
-            // D_k = (de[k], de[3 + k], de[6 + k]), E_k likewise from de0
-            const float r = pt[6 + k] * t[3] + pt[9 + k] * t[4] + pt[12 + k] * t[5] + pt[15 + k] * t[6] +
-                            pt[18 + k] * t[7] + pt[21 + k] * t[8];
-            rf[1 + k] = r;
+        for (int k = 0; k < 2; k++) {
+            const float *ue = pt + 6 * (k + 1), *us = ue + 3;
+            rf[1 + k] = ue[0] * Ux + ue[1] * Uy + ue[2] * Uz + us[0] * Vx + us[1] * Vy + us[2] * Vz;
         }
+        rf[3] = tt * (pt[1] * Ux - pt[0] * Uy + pt[4] * Vx - pt[3] * Vy);
         rf[4] = t[1];
         rf[5] = t[2];
     }
@@ -1262,9 +1270,12 @@ __device__ void evaluate(const DevObject &ob, const FitConfig &cfg, const SlotLa
     // one per sub-partition.
     const int pipe_sp = warp == 1 ? lane : -1;
     if constexpr (kPipe) {
-        if (ob.n_lc > 1 && pipe_sp >= 0 && pipe_sp < min(P, ob.lc_npts[0]))
-            setup_point<FORM>(ob, cfg, ob.lc_start[0] + pipe_sp, omg, s.bmat,
-                              s.pt + pipe_sp * kPointStride);
+        if (ob.n_lc > 1 && pipe_sp >= 0 && pipe_sp < min(P, ob.lc_npts[0])) {
+            const int q = ob.lc_start[0] + pipe_sp;
+            float *pt0 = s.pt + pipe_sp * kPointStride;
+            setup_mixed_phase(ob.tim[q], omg, cfg.phi0, pt0);
+            setup_mixed_geo(ob.geo_f[2 * q], ob.geo_f[2 * q + 1], s.bmat, pt0);
+        }
         __syncthreads();   // the first tile's facet stage reads it
     }
 
@@ -1488,9 +1499,9 @@ __device__ void evaluate(const DevObject &ob, const FitConfig &cfg, const SlotLa
             bool next_setup = false;
             if constexpr (kPipe) {
                 // point set-up of the next tile into the other buffer, one
-                // point per lane: the rotation phase on warp 1, the
-                // geometry on warp 2, then the rotation on warp 2 once warp
-                // 1 has published the phase (a named barrier of the two)
+                // point per lane: the rotation phase on warp 1, the pole
+                // products and phase function on warp 2 (the facet stage
+                // applies the rotation)
                 const int nlc = t0 + P < npts ? lc : lc + 1, nt0 = t0 + P < npts ? t0 + P : 0;
                 next_setup = nlc < ob.n_lc - 1;   // the last lightcurve is the convexity rows
                 if (next_setup && (warp == 1 || warp == 2)) {
@@ -1501,12 +1512,9 @@ __device__ void evaluate(const DevObject &ob, const FitConfig &cfg, const SlotLa
                     if (warp == 1) {
                         if (have) setup_mixed_phase(reinterpret_cast<const double *>(s.pref + kPrefTim)[lane], omg,
                                                     cfg.phi0, ptn);
-                        asm volatile("bar.arrive 2, 64;" ::: "memory");
                     } else {
                         const float4 *g = reinterpret_cast<const float4 *>(s.pref + kPrefGeo) + 2 * lane;
                         if (have) setup_mixed_geo(g[0], g[1], s.bmat, ptn);
-                        asm volatile("bar.sync 2, 64;" ::: "memory");
-                        if (have) setup_mixed_rotate(ptn);
                     }
                 }
                 contract_tc_finish<NT>(s, np, F, C, ma, conv, tcs, jscale);
