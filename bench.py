@@ -26,9 +26,11 @@ e2e        the same through the C ABI with host buffers: ps_prepare (host ->
 roofline   algorithmic FLOP of the fits (2 N F C + 60 N F + N m(m+1) + 9 F C
            per evaluation, 2 m^3 per solve) per launch over the launch time,
            against the FP32 (mixed) or FP64 FMA ceiling measured live on the
-           device; for the mixed form also the two contractions' share
-           (2 N F C + N m(m+1)) against the TF32 tensor peak (half the
-           measured dense BF16 figure);
+           device; for the mixed form also the two contractions' shares:
+           the shape contraction (2 N F C, FP16 high/low MMAs) against the
+           measured dense BF16 figure (the FP16 rate) and the alpha/beta
+           accumulation (N m(m+1), TF32 high/low MMAs) against half of it
+           (the TF32 rate);
 cpu_baseline  the CPU oracle (a restatement of the reference's FP64 path)
            on all host cores, one fit per thread, on a bounded sample.
 
@@ -72,7 +74,8 @@ def _args():
     ap.add_argument("--multi-object", type=int, default=0,
                     help="also time K small objects (Ndata logU[100, 2000]) packed into one launch against one "
                          "launch per object")
-    ap.add_argument("--periods-per-step", type=int, default=64)
+    ap.add_argument("--periods-per-step", type=int, default=0,
+                    help="trial periods per step (0: one per fit slot of the device, i.e. ten fits per slot)")
     ap.add_argument("--cpu-sample-fits", type=int, default=0, help="fits in the CPU baseline sample (0: 2 per core)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     return ap.parse_args()
@@ -345,11 +348,13 @@ def run_engine_arm(args):
 
     with tempfile.TemporaryDirectory() as td:
         path, data, obj = make_workload(Path(td))
-        chunk = args.periods_per_step
         probe = Engine(data, device=local, form=chosen)
         n_max = int(probe.info.n_max)
         info = probe.info
         probe.close()
+        # a step: one launch over a whole number of waves of the fit slots
+        # (ten poles per period), as inside a long scan
+        chunk = args.periods_per_step or int(info.slots)
         total_steps = args.warmup + args.steps
         # chunks spread over the scan, distinct per rank (weak scaling)
         starts = [1 + ((k * world + rank) * 7919) % (n_max - chunk) for k in range(total_steps)]
@@ -474,15 +479,20 @@ def run_engine_arm(args):
                     "fp64_fma_peak_tflops": p64.value, "fp32_fma_peak_tflops": p32.value}
             if mixed and info.tensor_cores:
                 peaks = _measured_peaks()
-                tf32 = peaks["bf16_tflops"] / 2 if peaks.get("bf16_tflops") else None
-                tensor_flops = main["evals"] * (2.0 * info.ndata * info.nfac * info.ncoef
-                                                + info.ndata * info.mfit * (info.mfit + 1))
-                ta = tensor_flops / max(launches, 1) / per_launch_s / 1e12
+                f16 = peaks.get("bf16_tflops")
+                tf32 = f16 / 2 if f16 else None
+                per_s = max(launches, 1) * per_launch_s * 1e12
+                shape = main["evals"] * 2.0 * info.ndata * info.nfac * info.ncoef / per_s
+                alpha = main["evals"] * info.ndata * info.mfit * (info.mfit + 1) / per_s
                 roof["tensor_contractions"] = {
-                    "achieved": ta, "peak": tf32, "unit": "TFLOP/s", "frac": ta / tf32 if tf32 else None,
-                    "peak_source": "half the measured dense BF16 figure of MEASURED_PEAKS.json (TF32 rate)",
-                    "what": "algorithmic FLOP of the shape contraction and alpha/beta (2 N F C + N m(m+1) per "
-                            "evaluation), run as TF32 high/low-split MMAs"}
+                    "shape": {"achieved": shape, "peak": f16, "unit": "TFLOP/s",
+                              "frac": shape / f16 if f16 else None,
+                              "peak_source": "measured dense BF16 figure of MEASURED_PEAKS.json (the FP16 rate)",
+                              "what": "2 N F C per evaluation, run as FP16 high/low-split MMAs (kind::f16)"},
+                    "alpha": {"achieved": alpha, "peak": tf32, "unit": "TFLOP/s",
+                              "frac": alpha / tf32 if tf32 else None,
+                              "peak_source": "half the measured dense BF16 figure (the TF32 rate)",
+                              "what": "N m(m+1) per evaluation, run as TF32 high/low-split MMAs"}}
             fp64 = None
             if plain is not None:
                 pv = plain["fits"] / (plain["kernel_ms"] / 1e3)
