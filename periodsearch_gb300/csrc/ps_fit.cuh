@@ -27,11 +27,13 @@
 // contraction with W[c][i] = Darea_i * g_i * n_i[c].
 //
 // The mixed form runs the contraction on the tensor cores when the shape
-// tables allow it (tensor_basis_ok): tcgen05 TF32 MMAs with the basis split
-// into high and low TF32 parts resident in Tensor Memory for the CTA's
-// lifetime (A = [Dsph_hi^T; Dsph_lo^T], 128 lanes x F columns) and W split
-// the same way in shared memory (B), so that the four partial products give
-// the contraction to FP32 accuracy; otherwise on the SIMT pipes.
+// tables allow it (tensor_basis_ok): tcgen05 FP16 MMAs with the basis split
+// into high and low FP16 parts (scaled by a power of two) resident in Tensor
+// Memory for the CTA's lifetime (A = [Dsph_hi^T; Dsph_lo^T], 128 lanes, two
+// facets per column) and W split the same way in shared memory (B), so that
+// the four partial products give the contraction to FP32 accuracy; the
+// normal-matrix accumulation runs as TF32 high/low MMAs.  Otherwise both run
+// on the SIMT pipes.
 #pragma once
 
 #include <cuda_runtime.h>
@@ -477,20 +479,19 @@ __device__ void contract_mixed(Smem<PS_FORM_MIXED> &s, const float *dsph, int np
     }
 }
 
-// Point set-up of observation q (bright.c:27-57, phasec.c, matrix.c): the
-// rotated Earth and Sun directions with their beta/lambda/omega derivatives,
-// the phase function and its derivatives, into pt[0..27].
-// Mixed-form point set-up in three parts, so that the tensor-core path can
-// run the first two on different warps (the FP64 rotation phase holds its
-// sub-partition's FP64 unit for the whole warp): setup_mixed_phase (the
-// rotation phase and its cos and sin into pt[28], pt[29]), setup_mixed_geo
-// (the phase function into pt[24..27], the products of the pole matrix and
-// its beta/lambda derivatives with the Earth and Sun vectors into pt[0..17],
-// the time into pt[30]) and setup_mixed_rotate (the rotation about the spin
-// axis into pt[0..23], by the thread that ran setup_mixed_geo).  The
+// Mixed-form point set-up in three parts (bright.c:27-57, phasec.c,
+// matrix.c): setup_mixed_phase (the rotation phase and its cos and sin into
+// pt[28], pt[29]), setup_mixed_geo (the phase function into pt[24..27], the
+// products of the pole matrix and its beta/lambda derivatives with the Earth
+// and Sun vectors into pt[0..17], the time into pt[30]) and
+// setup_mixed_rotate (the rotation about the spin axis into pt[0..23]).  The
 // rotation fm commutes out of the products (matrix.c): with u = B ee,
 // e = fm u, de/dbeta = fm (dB/dbeta ee), de/dlambda = fm (dB/dlambda ee) and
 // de/domega = (dfm/domega) u = t (e_y, -e_x, 0); the same for the Sun vector.
+// The tensor-core path runs the first two on different warps (the FP64
+// rotation phase holds its sub-partition's FP64 unit for the whole warp)
+// and applies the rotation where it reads the records; the SIMT variants
+// run all three (setup_point).
 __device__ inline void setup_mixed_phase(double td, double omg, double phi0, float *pt)
 {
     const float f = rotation_phase_mixed(omg, td, phi0);
@@ -560,6 +561,9 @@ __device__ inline void setup_mixed_rotate(float *pt)
     }
 }
 
+// Point set-up of observation q (bright.c:27-57, phasec.c, matrix.c): the
+// rotated Earth and Sun directions with their beta/lambda/omega derivatives,
+// the phase function and its derivatives, into pt[0..27].
 template <int FORM>
 __device__ inline void setup_point(const DevObject &ob, const FitConfig &cfg, int q, double omg,
                                    const typename RealOf<FORM>::T *bm, typename RealOf<FORM>::T *pt)
