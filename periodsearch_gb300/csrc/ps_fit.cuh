@@ -691,6 +691,7 @@ struct TcState {
     uint32_t phase = 0;     // parity of the contraction barrier's next phase
     uint32_t aphase = 0;    // parity of the alpha barrier's next phase
     bool apending = false;  // alpha MMAs committed and not waited for
+    bool adefer = false;    // alpha operands built, their MMAs not yet issued
     bool afresh = true;     // the alpha accumulator holds nothing since the last flush
 };
 
@@ -787,6 +788,27 @@ __device__ void tc_teardown(Smem<PS_FORM_MIXED> &s, const TcState &t, int F)
     if ((threadIdx.x >> 5) == 0) tc::tmem_dealloc(t.tbase, tc_cols(F));
 }
 
+// Issues the alpha/beta MMAs of the operands in s.aop (built and fenced,
+// behind a CTA barrier) and commits them to the alpha barrier.  Called by
+// every thread (thread 0 issues).
+__device__ inline void tc_alpha_issue(Smem<PS_FORM_MIXED> &s, TcState &t, int F)
+{
+    if (threadIdx.x == 0 && !*s.abort) {
+        tc::fence_after_sync();
+        const uint32_t idesc = tc::idesc_tf32(128, 128);
+        const uint32_t a0 = tc::smem_u32(s.aop), b0 = tc::smem_u32(s.aop + 16384), d = t.tbase + tc_acol(F);
+        for (int kk = 0; kk < 4; kk++) {
+            const uint32_t off = static_cast<uint32_t>(kk) * 256;
+            tc::mma_tf32_ss(d, tc::smem_desc(a0 + off, 128, 1024), tc::smem_desc(b0 + off, 128, 1024), idesc,
+                            (t.afresh && kk == 0) ? 0u : 1u);
+        }
+        tc::mma_commit(s.mbar2);
+    }
+    t.apending = true;
+    t.afresh = false;
+    t.adefer = false;
+}
+
 // Issues D = A [W_hi; W_lo]^T for the tile as Fp/16 FP16 MMAs of 128 x 64 x
 // 16 (one MMA costs the issuing thread about the same for N = 32 and N = 64,
 // and the same for K = 8 TF32 and K = 16 FP16 elements) and a commit to the
@@ -802,6 +824,7 @@ __device__ void contract_tc_issue(Smem<PS_FORM_MIXED> &s, int F, TcState &t)
     tc::fence_proxy_async();
     tc::fence_before_sync();
     __syncthreads();
+    if (t.adefer) tc_alpha_issue(s, t, F);   // the previous tile's alpha/beta MMAs first
     if (tid == 0 && !*s.abort) {
         tc::fence_after_sync();
         const uint32_t idesc = tc::idesc_f16(128, 64);
@@ -1026,10 +1049,13 @@ __device__ void contract_tc_finish(Smem<PS_FORM_MIXED> &s, int np, int F, int C,
 // from the parked rows (stride rw: renormalisation factor in column 0, y/ave
 // in ma, residual in ma + 1, weight in ma + 2), renormalising on the way
 // (mrqcof.c:90-104).
+// defer: leave the MMAs to the next contraction window's issuing thread
+// (contract_tc_issue) or the next flush, so that thread 0 does not enter
+// the next facet stage late.
 template <int NT>
 __device__ void accumulate_tile_tc(const DevObject &ob, Smem<PS_FORM_MIXED> &s, int np, int q0pt, bool conv,
                                    double conv_sig, TcState &t, bool prepared, const float *rows = nullptr,
-                                   int rw = 0)
+                                   int rw = 0, bool defer = false)
 {
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int ma = ob.ma, mf = ob.mfit;
@@ -1094,19 +1120,8 @@ __device__ void accumulate_tile_tc(const DevObject &ob, Smem<PS_FORM_MIXED> &s, 
     tc::fence_proxy_async();
     tc::fence_before_sync();
     __syncthreads();
-    if (tid == 0 && !*s.abort) {
-        tc::fence_after_sync();
-        const uint32_t idesc = tc::idesc_tf32(128, 128);
-        const uint32_t a0 = tc::smem_u32(Ab), b0 = tc::smem_u32(Bb), d = t.tbase + tc_acol(ob.nfac);
-        for (int kk = 0; kk < 4; kk++) {
-            const uint32_t off = static_cast<uint32_t>(kk) * 256;
-            tc::mma_tf32_ss(d, tc::smem_desc(a0 + off, 128, 1024), tc::smem_desc(b0 + off, 128, 1024), idesc,
-                            (t.afresh && kk == 0) ? 0u : 1u);
-        }
-        tc::mma_commit(s.mbar2);
-    }
-    t.apending = true;
-    t.afresh = false;
+    if (defer) t.adefer = true;
+    else tc_alpha_issue(s, t, ob.nfac);
 }
 
 // Adds the alpha accumulator to the FP64 normal matrix M (lower triangle)
@@ -1117,6 +1132,7 @@ __device__ void tc_alpha_flush(const DevObject &ob, Smem<PS_FORM_MIXED> &s, doub
 {
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int mf = ob.mfit;
+    if (t.adefer) tc_alpha_issue(s, t, ob.nfac);
     if (t.afresh) return;
     tc_alpha_wait(s, t);
     if (*s.abort) return;
@@ -1568,7 +1584,7 @@ __device__ void evaluate(const DevObject &ob, const FitConfig &cfg, const SlotLa
             }
             // 5. accumulate (mrqcof.c:106-136)
             if constexpr (kPipe) {
-                accumulate_tile_tc<NT>(ob, s, np, start + t0, conv, conv_sig, tcs, true);
+                accumulate_tile_tc<NT>(ob, s, np, start + t0, conv, conv_sig, tcs, true, nullptr, 0, true);
                 if (++tiles_since_flush == kTcTilesPerFlush) {
                     tc_alpha_flush<NT>(ob, s, M, bv, tcs);
                     tiles_since_flush = 0;
