@@ -114,9 +114,9 @@ constexpr int kPointStride = 33;   // reals of per-point set-up (odd: a warp wit
 constexpr int kRedStride = 8;      // doubles of per-point facet sums
 constexpr int kMisc = 40;
 // Prefetch area of the tensor-core path, for a 32-point tile: times (32
-// doubles), FP32 geometry (32 x 2 float4) and sig^-2, weight, brightness
-// (32 x 3 doubles).
-constexpr size_t kPrefTim = 0, kPrefGeo = 256, kPrefAcc = 1280, kPrefBytes = 2048;
+// doubles), two copies of the FP32 geometry (32 x 2 float4 each) and sig^-2,
+// weight, brightness (32 x 3 doubles).
+constexpr size_t kPrefTim = 0, kPrefGeo = 256, kPrefAcc = 1280, kPrefGeo2 = 2048, kPrefBytes = 3072;
 constexpr size_t kTcAlphaOperands = 32768;   // tensor-core alpha/beta operands: two 128 x 32 TF32 tiles
 
 

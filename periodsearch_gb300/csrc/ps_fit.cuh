@@ -501,20 +501,26 @@ __device__ inline void setup_mixed_phase(double td, double omg, double phi0, flo
     pt[29] = sf;
 }
 
-__device__ inline void setup_mixed_geo(float4 g0, float4 g1, const float *bm, float *pt)
+// part < 0: all of it; part 0: the phase function and the pole matrix's
+// products; part 1: its derivatives' products and the time (two warps of
+// the tensor-core path share the work).
+__device__ inline void setup_mixed_geo(float4 g0, float4 g1, const float *bm, float *pt, int part = -1)
 {
     const float ee[3] = {g0.x, g0.y, g0.z}, e0v[3] = {g1.x, g1.y, g1.z};
-    const float alpha = g0.w;
-    const float php0 = bm[27], php1 = bm[28], php2 = bm[29];
-    const float inv_w = 1.f / php1;
-    const float ex = expf(-alpha * inv_w);
-    pt[24] = 1 + php0 * ex + php2 * alpha;
-    pt[25] = ex;
-    pt[26] = php0 * ex * alpha * (inv_w * inv_w);
-    pt[27] = alpha;
-    pt[30] = g1.w;
+    if (part <= 0) {
+        const float alpha = g0.w;
+        const float php0 = bm[27], php1 = bm[28], php2 = bm[29];
+        const float inv_w = 1.f / php1;
+        const float ex = expf(-alpha * inv_w);
+        pt[24] = 1 + php0 * ex + php2 * alpha;
+        pt[25] = ex;
+        pt[26] = php0 * ex * alpha * (inv_w * inv_w);
+        pt[27] = alpha;
+    }
+    if (part != 0) pt[30] = g1.w;
 #pragma unroll
     for (int m = 0; m < 3; m++) {
+        if ((part == 0 && m != 0) || (part == 1 && m == 0)) continue;
 #pragma unroll
         for (int k = 0; k < 3; k++) {
             const float *row = bm + 9 * m + 3 * k;
@@ -691,7 +697,6 @@ struct TcState {
     uint32_t phase = 0;     // parity of the contraction barrier's next phase
     uint32_t aphase = 0;    // parity of the alpha barrier's next phase
     bool apending = false;  // alpha MMAs committed and not waited for
-    bool adefer = false;    // alpha operands built, their MMAs not yet issued
     bool afresh = true;     // the alpha accumulator holds nothing since the last flush
 };
 
@@ -790,7 +795,9 @@ __device__ void tc_teardown(Smem<PS_FORM_MIXED> &s, const TcState &t, int F)
 
 // Issues the alpha/beta MMAs of the operands in s.aop (built and fenced,
 // behind a CTA barrier) and commits them to the alpha barrier.  Called by
-// every thread (thread 0 issues).
+// every thread; thread 0 issues.  (Issuing them from an idle warp during
+// the next contraction window measured no faster: the MMA issue slots of an
+// SM are shared by its threads.)
 __device__ inline void tc_alpha_issue(Smem<PS_FORM_MIXED> &s, TcState &t, int F)
 {
     if (threadIdx.x == 0 && !*s.abort) {
@@ -806,7 +813,6 @@ __device__ inline void tc_alpha_issue(Smem<PS_FORM_MIXED> &s, TcState &t, int F)
     }
     t.apending = true;
     t.afresh = false;
-    t.adefer = false;
 }
 
 // Issues D = A [W_hi; W_lo]^T for the tile as Fp/16 FP16 MMAs of 128 x 64 x
@@ -824,7 +830,6 @@ __device__ void contract_tc_issue(Smem<PS_FORM_MIXED> &s, int F, TcState &t)
     tc::fence_proxy_async();
     tc::fence_before_sync();
     __syncthreads();
-    if (t.adefer) tc_alpha_issue(s, t, F);   // the previous tile's alpha/beta MMAs first
     if (tid == 0 && !*s.abort) {
         tc::fence_after_sync();
         const uint32_t idesc = tc::idesc_f16(128, 64);
@@ -1049,13 +1054,10 @@ __device__ void contract_tc_finish(Smem<PS_FORM_MIXED> &s, int np, int F, int C,
 // from the parked rows (stride rw: renormalisation factor in column 0, y/ave
 // in ma, residual in ma + 1, weight in ma + 2), renormalising on the way
 // (mrqcof.c:90-104).
-// defer: leave the MMAs to the next contraction window's issuing thread
-// (contract_tc_issue) or the next flush, so that thread 0 does not enter
-// the next facet stage late.
 template <int NT>
 __device__ void accumulate_tile_tc(const DevObject &ob, Smem<PS_FORM_MIXED> &s, int np, int q0pt, bool conv,
                                    double conv_sig, TcState &t, bool prepared, const float *rows = nullptr,
-                                   int rw = 0, bool defer = false)
+                                   int rw = 0)
 {
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int ma = ob.ma, mf = ob.mfit;
@@ -1120,8 +1122,7 @@ __device__ void accumulate_tile_tc(const DevObject &ob, Smem<PS_FORM_MIXED> &s, 
     tc::fence_proxy_async();
     tc::fence_before_sync();
     __syncthreads();
-    if (defer) t.adefer = true;
-    else tc_alpha_issue(s, t, ob.nfac);
+    tc_alpha_issue(s, t, ob.nfac);
 }
 
 // Adds the alpha accumulator to the FP64 normal matrix M (lower triangle)
@@ -1132,7 +1133,6 @@ __device__ void tc_alpha_flush(const DevObject &ob, Smem<PS_FORM_MIXED> &s, doub
 {
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int mf = ob.mfit;
-    if (t.adefer) tc_alpha_issue(s, t, ob.nfac);
     if (t.afresh) return;
     tc_alpha_wait(s, t);
     if (*s.abort) return;
@@ -1327,8 +1327,8 @@ __device__ void evaluate(const DevObject &ob, const FitConfig &cfg, const SlotLa
                 // 2. facet stage (bright.c:59-120), one warp per point
                 if constexpr (kPipe) {
                     // prefetch for the contraction window: the next tile's
-                    // times (warp 1) and geometry (warp 2), this tile's
-                    // accumulation data (warp 14)
+                    // times (warp 1) and geometry (warps 2 and 3, a copy
+                    // each), this tile's accumulation data (warp 14)
                     if (warp == 14) {
                         if (!rel && lane < np) {
                             const int q = start + t0 + lane;
@@ -1338,14 +1338,15 @@ __device__ void evaluate(const DevObject &ob, const FitConfig &cfg, const SlotLa
                             cp_async8(d + 2, ob.bright + q);
                         }
                         cp_async_commit();
-                    } else if (warp == 1 || warp == 2) {
+                    } else if (warp >= 1 && warp <= 3) {
                         const int nlc = t0 + P < npts ? lc : lc + 1, nt0 = t0 + P < npts ? t0 + P : 0;
                         if (nlc < ob.n_lc - 1 && lane < min(P, ob.lc_npts[nlc] - nt0)) {
                             const int q = ob.lc_start[nlc] + nt0 + lane;
                             if (warp == 1) {
                                 cp_async8(reinterpret_cast<double *>(s.pref + kPrefTim) + lane, ob.tim + q);
                             } else {
-                                float4 *g = reinterpret_cast<float4 *>(s.pref + kPrefGeo) + 2 * lane;
+                                float4 *g = reinterpret_cast<float4 *>(s.pref + (warp == 2 ? kPrefGeo : kPrefGeo2)) +
+                                            2 * lane;
                                 cp_async16(g, ob.geo_f + 2 * q);
                                 cp_async16(g + 1, ob.geo_f + 2 * q + 1);
                             }
@@ -1519,12 +1520,12 @@ __device__ void evaluate(const DevObject &ob, const FitConfig &cfg, const SlotLa
             bool next_setup = false;
             if constexpr (kPipe) {
                 // point set-up of the next tile into the other buffer, one
-                // point per lane: the rotation phase on warp 1, the pole
-                // products and phase function on warp 2 (the facet stage
-                // applies the rotation)
+                // point per lane: the rotation phase on warp 1, the phase
+                // function and pole products on warps 2 and 3 (the facet
+                // stage applies the rotation)
                 const int nlc = t0 + P < npts ? lc : lc + 1, nt0 = t0 + P < npts ? t0 + P : 0;
                 next_setup = nlc < ob.n_lc - 1;   // the last lightcurve is the convexity rows
-                if (next_setup && (warp == 1 || warp == 2)) {
+                if (next_setup && warp >= 1 && warp <= 3) {
                     const bool have = lane < min(P, ob.lc_npts[nlc] - nt0);
                     const int q = ob.lc_start[nlc] + nt0 + lane;
                     float *ptn = s.pt2 + lane * kPointStride;
@@ -1533,8 +1534,9 @@ __device__ void evaluate(const DevObject &ob, const FitConfig &cfg, const SlotLa
                         if (have) setup_mixed_phase(reinterpret_cast<const double *>(s.pref + kPrefTim)[lane], omg,
                                                     cfg.phi0, ptn);
                     } else {
-                        const float4 *g = reinterpret_cast<const float4 *>(s.pref + kPrefGeo) + 2 * lane;
-                        if (have) setup_mixed_geo(g[0], g[1], s.bmat, ptn);
+                        const float4 *g =
+                            reinterpret_cast<const float4 *>(s.pref + (warp == 2 ? kPrefGeo : kPrefGeo2)) + 2 * lane;
+                        if (have) setup_mixed_geo(g[0], g[1], s.bmat, ptn, warp - 2);
                     }
                 }
                 contract_tc_finish<NT>(s, np, F, C, ma, conv, tcs, jscale);
@@ -1584,7 +1586,7 @@ __device__ void evaluate(const DevObject &ob, const FitConfig &cfg, const SlotLa
             }
             // 5. accumulate (mrqcof.c:106-136)
             if constexpr (kPipe) {
-                accumulate_tile_tc<NT>(ob, s, np, start + t0, conv, conv_sig, tcs, true, nullptr, 0, true);
+                accumulate_tile_tc<NT>(ob, s, np, start + t0, conv, conv_sig, tcs, true);
                 if (++tiles_since_flush == kTcTilesPerFlush) {
                     tc_alpha_flush<NT>(ob, s, M, bv, tcs);
                     tiles_since_flush = 0;
