@@ -216,3 +216,34 @@ def test_c2_mixed_scan_matches_fp64(engine_lib, c2_object):
     assert signed.max() <= MAX_REL and signed.min() >= -MAX_REL_BELOW
     assert np.median(np.abs(signed)) <= MEDIAN_REL
     assert int(np.argmin(refined["rms"])) == int(np.argmin(ref["rms"]))
+
+
+@pytest.mark.parametrize("nrows", [5, 7, 8])
+def test_tensor_path_other_facet_grids(engine_lib, oracle, tmp_path, nrows):
+    """The tensor-core path on facet grids other than c1's 288 facets: 200
+    and 392 facets are padded with empty facets to a multiple of 32, 512
+    facets fill the largest basis Tensor Memory holds beside the
+    accumulators.  Evaluations against the oracle, a short scan against the
+    FP64 form."""
+    from periodsearch_gb300 import Engine, PS_FORM_FP64, PS_FORM_MIXED, read_input, synth
+
+    path = tmp_path / "period_search_in"
+    synth.write_object(path, synth.SynthConfig(name=f"grid{nrows}", nrows=nrows, n_periods=40), seed=60 + nrows)
+    data = read_input(path)
+    ora = oracle.OracleProblem(path)
+    conw_r = ora.info()["conw_r"]
+    with Engine(data, form=PS_FORM_MIXED) as eng:
+        assert eng.info.nfac == 8 * nrows * nrows and eng.info.tensor_cores == 1
+        for n, pole in [(1, 3), (7, 10)]:
+            cg = ora.initial_cg(n, pole)
+            a_g, b_g, x_g, _ = eng.eval(conw_r, cg)
+            a_o, b_o, x_o, _ = ora.eval(cg)
+            assert abs(x_g - x_o) <= 1e-5 * abs(x_o)
+            assert np.abs(a_g - a_o).max() <= 1e-4 * np.abs(a_o).max()
+            assert np.abs(b_g - b_o).max() <= 1e-3 * np.abs(b_o).max()
+        got = eng.scan(conw_r, 1, 12)
+    with Engine(data, form=PS_FORM_FP64) as e64:
+        ref = e64.scan(conw_r, 1, 12)
+    signed = (got["rms"] - ref["rms"]) / ref["rms"]
+    assert signed.max() <= MAX_REL and signed.min() >= -MAX_REL_BELOW
+    assert np.median(np.abs(signed)) <= MEDIAN_REL
