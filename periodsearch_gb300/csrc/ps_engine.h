@@ -223,10 +223,11 @@ int launch_pack(int form, const FitWork &w, int ncoef, int grid, int P, size_t s
 int set_pack_smem(int form, size_t smem, int ncoef, int dsph_smem);
 int occupancy_slots(int form, size_t smem, int ncoef, int dsph_smem, int *per_sm);
 // Whether the tensor-core path supports an object: at most 64 coefficients
-// (the high and low TF32 parts of the basis fill 128 Tensor Memory lanes),
-// at most 63 free parameters (alpha and the beta column in 64 rows), a facet
-// count that is a multiple of 8 and leaves the 64 contraction and 128 alpha
-// accumulator columns within 512, and 32-point tiles.
+// (the high and low FP16 parts of the basis fill 128 Tensor Memory lanes),
+// at most 63 free parameters (alpha and the beta column in 64 rows), a
+// padded facet count whose basis columns (two facets each) leave the 64
+// contraction and 128 alpha accumulator columns within 512, and 32-point
+// tiles.
 PSG_HD inline bool tensor_basis_ok(int nfac, int ncoef, int mfit, int P)
 {
     return ncoef <= 64 && mfit <= 63 && (((tc_kpad(nfac) >> 1) + 31) & ~31) + 64 + 128 <= 512 && P == 32;
