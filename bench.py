@@ -78,6 +78,9 @@ def _args():
                     help="trial periods per step (0: one per fit slot of the device, i.e. ten fits per slot)")
     ap.add_argument("--cpu-sample-fits", type=int, default=0, help="fits in the CPU baseline sample (0: 2 per core)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--full-scan", action="store_true",
+                    help="also run the whole scan of the workload as one refined scan (rank 0) and report its "
+                         "time and best period (full_scan)")
     return ap.parse_args()
 
 
@@ -448,6 +451,21 @@ def run_engine_arm(args):
                      "rms_rel_window_median": float(np.median(rel_w)), "rms_rel_window_max": float(rel_w.max()),
                      "rms_rel_timed_median": float(np.median(rel_c)), "rms_rel_timed_max": float(rel_c.max())}
 
+        # the whole job: every period of the scan, chosen form, then the FP64
+        # refit of the minimum region; wall clock through the Python API
+        full = None
+        if args.full_scan and rank == 0:
+            eng = main["engine"]
+            torch.cuda.synchronize()
+            t_full0 = time.perf_counter()
+            rows, st = eng.scan_refined(main["conw_r"], 1, n_max)
+            torch.cuda.synchronize()
+            t_full = time.perf_counter() - t_full0
+            b = int(st["best_index"])
+            full = {"periods": n_max, "fits": n_max * 10, "fp64_refits": int(st["fits_refit"]), "seconds": t_full,
+                    "fits_per_s": n_max * 10 / t_full, "best_index": b,
+                    "best_period_h": float(rows["period_h"][b - 1]), "truth_period_h": obj.truth["period_h"]}
+
         vals = torch.tensor([main["kernel_ms"] / 1e3, e2e_t, float(main["fits"]), float(e2e_fits)],
                             dtype=torch.float64, device=f"cuda:{local}")
         if world > 1:
@@ -510,6 +528,9 @@ def run_engine_arm(args):
             if not args.no_cpu_baseline:
                 periods = [n for st in starts[args.warmup:] for n in range(st, st + chunk)]
                 cb = cpu_baseline(path, periods, args.cpu_sample_fits)
+            if full is not None and cb is not None:
+                # the same job on the host cores at the measured CPU rate
+                full["cpu_baseline_hours"] = full["fits"] / cb["value"] / 3600
             line = {"metric": METRIC, "value": value, "unit": "fits/s", "n_gpus": world, "steps": args.steps,
                     "warmup": args.warmup, "ms_per_step": main["kernel_ms"] / args.steps, "higher_is_better": True,
                     "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64" if mixed else "f64",
@@ -523,7 +544,7 @@ def run_engine_arm(args):
                     "e2e": {"value": e2e_fits_all / e2e_s, "unit": "fits/s", "h2d_bytes_per_step": h2d,
                             "d2h_bytes_per_step": d2h},
                     "gpu_launches": launches, "roofline": roof, "plain_fp64": fp64, "validation": valid,
-                    "multi_object": mo,
+                    "multi_object": mo, "full_scan": full,
                     "cpu_baseline": cb, "clocks": sampler.summary() if sampler else None, "wall_s": wall}
             print(json.dumps(line))
         main["engine"].close()
