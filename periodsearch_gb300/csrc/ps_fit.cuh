@@ -1285,9 +1285,10 @@ __device__ void evaluate(const DevObject &ob, const FitConfig &cfg, const SlotLa
     // Point set-up threads.  An FP64 instruction holds its sub-partition's
     // FP64 unit for the whole warp however few lanes are active, so the
     // set-up keeps its points on as few warps as possible: the mixed form
-    // (FP64 only for the rotation phase) on one warp, lane = point -- warp 1
-    // when it runs beside thread 0's MMA issue; the FP64 form on warps 0..3,
-    // one per sub-partition.
+    // (FP64 only for the rotation phase) on one warp, lane = point; the FP64
+    // form on warps 0..3, one per sub-partition.  On the tensor-core path
+    // warp 1 sets up the evaluation's first tile here; later tiles are set
+    // up in the contraction window of the tile before (warps 1..3).
     const int pipe_sp = warp == 1 ? lane : -1;
     if constexpr (kPipe) {
         if (ob.n_lc > 1 && pipe_sp >= 0 && pipe_sp < min(P, ob.lc_npts[0])) {
