@@ -13,6 +13,8 @@ sys.path.insert(0, str(ROOT / "tests"))
 
 GOLDEN = ROOT / "tests" / "golden"
 SYNTH_CASES = ["tiny_cal", "tiny_rel", "tiny_mix", "tiny_stop", "c0_12"]
+# four of the reference's real work units, cut to 12 periods (tests/golden/make_fixtures.py)
+WU_CASES = ["wu_17979", "wu_4332", "wu_26380", "wu_2543"]
 
 
 def pytest_configure(config):

@@ -11,12 +11,17 @@ into oracle/_ref/ps_ref.  Writes:
 * <case>/period_search_in, <case>/period_search_out, <case>/ref.full -- the
   seeded synthetic cases of periodsearch_gb300.synth and the reference
   binary's output for each (text and %.17g);
+* wu_<id>/period_search_in, wu_<id>/period_search_out, wu_<id>/ref.full --
+  four of the reference's real work units
+  (period_search/input_period_search/period_search_in_<id>: survey
+  photometry, all relative, L = M = 3, 288 facets, 2-1000 h), each cut to
+  its first 12 trial periods, and the reference binary's output for each;
 * unit_arrays.json -- golden arrays of the reference's unit tests
   (period_search_pure_cpu_win/UnitTest_pure_cpu_win/arrangers.cpp and the
   test inputs of InnerFunctionsTests.cpp): trifac vertex triplets, normal
   angles, the Laplace basis, the ellipsoid coefficients and the phase function.
 
-Usage: python tests/golden/make_fixtures.py [REFERENCE_ROOT]
+Usage: python tests/golden/make_fixtures.py [REFERENCE_ROOT] [--only-work-units]
 """
 from __future__ import annotations
 
@@ -38,6 +43,9 @@ from oracle_binding import REF_BIN  # noqa: E402
 from periodsearch_gb300 import synth  # noqa: E402
 
 SYNTH_CASES = ["tiny_cal", "tiny_rel", "tiny_mix", "tiny_stop", "c0_12"]
+# real work units of the reference: 1, 8, 9 and 19 lightcurves (about 100,
+# 260, 640 and 840 points)
+WORK_UNITS = ["17979", "4332", "26380", "2543"]
 
 
 def _truncate_periods(text: str, n_periods: int) -> str:
@@ -130,10 +138,25 @@ def unit_arrays(ref_root: Path) -> dict:
     return out
 
 
-def main(ref_root: Path) -> None:
+def work_units(ref_root: Path) -> None:
+    src = ref_root / "period_search" / "input_period_search"
+    for wu in WORK_UNITS:
+        d = HERE / f"wu_{wu}"
+        d.mkdir(exist_ok=True)
+        (d / "period_search_in").write_text(_truncate_periods((src / f"period_search_in_{wu}").read_text(), 12))
+        _run_ref(d)
+        for junk in ("temp", "period_search_state"):
+            (d / junk).unlink(missing_ok=True)
+
+
+def main(ref_root: Path, only_work_units: bool = False) -> None:
     if not REF_BIN.exists():
         subprocess.run(["make", "-s", "-C", str(ROOT / "oracle"), "ref", f"REF_DIR={ref_root / 'period_search'}"],
                        check=True)
+    work_units(ref_root)
+    if only_work_units:
+        print("work-unit fixtures written to", HERE)
+        return
     gold_in = ref_root / "period_search" / "period_search_in"
     shutil.copy(gold_in, HERE / "period_search_in")
     shutil.copy(ref_root / "period_search" / "period_search_out", HERE / "period_search_out")
@@ -173,4 +196,5 @@ def main(ref_root: Path) -> None:
 
 
 if __name__ == "__main__":
-    main(Path(sys.argv[1]) if len(sys.argv) > 1 else Path("/root/reference"))
+    args = [a for a in sys.argv[1:] if not a.startswith("--")]
+    main(Path(args[0]) if args else Path("/root/reference"), "--only-work-units" in sys.argv)

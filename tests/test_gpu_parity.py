@@ -20,12 +20,12 @@ from __future__ import annotations
 import numpy as np
 import pytest
 
-from conftest import GOLDEN, SYNTH_CASES
+from conftest import GOLDEN, SYNTH_CASES, WU_CASES
 
 pytestmark = pytest.mark.gpu
 
 RTOL = 1e-6
-CASES = SYNTH_CASES + ["golden"]
+CASES = SYNTH_CASES + WU_CASES + ["golden"]
 
 
 def _path(case):

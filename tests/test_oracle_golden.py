@@ -15,7 +15,7 @@ from concurrent.futures import ThreadPoolExecutor
 import numpy as np
 import pytest
 
-from conftest import GOLDEN, SYNTH_CASES
+from conftest import GOLDEN, SYNTH_CASES, WU_CASES
 
 BITEXACT = platform.machine() == "x86_64"
 
@@ -26,6 +26,33 @@ def _rows_array(rows):
 
 def _format(r):
     return "%.8f  %.6f  %.6f %4.1f %4.0f %4.0f\n" % tuple(r)
+
+
+@pytest.mark.parametrize("case", WU_CASES)
+def test_work_units_match_reference_binary(oracle, case):
+    """Real work units of the reference (survey photometry, all relative,
+    1-19 lightcurves): the first 3 periods, fitted in parallel, at the
+    convexity weight of the reference's pre-pass. The pre-pass doubles the
+    starting weight k times; row 1 prints conw_r * escl^2, which gives k. The
+    GPU tests check the pre-pass itself on these units."""
+    d = GOLDEN / case
+    ref = np.loadtxt(d / "ref.full", ndmin=2)
+    p0 = oracle.OracleProblem(d / "period_search_in")
+    inf = p0.info()
+    k = int(round(math.log2(ref[0][3] / (inf["conw_r"] * inf["escl"] ** 2))))
+    conw_r = inf["conw_r"] * 2.0 ** k
+
+    def one(n):
+        p = oracle.OracleProblem(d / "period_search_in")
+        p.setup(conw_r)
+        return p.scan(conw_r, n, n)[0]
+
+    with ThreadPoolExecutor(3) as ex:
+        got = _rows_array(list(ex.map(one, (1, 2, 3))))
+    if BITEXACT:
+        assert np.array_equal(got, ref[:3])
+    else:
+        np.testing.assert_allclose(got, ref[:3], rtol=1e-6, atol=1e-9)
 
 
 @pytest.mark.parametrize("case", [c for c in SYNTH_CASES if c != "c0_12"])
