@@ -1278,6 +1278,56 @@ double pso_phasec_export(double alpha, const double *p3, double *dcdp3)
     return scale;
 }
 
+/* One observation's brightness and derivatives (bright.c:14-126) on the
+ * nrows-row grid with the Laplace series of degree and order lmax, at
+ * parameters cg1[ma] (0-based; ma = (lmax+1)^2 + 8, three phase parameters),
+ * facet areas by curv and pole matrices by blmatrix from cg1: the
+ * quantities the reference's unit test of bright() pins.  ee, ee0: unit
+ * vectors [3]; dyda_out[ma] (0-based).  Test infrastructure. */
+double pso_unit_bright(int nrows, int lmax, const double *cg1, const double *ee3, const double *ee03, double t,
+                       double phi0, double *dyda_out)
+{
+    pso_shape *s = (pso_shape *)calloc(1, sizeof(pso_shape));
+    pso_eval_ws *w = (pso_eval_ws *)calloc(1, sizeof(pso_eval_ws));
+    pso_shape_build(s, nrows, lmax, lmax);
+    const int nphpar = 3, ma = s->ncoef + 5 + nphpar;
+    double cg[PSO_MAX_N_PAR + 1], dyda[PSO_MAX_N_PAR + 1], ee[4], ee0[4];
+    cg[0] = 0;
+    for (int k = 1; k <= ma; k++) cg[k] = cg1[k - 1];
+    ee[0] = ee0[0] = 0;
+    for (int k = 1; k <= 3; k++) {
+        ee[k] = ee3[k - 1];
+        ee0[k] = ee03[k - 1];
+    }
+    pso_curv(s, w, cg);
+    pso_blmatrix(w, cg[ma - 4 - nphpar], cg[ma - 3 - nphpar]);
+    double y = pso_bright(s, w, ee, ee0, t, cg, dyda, ma, nphpar, phi0);
+    for (int k = 1; k <= ma; k++) dyda_out[k - 1] = dyda[k];
+    free(w);
+    free(s);
+    return y;
+}
+
+/* Convexity row nc (conv.c:12-29) on the same grid at parameters cg1[ma]:
+ * returns the residual, derivatives in dres_out[ma] (0-based).  Test
+ * infrastructure. */
+double pso_unit_conv(int nrows, int lmax, const double *cg1, int nc, double *dres_out)
+{
+    pso_shape *s = (pso_shape *)calloc(1, sizeof(pso_shape));
+    pso_eval_ws *w = (pso_eval_ws *)calloc(1, sizeof(pso_eval_ws));
+    pso_shape_build(s, nrows, lmax, lmax);
+    const int ma = s->ncoef + 8;
+    double cg[PSO_MAX_N_PAR + 1], dres[PSO_MAX_N_PAR + 1];
+    cg[0] = 0;
+    for (int k = 1; k <= ma; k++) cg[k] = cg1[k - 1];
+    pso_curv(s, w, cg);
+    double r = pso_conv(s, w, nc, dres, ma);
+    for (int k = 1; k <= ma; k++) dres_out[k - 1] = dres[k];
+    free(w);
+    free(s);
+    return r;
+}
+
 /* Starting parameter vector (0-based, ma values) of the fit of period index
  * n from pole m, period_search_BOINC.cpp:819-844. */
 void pso_initial_cg(const pso_problem *p, int n, int pole, double *cg0)

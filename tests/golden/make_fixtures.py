@@ -21,7 +21,7 @@ into oracle/_ref/ps_ref.  Writes:
   test inputs of InnerFunctionsTests.cpp): trifac vertex triplets, normal
   angles, the Laplace basis, the ellipsoid coefficients and the phase function.
 
-Usage: python tests/golden/make_fixtures.py [REFERENCE_ROOT] [--only-work-units]
+Usage: python tests/golden/make_fixtures.py [REFERENCE_ROOT] [--only-work-units | --only-unit-arrays]
 """
 from __future__ import annotations
 
@@ -135,6 +135,25 @@ def unit_arrays(ref_root: Path) -> dict:
     cg = _arrays(src, "get_cg24")["_cg"]
     out["phasec"] = {"xx1": x1, "xx2": x2, "par": cg[20:23], "dphp": _arrays(src, "get_dphp")["__dphp"][1:4],
                      "scale": 1.214621163362573641464337015350}
+    # TestBright / TestConv (InnerFunctionsTests.cpp): one observation (the
+    # first point of the test object) at the 24 parameters of get_cg24;
+    # expected brightness (TestBright's _ymod), derivatives (get_dyda, index
+    # 0 = the first parameter), and the convexity row 1 (TestConv's _ymod,
+    # get_dyda_after_conv, same indexing, except that index 0 keeps the
+    # value the test array held before the call, get_dyda_before_conv's)
+    tests = (ut / "InnerFunctionsTests.cpp").read_text()
+
+    def ymod_of(method):
+        i = tests.index(f"TEST_METHOD({method})")
+        return float(re.search(r"_ymod\s*=\s*([-+0-9.eE]+)\s*;", tests[i:]).group(1))
+
+    out["bright"] = {"cg": cg[1:25], "ee": x1, "ee0": x2, "t": _arrays(src, "get_tim")["_tim"][1], "phi0": 0.0,
+                     "ymod": ymod_of("TestBright"), "dyda": _arrays(src, "get_dyda")["__dyda"][0:24],
+                     "source": "InnerFunctionsTests.cpp TestBright, arrangers.cpp get_cg24/get_tim/get_xx1/"
+                               "get_xx2/get_dyda"}
+    out["conv"] = {"cg": cg[1:25], "nc": 1, "ymod": ymod_of("TestConv"),
+                   "dyda": _arrays(src, "get_dyda_after_conv")["__dyda"][0:24],
+                   "source": "InnerFunctionsTests.cpp TestConv, arrangers.cpp get_dyda_after_conv"}
     return out
 
 
@@ -149,7 +168,11 @@ def work_units(ref_root: Path) -> None:
             (d / junk).unlink(missing_ok=True)
 
 
-def main(ref_root: Path, only_work_units: bool = False) -> None:
+def main(ref_root: Path, only_work_units: bool = False, only_unit_arrays: bool = False) -> None:
+    if only_unit_arrays:
+        (HERE / "unit_arrays.json").write_text(json.dumps(unit_arrays(ref_root)))
+        print("unit arrays written to", HERE)
+        return
     if not REF_BIN.exists():
         subprocess.run(["make", "-s", "-C", str(ROOT / "oracle"), "ref", f"REF_DIR={ref_root / 'period_search'}"],
                        check=True)
@@ -197,4 +220,5 @@ def main(ref_root: Path, only_work_units: bool = False) -> None:
 
 if __name__ == "__main__":
     args = [a for a in sys.argv[1:] if not a.startswith("--")]
-    main(Path(args[0]) if args else Path("/root/reference"), "--only-work-units" in sys.argv)
+    main(Path(args[0]) if args else Path("/root/reference"), "--only-work-units" in sys.argv,
+         "--only-unit-arrays" in sys.argv)

@@ -7,6 +7,7 @@ the reference's unit tests.  The oracle must be bit-identical on x86-64.
 """
 from __future__ import annotations
 
+import ctypes as C
 import json
 import math
 import platform
@@ -185,3 +186,42 @@ def test_reference_cross_build_agreement():
     lines = [_format(r) for r in base]
     committed = (GOLDEN / "period_search_out").read_text().splitlines(keepends=True)
     assert sum(a != b for a, b in zip(lines, committed)) == 3   # rows 59, 81, 115
+
+
+def test_bright_matches_reference_unit_test(oracle, unit):
+    """The reference's TestBright: one observation of its test object
+    (L = M = 3, 288 facets) at the 24 parameters of get_cg24 -- brightness
+    and all derivatives, with the facet areas and pole matrices computed from
+    those parameters (the reference test injects the same quantities from
+    its arrays); derivatives to the test's own 1e-9."""
+    L = oracle.lib()
+    L.pso_unit_bright.argtypes = [C.c_int, C.c_int] + [C.POINTER(C.c_double)] * 3 + [C.c_double, C.c_double,
+                                                                                       C.POINTER(C.c_double)]
+    L.pso_unit_bright.restype = C.c_double
+    b = unit["bright"]
+    dp = lambda a: a.ctypes.data_as(C.POINTER(C.c_double))   # noqa: E731
+    cg, ee, ee0 = (np.array(b[k], dtype=np.float64) for k in ("cg", "ee", "ee0"))
+    dyda = np.zeros(24)
+    ymod = L.pso_unit_bright(6, 3, dp(cg), dp(ee), dp(ee0), b["t"], b["phi0"], dp(dyda))
+    assert abs(ymod - b["ymod"]) <= 1e-15
+    np.testing.assert_allclose(dyda, b["dyda"], rtol=0, atol=1e-9)
+
+
+def test_conv_matches_reference_unit_test(oracle, unit):
+    """The reference's TestConv: convexity row 1 (sum Area n_x, which nearly
+    vanishes for this shape) and its derivatives at the same parameters.
+    The residual and several derivatives are cancellation residues of 288
+    terms; recomputing the areas here instead of injecting the test's arrays
+    moves them by up to 3e-16, so they are held to 1e-15 (the test's own
+    bound is DBL_EPSILON).  Index 0 of the expected array keeps the value the
+    test's array held before the call and is not compared."""
+    L = oracle.lib()
+    L.pso_unit_conv.argtypes = [C.c_int, C.c_int, C.POINTER(C.c_double), C.c_int, C.POINTER(C.c_double)]
+    L.pso_unit_conv.restype = C.c_double
+    c = unit["conv"]
+    cg = np.array(c["cg"], dtype=np.float64)
+    dres = np.zeros(24)
+    res = L.pso_unit_conv(6, 3, cg.ctypes.data_as(C.POINTER(C.c_double)), c["nc"],
+                          dres.ctypes.data_as(C.POINTER(C.c_double)))
+    assert abs(res - c["ymod"]) <= 2.3e-16
+    np.testing.assert_allclose(dres[1:], np.array(c["dyda"])[1:], rtol=0, atol=1e-15)
