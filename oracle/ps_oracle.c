@@ -1308,6 +1308,29 @@ double pso_unit_bright(int nrows, int lmax, const double *cg1, const double *ee3
     return y;
 }
 
+/* Facet areas and g Dsph (curv.c:10-39) on the nrows-row grid with the
+ * Laplace series of degree and order lmax, at shape coefficients
+ * cg1[ncoef] (0-based): area_out[nfac], dg_out[nfac][ncoef] (row-major).
+ * Returns nfac.  Test infrastructure. */
+int pso_unit_curv(int nrows, int lmax, const double *cg1, double *area_out, double *dg_out)
+{
+    pso_shape *s = (pso_shape *)calloc(1, sizeof(pso_shape));
+    pso_eval_ws *w = (pso_eval_ws *)calloc(1, sizeof(pso_eval_ws));
+    pso_shape_build(s, nrows, lmax, lmax);
+    double cg[PSO_MAX_N_PAR + 1];
+    cg[0] = 0;
+    for (int k = 1; k <= s->ncoef; k++) cg[k] = cg1[k - 1];
+    pso_curv(s, w, cg);
+    for (int i = 1; i <= s->nfac; i++) {
+        area_out[i - 1] = w->area[i];
+        for (int k = 1; k <= s->ncoef; k++) dg_out[(size_t)(i - 1) * s->ncoef + k - 1] = w->dg[i][k];
+    }
+    const int nf = s->nfac;
+    free(w);
+    free(s);
+    return nf;
+}
+
 /* Convexity row nc (conv.c:12-29) on the same grid at parameters cg1[ma]:
  * returns the residual, derivatives in dres_out[ma] (0-based).  Test
  * infrastructure. */

@@ -166,6 +166,7 @@ double pso_phasec_export(double alpha, const double *p3, double *dcdp3);
 double pso_unit_bright(int nrows, int lmax, const double *cg1, const double *ee3, const double *ee03, double t,
                        double phi0, double *dyda_out);
 double pso_unit_conv(int nrows, int lmax, const double *cg1, int nc, double *dres_out);
+int pso_unit_curv(int nrows, int lmax, const double *cg1, double *area_out, double *dg_out);
 void pso_initial_cg(const pso_problem *p, int n, int pole, double *cg0);
 double pso_freq(const pso_problem *p, int n);
 

@@ -151,6 +151,13 @@ def unit_arrays(ref_root: Path) -> dict:
                      "ymod": ymod_of("TestBright"), "dyda": _arrays(src, "get_dyda")["__dyda"][0:24],
                      "source": "InnerFunctionsTests.cpp TestBright, arrangers.cpp get_cg24/get_tim/get_xx1/"
                                "get_xx2/get_dyda"}
+    # TestCurv: facet areas (get_area) and g Dsph (get_dg, one array per
+    # coefficient) of the initial ellipsoid (cg_first_l3), facets and
+    # coefficients from index 0
+    dg = _arrays(src, "get_dg")
+    out["curv"] = {"area": _arrays(src, "get_area")["_area_a"][0:288],
+                   "dg": [[dg[f"_dg_{k}"][i] for k in range(16)] for i in range(288)],
+                   "source": "InnerFunctionsTests.cpp TestCurv, arrangers.cpp get_area/get_dg"}
     out["conv"] = {"cg": cg[1:25], "nc": 1, "ymod": ymod_of("TestConv"),
                    "dyda": _arrays(src, "get_dyda_after_conv")["__dyda"][0:24],
                    "source": "InnerFunctionsTests.cpp TestConv, arrangers.cpp get_dyda_after_conv"}

@@ -225,3 +225,22 @@ def test_conv_matches_reference_unit_test(oracle, unit):
                           dres.ctypes.data_as(C.POINTER(C.c_double)))
     assert abs(res - c["ymod"]) <= 2.3e-16
     np.testing.assert_allclose(dres[1:], np.array(c["dyda"])[1:], rtol=0, atol=1e-15)
+
+
+def test_curv_matches_reference_unit_test(oracle, unit):
+    """The reference's TestCurv: facet areas and g Dsph of the initial
+    ellipsoid on the 288-facet grid, L = M = 3. The check is two-sided here,
+    where the reference's own assertion is one-sided. The golden arrays come
+    from another libm (exp, and the cos/sin of the basis), hence 1e-14
+    relative and 5e-15 absolute on entries of order 1: basis values near
+    zero carry the other libm's rounding."""
+    L = oracle.lib()
+    L.pso_unit_curv.argtypes = [C.c_int, C.c_int] + [C.POINTER(C.c_double)] * 3
+    L.pso_unit_curv.restype = C.c_int
+    cg = np.array(unit["cg_first_l3"], dtype=np.float64)
+    area = np.zeros(288)
+    dg = np.zeros((288, 16))
+    dp = lambda a: a.ctypes.data_as(C.POINTER(C.c_double))   # noqa: E731
+    assert L.pso_unit_curv(6, 3, dp(cg), dp(area), dp(dg)) == 288
+    np.testing.assert_allclose(area, unit["curv"]["area"], rtol=1e-14, atol=0)
+    np.testing.assert_allclose(dg, unit["curv"]["dg"], rtol=1e-14, atol=5e-15)
