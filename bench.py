@@ -1,41 +1,51 @@
 """Benchmark: LM period fits/s on one GB300 (per GPU under torchrun).
 
-Workload: the batched scan of one synthetic asteroid with 8 dense
-relative lightcurves (3 h, 60 points each, 0.02 mag) and 500 sparse
-calibrated points over 8 years (Ndata = 980), trial periods 2-50 h with the
-reference's step rule (~40k periods x 10 initial poles), Laplace series
-L = M = 6 on the 288-facet grid, 50 LM iterations per fit.  A step is one
-contiguous chunk of the period scan (all 10 poles of each period), fitted by
-one launch of the persistent fit kernel; successive steps take chunks spread
-over the whole 2-50 h range.  Seeded synthetic data (no external dataset).
+Workload (c1): one synthetic asteroid with 8 dense relative lightcurves
+(3 h, 60 points each, 0.02 mag) and 500 sparse calibrated points over 8
+years (Ndata = 980), trial periods 2-50 h with the reference's step rule
+(40 000 periods x 10 initial poles), Laplace series L = M = 6 on the
+288-facet grid, 50 LM iterations per fit.  Seeded synthetic data (no
+external dataset).
 
-value      fits/s of the chosen form (--form, default mixed: FP32 facet stage,
-           shape contraction and alpha/beta on the tensor cores, FP64 phase,
-           chi^2, solve) with the object resident in HBM, from CUDA events
-           around the fit kernel on its own stream (sum over steps); the plain
-           FP64 form is timed on the same chunks (plain_fp64); on a window of
-           --validation-window periods around the true period every scan
-           type -- full FP64, full mixed, refined (mixed scan plus FP64 refit
-           of the minimum region) and the learned early-stop cascade -- is
-           timed and its best period compared with the full FP64 scan's
-           (validation.scans, fits/s = the window's fits over the scan's
-           kernel time);
-e2e        the same through the C ABI with host buffers: ps_prepare (host ->
-           device copy of the tables), ps_scan (rows back to the host) and
-           ps_destroy per step, wall clock;
-roofline   algorithmic FLOP of the fits (2 N F C + 60 N F + N m(m+1) + 9 F C
-           per evaluation, 2 m^3 per solve) per launch over the launch time,
-           against the FP32 (mixed) or FP64 FMA ceiling measured live on the
-           device; for the mixed form also the two contractions' shares:
-           the shape contraction (2 N F C, FP16 high/low MMAs) against the
-           measured dense BF16 figure (the FP16 rate) and the alpha/beta
-           accumulation (N m(m+1), TF32 high/low MMAs) against half of it
-           (the TF32 rate);
-cpu_baseline  the CPU oracle (a restatement of the reference's FP64 path)
-           on all host cores, one fit per thread, on a bounded sample.
+A step is one scan of a window of --window consecutive trial periods (x 10
+poles; 2000 periods = 20 000 fits by default) around the true period, in the
+chosen form (--form):
 
-`--impl reference` times that CPU implementation alone as the reference arm.
-Between timed steps a 256 MiB buffer is rewritten to flush the 126 MB L2.
+learned    (default) the learned early-stop cascade (ps_scan_learned): every
+           fit screened by 4 mixed-precision LM iterations and the in-kernel
+           predictor, the best-predicted pole of every period and all poles
+           of the periods near the best row completed in the mixed form, the
+           minimum region refitted in full by the plain FP64 form;
+refined    the full mixed-precision scan and the same FP64 refit
+           (ps_scan_refined);
+mixed      the full mixed-precision scan alone (no refit: its best period
+           is not guaranteed to be the FP64 form's);
+fp64       the plain FP64 scan.
+
+value      fits of the window per second of device time of the step's
+           fit-kernel launches (CUDA events on the engine's stream), the
+           object resident in HBM; the plain FP64 scan of the SAME window is
+           timed beside it (plain_fp64), and every step's best period is
+           compared with the FP64 scan's (validation.same_best_period), its
+           chi^2 there with the FP64 form's and with the CPU oracle's (the
+           reference's FP64 algorithm) at that period;
+e2e        the same steps through the C ABI with host buffers: ps_prepare
+           (host -> device copy of the tables), the scan (rows back to the
+           host) and ps_destroy per step, wall clock;
+roofline   the kernel with the largest share of the step's device time:
+           algorithmic FLOP of its launches (2 N F C + 60 N F + N m(m+1) +
+           9 F C per evaluation, 2 m^3 per solve) over their time, against
+           the measured dense BF16 rate (mixed kernel: its contractions run
+           on the tensor cores) or the FP64 FMA ceiling measured live (FP64
+           kernel; MEASURED_PEAKS.json has no FP64 figure); every kernel's
+           share in kernels;
+cpu_baseline  the reference's own CPU app (oracle/_ref/ps_ref, built from
+           its sources) on all host cores, one process per core, each
+           fitting one trial period of the window (10 fits) through the
+           reference's resume path.
+
+`--impl reference` times that CPU app alone as the reference arm.  Between
+timed steps a 256 MiB buffer is rewritten to flush the 126 MB L2.
 """
 from __future__ import annotations
 
@@ -49,6 +59,7 @@ import sys
 import tempfile
 import threading
 import time
+from concurrent.futures import ThreadPoolExecutor
 from pathlib import Path
 
 ROOT = Path(__file__).resolve().parent
@@ -57,6 +68,19 @@ sys.path.insert(0, str(ROOT))
 METRIC = "LM period fits/s on 1 GB300: chosen form vs plain FP64, same best P, χ² in tol"
 WORKLOAD = "c1: 8 dense relative LCs + 500 sparse points (Ndata 980), scan 2-50 h, L=M=6, 288 facets, 10 poles, 50 LM iterations"
 PROFILES = {False: ROOT / "profiles" / "fit_kernel_fp64_c1.md", True: ROOT / "profiles" / "fit_kernel_mixed_c1.md"}
+REF_BIN = ROOT / "oracle" / "_ref" / "ps_ref"
+# the c1 object (periodsearch_gb300.synth, seed 1) as committed by
+# tests/golden/make_fixtures.py --only-bench-inputs, with its generating
+# parameters: both arms read the same file
+WORKLOAD_IN = ROOT / "tests" / "golden" / "c1" / "period_search_in"
+WORKLOAD_TRUTH = ROOT / "tests" / "golden" / "c1" / "truth.json"
+# The reference app runs its convexity-weight pre-pass (at least 100 fits)
+# before any scan while the input's convexity weight is below 10
+# (conw_r * escl^2 < 10, period_search_BOINC.cpp:485-489); the timed processes
+# start at a weight above that so that they run the scan fits alone.  Every
+# fit costs the same at any weight: 51 model evaluations and 50 solves with
+# N + 3 rows (stop condition 50).
+REF_CONW = 10.5
 
 
 def _args():
@@ -65,18 +89,12 @@ def _args():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="engine", choices=["engine", "reference"])
-    ap.add_argument("--form", default="mixed", choices=["fp64", "mixed"])
-    ap.add_argument("--no-fp64-compare", action="store_true", help="skip timing the plain FP64 form")
-    ap.add_argument("--simt-compare", action="store_true",
-                    help="also time the mixed form with its contractions on the SIMT pipes")
-    ap.add_argument("--validation-window", type=int, default=300,
-                    help="periods of the window around the true period on which every scan type is compared")
+    ap.add_argument("--form", default="learned", choices=["learned", "refined", "mixed", "fp64"])
+    ap.add_argument("--window", type=int, default=2000, help="trial periods per step (x 10 poles)")
+    ap.add_argument("--no-fp64-compare", action="store_true", help="skip the FP64 scan of the window")
     ap.add_argument("--multi-object", type=int, default=0,
                     help="also time K small objects (Ndata logU[100, 2000]) packed into one launch against one "
                          "launch per object")
-    ap.add_argument("--periods-per-step", type=int, default=0,
-                    help="trial periods per step (0: one per fit slot of the device, i.e. ten fits per slot)")
-    ap.add_argument("--cpu-sample-fits", type=int, default=0, help="fits in the CPU baseline sample (0: 2 per core)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--full-scan", action="store_true",
                     help="also run the whole scan of the workload as one refined scan (rank 0) and report its "
@@ -91,16 +109,16 @@ def _dist():
     return rank, world, local
 
 
-def make_workload(tmpdir: Path):
-    from periodsearch_gb300 import read_input, synth
-
-    path = tmpdir / "period_search_in"
-    obj = synth.write_object(path, "c1")
-    return path, read_input(path), obj
-
-
 def flops_per_eval(ndata, nfac, ncoef, mfit):
     return 2.0 * ndata * nfac * ncoef + 60.0 * ndata * nfac + ndata * mfit * (mfit + 1) + 9.0 * nfac * ncoef
+
+
+def window_of(n_max: int, freq_start: float, freq_step: float, truth_h: float, width: int, rank: int = 0):
+    """[lo, hi] of `width` periods around the true period (rank r > 0: the
+    r-th window after it, so that ranks scan disjoint windows)."""
+    n_truth = int(round((freq_start - 1 / truth_h) / freq_step)) + 1
+    lo = max(1, min(n_max - width + 1, n_truth - width // 2 + rank * width))
+    return lo, lo + width - 1
 
 
 class ClockSampler:
@@ -158,21 +176,69 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def cpu_baseline(path: Path, periods, sample_fits: int):
-    """The CPU oracle on all host cores: one fit per thread (ctypes releases
-    the GIL), a bounded sample of fits of the same scan."""
+# ---------------------------------------------------------------------------
+# The reference's CPU app, one process per core (the CPU baseline and the
+# reference arm)
+# ---------------------------------------------------------------------------
+
+def _input_for_period(text: str, n: int) -> str:
+    """period_search_in whose scan ends at period index n (per_end set so
+    that n_max = n; the other tokens of line 1 are kept as written, so the
+    frequency grid is the original one) and whose convexity weight skips
+    the pre-pass (REF_CONW)."""
+    lines = text.split("\n")
+    tok = lines[0].split()
+    per_start, coef = float(tok[0]), float(tok[1])
+    jd, i, n_lc = [], 15, int(lines[14].split()[0])
+    for _ in range(n_lc):
+        npts = int(lines[i].split()[0])
+        jd.extend(float(l.split()[0]) for l in lines[i + 1:i + 1 + npts])
+        i += 1 + npts
+    step = 0.5 / (max(jd) - min(jd)) / 24 * coef          # period_search_BOINC.cpp:786
+    f_end = 1 / per_start - (n - 0.5) * step              # n_max = floor((f_s - f_e) / step) + 1 = n
+    lines[0] = " ".join([tok[0], tok[1], repr(1 / f_end), tok[3]]) + "\tperiod_start period_step period_end fixed/free"
+    lines[3] = f"{REF_CONW}\tconvexity weight"
+    return "\n".join(lines)
+
+
+def reference_step(text: str, periods: list[int]) -> float:
+    """One process of the reference app per period index, all at once, each
+    resuming at that period (period_search_state = n - 1,
+    period_search_BOINC.cpp:237-251) so that it fits that one period (10
+    poles).  Returns the wall time."""
+    with tempfile.TemporaryDirectory() as td:
+        dirs = []
+        for n in periods:
+            d = Path(td) / str(n)
+            d.mkdir()
+            (d / "period_search_in").write_text(_input_for_period(text, n))
+            (d / "period_search_state").write_text(str(n - 1))
+            dirs.append(d)
+        t0 = time.perf_counter()
+        procs = [subprocess.Popen([str(REF_BIN)], cwd=d, stdout=subprocess.DEVNULL, stderr=subprocess.DEVNULL)
+                 for d in dirs]
+        rcs = [p.wait() for p in procs]
+        dt = time.perf_counter() - t0
+        if any(rcs):
+            raise RuntimeError(f"reference app failed: exit codes {rcs}")
+        for d in dirs:
+            if len((d / "period_search_out").read_text().splitlines()) != 1:
+                raise RuntimeError("reference app did not write one row")
+    return dt
+
+
+def oracle_step(path: Path, periods: list[int], cores: int) -> float:
+    """Fallback when the reference app is not built: the CPU oracle (the
+    reference's FP64 algorithm restated), one thread per fit."""
     sys.path.insert(0, str(ROOT / "tests"))
     import oracle_binding
-    from concurrent.futures import ThreadPoolExecutor
 
     oracle_binding.build_oracle()
-    cores = os.cpu_count() or 1
-    n = sample_fits or 2 * cores
     probs = [oracle_binding.OracleProblem(path) for _ in range(cores)]
     cw = probs[0].info()["conw_r"]
     for p in probs:
         p.setup(cw)
-    jobs = [(int(periods[i % len(periods)]), 1 + i % 10) for i in range(n)]
+    jobs = [(n, m) for n in periods for m in range(1, 11)]
     lock = threading.Lock()
     free = list(range(cores))
 
@@ -189,45 +255,74 @@ def cpu_baseline(path: Path, periods, sample_fits: int):
     t0 = time.perf_counter()
     with ThreadPoolExecutor(cores) as ex:
         list(ex.map(one, jobs))
-    dt = time.perf_counter() - t0
-    return {"value": n / dt, "unit": "fits/s", "cores": cores, "kind": "port",
-            "sample": f"{n} fits (period indices of the timed chunks x poles 1-10) of the c1 scan, {cores} threads, "
-                      f"{dt:.1f} s wall"}
+    return time.perf_counter() - t0
+
+
+def cpu_rate(path: Path, text: str, periods: list[int], cores: int) -> dict:
+    """fits/s of the reference's CPU app (or the oracle port) on the given
+    periods (10 fits each)."""
+    if REF_BIN.exists():
+        dt = reference_step(text, periods)
+        kind, how = "reference", "processes of the reference app (oracle/_ref/ps_ref), one per core"
+    else:
+        dt = oracle_step(path, periods[:cores], cores)
+        kind, how = "port", "threads of the CPU oracle (reference app not built)"
+    return {"value": 10 * len(periods) / dt, "unit": "fits/s", "cores": cores, "kind": kind,
+            "sample": f"{len(periods)} trial periods x 10 poles of the c1 window, {how}, {dt:.1f} s wall",
+            "wall_s": dt}
 
 
 def run_reference_arm(args):
     rank, world, _ = _dist()
     if rank != 0:
         return
-    with tempfile.TemporaryDirectory() as td:
-        path, data, _ = make_workload(Path(td))
-        sys.path.insert(0, str(ROOT / "tests"))
-        import oracle_binding
+    # (the input is parsed by the oracle: this arm loads nothing of the engine)
+    sys.path.insert(0, str(ROOT / "tests"))
+    import oracle_binding
 
-        probe = oracle_binding.OracleProblem(path)
-        n_max = probe.info()["n_max"]
-        cores = os.cpu_count() or 1
-        periods = [1 + (k * 7919) % n_max for k in range(4 * cores)]
-        for _ in range(args.warmup):
-            cpu_baseline(path, periods, cores)
-        vals = []
-        t0 = time.perf_counter()
-        for _ in range(args.steps):
-            vals.append(cpu_baseline(path, periods, cores))
-        dt = time.perf_counter() - t0
-        fits = cores * args.steps
-        v = fits / dt
-        cb = dict(vals[-1])
-        cb["value"] = v
-        cb["sample"] = f"{args.steps} steps of {cores} fits (one per core) of the c1 scan, oracle port of the reference FP64 path"
-        line = {"metric": METRIC, "value": v, "unit": "fits/s", "n_gpus": world, "steps": args.steps,
-                "warmup": args.warmup, "ms_per_step": 1000 * dt / args.steps, "higher_is_better": True,
-                "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded generator, c1)",
-                "config": {"workload": WORKLOAD, "form": "cpu fp64 (reference algorithm)"}, "impl": "reference",
-                "cpu_baseline": cb, "e2e": {"value": v, "unit": "fits/s", "h2d_bytes_per_step": 0,
-                                            "d2h_bytes_per_step": 0}}
-        print(json.dumps(line))
+    truth = json.loads(WORKLOAD_TRUTH.read_text())
+    path = WORKLOAD_IN
+    text = path.read_text()
+    ora = oracle_binding.OracleProblem(path)
+    inf = ora.info()
+    n_max = inf["n_max"]
+    f1, f2 = ora.freq(1), ora.freq(2)
+    ora.close()
+    lo, hi = window_of(n_max, f1, f1 - f2, truth["period_h"], args.window)
+    cores = os.cpu_count() or 1
 
+    def periods_of(step):
+        return [lo + ((step * cores + i) * 7919) % (hi - lo + 1) for i in range(cores)]
+
+    for s in range(args.warmup):
+        cpu_rate(path, text, periods_of(s), cores)
+    walls, fits, kind = 0.0, 0, None
+    t0 = time.perf_counter()
+    for s in range(args.warmup, args.warmup + args.steps):
+        r = cpu_rate(path, text, periods_of(s), cores)
+        walls += r["wall_s"]
+        fits += 10 * cores
+        kind = r["kind"]
+    total = time.perf_counter() - t0
+    v = fits / walls
+    cb = {"value": v, "unit": "fits/s", "cores": cores, "kind": kind,
+          "sample": f"{args.steps} steps of {cores} trial periods x 10 poles of the c1 window "
+                    f"[{lo}, {hi}], " + ("one reference-app process per core resuming at its period; "
+                                         f"convexity weight {REF_CONW} (pre-pass skipped)"
+                                         if kind == "reference" else "CPU oracle threads")}
+    line = {"metric": METRIC, "value": v, "unit": "fits/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1000 * walls / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded generator, c1)",
+            "config": {"workload": WORKLOAD, "form": "reference CPU app, FP64", "window": [lo, hi]},
+            "impl": "reference", "cpu_baseline": cb,
+            "e2e": {"value": v, "unit": "fits/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "wall_s": total}
+    print(json.dumps(line))
+
+
+# ---------------------------------------------------------------------------
+# The engine arm
+# ---------------------------------------------------------------------------
 
 def multi_object(K: int, form: int, local: int, units_per_object: int = 8) -> dict:
     """Packed launch of K objects (sparse calibrated data, Ndata log-uniform
@@ -292,50 +387,69 @@ def _profile_traffic(mixed: bool):
     return None
 
 
-def _time_form(Engine, data, form, local, starts, chunk, warmup, steps, flush, sampler=None, tensor_cores=True):
-    """Warm-up and timed steps of one form on the given chunk starts."""
-    import torch
+class Scanner:
+    """One scan of [lo, hi] in the chosen form through the engine, with the
+    device time and algorithmic FLOP of each kernel's launches."""
 
-    eng = Engine(data, device=local, form=form, tensor_cores=tensor_cores)
-    info = eng.info
-    conw_r, _ = eng.precalc_conw()
-    fe = flops_per_eval(info.ndata, info.nfac, info.ncoef, info.mfit)
-    fs = 2.0 * info.mfit ** 3
-    for k in range(warmup):
-        flush.zero_()
-        torch.cuda.synchronize()
-        eng.scan(conw_r, starts[k], starts[k] + chunk - 1)
-    torch.cuda.synchronize()
-    kernel_ms, fits, flops, launches, rows, evals = 0.0, 0, 0.0, 0, [], 0
-    if sampler:
-        sampler.__enter__()
-    try:
-        for k in range(warmup, warmup + steps):
-            flush.zero_()
-            torch.cuda.synchronize()
-            r = eng.scan(conw_r, starts[k], starts[k] + chunk - 1)
+    def __init__(self, form: str, eng, eng64, conw_r: float, fe: float, fs: float):
+        self.form, self.eng, self.eng64, self.conw_r, self.fe, self.fs = form, eng, eng64, conw_r, fe, fs
+
+    def __call__(self, lo: int, hi: int):
+        from periodsearch_gb300 import learned
+
+        nfits = (hi - lo + 1) * 10
+        if self.form == "learned":
+            rows, st = self.eng.scan_learned(self.conw_r, lo, hi, **learned.CASCADE)
+        elif self.form == "refined":
+            rows, st = self.eng.scan_refined(self.conw_r, lo, hi)
+        else:
+            eng = self.eng64 if self.form == "fp64" else self.eng
+            rows = eng.scan(self.conw_r, lo, hi)
             t = eng.timing()
-            kernel_ms += t["kernel_ms"]
-            fits += t["fits"]
-            launches += t["launches"]
-            flops += t["evals"] * fe + (t["evals"] - t["fits"]) * fs
-            evals += t["evals"]
-            rows.append(r)
-    finally:
-        if sampler:
-            sampler.__exit__(None, None, None)
-    torch.cuda.synchronize()
-    return {"engine": eng, "conw_r": conw_r, "kernel_ms": kernel_ms, "fits": fits, "flops": flops, "evals": evals,
-            "launches": launches, "rows": rows}
+            key = "refit" if self.form == "fp64" else "complete"
+            st = {"fits_total": nfits, "launches": t["launches"], "screen_ms": 0.0, "complete_ms": 0.0,
+                  "refit_ms": 0.0, "evals_screen": 0, "evals_complete": 0, "evals_refit": 0, "fits_completed": 0,
+                  "fits_refit": 0, "fits_screened_out": 0, "refit_rounds": 0}
+            st[f"{key}_ms"] = t["kernel_ms"]
+            st[f"evals_{key}"] = t["evals"]
+            st["fits_completed" if key == "complete" else "fits_refit"] = nfits
+        screen_fits = nfits if st["evals_screen"] else 0
+        mixed_ms = st["screen_ms"] + st["complete_ms"]
+        mixed_flop = ((st["evals_screen"] + st["evals_complete"]) * self.fe +
+                      (st["evals_screen"] - screen_fits + st["evals_complete"] - st["fits_completed"]) * self.fs)
+        fp64_flop = st["evals_refit"] * self.fe + (st["evals_refit"] - st["fits_refit"]) * self.fs
+        # the FP64 refit launches are the refit rounds; every other launch is the mixed kernel
+        mixed_launches = st["launches"] - st["refit_rounds"]
+        if self.form in ("mixed", "fp64"):
+            mixed_launches = st["launches"] if self.form == "mixed" else 0
+        fp64_launches = st["launches"] - mixed_launches
+        return rows, {"device_ms": mixed_ms + st["refit_ms"], "fits": nfits, "launches": st["launches"],
+                      "mixed_ms": mixed_ms, "mixed_flop": mixed_flop, "mixed_launches": mixed_launches,
+                      "mixed_evals": st["evals_screen"] + st["evals_complete"],
+                      "fp64_ms": st["refit_ms"], "fp64_flop": fp64_flop, "fp64_launches": fp64_launches,
+                      "fp64_evals": st["evals_refit"], "stats": st}
+
+
+def _oracle_at(path: Path, conw_r: float, n: int) -> dict:
+    """The CPU oracle's row at period index n (10 poles, one thread each)."""
+    sys.path.insert(0, str(ROOT / "tests"))
+    import oracle_binding
+
+    probs = [oracle_binding.OracleProblem(path) for _ in range(10)]
+    for p in probs:
+        p.setup(conw_r)
+    with ThreadPoolExecutor(10) as ex:
+        fits = list(ex.map(lambda m: probs[m - 1].fit_n(n, m), range(1, 11)))
+    return {"rms": min(f["dev"] for f in fits)}
 
 
 def run_engine_arm(args):
-    import ctypes as C
-
     import numpy as np
     import torch
 
-    from periodsearch_gb300 import Engine, PS_FORM_FP64, PS_FORM_MIXED, _abi, build
+    import ctypes as C
+
+    from periodsearch_gb300 import Engine, PS_FORM_FP64, PS_FORM_MIXED, _abi, build, read_input
 
     rank, world, local = _dist()
     if world > 1:
@@ -344,212 +458,202 @@ def run_engine_arm(args):
         dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
     build.build()
     torch.cuda.set_device(local)
-    chosen = PS_FORM_MIXED if args.form == "mixed" else PS_FORM_FP64
     L = _abi.lib()
     p64, p32 = C.c_double(), C.c_double()
     _abi.check(L.ps_device_fma_peaks(local, C.byref(p64), C.byref(p32)), "ps_device_fma_peaks")
+    peaks = _measured_peaks()
+    bf16 = peaks.get("bf16_tflops")
 
-    with tempfile.TemporaryDirectory() as td:
-        path, data, obj = make_workload(Path(td))
-        probe = Engine(data, device=local, form=chosen)
-        n_max = int(probe.info.n_max)
-        info = probe.info
-        probe.close()
-        # a step: one launch over a whole number of waves of the fit slots
-        # (ten poles per period), as inside a long scan
-        chunk = args.periods_per_step or int(info.slots)
-        total_steps = args.warmup + args.steps
-        # chunks spread over the scan, distinct per rank (weak scaling)
-        starts = [1 + ((k * world + rank) * 7919) % (n_max - chunk) for k in range(total_steps)]
-        flush = torch.empty(256 << 20, dtype=torch.uint8, device=f"cuda:{local}")
+    truth = json.loads(WORKLOAD_TRUTH.read_text())
+    path = WORKLOAD_IN
+    text = path.read_text()
+    data = read_input(path)
+    eng = Engine(data, device=local, form=PS_FORM_MIXED)
+    eng64 = Engine(data, device=local, form=PS_FORM_FP64)
+    info = eng.info
+    n_max = int(info.n_max)
+    conw_r, _ = eng.precalc_conw()
+    fe = flops_per_eval(info.ndata, info.nfac, info.ncoef, info.mfit)
+    fs = 2.0 * info.mfit ** 3
+    scan = Scanner(args.form, eng, eng64, conw_r, fe, fs)
+    lo, hi = window_of(n_max, info.freq_start, info.freq_step, truth["period_h"], args.window, rank)
+    wfits = (hi - lo + 1) * 10
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=f"cuda:{local}")
 
-        if world > 1:
-            torch.distributed.barrier()
-        sampler = ClockSampler(local) if rank == 0 else None
-        t0 = time.perf_counter()
-        main = _time_form(Engine, data, chosen, local, starts, chunk, args.warmup, args.steps, flush, sampler)
-        if world > 1:
-            torch.distributed.barrier()
-        wall = time.perf_counter() - t0
-        # plain FP64 on the same chunks (the comparison the metric asks for)
-        plain = None
-        if chosen != PS_FORM_FP64 and not args.no_fp64_compare:
-            plain = _time_form(Engine, data, PS_FORM_FP64, local, starts, chunk, 1, args.steps, flush)
-        simt = None
-        if chosen == PS_FORM_MIXED and args.simt_compare:
-            simt = _time_form(Engine, data, chosen, local, starts, chunk, 1, args.steps, flush, tensor_cores=False)
-            simt["engine"].close()
-
-        # e2e: the whole C-ABI path with host buffers, per step
-        e2e_t, e2e_fits, h2d, d2h = 0.0, 0, 0, 0
-        for k in range(args.steps):
-            n0 = starts[args.warmup + k]
+    for _ in range(args.warmup):
+        flush.zero_()
+        torch.cuda.synchronize()
+        scan(lo, hi)
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    sampler = ClockSampler(local) if rank == 0 else None
+    if sampler:
+        sampler.__enter__()
+    steps, t0 = [], time.perf_counter()
+    try:
+        for _ in range(args.steps):
             flush.zero_()
             torch.cuda.synchronize()
             s0 = time.perf_counter()
-            e2 = Engine(data, device=local, form=chosen)
-            rows = e2.scan(main["conw_r"], n0, n0 + chunk - 1)
-            h2d = e2.info.h2d_bytes
-            e2.close()
-            e2e_t += time.perf_counter() - s0
-            e2e_fits += chunk * 10
-            d2h = chunk * 10 * C.sizeof(_abi.Fit)
-            assert np.isfinite(rows["rms"]).any()
+            rows, t = scan(lo, hi)
+            t["wall_s"] = time.perf_counter() - s0
+            steps.append((rows, t))
+    finally:
+        if sampler:
+            sampler.__exit__(None, None, None)
+    torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    wall = time.perf_counter() - t0
 
-        # validation window around the true period: same best period?
-        valid = None
-        if plain is not None and rank == 0:
-            n_truth = int(round((info.freq_start - 1 / obj.truth["period_h"]) / info.freq_step)) + 1
-            half = max(args.validation_window // 2, 1)
-            lo, hi = max(1, n_truth - half), min(n_max, n_truth + half - 1)
-            wfits = (hi - lo + 1) * 10
+    # e2e: the same steps through the C ABI with host buffers
+    e2e_t, h2d, d2h = 0.0, 0, 0
+    for _ in range(args.steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        s0 = time.perf_counter()
+        e_m = Engine(data, device=local, form=PS_FORM_MIXED)
+        e_64 = Engine(data, device=local, form=PS_FORM_FP64) if args.form in ("fp64",) else None
+        Scanner(args.form, e_m, e_64, conw_r, fe, fs)(lo, hi)
+        h2d = e_m.info.h2d_bytes + (e_64.info.h2d_bytes if e_64 else 0)
+        e_m.close()
+        if e_64:
+            e_64.close()
+        e2e_t += time.perf_counter() - s0
+    d2h = (hi - lo + 1) * C.sizeof(_abi.Row)
 
-            def _timed(fn):
-                torch.cuda.synchronize()
-                out = fn()
-                torch.cuda.synchronize()
-                return out
+    dev_s = sum(t["device_ms"] for _, t in steps) / 1e3
+    vals = torch.tensor([dev_s, e2e_t, float(wfits * args.steps)], dtype=torch.float64, device=f"cuda:{local}")
+    if world > 1:
+        import torch.distributed as dist
 
-            w_main = _timed(lambda: main["engine"].scan(main["conw_r"], lo, hi))
-            t_main = main["engine"].timing()["kernel_ms"]
-            w_plain = _timed(lambda: plain["engine"].scan(plain["conw_r"], lo, hi))
-            t_plain = plain["engine"].timing()["kernel_ms"]
-            rel_w = np.abs(w_main["rms"] - w_plain["rms"]) / w_plain["rms"]
-            rel_c = np.concatenate([np.abs(a["rms"] - b["rms"]) / b["rms"] for a, b in zip(main["rows"], plain["rows"])])
-            bm, bp = int(np.argmin(w_main["rms"])), int(np.argmin(w_plain["rms"]))
-            w_ref, st_ref = main["engine"].scan_refined(main["conw_r"], lo, hi)
-            t_ref = st_ref["complete_ms"] + st_ref["refit_ms"]
-            scans = {"fp64": {"fits_per_s": wfits / (t_plain / 1e3)},
-                     "mixed": {"fits_per_s": wfits / (t_main / 1e3)},
-                     "refined": {"fits_per_s": wfits / (t_ref / 1e3), "fp64_refits": int(st_ref["fits_refit"]),
-                                 "best_index": int(st_ref["best_index"])}}
-            try:
-                from periodsearch_gb300 import learned
+        mx = vals[:2].clone()
+        dist.all_reduce(mx, op=dist.ReduceOp.MAX)
+        sm = vals[2:].clone()
+        dist.all_reduce(sm, op=dist.ReduceOp.SUM)
+        vals = torch.cat([mx, sm])
+    dev_all, e2e_all, fits_all = vals.tolist()
 
-                _, st_l = main["engine"].scan_learned(main["conw_r"], lo, hi, **learned.CASCADE)
-                scans["learned"] = {"fits_per_s": wfits / ((st_l["screen_ms"] + st_l["complete_ms"] + st_l["refit_ms"])
-                                                           / 1e3),
-                                    "fits_screened_out": int(st_l["fits_screened_out"]),
-                                    "best_index": int(st_l["best_index"])}
-            except Exception as exc:   # no committed predictor
-                scans["learned"] = {"unavailable": str(exc)[:120]}
-            bp_all = lo + int(np.argmin(w_plain["rms"]))
-            scans["fp64"]["best_index"] = bp_all
-            scans["mixed"]["best_index"] = lo + int(np.argmin(w_main["rms"]))
-            for v in scans.values():
-                if "best_index" in v:
-                    v["same_best_period_as_fp64"] = v["best_index"] == bp_all
-            valid = {"window": [lo, hi], "truth_period_h": obj.truth["period_h"],
-                     "scans": scans,
-                     "refined_best_index": int(st_ref["best_index"]),
-                     "refined_same_best_period": int(st_ref["best_index"]) == bp_all,
-                     "refined_fp64_refits": int(st_ref["fits_refit"]),
-                     "best_index_chosen": lo + bm, "best_index_fp64": lo + bp, "same_best_period": bm == bp,
-                     "best_period_h_chosen": float(w_main["period_h"][bm]),
-                     "best_period_h_fp64": float(w_plain["period_h"][bp]),
-                     "chi2_rel_at_best": float(abs(w_main["chi2"][bm] - w_plain["chi2"][bp]) / w_plain["chi2"][bp]),
-                     "rms_rel_window_median": float(np.median(rel_w)), "rms_rel_window_max": float(rel_w.max()),
-                     "rms_rel_timed_median": float(np.median(rel_c)), "rms_rel_timed_max": float(rel_c.max())}
-
-        # the whole job: every period of the scan, chosen form, then the FP64
-        # refit of the minimum region; wall clock through the Python API
+    if rank == 0:
+        value = fits_all / dev_all
+        best_steps = [lo + int(np.argmin(r["rms"])) for r, _ in steps]
+        # ---- validation on the same window ----
+        valid, fp64 = {"window": [lo, hi], "truth_period_h": truth["period_h"],
+                       "best_index_steps": sorted(set(best_steps))}, None
+        if not args.no_fp64_compare:
+            r64 = eng64.scan(conw_r, lo, hi)
+            t64 = eng64.timing()
+            b64 = lo + int(np.argmin(r64["rms"]))
+            pv = wfits / (t64["kernel_ms"] / 1e3)
+            pflop = t64["evals"] * fe + (t64["evals"] - t64["fits"]) * fs
+            pa = pflop / (t64["kernel_ms"] / 1e3) / 1e12
+            fp64 = {"value": pv, "unit": "fits/s", "window": [lo, hi], "fits": wfits,
+                    "seconds": t64["kernel_ms"] / 1e3, "best_index": b64,
+                    "speedup_chosen_over_fp64": value / pv,
+                    "roofline": {"bound": "fp64", "achieved": pa, "peak": p64.value, "unit": "TFLOP/s",
+                                 "frac": pa / p64.value,
+                                 "peak_source": "FP64 FMA ceiling measured live by ps_device_fma_peaks"}}
+            rows_c = steps[-1][0]
+            bc = best_steps[-1]
+            orc = _oracle_at(path, conw_r, bc)
+            valid.update({
+                "best_index_fp64": b64, "same_best_period": all(b == b64 for b in best_steps),
+                "best_period_h": float(rows_c["period_h"][bc - lo]),
+                "chi2_rel_at_best_vs_fp64_form": float(abs(rows_c["chi2"][bc - lo] - r64["chi2"][b64 - lo]) /
+                                                       r64["chi2"][b64 - lo]),
+                "rms_rel_at_best_vs_oracle": float(abs(rows_c["rms"][bc - lo] - orc["rms"]) / orc["rms"]),
+                "oracle_rms_at_best": orc["rms"], "rms_at_best": float(rows_c["rms"][bc - lo])})
+            # the other forms on the same window
+            others = {}
+            for f in ("learned", "refined", "mixed"):
+                if f == args.form:
+                    continue
+                rr, tt = Scanner(f, eng, eng64, conw_r, fe, fs)(lo, hi)
+                bo = lo + int(np.argmin(rr["rms"]))
+                rel = np.abs(rr["rms"] - r64["rms"]) / r64["rms"]
+                others[f] = {"fits_per_s": wfits / (tt["device_ms"] / 1e3), "best_index": bo,
+                             "same_best_period_as_fp64": bo == b64,
+                             "rms_rel_vs_fp64_median": float(np.median(rel)),
+                             "rms_rel_vs_fp64_max": float(rel.max())}
+                if f != "mixed":
+                    others[f]["fp64_refits"] = int(tt["stats"]["fits_refit"])
+                    others[f]["refit_rounds"] = int(tt["stats"]["refit_rounds"])
+            valid["other_forms"] = others
+        # ---- per-kernel shares and the dominant kernel's roofline ----
+        mixed_ms = sum(t["mixed_ms"] for _, t in steps)
+        fp64_ms = sum(t["fp64_ms"] for _, t in steps)
+        mixed_flop = sum(t["mixed_flop"] for _, t in steps)
+        fp64_flop = sum(t["fp64_flop"] for _, t in steps)
+        mixed_l = sum(t["mixed_launches"] for _, t in steps)
+        fp64_l = sum(t["fp64_launches"] for _, t in steps)
+        launches = mixed_l + fp64_l
+        tot_ms = mixed_ms + fp64_ms
+        kname = "fit_kernel<mixed,tensor>" if info.tensor_cores else "fit_kernel<mixed>"
+        kernels = {kname: {"launches": mixed_l, "ms": mixed_ms, "share": mixed_ms / tot_ms if tot_ms else 0,
+                           "tflops": mixed_flop / (mixed_ms / 1e3) / 1e12 if mixed_ms else None},
+                   "fit_kernel<fp64>": {"launches": fp64_l, "ms": fp64_ms,
+                                        "share": fp64_ms / tot_ms if tot_ms else 0,
+                                        "tflops": fp64_flop / (fp64_ms / 1e3) / 1e12 if fp64_ms else None}}
+        if mixed_ms >= fp64_ms:
+            ach = mixed_flop / (mixed_ms / 1e3) / 1e12
+            tr = _profile_traffic(True)
+            roof = {"bound": "tensor", "kernel": kname, "achieved": ach, "peak": bf16, "unit": "TFLOP/s",
+                    "frac": ach / bf16 if bf16 else None,
+                    "traffic": tr * (wfits * args.steps / max(mixed_l, 1)) if tr else None,
+                    "peak_source": "measured dense BF16 burst of MEASURED_PEAKS.json (the FP16 MMA rate)",
+                    "algorithmic_flop_per_launch": mixed_flop / max(mixed_l, 1),
+                    "fp32_simt": {"peak": p32.value, "frac": ach / p32.value,
+                                  "peak_source": "FP32 FMA ceiling measured live by ps_device_fma_peaks"}}
+        else:
+            ach = fp64_flop / (fp64_ms / 1e3) / 1e12
+            tr = _profile_traffic(False)
+            roof = {"bound": "fp64", "kernel": "fit_kernel<fp64>", "achieved": ach, "peak": p64.value,
+                    "unit": "TFLOP/s", "frac": ach / p64.value,
+                    "traffic": None,
+                    "peak_source": "FP64 FMA ceiling measured live by ps_device_fma_peaks "
+                                   "(MEASURED_PEAKS.json has no FP64 figure)",
+                    "algorithmic_flop_per_launch": fp64_flop / max(fp64_l, 1)}
+        st = steps[-1][1]["stats"]
+        cascade = {k: st.get(k) for k in ("fits_total", "fits_screened_out", "fits_completed", "fits_refit",
+                                          "refit_rounds", "region_periods", "launches")}
+        cascade["device_ms_per_step"] = 1000 * dev_all / args.steps
+        cascade["wall_ms_per_step"] = 1000 * statistics.mean(t["wall_s"] for _, t in steps)
+        mo = multi_object(args.multi_object, PS_FORM_MIXED, local) if args.multi_object > 0 else None
         full = None
-        if args.full_scan and rank == 0:
-            eng = main["engine"]
+        if args.full_scan:
             torch.cuda.synchronize()
             t_full0 = time.perf_counter()
-            rows, st = eng.scan_refined(main["conw_r"], 1, n_max)
+            rows_f, stf = eng.scan_refined(conw_r, 1, n_max)
             torch.cuda.synchronize()
             t_full = time.perf_counter() - t_full0
-            b = int(st["best_index"])
-            full = {"periods": n_max, "fits": n_max * 10, "fp64_refits": int(st["fits_refit"]), "seconds": t_full,
-                    "fits_per_s": n_max * 10 / t_full, "best_index": b,
-                    "best_period_h": float(rows["period_h"][b - 1]), "truth_period_h": obj.truth["period_h"]}
-
-        vals = torch.tensor([main["kernel_ms"] / 1e3, e2e_t, float(main["fits"]), float(e2e_fits)],
-                            dtype=torch.float64, device=f"cuda:{local}")
-        if world > 1:
-            import torch.distributed as dist
-
-            mx = vals[:2].clone()
-            dist.all_reduce(mx, op=dist.ReduceOp.MAX)
-            sm = vals[2:].clone()
-            dist.all_reduce(sm, op=dist.ReduceOp.SUM)
-            vals = torch.cat([mx, sm])
-        dev_s, e2e_s, fits_all, e2e_fits_all = vals.tolist()
-
-        if rank == 0:
-            value = fits_all / dev_s
-            launches = main["launches"]
-            per_launch_s = (main["kernel_ms"] / 1e3) / max(launches, 1)
-            achieved = main["flops"] / max(launches, 1) / per_launch_s / 1e12
-            mixed = chosen == PS_FORM_MIXED
-            peak = p32.value if mixed else p64.value
-            traffic_fit = _profile_traffic(mixed)
-            roof = {"bound": "fp32" if mixed else "fp64", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
-                    "frac": achieved / peak if peak else None,
-                    "traffic": traffic_fit * chunk * 10 if traffic_fit else None,
-                    "peak_source": ("FP32" if mixed else "FP64") + " FMA ceiling measured live on this device by "
-                                   "ps_device_fma_peaks (MEASURED_PEAKS.json has no FP32/FP64 SIMT figure)",
-                    "kernel": ("fit_kernel<mixed,tensor>" if info.tensor_cores else "fit_kernel<mixed>")
-                    if mixed else "fit_kernel<fp64>",
-                    "algorithmic_flop_per_launch": main["flops"] / max(launches, 1),
-                    "fp64_fma_peak_tflops": p64.value, "fp32_fma_peak_tflops": p32.value}
-            if mixed and info.tensor_cores:
-                peaks = _measured_peaks()
-                f16 = peaks.get("bf16_tflops")
-                tf32 = f16 / 2 if f16 else None
-                per_s = max(launches, 1) * per_launch_s * 1e12
-                shape = main["evals"] * 2.0 * info.ndata * info.nfac * info.ncoef / per_s
-                alpha = main["evals"] * info.ndata * info.mfit * (info.mfit + 1) / per_s
-                roof["tensor_contractions"] = {
-                    "shape": {"achieved": shape, "peak": f16, "unit": "TFLOP/s",
-                              "frac": shape / f16 if f16 else None,
-                              "peak_source": "measured dense BF16 figure of MEASURED_PEAKS.json (the FP16 rate)",
-                              "what": "2 N F C per evaluation, run as FP16 high/low-split MMAs (kind::f16)"},
-                    "alpha": {"achieved": alpha, "peak": tf32, "unit": "TFLOP/s",
-                              "frac": alpha / tf32 if tf32 else None,
-                              "peak_source": "half the measured dense BF16 figure (the TF32 rate)",
-                              "what": "N m(m+1) per evaluation, run as TF32 high/low-split MMAs"}}
-            fp64 = None
-            if plain is not None:
-                pv = plain["fits"] / (plain["kernel_ms"] / 1e3)
-                pl = plain["launches"]
-                pa = plain["flops"] / max(pl, 1) / ((plain["kernel_ms"] / 1e3) / max(pl, 1)) / 1e12
-                fp64 = {"value": pv, "unit": "fits/s", "speedup_chosen_over_fp64": value / pv,
-                        "roofline": {"bound": "fp64", "achieved": pa, "peak": p64.value, "unit": "TFLOP/s",
-                                     "frac": pa / p64.value,
-                                     "traffic": (_profile_traffic(False) or 0) * chunk * 10 or None}}
-            if simt is not None:
-                sv = simt["fits"] / (simt["kernel_ms"] / 1e3)
-                roof["mixed_simt_contractions"] = {"value": sv, "unit": "fits/s", "tensor_speedup": value / sv}
-            mo = multi_object(args.multi_object, chosen, local) if args.multi_object > 0 else None
-            cb = None
-            if not args.no_cpu_baseline:
-                periods = [n for st in starts[args.warmup:] for n in range(st, st + chunk)]
-                cb = cpu_baseline(path, periods, args.cpu_sample_fits)
-            if full is not None and cb is not None:
-                # the same job on the host cores at the measured CPU rate
-                full["cpu_baseline_hours"] = full["fits"] / cb["value"] / 3600
-            line = {"metric": METRIC, "value": value, "unit": "fits/s", "n_gpus": world, "steps": args.steps,
-                    "warmup": args.warmup, "ms_per_step": main["kernel_ms"] / args.steps, "higher_is_better": True,
-                    "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64" if mixed else "f64",
-                    "data": "synthetic (seeded generator, c1 shapes; no external dataset)",
-                    "config": {"workload": WORKLOAD, "form": args.form, "periods_per_step": chunk,
-                               "fits_per_step": chunk * 10, "ndata": info.ndata, "nfac": info.nfac,
-                               "ncoef": info.ncoef, "mfit": info.mfit, "n_max": n_max, "conw_r": main["conw_r"],
-                               "slots": info.slots, "tensor_cores": bool(info.tensor_cores),
-                               "tile_points": info.tile_points, "l2": "flushed between steps (256 MiB rewrite)",
-                               "truth": obj.truth},
-                    "e2e": {"value": e2e_fits_all / e2e_s, "unit": "fits/s", "h2d_bytes_per_step": h2d,
-                            "d2h_bytes_per_step": d2h},
-                    "gpu_launches": launches, "roofline": roof, "plain_fp64": fp64, "validation": valid,
-                    "multi_object": mo, "full_scan": full,
-                    "cpu_baseline": cb, "clocks": sampler.summary() if sampler else None, "wall_s": wall}
-            print(json.dumps(line))
-        main["engine"].close()
-        if plain is not None:
-            plain["engine"].close()
+            b = int(stf["best_index"])
+            full = {"periods": n_max, "fits": n_max * 10, "fp64_refits": int(stf["fits_refit"]),
+                    "seconds": t_full, "fits_per_s": n_max * 10 / t_full, "best_index": b,
+                    "best_period_h": float(rows_f["period_h"][b - 1]), "truth_period_h": truth["period_h"]}
+        cb = None
+        if not args.no_cpu_baseline and world == 1:
+            cores = os.cpu_count() or 1
+            cb = cpu_rate(path, text, [lo + (i * 7919) % (hi - lo + 1) for i in range(cores)], cores)
+            cb.pop("wall_s", None)
+        line = {"metric": METRIC, "value": value, "unit": "fits/s", "n_gpus": world, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": 1000 * dev_all / args.steps, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None,
+                "dtype": "f64" if args.form == "fp64" else "f16/tf32 tensor + f32 + f64",
+                "data": "synthetic (seeded generator, c1 shapes; no external dataset)",
+                "config": {"workload": WORKLOAD, "form": args.form, "window": [lo, hi], "fits_per_step": wfits,
+                           "ndata": info.ndata, "nfac": info.nfac, "ncoef": info.ncoef, "mfit": info.mfit,
+                           "n_max": n_max, "conw_r": conw_r, "slots": info.slots,
+                           "tensor_cores": bool(info.tensor_cores), "tile_points": info.tile_points,
+                           "l2": "flushed between steps (256 MiB rewrite)", "truth": truth},
+                "e2e": {"value": fits_all / e2e_all, "unit": "fits/s", "h2d_bytes_per_step": h2d,
+                        "d2h_bytes_per_step": d2h},
+                "gpu_launches": launches, "roofline": roof, "kernels": kernels, "cascade": cascade,
+                "plain_fp64": fp64, "validation": valid, "multi_object": mo, "full_scan": full,
+                "cpu_baseline": cb, "clocks": sampler.summary() if sampler else None, "wall_s": wall}
+        print(json.dumps(line))
+    eng.close()
+    eng64.close()
     if world > 1:
         import torch.distributed as dist
 

@@ -41,7 +41,7 @@
 extern "C" {
 #endif
 
-#define PS_ABI_VERSION 1
+#define PS_ABI_VERSION 2
 #define PS_N_POLES 10          /* period_search/constants.h:11 */
 #define PS_POINTS_MAX 1000     /* points per lightcurve, period_search/constants.h:1 */
 #define PS_MAX_N_OBS 20000     /* points per object, period_search/constants.h:2 */
@@ -211,11 +211,19 @@ ps_status ps_fit_batch(ps_ctx *ctx, double conw_r, int64_t n_fits, const int64_t
  * device address (cudaGetSymbolAddress); make that first call before any
  * stream capture.  Every call shares the one array, so calls whose work
  * overlaps on the GPU (other streams, other contexts, other threads) race;
- * serialise them.  An object whose single fit slot needs more scratch than
- * the array holds (max relative-lightcurve points * (ma+1) doubles > 4 MiB)
- * is rejected with PS_ERR_LIMIT.  FP64 form only.  Entries of the device
- * lists must be valid (period index >= 1, pole 1..10); they are not checked.
- * ps_last_timing is not updated. */
+ * serialise them.  Fit slots: where ps_prepare parked the rows of the
+ * relative lightcurves in shared memory (e.g. 60-point lightcurves), every
+ * slot of the device runs and the array holds only the work counter.  Else
+ * each slot takes a scratch block of S = (longest relative lightcurve's
+ * points) * (ma + 3) doubles, rounded up to a multiple of 32, and the launch
+ * runs min(device slots, floor((4 MiB - 256 B) / (8 S))) slots: 17 for a
+ * 500-point relative lightcurve with ma = 57, i.e. about a ninth of a
+ * GB300's 152 slots.  An object whose S exceeds the array is rejected with
+ * PS_ERR_LIMIT; within the input limits (PS_POINTS_MAX points per
+ * lightcurve, at most 121 coefficients) S stays below 1.1 MB, so that check
+ * is a guard.  FP64 form only (a mixed-form context returns PS_ERR_ARG).
+ * Entries of the device lists must be valid (period index >= 1, pole
+ * 1..10); they are not checked.  ps_last_timing is not updated. */
 ps_status ps_fit_batch_noalloc(ps_ctx *ctx, double conw_r, int64_t n_fits, const int64_t *d_period_index,
                                const int32_t *d_pole, ps_fit *d_out, void *stream);
 /* One model evaluation (the reference's mrqcof) at parameters cg[ma]
@@ -251,6 +259,9 @@ typedef struct ps_learned_stats {
     double screen_ms, complete_ms, refit_ms;   /* kernel time of the stages */
     int64_t best_index;        /* period index of the best row */
     int64_t region_periods;    /* periods completed in all poles at stage 3 */
+    int64_t evals_screen, evals_complete, evals_refit;   /* model evaluations of each stage */
+    int32_t refit_rounds;      /* FP64 refit launches */
+    int32_t launches;          /* fit-kernel launches of the call */
 } ps_learned_stats;
 
 /* Full fits of periods n_lo..n_hi (10 poles each) in the context's form,
@@ -323,6 +334,14 @@ ps_status ps_tc_selftest(int32_t device, const float *A, const float *B, int32_t
  * Memory column, K = 16 per MMA): A and B rounded to FP16 on the device, K a
  * multiple of 16 up to 960. */
 ps_status ps_tc_selftest_f16(int32_t device, const float *A, const float *B, int32_t K, float *D);
+
+/* The bounded-wait path of the tensor-core kernels, run on purpose: one CTA
+ * holds Tensor Memory and waits on an mbarrier phase that nothing completes
+ * (no MMA issued, nothing in flight), gives up after max_polls polls
+ * (1 .. 2^22), then frees its Tensor Memory and returns.  PS_ERR_TIMEOUT is
+ * the expected result; the context stays usable.  No counterpart in the
+ * reference (the CUDA port's kernels have no bounded waits). */
+ps_status ps_tc_wait_selftest(int32_t device, int32_t max_polls);
 
 /* ---- the reference's prepared state (CUDA port host calls) ---- */
 
@@ -448,6 +467,11 @@ ps_status ps_validate_files(const char *path_a, const char *path_b, const double
 /* Writes one row in the reference's format "%.8f  %.6f  %.6f %4.1f %4.0f %4.0f\n"
  * (period_search_BOINC.cpp:928,931).  Returns the number of characters. */
 int32_t ps_format_row(const ps_row *row, char *buf, size_t len);
+/* Rows of n_periods periods from their fits (PS_N_POLES consecutive fits per
+ * period, poles 1..10): the best pole by rms, its period, pole and dark-facet
+ * % (period_search_BOINC.cpp:913-931); chi^2 = rms^2 * ndata.  The reduction
+ * ps_scan applies, for callers that run the fits with ps_fit_batch. */
+ps_status ps_rows_from_fits(const ps_fit *fits, int64_t n_periods, int32_t ndata, ps_row *out);
 
 /* ---- process-level drop-in ---- */
 /* Runs the BOINC app's job on files: reads in_path (period_search_in), resumes

@@ -232,6 +232,17 @@ class Engine:
         _abi.check(st, "ps_fit_batch", self._ctx)
         return out
 
+    def rows_of_periods(self, conw_r: float, period_index) -> np.ndarray:
+        """Rows of the given periods (all ten poles each, ps_fit_batch in
+        one launch, then the best-of-poles reduction ps_rows_from_fits)."""
+        per = np.ascontiguousarray(period_index, np.int64)
+        fits = self.fit_batch(conw_r, np.repeat(per, N_POLES), np.tile(np.arange(1, N_POLES + 1), len(per)))
+        out = np.zeros(len(per), ROW_DTYPE)
+        st = self._L.ps_rows_from_fits(fits.ctypes.data_as(C.POINTER(_abi.Fit)), len(per), self.info.ndata,
+                                       out.ctypes.data_as(C.POINTER(_abi.Row)))
+        _abi.check(st, "ps_rows_from_fits")
+        return out
+
     def eval(self, conw_r: float, cg):
         cg = np.ascontiguousarray(cg, np.float64)
         mf = self.info.mfit

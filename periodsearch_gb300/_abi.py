@@ -74,7 +74,8 @@ class LearnedStats(C.Structure):
     _fields_ = [("fits_total", C.c_int64), ("fits_screened_out", C.c_int64), ("fits_completed", C.c_int64),
                 ("fits_refit", C.c_int64), ("evals", C.c_int64), ("screen_ms", C.c_double),
                 ("complete_ms", C.c_double), ("refit_ms", C.c_double), ("best_index", C.c_int64),
-                ("region_periods", C.c_int64)]
+                ("region_periods", C.c_int64), ("evals_screen", C.c_int64), ("evals_complete", C.c_int64),
+                ("evals_refit", C.c_int64), ("refit_rounds", C.c_int32), ("launches", C.c_int32)]
 
 
 class ValidateReport(C.Structure):
@@ -155,6 +156,7 @@ SIGNATURES = {
                                  C.POINTER(C.c_float)]),
     "ps_tc_selftest_f16": (C.c_int, [C.c_int32, C.POINTER(C.c_float), C.POINTER(C.c_float), C.c_int32,
                                  C.POINTER(C.c_float)]),
+    "ps_tc_wait_selftest": (C.c_int, [C.c_int32, C.c_int32]),
     "ps_prepare_state": (C.c_int, [C.POINTER(State), C.POINTER(Options), C.POINTER(C.c_void_p)]),
     "ps_precalc_step": (C.c_int, [_CTX, C.POINTER(C.c_double), C.POINTER(C.c_int32)]),
     "ps_autotune": (C.c_int, [_CTX, C.c_double, C.c_int32, C.c_int32, C.POINTER(TuneReport)]),
@@ -175,6 +177,7 @@ SIGNATURES = {
     "ps_destroy": (None, [_CTX]),
     "ps_device_fma_peaks": (C.c_int, [C.c_int32, _D, _D]),
     "ps_format_row": (C.c_int32, [C.POINTER(Row), C.c_char_p, C.c_size_t]),
+    "ps_rows_from_fits": (C.c_int, [C.POINTER(Fit), C.c_int64, C.c_int32, C.POINTER(Row)]),
     "ps_run_files": (C.c_int, [C.c_char_p, C.c_char_p, C.c_char_p, C.POINTER(Options), C.c_int32]),
     "ps_shape_tables": (C.c_int, [C.c_int32, C.c_int32, C.c_int32, _I32, _I32, _D, _D, _D]),
 }

@@ -348,14 +348,22 @@ struct ScanFits {
 // rel (relative) of the best row or within halfwidth periods of it, and
 // repeats with the new rows until the set is closed: the best row and its
 // neighbourhood then carry FP64 values, and no row outside the set comes
-// within rel of it.
+// within rel of it.  A refit launch takes one FP64 fit's time whether it
+// fills the device's fit slots or not, so each launch is topped up with the
+// next-lowest rows (whole periods) until its last wave of slots is full:
+// periods that a later round would likely have needed come at no extra
+// time, and fewer rounds run.
 ps_status refit_minimum(ps_ctx *c, double conw_r, ScanFits &sf, double rel, int32_t halfwidth, double *ms,
-                        int64_t *nrefit, int64_t *evals)
+                        int64_t *nrefit, int64_t *evals, int32_t *rounds)
 {
+    ps_status st = make_plan(c, PS_FORM_FP64);
+    if (st != PS_OK) return st;
+    const int64_t slots = std::max(c->plan[PS_FORM_FP64].slots, 1);
     std::vector<ps_row> rows;
     std::vector<int64_t> pidx;
     std::vector<int32_t> pole;
-    std::vector<int64_t> per;
+    std::vector<int64_t> per, order;
+    std::vector<char> picked;
     for (int round = 0; round < 64; round++) {
         sf.rows(rows, c->obj.ndata);
         const int64_t best = ScanFits::best(rows);
@@ -363,21 +371,42 @@ ps_status refit_minimum(ps_ctx *c, double conw_r, ScanFits &sf, double rel, int3
         pidx.clear();
         pole.clear();
         per.clear();
+        picked.assign(static_cast<size_t>(sf.nper), 0);
         for (int64_t n = 0; n < sf.nper; n++) {
             if (sf.fp64[static_cast<size_t>(n)]) continue;
             if (!(std::llabs(n - best) <= halfwidth || rows[static_cast<size_t>(n)].rms <= lim)) continue;
             per.push_back(n);
+            picked[static_cast<size_t>(n)] = 1;
+        }
+        if (per.empty()) return PS_OK;
+        // top up the last wave with the lowest remaining rows
+        const int64_t need = static_cast<int64_t>(per.size()) * PS_N_POLES;
+        const int64_t cap = (need + slots - 1) / slots * slots;
+        if (need + PS_N_POLES <= cap) {
+            order.clear();
+            for (int64_t n = 0; n < sf.nper; n++)
+                if (!sf.fp64[static_cast<size_t>(n)] && !picked[static_cast<size_t>(n)] &&
+                    !std::isnan(rows[static_cast<size_t>(n)].rms))
+                    order.push_back(n);
+            const size_t extra = static_cast<size_t>((cap - need) / PS_N_POLES);
+            const size_t k = std::min(extra, order.size());
+            std::partial_sort(order.begin(), order.begin() + static_cast<std::ptrdiff_t>(k), order.end(),
+                              [&](int64_t a, int64_t b) {
+                                  return rows[static_cast<size_t>(a)].rms < rows[static_cast<size_t>(b)].rms;
+                              });
+            per.insert(per.end(), order.begin(), order.begin() + static_cast<std::ptrdiff_t>(k));
+        }
+        for (int64_t n : per)
             for (int m = 0; m < PS_N_POLES; m++) {
                 pidx.push_back(sf.n_lo + n);
                 pole.push_back(m + 1);
             }
-        }
-        if (per.empty()) return PS_OK;
-        ps_status st = run_list(c, conw_r, pidx.data(), pole.data(), static_cast<int64_t>(pidx.size()), PS_FORM_FP64);
+        st = run_list(c, conw_r, pidx.data(), pole.data(), static_cast<int64_t>(pidx.size()), PS_FORM_FP64);
         if (st != PS_OK) return st;
         *ms += c->timing.kernel_ms;
         *evals += c->timing.evals;
         *nrefit += static_cast<int64_t>(pidx.size());
+        *rounds += 1;
         for (size_t k = 0; k < per.size(); k++) {
             const int64_t n = per[k];
             sf.fp64[static_cast<size_t>(n)] = 1;
@@ -752,6 +781,7 @@ ps_status ps_fit_batch_noalloc(ps_ctx *c, double conw_r, int64_t n_fits, const i
     w.period_index = d_period_index;
     w.pole = d_pole;
     w.scratch_stride = c->scratch_stride;
+    w.rel_rows = c->rel_rows;   // rows in shared memory where the plan put them there
     w.out = d_out;
     int grid = 0;
     int e = psg::launch_fits_noalloc(c->opt.form, c->dob, cfg, w, c->slots, c->P, c->smem, stream, &grid);
@@ -894,6 +924,7 @@ ps_status ps_scan_learned(ps_ctx *c, double conw_r, int64_t n_lo, int64_t n_hi, 
     if (st != PS_OK) return st;
     stt.screen_ms = c->timing.kernel_ms;
     stt.evals += c->timing.evals;
+    stt.evals_screen = c->timing.evals;
     sf.fits = c->h_fits;
     sf.done.assign(static_cast<size_t>(nfits), 0);
     sf.fp64.assign(static_cast<size_t>(sf.nper), 0);
@@ -913,6 +944,7 @@ ps_status ps_scan_learned(ps_ctx *c, double conw_r, int64_t n_lo, int64_t n_hi, 
         if (r != PS_OK) return r;
         stt.complete_ms += c->timing.kernel_ms;
         stt.evals += c->timing.evals;
+        stt.evals_complete += c->timing.evals;
         for (int64_t k = 0; k < n; k++)
             sf.fits[static_cast<size_t>(slot[static_cast<size_t>(k)])] = c->h_fits[static_cast<size_t>(k)];
         pidx.clear();
@@ -956,8 +988,11 @@ ps_status ps_scan_learned(ps_ctx *c, double conw_r, int64_t n_lo, int64_t n_hi, 
     for (char d : sf.done) stt.fits_completed += d;
     stt.fits_screened_out = nfits - stt.fits_completed;
     // (4) FP64 refit of the periods nearest the best row
-    st = refit_minimum(c, conw_r, sf, o.refit_rel, o.refit_halfwidth, &stt.refit_ms, &stt.fits_refit, &stt.evals);
+    const int64_t ev0 = stt.evals;
+    st = refit_minimum(c, conw_r, sf, o.refit_rel, o.refit_halfwidth, &stt.refit_ms, &stt.fits_refit, &stt.evals,
+                       &stt.refit_rounds);
     if (st != PS_OK) return st;
+    stt.evals_refit = stt.evals - ev0;
     sf.rows(rows, c->obj.ndata);
     best = ScanFits::best(rows);
     for (int64_t n = 0; n < sf.nper; n++) out[n] = rows[static_cast<size_t>(n)];
@@ -967,6 +1002,7 @@ ps_status ps_scan_learned(ps_ctx *c, double conw_r, int64_t n_lo, int64_t n_hi, 
     c->timing.fits = nfits;
     c->timing.evals = stt.evals;
     c->timing.launches = static_cast<int32_t>(c->launch_total - launch0);
+    stt.launches = c->timing.launches;
     if (stats) *stats = stt;
     return PS_OK;
 }
@@ -991,12 +1027,15 @@ ps_status ps_scan_refined(ps_ctx *c, double conw_r, int64_t n_lo, int64_t n_hi, 
     if (st != PS_OK) return st;
     stt.complete_ms = c->timing.kernel_ms;
     stt.evals = c->timing.evals;
+    stt.evals_complete = c->timing.evals;
     stt.fits_completed = nfits;
     sf.fits = c->h_fits;
     sf.done.assign(static_cast<size_t>(nfits), 1);
     sf.fp64.assign(static_cast<size_t>(sf.nper), c->opt.form == PS_FORM_FP64 ? 1 : 0);
-    st = refit_minimum(c, conw_r, sf, refit_rel, refit_halfwidth, &stt.refit_ms, &stt.fits_refit, &stt.evals);
+    st = refit_minimum(c, conw_r, sf, refit_rel, refit_halfwidth, &stt.refit_ms, &stt.fits_refit, &stt.evals,
+                       &stt.refit_rounds);
     if (st != PS_OK) return st;
+    stt.evals_refit = stt.evals - stt.evals_complete;
     std::vector<ps_row> rows;
     sf.rows(rows, c->obj.ndata);
     for (int64_t n = 0; n < sf.nper; n++) out[n] = rows[static_cast<size_t>(n)];
@@ -1006,6 +1045,7 @@ ps_status ps_scan_refined(ps_ctx *c, double conw_r, int64_t n_lo, int64_t n_hi, 
     c->timing.fits = nfits;
     c->timing.evals = stt.evals;
     c->timing.launches = static_cast<int32_t>(c->launch_total - launch0);
+    stt.launches = c->timing.launches;
     if (stats) *stats = stt;
     return PS_OK;
 }
@@ -1349,6 +1389,13 @@ ps_status ps_device_fma_peaks(int32_t device, double *fp64_tflops, double *fp32_
     if (cudaSetDevice(device) != cudaSuccess) return PS_ERR_NO_DEVICE;
     int e = psg::measure_fma_peaks(fp64_tflops, fp32_tflops, nullptr);
     return e == 0 ? PS_OK : PS_ERR_CUDA;
+}
+
+ps_status ps_rows_from_fits(const ps_fit *fits, int64_t n_periods, int32_t ndata, ps_row *out)
+{
+    if (!fits || !out || n_periods < 0 || ndata < 1) return PS_ERR_ARG;
+    for (int64_t n = 0; n < n_periods; n++) out[n] = psg::best_of_poles(fits + n * PS_N_POLES, ndata);
+    return PS_OK;
 }
 
 int32_t ps_format_row(const ps_row *r, char *buf, size_t len)

@@ -82,7 +82,12 @@ static __device__ __align__(256) double g_noalloc_scratch[kStaticScratchDoubles]
 
 namespace {
 std::mutex g_noalloc_mutex;
-double *g_noalloc_ptr[64] = {};  // device address of g_noalloc_scratch, per device ordinal
+// Device address of g_noalloc_scratch, per device ordinal, looked up once.
+// The cache assumes that the device's primary context outlives every call:
+// after cudaDeviceReset (or a reset of the primary context) the address is
+// stale, so a process that resets a device must not call the entry point on
+// it again.
+double *g_noalloc_ptr[64] = {};
 }  // namespace
 
 int launch_fits_noalloc(int form, const DevObject &ob, const FitConfig &cfg, FitWork w, int max_grid, int P,
@@ -107,8 +112,11 @@ int launch_fits_noalloc(int form, const DevObject &ob, const FitConfig &cfg, Fit
         }
         base = g_noalloc_ptr[dev];
     }
+    // Rows parked in shared memory (w.rel_rows > 0): the kernel reads no
+    // global scratch, only the counter, and every slot of the plan runs.
+    // Otherwise each slot takes a scratch block of the array.
     const size_t usable = kStaticScratchDoubles - kStaticCounterDoubles;
-    const int64_t slots = static_cast<int64_t>(usable / w.scratch_stride);
+    const int64_t slots = w.rel_rows > 0 ? max_grid : static_cast<int64_t>(usable / w.scratch_stride);
     if (slots < 1) return -1;  // one slot's scratch exceeds the array
     int64_t grid = slots < max_grid ? slots : max_grid;
     if (grid > w.nfits) grid = w.nfits;

@@ -96,6 +96,29 @@ tc_selftest_kernel(const float *A, const float *B, int K, float *D, int *status)
     if (warp == 0) tc::tmem_dealloc(tbase, kTmemCols);
 }
 
+// The bounded-wait path of the kernels, exercised on purpose: the CTA holds
+// Tensor Memory, waits on an mbarrier phase that nothing will complete (no
+// MMA is issued, nothing arrives), gives up after max_polls polls, records
+// the timeout and frees its Tensor Memory -- what a fit slot does when a
+// tensor-core wait expires.  Nothing is in flight when it gives up.
+__global__ void __launch_bounds__(128, 1) tc_wait_selftest_kernel(uint32_t max_polls, int *status)
+{
+    __shared__ __align__(16) uint64_t mbar;
+    __shared__ uint32_t slot;
+    const int tid = threadIdx.x, warp = tid >> 5;
+    if (warp == 0) tc::tmem_alloc(&slot, 32);
+    if (tid == 0) tc::mbar_init(&mbar, 1);
+    tc::fence_before_sync();
+    __syncthreads();
+    tc::fence_after_sync();
+    const uint32_t tbase = slot;
+    const bool ok = __syncthreads_and(tc::mbar_wait(&mbar, 0, max_polls));
+    if (tid == 0) *status = ok ? 2 : 1;   // 1: the wait gave up (expected); 2: the phase completed
+    tc::fence_before_sync();
+    __syncthreads();
+    if (warp == 0) tc::tmem_dealloc(tbase, 32);
+}
+
 }  // namespace
 }  // namespace psg
 
@@ -152,4 +175,27 @@ extern "C" ps_status ps_tc_selftest_f16(int32_t device, const float *A, const fl
 {
     if (!A || !B || !D || K < 16 || K > 960 || K % 16) return PS_ERR_ARG;
     return run_selftest<1>(device, A, B, K, D);
+}
+
+extern "C" ps_status ps_tc_wait_selftest(int32_t device, int32_t max_polls)
+{
+    if (max_polls < 1 || max_polls > (1 << 22)) return PS_ERR_ARG;
+    if (cudaSetDevice(device) != cudaSuccess) return PS_ERR_NO_DEVICE;
+    int *dS = nullptr;
+    if (cudaMalloc(&dS, sizeof(int)) != cudaSuccess) return PS_ERR_CUDA;
+    int hs = 0;
+    ps_status st = PS_OK;
+    if (cudaMemset(dS, 0, sizeof(int)) != cudaSuccess) st = PS_ERR_CUDA;
+    if (st == PS_OK) {
+        psg::tc_wait_selftest_kernel<<<1, 128>>>(static_cast<uint32_t>(max_polls), dS);
+        if (cudaDeviceSynchronize() != cudaSuccess || cudaMemcpy(&hs, dS, sizeof(int), cudaMemcpyDeviceToHost) !=
+                                                          cudaSuccess)
+            st = PS_ERR_CUDA;
+        else if (hs == 1)
+            st = PS_ERR_TIMEOUT;
+        else if (hs != 2)
+            st = PS_ERR_CUDA;
+    }
+    cudaFree(dS);
+    return st;
 }

@@ -10,12 +10,14 @@ is the argmin of the concatenated rms column.  The only exchange is that
 host-side gather of the rows (``torch.distributed.all_gather_object``; gloo
 or NCCL process group), after the GPU work.
 
-With ``refine`` every rank refits the minimum region of its own range with
-the FP64 form (ps_scan_refined).  The global best row is some rank's local
-best, and every row within ``refit_rel`` of the global best lies within
-``refit_rel`` of its own range's best, so the union of the local refits
-covers the global refit set except the +-``refit_halfwidth`` neighbours that
-fall across a range boundary.
+With ``refine`` the minimum region is refitted with the plain FP64 form
+over the GATHERED rows (``refine_sharded``), the rule of ps_scan_refined
+applied to the whole range: every rank knows every row after the gather, so
+all ranks compute the same refit set (the periods within ``refit_rel`` of
+the global best row and the +-``refit_halfwidth`` periods around it, also
+across range boundaries); each rank refits the part of the set in its own
+range, the refitted rows are gathered, and the rounds repeat until the set
+is closed.  The only exchanges are these host-side gathers.
 
 Objects of a multi-object run (many small work units) are balanced by
 Ndata x periods with a longest-first greedy assignment.
@@ -95,12 +97,55 @@ def scan_sharded(scan: Callable[[int, int], np.ndarray], n_lo: int, n_hi: int, g
     return rows, n_lo + int(np.argmin(rows["rms"]))
 
 
+def refine_sharded(rows: np.ndarray, refit: Callable[[list], np.ndarray], n_lo: int, rel: float = 0.01,
+                   halfwidth: int = 2, group=None, max_rounds: int = 64):
+    """FP64 refit of the minimum region of gathered rows (every rank holds
+    the same rows).  Each round computes the refit set of the whole range --
+    the periods not yet refitted whose row lies within ``rel`` of the best
+    row, or within ``halfwidth`` periods of it -- refits this rank's share
+    with ``refit(period_indices) -> rows`` and gathers the refitted rows.
+    Returns (rows, index of the best period, periods refitted)."""
+    import torch.distributed as dist
+
+    if dist.is_available() and dist.is_initialized():
+        rank, world = dist.get_rank(group), dist.get_world_size(group)
+    else:
+        rank, world = 0, 1
+    rows = rows.copy()
+    n = len(rows)
+    shards = period_shards(n_lo, n_lo + n - 1, world)
+    lo, hi = shards[rank]
+    done = np.zeros(n, bool)
+    for _ in range(max_rounds):
+        best = int(np.argmin(rows["rms"]))
+        lim = rows["rms"][best] * (1 + rel)
+        idx = np.arange(n)
+        want = ~done & ((np.abs(idx - best) <= halfwidth) | (rows["rms"] <= lim))
+        if not want.any():
+            break
+        mine = [n_lo + int(i) for i in np.flatnonzero(want) if lo <= n_lo + i <= hi]
+        local = (mine, refit(mine) if mine else None)
+        if world > 1:
+            parts = [None] * world
+            dist.all_gather_object(parts, local, group=group)
+        else:
+            parts = [local]
+        for per, new_rows in parts:
+            if per:
+                rows[np.asarray(per) - n_lo] = new_rows
+        done |= want
+    return rows, n_lo + int(np.argmin(rows["rms"])), int(done.sum())
+
+
 def main(argv=None) -> int:
     ap = argparse.ArgumentParser(description="sharded period scan, one process per GPU")
     ap.add_argument("input")
     ap.add_argument("output")
     ap.add_argument("--form", choices=("fp64", "mixed"), default="fp64")
-    ap.add_argument("--refine", action="store_true", help="FP64 refit of each range's minimum region")
+    ap.add_argument("--refine", action="store_true",
+                    help="FP64 refit of the minimum region of the gathered rows (refine_sharded)")
+    ap.add_argument("--backend", choices=("nccl", "gloo"), default=None,
+                    help="process group backend (default: nccl with GPUs, else gloo)")
     args = ap.parse_args(argv)
     import torch
     import torch.distributed as dist
@@ -110,16 +155,16 @@ def main(argv=None) -> int:
     world = int(os.environ.get("WORLD_SIZE", "1"))
     local_rank = int(os.environ.get("LOCAL_RANK", "0"))
     if world > 1:
-        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+        dist.init_process_group(args.backend or ("nccl" if torch.cuda.is_available() else "gloo"))
     build.build()
     form = PS_FORM_MIXED if args.form == "mixed" else PS_FORM_FP64
-    with Engine(read_input(args.input), device=local_rank, form=form) as eng:
+    data = read_input(args.input)
+    with Engine(data, device=local_rank, form=form) as eng:
         conw_r, _ = eng.precalc_conw()          # deterministic: the same on every rank
-        if args.refine:
-            fn = lambda lo, hi: eng.scan_refined(conw_r, lo, hi)[0]   # noqa: E731
-        else:
-            fn = lambda lo, hi: eng.scan(conw_r, lo, hi)              # noqa: E731
-        rows, best = scan_sharded(fn, 1, int(eng.info.n_max))
+        rows, best = scan_sharded(lambda lo, hi: eng.scan(conw_r, lo, hi), 1, int(eng.info.n_max))
+        if args.refine and form != PS_FORM_FP64:
+            with Engine(data, device=local_rank, form=PS_FORM_FP64) as eng64:
+                rows, best, _ = refine_sharded(rows, lambda per: eng64.rows_of_periods(conw_r, per), 1)
     if int(os.environ.get("RANK", "0")) == 0:
         with open(args.output, "w") as f:
             f.writelines(format_row(r) for r in rows)

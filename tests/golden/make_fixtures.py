@@ -1,8 +1,8 @@
 """Generates the golden fixtures of tests/golden/ from the reference tree.
 
-Run in a container where the reference project is mounted (default
-/root/reference) after `make -C oracle ref` has built the reference CPU app
-into oracle/_ref/ps_ref.  Writes:
+Run where the reference project is present, after `make -C oracle ref
+REF_DIR=<reference root>/period_search` has built the reference CPU app into
+oracle/_ref/ps_ref.  Writes:
 
 * period_search_in / period_search_out -- the reference's own committed
   golden input/output pair (period_search/period_search_in and _out);
@@ -16,12 +16,18 @@ into oracle/_ref/ps_ref.  Writes:
   (period_search/input_period_search/period_search_in_<id>: survey
   photometry, all relative, L = M = 3, 288 facets, 2-1000 h), each cut to
   its first 12 trial periods, and the reference binary's output for each;
+* c1/period_search_in, c1/truth.json -- the benchmark's workload (the
+  seeded c1 object of periodsearch_gb300.synth) and its generating
+  parameters, so that the benchmark's CPU arms read the input without the
+  engine's library (also written alone by --only-bench-inputs, which needs
+  no reference tree);
 * unit_arrays.json -- golden arrays of the reference's unit tests
   (period_search_pure_cpu_win/UnitTest_pure_cpu_win/arrangers.cpp and the
   test inputs of InnerFunctionsTests.cpp): trifac vertex triplets, normal
   angles, the Laplace basis, the ellipsoid coefficients and the phase function.
 
-Usage: python tests/golden/make_fixtures.py [REFERENCE_ROOT] [--only-work-units | --only-unit-arrays]
+Usage: python tests/golden/make_fixtures.py REFERENCE_ROOT [--only-work-units | --only-unit-arrays]
+       python tests/golden/make_fixtures.py --only-bench-inputs
 """
 from __future__ import annotations
 
@@ -175,7 +181,20 @@ def work_units(ref_root: Path) -> None:
             (d / junk).unlink(missing_ok=True)
 
 
+BENCH_CASES = ["c1"]
+
+
+def bench_inputs() -> None:
+    for case in BENCH_CASES:
+        d = HERE / case
+        d.mkdir(exist_ok=True)
+        obj = synth.make_object(case)
+        (d / "period_search_in").write_text(obj.text)
+        (d / "truth.json").write_text(json.dumps(obj.truth, indent=1) + "\n")
+
+
 def main(ref_root: Path, only_work_units: bool = False, only_unit_arrays: bool = False) -> None:
+    bench_inputs()
     if only_unit_arrays:
         (HERE / "unit_arrays.json").write_text(json.dumps(unit_arrays(ref_root)))
         print("unit arrays written to", HERE)
@@ -227,5 +246,9 @@ def main(ref_root: Path, only_work_units: bool = False, only_unit_arrays: bool =
 
 if __name__ == "__main__":
     args = [a for a in sys.argv[1:] if not a.startswith("--")]
-    main(Path(args[0]) if args else Path("/root/reference"), "--only-work-units" in sys.argv,
-         "--only-unit-arrays" in sys.argv)
+    if "--only-bench-inputs" in sys.argv:
+        bench_inputs()
+        sys.exit(0)
+    if not args:
+        sys.exit("\n".join(__doc__.strip().splitlines()[-2:]))
+    main(Path(args[0]), "--only-work-units" in sys.argv, "--only-unit-arrays" in sys.argv)

@@ -102,3 +102,28 @@ def test_tc_f16_random_matches_f16_reference(engine_lib):
     got = _tc16(A, B)
     scale = np.abs(A).astype(np.float64) @ np.abs(B).T.astype(np.float64)
     assert np.max(np.abs(got - ref) / scale) < 1e-5
+
+
+def test_bounded_wait_gives_up_and_context_stays_usable(engine_lib):
+    """A wait on an mbarrier phase that nothing completes gives up after its
+    poll limit, reports PS_ERR_TIMEOUT and frees its Tensor Memory; the
+    device context then still runs the tensor-core self-test (exact integer
+    products) and a mixed-form scan that matches the FP64 form."""
+    from conftest import GOLDEN
+    from periodsearch_gb300 import PS_FORM_FP64, PS_FORM_MIXED, Engine, _abi, read_input
+
+    L = _abi.lib()
+    assert L.ps_tc_wait_selftest(0, 64) == _abi.PS_ERR_TIMEOUT
+    assert L.ps_tc_wait_selftest(0, 0) == _abi.PS_ERR_ARG
+    assert L.ps_tc_wait_selftest(0, 4096) == _abi.PS_ERR_TIMEOUT     # twice in a row
+    rng = np.random.default_rng(11)
+    A = rng.integers(-8, 9, (128, 64)).astype(np.float32)
+    B = rng.integers(-8, 9, (32, 64)).astype(np.float32)
+    np.testing.assert_array_equal(_tc(A, B), A.astype(np.float64) @ B.T.astype(np.float64))
+    data = read_input(GOLDEN / "tiny_cal" / "period_search_in")
+    with Engine(data, form=PS_FORM_MIXED) as eng, Engine(data, form=PS_FORM_FP64) as e64:
+        assert eng.info.tensor_cores == 1
+        conw_r = eng.info.conw_r0
+        mixed = eng.scan(conw_r, 1, 3)
+        ref = e64.scan(conw_r, 1, 3)
+    np.testing.assert_allclose(mixed["rms"], ref["rms"], rtol=5e-2)

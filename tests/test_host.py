@@ -26,7 +26,7 @@ def test_library_exports_every_declared_symbol(engine_lib):
     for n in names:
         assert hasattr(engine_lib, n), n
         assert n in _abi.SIGNATURES, f"{n} has no ctypes signature"
-    assert engine_lib.ps_abi_version() == 1
+    assert engine_lib.ps_abi_version() == 2
 
 
 def test_reader_matches_oracle(engine_lib, oracle):
@@ -114,3 +114,16 @@ def test_prepare_without_device_fails_loudly(engine_lib):
     with pytest.raises(EngineError) as e:
         Engine(read_input(GOLDEN / "tiny_cal" / "period_search_in"))
     assert e.value.status == _abi.PS_ERR_NO_DEVICE
+
+
+def test_bench_workload_fixture_is_the_generator_output():
+    """The benchmark's committed c1 input is exactly what the seeded
+    generator writes (tests/golden/make_fixtures.py --only-bench-inputs)."""
+    import json
+
+    from periodsearch_gb300 import synth
+
+    obj = synth.make_object("c1")
+    d = GOLDEN / "c1"
+    assert (d / "period_search_in").read_text() == obj.text
+    assert json.loads((d / "truth.json").read_text()) == obj.truth

@@ -115,3 +115,83 @@ def test_gloo_rank_with_empty_range(oracle):
     res = _run(2, path, 4, 4)
     assert res[0][0] == [(4, 4)] and res[1][0] == []
     assert len(res[1][1]) == 1 and res[0][2] == res[1][2] == 4
+
+
+def _synthetic_rows(n, best):
+    """Rows whose minimum lies at index best, with a near tie four periods
+    away, and a refit that lowers every row by a period-dependent amount."""
+    from periodsearch_gb300 import ROW_DTYPE
+
+    rows = np.zeros(n, ROW_DTYPE)
+    k = np.arange(n)
+    rows["rms"] = 0.1 + 0.001 * np.abs(k - best) + 0.0002 * np.sin(k)
+    rows["rms"][best + 4] = rows["rms"][best] * 1.004
+    rows["period_h"] = 5.0 + 0.01 * k
+    return rows
+
+
+def _refit_rows(n_lo, base):
+    def refit(per):
+        out = base[np.asarray(per) - n_lo].copy()
+        out["rms"] -= 1e-4 * (np.asarray(per) % 7)
+        out["chi2"] = 1.0
+        return out
+    return refit
+
+
+def _refine_rank(rank, world, port, n_lo, rows, q):
+    try:
+        import torch.distributed as dist
+
+        from periodsearch_gb300.shard import refine_sharded
+
+        dist.init_process_group("gloo", init_method=f"tcp://127.0.0.1:{port}", rank=rank, world_size=world)
+        calls = []
+        base = _refit_rows(n_lo, rows)
+
+        def refit(per):
+            calls.append(list(per))
+            return base(per)
+
+        out, best, nref = refine_sharded(rows, refit, n_lo, rel=0.005, halfwidth=2)
+        q.put((rank, calls, out, best, nref))
+        dist.destroy_process_group()
+    except Exception as e:          # reported to the parent
+        q.put((rank, repr(e), None, None, None))
+
+
+def test_gloo_refine_across_range_boundary():
+    """The FP64 refit of the minimum region runs on the gathered rows: with
+    the best period right at the boundary between two ranks' ranges, its
+    neighbours on the other rank's side are refitted too, and the two ranks'
+    result equals one process's."""
+    from periodsearch_gb300.shard import period_shards, refine_sharded
+
+    n_lo, n = 11, 20
+    lo1 = period_shards(n_lo, n_lo + n - 1, 2)[1][0]
+    best = lo1 - n_lo - 1                    # last period of rank 0's range
+    rows = _synthetic_rows(n, best)
+    want, want_best, want_n = refine_sharded(rows, _refit_rows(n_lo, rows), n_lo, rel=0.005, halfwidth=2)
+    ctx = mp.get_context("spawn")
+    q = ctx.Queue()
+    port = _free_port()
+    ps = [ctx.Process(target=_refine_rank, args=(r, 2, port, n_lo, rows, q)) for r in range(2)]
+    for p in ps:
+        p.start()
+    res = {}
+    for _ in ps:
+        rank, calls, out, b, nref = q.get(timeout=300)
+        assert not isinstance(calls, str), calls
+        res[rank] = (calls, out, b, nref)
+    for p in ps:
+        p.join(timeout=60)
+        assert p.exitcode == 0
+    refitted = sorted(i for r in res.values() for c in r[0] for i in c)
+    assert refitted == sorted(set(refitted))                    # every period refitted once
+    for k in (1, 2):
+        assert n_lo + best + k in refitted                      # across the boundary (rank 1's range)
+        assert n_lo + best - k in refitted
+    assert all(i >= lo1 for c in res[1][0] for i in c) and all(i < lo1 for c in res[0][0] for i in c)
+    for calls, out, b, nref in res.values():
+        np.testing.assert_array_equal(out, want)
+        assert b == want_best and nref == want_n
