@@ -12,10 +12,11 @@ poles; 2000 periods = 20 000 fits by default) around the true period, in the
 chosen form (--form):
 
 learned    (default) the learned early-stop cascade (ps_scan_learned): every
-           fit screened by 4 mixed-precision LM iterations and the in-kernel
-           predictor, the best-predicted pole of every period and all poles
-           of the periods near the best row completed in the mixed form, the
-           minimum region refitted in full by the plain FP64 form;
+           fit screened by 8 mixed-precision LM iterations and the in-kernel
+           predictor, periods completed (resumed from their screening state)
+           in the order of their predicted rows until none can beat the best
+           completed row by the calibrated margin, the minimum region
+           refitted in full by the plain FP64 form;
 refined    the full mixed-precision scan and the same FP64 refit
            (ps_scan_refined);
 mixed      the full mixed-precision scan alone (no refit: its best period
@@ -399,7 +400,7 @@ class Scanner:
 
         nfits = (hi - lo + 1) * 10
         if self.form == "learned":
-            rows, st = self.eng.scan_learned(self.conw_r, lo, hi, **learned.CASCADE)
+            rows, st = self.eng.scan_learned(self.conw_r, lo, hi, **learned.cascade_defaults())
         elif self.form == "refined":
             rows, st = self.eng.scan_refined(self.conw_r, lo, hi)
         else:

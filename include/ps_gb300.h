@@ -240,33 +240,40 @@ void ps_destroy(ps_ctx *ctx);
 ps_status ps_device_fma_peaks(int32_t device, double *fp64_tflops, double *fp32_tflops);
 
 /* ---- learned early stop ----
- * A 10-64-64-1 GELU perceptron (FP32) predicts, from the first 4 LM
- * iterations of a fit (log ratios of the accepted chi^2 to the starting
- * chi^2, log10 lambda after each iteration, log Ndata, log trial period [h]),
- * log(final rms / rms after 4 iterations).  Weights: PS_MLP_FLOATS floats
- * (input mean/std, W1[64][10], b1, W2[64][64], b2, W3[64], b3, target
- * mean/std).  No counterpart in the reference. */
+ * A 10-64-64-1 GELU perceptron (FP32) predicts, from the first K LM
+ * iterations of a fit (K = the screening depth, a multiple of 4: log ratios
+ * of the accepted chi^2 after iterations K/4, K/2, 3K/4 and K to the
+ * starting chi^2, log10 lambda after the same iterations, log Ndata, log
+ * trial period [h]), log(final rms / rms after K iterations).  Weights:
+ * PS_MLP_FLOATS floats (input mean/std, W1[64][10], b1, W2[64][64], b2,
+ * W3[64], b3, target mean/std); a network is trained for one K.  No
+ * counterpart in the reference. */
 #define PS_MLP_FEATURES 10
 #define PS_MLP_FLOATS 4951
-#define PS_TRAJ_FLOATS 16   /* features[10], rms after 4 iterations, final rms, iterations, 3 spare */
+#define PS_TRAJ_FLOATS 16   /* features[10] after K iterations, rms after K iterations, final rms,
+                               iterations, rms after 8, 16 and 32 iterations (0 if the fit stopped
+                               before) */
 
 typedef struct ps_learned_stats {
     int64_t fits_total;        /* fits of the scan (periods x 10 poles) */
     int64_t fits_screened_out; /* never run beyond the screening iterations */
-    int64_t fits_completed;    /* run in full in the mixed form (stages 2 and 3) */
+    int64_t fits_completed;    /* run to the end in the mixed form, resumed from their screening
+                                  state (stages 2 and 3) */
     int64_t fits_refit;        /* refitted in full in the FP64 form (stage 4) */
     int64_t evals;             /* model evaluations of all stages */
     double screen_ms, complete_ms, refit_ms;   /* kernel time of the stages */
     int64_t best_index;        /* period index of the best row */
-    int64_t region_periods;    /* periods completed in all poles at stage 3 */
+    int64_t region_periods;    /* periods whose fits were completed (stages 2 and 3) */
     int64_t evals_screen, evals_complete, evals_refit;   /* model evaluations of each stage */
     int32_t refit_rounds;      /* FP64 refit launches */
     int32_t launches;          /* fit-kernel launches of the call */
 } ps_learned_stats;
 
 /* Full fits of periods n_lo..n_hi (10 poles each) in the context's form,
- * recording for every fit PS_TRAJ_FLOATS floats into traj (host). */
-ps_status ps_trajectories(ps_ctx *ctx, double conw_r, int64_t n_lo, int64_t n_hi, float *traj);
+ * recording for every fit PS_TRAJ_FLOATS floats into traj (host), the
+ * features after feat_iters iterations (a multiple of 4, 4..48). */
+ps_status ps_trajectories(ps_ctx *ctx, double conw_r, int64_t n_lo, int64_t n_hi, int32_t feat_iters,
+                          float *traj);
 /* Trains the predictor on n samples (features x[n][10], targets y[n]) with
  * the engine's own CUDA kernels (mini-batch Adam on mean squared error).
  * weights: in = initial parameters with the standardisation constants set,
@@ -278,16 +285,19 @@ ps_status ps_mlp_predict(int32_t device, const float *weights, const float *x, i
  * holds d loss / d W1..b3 at their offsets, zero elsewhere. */
 ps_status ps_mlp_grad(int32_t device, const float *weights, const float *x, const float *y, int64_t n, float *loss,
                       float *grad);
-/* The screening pass alone: every fit of periods n_lo..n_hi runs 4 LM
- * iterations in the mixed form; out[fit] holds the rms after them (dev), the
- * predicted final rms (pred_dev) and screened = 1.  Fit f is period
- * n_lo + f / 10, pole f % 10 + 1. */
-ps_status ps_screen(ps_ctx *ctx, double conw_r, int64_t n_lo, int64_t n_hi, const float *weights, ps_fit *out);
+/* The screening pass alone: every fit of periods n_lo..n_hi runs
+ * screen_iters LM iterations (a multiple of 4, 4..48) in the mixed form;
+ * out[fit] holds the rms after them (dev), the predicted final rms
+ * (pred_dev) and screened = 1.  Fit f is period n_lo + f / 10, pole
+ * f % 10 + 1. */
+ps_status ps_screen(ps_ctx *ctx, double conw_r, int64_t n_lo, int64_t n_hi, int32_t screen_iters,
+                    const float *weights, ps_fit *out);
 /* Period scan in the context's form followed by a full FP64 refit of the
  * minimum region: every period whose row lies within refit_rel (relative)
  * of the best row, or within refit_halfwidth periods of it, is refitted by
  * the plain FP64 form, repeated with the new rows until no further period
- * qualifies.  With the mixed form this gives the FP64 form's best period
+ * qualifies; each refit launch is topped up with the next-lowest rows until
+ * its last wave of fit slots is full.  With the mixed form this gives the FP64 form's best period
  * and FP64 values there at close to the mixed form's cost.  Statistics in
  * the ps_learned_stats fields fits_total, fits_completed (the scan),
  * fits_refit, complete_ms (scan), refit_ms, evals, best_index.  stats may
@@ -297,29 +307,39 @@ ps_status ps_scan_refined(ps_ctx *ctx, double conw_r, int64_t n_lo, int64_t n_hi
 
 /* Options of the learned scan (ps_scan_learned). */
 typedef struct ps_learned_opts {
-    int32_t top_k;           /* complete the top_k best-predicted poles of every period (>= 1) */
-    double margin;           /* and every fit predicted within (1 + margin) of the scan's best prediction;
-                                < 0 disables (the default: in flat scans it would complete everything) */
-    double region_rel;       /* complete all poles of the periods whose row lies within region_rel
-                                (relative) of the best row, and of region_halfwidth periods around it */
-    int32_t region_halfwidth;
-    double refit_rel;        /* refit in full with the FP64 form the periods within refit_rel of the
-                                best row after the region pass, */
-    int32_t refit_halfwidth; /* and refit_halfwidth periods on each side of the best */
+    int32_t screen_iters;     /* LM iterations of the screening pass (a multiple of 4, 4..48); the
+                                 predictor's weights must have been trained for it */
+    double margin;            /* stopping rule of the completion: periods are completed in the order of
+                                 their predicted rows until the next one's predicted row times
+                                 exp(-margin) lies above the best completed row */
+    int32_t batch_periods;    /* periods completed per launch (0: as many as the device's fit slots hold) */
+    int32_t region_halfwidth; /* the periods within region_halfwidth of the best completed row are
+                                 completed too */
+    double refit_rel;         /* refit in full with the FP64 form the periods within refit_rel of the
+                                 best row after the completion, */
+    int32_t refit_halfwidth;  /* and refit_halfwidth periods on each side of the best */
+    int32_t fill_refit_waves; /* 1: top every FP64 refit launch up with the next-lowest rows (whole
+                                 periods) until its last wave of fit slots is full -- no extra time, fewer
+                                 refit rounds (ps_scan_refined always does); 0: refit exactly the set */
 } ps_learned_opts;
 
 /* Period scan with the learned early stop, a cascade in which only the fits
- * that can matter run in full: (1) every fit runs 4 LM iterations in the
- * mixed form and the predictor estimates its final rms (ps_screen); (2) the
- * top_k best-predicted poles of every period (and fits within `margin` of
- * the best prediction) run in full in the mixed form, giving an upper bound
- * of every period's row; (3) every pole of the periods near the best row
- * runs in full in the mixed form; (4) the periods nearest the best row are
- * refitted in full by the plain FP64 form, so that the reported minimum
- * carries FP64 values.  Rows of periods that stopped at stage (2) carry the
- * best completed pole.  opts NULL selects the defaults (top_k 1, margin off,
- * region 3 % and +-2 periods, FP64 refit 0.5 % and +-2 periods).  stats may
- * be NULL. */
+ * that can matter run to the end: (1) every fit runs screen_iters LM
+ * iterations in the mixed form, the predictor estimates its final rms and
+ * its LM state is kept on the device; (2) periods are completed -- all ten
+ * poles resumed from their saved states, continuing exactly as
+ * uninterrupted fits -- in the order of their predicted rows (the lowest
+ * prediction of their poles), launch by launch, until no remaining period's
+ * predicted row, lowered by the margin, can beat the best completed row:
+ * the fits that cannot beat the current best are stopped after screening;
+ * (3) the periods around the best completed row are completed; (4) the
+ * minimum region is refitted in full by the plain FP64 form (as in
+ * ps_scan_refined), so that the reported minimum carries FP64 values.  Rows
+ * of periods that stopped at screening carry their screened fits' rms
+ * (above what full fits reach).  opts NULL selects the defaults
+ * (screen_iters 8, margin 0.02, batch from the slots, region +-2 periods,
+ * FP64 refit 0.5 % and +-2 periods, refit waves filled).  stats may be
+ * NULL. */
 ps_status ps_scan_learned(ps_ctx *ctx, double conw_r, int64_t n_lo, int64_t n_hi, const float *weights,
                           const ps_learned_opts *opts, ps_row *out, ps_learned_stats *stats);
 
@@ -426,8 +446,20 @@ ps_status ps_pack_create(ps_ctx *const *ctxs, int32_t n_objects, int32_t form, p
  * (Ndata) for load balance; out[] is in the caller's order. */
 ps_status ps_pack_fit(ps_pack *pack, const double *conw_r, int64_t n_fits, const int32_t *object,
                       const int64_t *period_index, const int32_t *pole, ps_fit *out);
+/* The learned stop's screening pass over packed units (ps_screen for many
+ * objects): every unit runs screen_iters LM iterations, out[] holds the rms
+ * after them (dev) and the predictor's estimate of the final rms
+ * (pred_dev). */
+ps_status ps_pack_screen(ps_pack *pack, const double *conw_r, int64_t n_fits, const int32_t *object,
+                         const int64_t *period_index, const int32_t *pole, int32_t screen_iters,
+                         const float *weights, ps_fit *out);
+/* Full fits of packed units recording PS_TRAJ_FLOATS floats per unit into
+ * traj (host, caller's order), as ps_trajectories does for one object. */
+ps_status ps_pack_trajectories(ps_pack *pack, const double *conw_r, int64_t n_fits, const int32_t *object,
+                               const int64_t *period_index, const int32_t *pole, int32_t feat_iters, float *traj,
+                               ps_fit *out);
 
-/* Device timing of the last ps_pack_fit. */
+/* Device timing of the last packed launch. */
 ps_status ps_pack_timing(const ps_pack *pack, ps_timing *out);
 const char *ps_pack_last_error(const ps_pack *pack);
 void ps_pack_destroy(ps_pack *pack);

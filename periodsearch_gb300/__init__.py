@@ -98,18 +98,37 @@ class Pack:
         _abi.check(self._L.ps_pack_create(arr, len(self._engines), form, C.byref(h)), "ps_pack_create")
         self._h = h
 
-    def fit(self, conw_r, object_index, period_index, pole) -> np.ndarray:
+    def _call(self, name, conw_r, object_index, period_index, pole, *extra):
         cw = np.ascontiguousarray(conw_r, np.float64)
         ob = np.ascontiguousarray(object_index, np.int32)
         pi = np.ascontiguousarray(period_index, np.int64)
         po = np.ascontiguousarray(pole, np.int32)
         out = np.zeros(len(pi), FIT_DTYPE)
-        st = self._L.ps_pack_fit(self._h, cw.ctypes.data_as(C.POINTER(C.c_double)), len(pi),
-                                 ob.ctypes.data_as(C.POINTER(C.c_int32)), pi.ctypes.data_as(C.POINTER(C.c_int64)),
-                                 po.ctypes.data_as(C.POINTER(C.c_int32)), out.ctypes.data_as(C.POINTER(_abi.Fit)))
+        st = getattr(self._L, name)(self._h, cw.ctypes.data_as(C.POINTER(C.c_double)), len(pi),
+                                    ob.ctypes.data_as(C.POINTER(C.c_int32)), pi.ctypes.data_as(C.POINTER(C.c_int64)),
+                                    po.ctypes.data_as(C.POINTER(C.c_int32)), *extra,
+                                    out.ctypes.data_as(C.POINTER(_abi.Fit)))
         if st != _abi.PS_OK:
-            raise EngineError(st, "ps_pack_fit", self._L.ps_pack_last_error(self._h).decode())
+            raise EngineError(st, name, self._L.ps_pack_last_error(self._h).decode())
         return out
+
+    def fit(self, conw_r, object_index, period_index, pole) -> np.ndarray:
+        return self._call("ps_pack_fit", conw_r, object_index, period_index, pole)
+
+    def screen(self, conw_r, object_index, period_index, pole, weights, screen_iters: int) -> np.ndarray:
+        """screen_iters LM iterations of every unit with the in-kernel
+        predictor (ps_pack_screen)."""
+        w = np.ascontiguousarray(weights, np.float32)
+        return self._call("ps_pack_screen", conw_r, object_index, period_index, pole, int(screen_iters),
+                          w.ctypes.data_as(C.POINTER(C.c_float)))
+
+    def trajectories(self, conw_r, object_index, period_index, pole, feat_iters: int):
+        """Full fits with their trajectory records (ps_pack_trajectories),
+        features after feat_iters iterations: returns (fits, records[n][16])."""
+        traj = np.zeros((len(period_index), _abi.TRAJ_FLOATS), np.float32)
+        fits = self._call("ps_pack_trajectories", conw_r, object_index, period_index, pole, int(feat_iters),
+                          traj.ctypes.data_as(C.POINTER(C.c_float)))
+        return fits, traj
 
     def timing(self) -> dict:
         t = _abi.Timing()
@@ -255,17 +274,20 @@ class Engine:
         _abi.check(st, "ps_eval", self._ctx)
         return alpha, beta, c2.value, area
 
-    def trajectories(self, conw_r: float, n_lo: int, n_hi: int) -> np.ndarray:
+    def trajectories(self, conw_r: float, n_lo: int, n_hi: int, feat_iters: int | None = None) -> np.ndarray:
         from . import learned
 
-        return learned.trajectories(self, conw_r, n_lo, n_hi)
+        return learned.trajectories(self, conw_r, n_lo, n_hi, feat_iters)
 
-    def screen(self, conw_r: float, n_lo: int, n_hi: int, weights) -> np.ndarray:
-        """The screening pass alone (ps_screen): per fit the rms after four
-        iterations and the predicted final rms."""
+    def screen(self, conw_r: float, n_lo: int, n_hi: int, weights, screen_iters: int | None = None) -> np.ndarray:
+        """The screening pass alone (ps_screen): per fit the rms after the
+        screening iterations and the predicted final rms."""
+        from . import learned
+
+        k = learned.SCREEN_ITERS if screen_iters is None else int(screen_iters)
         w = np.ascontiguousarray(weights, np.float32)
         out = np.zeros((n_hi - n_lo + 1) * N_POLES, FIT_DTYPE)
-        r = self._L.ps_screen(self._ctx, conw_r, n_lo, n_hi, w.ctypes.data_as(C.POINTER(C.c_float)),
+        r = self._L.ps_screen(self._ctx, conw_r, n_lo, n_hi, k, w.ctypes.data_as(C.POINTER(C.c_float)),
                               out.ctypes.data_as(C.POINTER(_abi.Fit)))
         _abi.check(r, "ps_screen", self._ctx)
         return out
@@ -298,16 +320,18 @@ class Engine:
 
     def scan_learned(self, conw_r: float, n_lo: int, n_hi: int, weights=None, **opts):
         """Period scan with the learned early stop (ps_scan_learned); returns
-        the rows and the stage statistics.  Options (ps_learned_opts): top_k,
-        margin, region_rel, region_halfwidth, refit_rel, refit_halfwidth.
-        Without weights the committed predictor is used."""
+        the rows and the stage statistics.  Options (ps_learned_opts):
+        screen_iters, margin, batch_periods, region_halfwidth, refit_rel,
+        refit_halfwidth, fill_refit_waves.  Without weights the committed
+        predictor is used, with the screening depth and margin it was
+        calibrated for (learned.CASCADE)."""
         from . import learned
 
         if weights is None:
             weights, _ = learned.load_default()
             if weights is None:
                 raise EngineError(_abi.PS_ERR_ARG, "scan_learned", "no trained predictor available")
-        o = _abi.LearnedOpts(1, -1.0, 0.03, 2, 0.005, 2)
+        o = _abi.LearnedOpts(**learned.cascade_defaults())
         for k, v in opts.items():
             setattr(o, k, v)
         w = np.ascontiguousarray(weights, np.float32)

@@ -110,8 +110,9 @@ class TuneReport(C.Structure):
 
 
 class LearnedOpts(C.Structure):
-    _fields_ = [("top_k", C.c_int32), ("margin", C.c_double), ("region_rel", C.c_double),
-                ("region_halfwidth", C.c_int32), ("refit_rel", C.c_double), ("refit_halfwidth", C.c_int32)]
+    _fields_ = [("screen_iters", C.c_int32), ("margin", C.c_double), ("batch_periods", C.c_int32),
+                ("region_halfwidth", C.c_int32), ("refit_rel", C.c_double), ("refit_halfwidth", C.c_int32),
+                ("fill_refit_waves", C.c_int32)]
 
 
 MLP_FEATURES = 10
@@ -144,14 +145,15 @@ SIGNATURES = {
                                        C.c_void_p]),
     "ps_eval": (C.c_int, [_CTX, C.c_double, _D, _D, _D, _D, _D]),
     "ps_last_timing": (C.c_int, [_CTX, C.POINTER(Timing)]),
-    "ps_trajectories": (C.c_int, [_CTX, C.c_double, C.c_int64, C.c_int64, C.POINTER(C.c_float)]),
+    "ps_trajectories": (C.c_int, [_CTX, C.c_double, C.c_int64, C.c_int64, C.c_int32, C.POINTER(C.c_float)]),
     "ps_mlp_train": (C.c_int, [C.c_int32, C.POINTER(C.c_float), C.POINTER(C.c_float), C.POINTER(C.c_float),
                                C.c_int64, C.c_int32, C.c_int32, C.c_float, C.c_uint64, C.POINTER(C.c_float)]),
     "ps_mlp_predict": (C.c_int, [C.c_int32, C.POINTER(C.c_float), C.POINTER(C.c_float), C.c_int64,
                                  C.POINTER(C.c_float)]),
     "ps_mlp_grad": (C.c_int, [C.c_int32, C.POINTER(C.c_float), C.POINTER(C.c_float), C.POINTER(C.c_float),
                               C.c_int64, C.POINTER(C.c_float), C.POINTER(C.c_float)]),
-    "ps_screen": (C.c_int, [_CTX, C.c_double, C.c_int64, C.c_int64, C.POINTER(C.c_float), C.POINTER(Fit)]),
+    "ps_screen": (C.c_int, [_CTX, C.c_double, C.c_int64, C.c_int64, C.c_int32, C.POINTER(C.c_float),
+                            C.POINTER(Fit)]),
     "ps_tc_selftest": (C.c_int, [C.c_int32, C.POINTER(C.c_float), C.POINTER(C.c_float), C.c_int32,
                                  C.POINTER(C.c_float)]),
     "ps_tc_selftest_f16": (C.c_int, [C.c_int32, C.POINTER(C.c_float), C.POINTER(C.c_float), C.c_int32,
@@ -163,6 +165,12 @@ SIGNATURES = {
     "ps_pack_create": (C.c_int, [C.POINTER(C.c_void_p), C.c_int32, C.c_int32, C.POINTER(C.c_void_p)]),
     "ps_pack_fit": (C.c_int, [C.c_void_p, C.POINTER(C.c_double), C.c_int64, C.POINTER(C.c_int32),
                               C.POINTER(C.c_int64), C.POINTER(C.c_int32), C.POINTER(Fit)]),
+    "ps_pack_screen": (C.c_int, [C.c_void_p, C.POINTER(C.c_double), C.c_int64, C.POINTER(C.c_int32),
+                                 C.POINTER(C.c_int64), C.POINTER(C.c_int32), C.c_int32, C.POINTER(C.c_float),
+                                 C.POINTER(Fit)]),
+    "ps_pack_trajectories": (C.c_int, [C.c_void_p, C.POINTER(C.c_double), C.c_int64, C.POINTER(C.c_int32),
+                                       C.POINTER(C.c_int64), C.POINTER(C.c_int32), C.c_int32, C.POINTER(C.c_float),
+                                       C.POINTER(Fit)]),
     "ps_pack_timing": (C.c_int, [C.c_void_p, C.POINTER(Timing)]),
     "ps_pack_last_error": (C.c_char_p, [C.c_void_p]),
     "ps_pack_destroy": (None, [C.c_void_p]),

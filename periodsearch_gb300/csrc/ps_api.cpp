@@ -53,6 +53,10 @@ struct ps_ctx {
     size_t list_cap = 0;
     int64_t launch_total = 0;   // fit-kernel launches since ps_prepare
     double *d_eval = nullptr;          // cg, alpha, beta, chisq, area of ps_eval
+    double *d_state = nullptr;         // saved LM states of screened fits (learned scan)
+    size_t state_cap = 0;              // fits
+    int64_t *d_slot = nullptr;         // state rows of resumed fits
+    size_t slot_cap = 0;
     std::vector<ps_fit> h_fits;
     ps_timing timing{};
     std::string err;
@@ -292,7 +296,7 @@ ps_status scan_rows(ps_ctx *c, double conw_r, int64_t n_lo, int64_t n_hi, ps_row
 // Fits given as (period index, pole) lists on the host: copied to the
 // device and launched in the given form; results in c->h_fits.
 ps_status run_list(ps_ctx *c, double conw_r, const int64_t *pidx, const int32_t *pole, int64_t n, int form,
-                   int iter_limit = 0)
+                   int iter_limit = 0, const int64_t *resume_slots = nullptr)
 {
     if (static_cast<size_t>(n) > c->list_cap) {
         cudaFree(c->d_pidx);
@@ -311,6 +315,19 @@ ps_status run_list(ps_ctx *c, double conw_r, const int64_t *pidx, const int32_t 
     w.period_index = c->d_pidx;
     w.pole = c->d_pole;
     w.iter_limit = iter_limit;
+    if (resume_slots) {
+        // continue fits from the states a screening launch saved
+        if (static_cast<size_t>(n) > c->slot_cap) {
+            cudaFree(c->d_slot);
+            c->d_slot = nullptr;
+            PSG_CUDA(c, cudaMalloc(&c->d_slot, n * sizeof(int64_t)));
+            c->slot_cap = static_cast<size_t>(n);
+        }
+        PSG_CUDA(c, cudaMemcpyAsync(c->d_slot, resume_slots, n * sizeof(int64_t), cudaMemcpyHostToDevice, c->stream));
+        w.state = c->d_state;
+        w.state_slot = c->d_slot;
+        w.resume = 1;
+    }
     return run_fits(c, conw_r, w, form);
 }
 
@@ -321,12 +338,18 @@ struct ScanFits {
     std::vector<char> done;     // run in full (a candidate of its period's row)
     std::vector<char> fp64;     // period refitted in full by the FP64 form
 
+    // The row of period n from its fits run in full; a period none of whose
+    // fits ran in full (the learned scan skipped it) gets the row of its
+    // screened fits, whose rms after the screening iterations lies above
+    // what the full fits would reach.
     ps_row row(int64_t n, int32_t ndata) const
     {
         ps_fit tmp[PS_N_POLES];
+        bool any = false;
+        for (int m = 0; m < PS_N_POLES; m++) any = any || done[static_cast<size_t>(n * PS_N_POLES + m)];
         for (int m = 0; m < PS_N_POLES; m++) {
             tmp[m] = fits[static_cast<size_t>(n * PS_N_POLES + m)];
-            if (!done[static_cast<size_t>(n * PS_N_POLES + m)]) tmp[m].dev = NAN;  // not a candidate
+            if (any && !done[static_cast<size_t>(n * PS_N_POLES + m)]) tmp[m].dev = NAN;  // not a candidate
         }
         return psg::best_of_poles(tmp, ndata);
     }
@@ -353,8 +376,8 @@ struct ScanFits {
 // next-lowest rows (whole periods) until its last wave of slots is full:
 // periods that a later round would likely have needed come at no extra
 // time, and fewer rounds run.
-ps_status refit_minimum(ps_ctx *c, double conw_r, ScanFits &sf, double rel, int32_t halfwidth, double *ms,
-                        int64_t *nrefit, int64_t *evals, int32_t *rounds)
+ps_status refit_minimum(ps_ctx *c, double conw_r, ScanFits &sf, double rel, int32_t halfwidth, bool fill,
+                        double *ms, int64_t *nrefit, int64_t *evals, int32_t *rounds)
 {
     ps_status st = make_plan(c, PS_FORM_FP64);
     if (st != PS_OK) return st;
@@ -382,7 +405,7 @@ ps_status refit_minimum(ps_ctx *c, double conw_r, ScanFits &sf, double rel, int3
         // top up the last wave with the lowest remaining rows
         const int64_t need = static_cast<int64_t>(per.size()) * PS_N_POLES;
         const int64_t cap = (need + slots - 1) / slots * slots;
-        if (need + PS_N_POLES <= cap) {
+        if (fill && need + PS_N_POLES <= cap) {
             order.clear();
             for (int64_t n = 0; n < sf.nper; n++)
                 if (!sf.fp64[static_cast<size_t>(n)] && !picked[static_cast<size_t>(n)] &&
@@ -821,9 +844,11 @@ ps_status ps_eval(ps_ctx *c, double conw_r, const double *cg, double *alpha, dou
     return PS_OK;
 }
 
-ps_status ps_trajectories(ps_ctx *c, double conw_r, int64_t n_lo, int64_t n_hi, float *traj)
+ps_status ps_trajectories(ps_ctx *c, double conw_r, int64_t n_lo, int64_t n_hi, int32_t feat_iters, float *traj)
 {
-    if (!c || !traj || n_lo < 1 || n_hi < n_lo || !(conw_r > 0)) return PS_ERR_ARG;
+    if (!c || !traj || n_lo < 1 || n_hi < n_lo || !(conw_r > 0) || feat_iters < 4 || feat_iters > 48 ||
+        feat_iters % 4)
+        return PS_ERR_ARG;
     PSG_CUDA(c, cudaSetDevice(c->opt.device));
     const int64_t nfits = (n_hi - n_lo + 1) * PS_N_POLES;
     float *d_traj = nullptr;
@@ -833,6 +858,7 @@ ps_status ps_trajectories(ps_ctx *c, double conw_r, int64_t n_lo, int64_t n_hi, 
     w.n_lo = n_lo;
     w.nfits = nfits;
     w.traj = d_traj;
+    w.screen_iters = feat_iters;
     ps_status st = run_fits(c, conw_r, w, c->opt.form);
     if (st == PS_OK) {
         cudaError_t e = cudaMemcpy(traj, d_traj, nfits * psg::kTrajFloats * sizeof(float), cudaMemcpyDeviceToHost);
@@ -870,10 +896,21 @@ ps_status ps_mlp_grad(int32_t device, const float *weights, const float *x, cons
 
 namespace {
 
-// Screening launch: kScreenIters iterations of every fit of n_lo..n_hi in the
-// mixed form with the in-kernel predictor; results in c->h_fits.
-ps_status screen_fits(ps_ctx *c, double conw_r, int64_t n_lo, int64_t n_hi, const float *weights)
+// Screening launch: screen_iters iterations of every fit of n_lo..n_hi in
+// the mixed form with the in-kernel predictor; results in c->h_fits.  With
+// save_state every fit's LM state is kept on the device (c->d_state, fit f
+// in row f) for a later resume.
+ps_status screen_fits(ps_ctx *c, double conw_r, int64_t n_lo, int64_t n_hi, const float *weights, int screen_iters,
+                      bool save_state)
 {
+    const int64_t nfits = (n_hi - n_lo + 1) * PS_N_POLES;
+    if (save_state && static_cast<size_t>(nfits) > c->state_cap) {
+        cudaFree(c->d_state);
+        c->d_state = nullptr;
+        c->state_cap = 0;
+        PSG_CUDA(c, cudaMalloc(&c->d_state, nfits * psg::state_stride(c->obj.ma) * sizeof(double)));
+        c->state_cap = static_cast<size_t>(nfits);
+    }
     float *d_w = nullptr;
     PSG_CUDA(c, cudaMalloc(&d_w, psg::kMlpFloats * sizeof(float)));
     cudaError_t ce = cudaMemcpy(d_w, weights, psg::kMlpFloats * sizeof(float), cudaMemcpyHostToDevice);
@@ -883,21 +920,27 @@ ps_status screen_fits(ps_ctx *c, double conw_r, int64_t n_lo, int64_t n_hi, cons
     }
     psg::FitWork w{};
     w.n_lo = n_lo;
-    w.nfits = (n_hi - n_lo + 1) * PS_N_POLES;
-    w.iter_limit = psg::kScreenIters;
+    w.nfits = nfits;
+    w.iter_limit = screen_iters;
+    w.screen_iters = screen_iters;
     w.mlp = d_w;
+    if (save_state) w.state = c->d_state;
     ps_status st = run_fits(c, conw_r, w, PS_FORM_MIXED);
     cudaFree(d_w);
     return st;
 }
 
+bool screen_iters_ok(int k) { return k >= 4 && k <= 48 && k % 4 == 0; }
+
 }  // namespace
 
-ps_status ps_screen(ps_ctx *c, double conw_r, int64_t n_lo, int64_t n_hi, const float *weights, ps_fit *out)
+ps_status ps_screen(ps_ctx *c, double conw_r, int64_t n_lo, int64_t n_hi, int32_t screen_iters, const float *weights,
+                    ps_fit *out)
 {
-    if (!c || !weights || !out || n_lo < 1 || n_hi < n_lo || !(conw_r > 0)) return PS_ERR_ARG;
+    if (!c || !weights || !out || n_lo < 1 || n_hi < n_lo || !(conw_r > 0) || !screen_iters_ok(screen_iters))
+        return PS_ERR_ARG;
     PSG_CUDA(c, cudaSetDevice(c->opt.device));
-    ps_status st = screen_fits(c, conw_r, n_lo, n_hi, weights);
+    ps_status st = screen_fits(c, conw_r, n_lo, n_hi, weights, screen_iters, false);
     if (st != PS_OK) return st;
     std::memcpy(out, c->h_fits.data(), c->h_fits.size() * sizeof(ps_fit));
     return PS_OK;
@@ -906,10 +949,11 @@ ps_status ps_screen(ps_ctx *c, double conw_r, int64_t n_lo, int64_t n_hi, const 
 ps_status ps_scan_learned(ps_ctx *c, double conw_r, int64_t n_lo, int64_t n_hi, const float *weights,
                           const ps_learned_opts *opts, ps_row *out, ps_learned_stats *stats)
 {
-    ps_learned_opts o{1, -1.0, 0.03, 2, 0.005, 2};
+    ps_learned_opts o{8, 0.02, 0, 2, 0.005, 2, 1};
     if (opts) o = *opts;
-    if (!c || !weights || !out || n_lo < 1 || n_hi < n_lo || !(conw_r > 0) || o.top_k < 1 ||
-        !(o.region_rel >= 0) || !(o.refit_rel >= 0) || o.region_halfwidth < 0 || o.refit_halfwidth < 0)
+    if (!c || !weights || !out || n_lo < 1 || n_hi < n_lo || !(conw_r > 0) || !screen_iters_ok(o.screen_iters) ||
+        !(o.margin >= 0) || o.batch_periods < 0 || o.region_halfwidth < 0 || !(o.refit_rel >= 0) ||
+        o.refit_halfwidth < 0)
         return PS_ERR_ARG;
     PSG_CUDA(c, cudaSetDevice(c->opt.device));
     ScanFits sf;
@@ -919,8 +963,9 @@ ps_status ps_scan_learned(ps_ctx *c, double conw_r, int64_t n_lo, int64_t n_hi, 
     ps_learned_stats stt{};
     stt.fits_total = nfits;
     const int64_t launch0 = c->launch_total;
-    // (1) screening: 4 iterations of every fit, predicted final rms
-    ps_status st = screen_fits(c, conw_r, n_lo, n_hi, weights);
+    // (1) screening: screen_iters iterations of every fit, the predicted
+    // final rms, the LM states kept for the completion
+    ps_status st = screen_fits(c, conw_r, n_lo, n_hi, weights, o.screen_iters, true);
     if (st != PS_OK) return st;
     stt.screen_ms = c->timing.kernel_ms;
     stt.evals += c->timing.evals;
@@ -928,73 +973,109 @@ ps_status ps_scan_learned(ps_ctx *c, double conw_r, int64_t n_lo, int64_t n_hi, 
     sf.fits = c->h_fits;
     sf.done.assign(static_cast<size_t>(nfits), 0);
     sf.fp64.assign(static_cast<size_t>(sf.nper), 0);
+    // predicted row of every period: the lowest predicted final rms of its poles
+    std::vector<double> pred(static_cast<size_t>(sf.nper));
+    for (int64_t n = 0; n < sf.nper; n++) {
+        double p = INFINITY;
+        for (int m = 0; m < PS_N_POLES; m++) {
+            const double v = sf.fits[static_cast<size_t>(n * PS_N_POLES + m)].pred_dev;
+            if (v > 0 && v < p) p = v;
+        }
+        pred[static_cast<size_t>(n)] = p;
+    }
+    std::vector<int64_t> order(static_cast<size_t>(sf.nper));
+    for (int64_t n = 0; n < sf.nper; n++) order[static_cast<size_t>(n)] = n;
+    std::stable_sort(order.begin(), order.end(),
+                     [&](int64_t a, int64_t b) { return pred[static_cast<size_t>(a)] < pred[static_cast<size_t>(b)]; });
+    std::vector<char> period_done(static_cast<size_t>(sf.nper), 0);
     std::vector<int64_t> pidx, slot;
     std::vector<int32_t> pole;
-    auto queue = [&](int64_t i) {
-        if (sf.done[static_cast<size_t>(i)]) return;
-        sf.done[static_cast<size_t>(i)] = 1;
-        pidx.push_back(n_lo + i / PS_N_POLES);
-        pole.push_back(static_cast<int32_t>(i % PS_N_POLES) + 1);
-        slot.push_back(i);
-    };
-    auto complete = [&]() -> ps_status {
-        const int64_t n = static_cast<int64_t>(pidx.size());
-        if (n == 0) return PS_OK;
-        ps_status r = run_list(c, conw_r, pidx.data(), pole.data(), n, PS_FORM_MIXED);
+    // completes every pole of the listed periods from its saved state
+    auto complete = [&](const std::vector<int64_t> &periods) -> ps_status {
+        pidx.clear();
+        pole.clear();
+        slot.clear();
+        for (int64_t n : periods) {
+            period_done[static_cast<size_t>(n)] = 1;
+            stt.region_periods++;
+            for (int m = 0; m < PS_N_POLES; m++) {
+                const int64_t i = n * PS_N_POLES + m;
+                sf.done[static_cast<size_t>(i)] = 1;
+                // a fit that the screening already ended (stop rule) is final
+                if (!sf.fits[static_cast<size_t>(i)].screened) continue;
+                pidx.push_back(n_lo + n);
+                pole.push_back(m + 1);
+                slot.push_back(i);
+            }
+        }
+        const int64_t k = static_cast<int64_t>(pidx.size());
+        if (k == 0) return PS_OK;
+        ps_status r = run_list(c, conw_r, pidx.data(), pole.data(), k, PS_FORM_MIXED, 0, slot.data());
         if (r != PS_OK) return r;
         stt.complete_ms += c->timing.kernel_ms;
         stt.evals += c->timing.evals;
         stt.evals_complete += c->timing.evals;
-        for (int64_t k = 0; k < n; k++)
-            sf.fits[static_cast<size_t>(slot[static_cast<size_t>(k)])] = c->h_fits[static_cast<size_t>(k)];
-        pidx.clear();
-        pole.clear();
-        slot.clear();
+        for (int64_t q = 0; q < k; q++)
+            sf.fits[static_cast<size_t>(slot[static_cast<size_t>(q)])] = c->h_fits[static_cast<size_t>(q)];
         return PS_OK;
     };
-    // (2) the top_k predicted poles of every period, and fits near the best prediction
-    double best_pred = 1e300;
-    for (const ps_fit &f : sf.fits)
-        if (f.pred_dev > 0 && f.pred_dev < best_pred) best_pred = f.pred_dev;
-    for (int64_t n = 0; n < sf.nper; n++) {
-        int order[PS_N_POLES];
-        for (int m = 0; m < PS_N_POLES; m++) order[m] = m;
-        const ps_fit *pf = &sf.fits[static_cast<size_t>(n * PS_N_POLES)];
-        std::stable_sort(order, order + PS_N_POLES, [&](int a, int b) {
-            const double pa = std::isnan(pf[a].pred_dev) ? 1e300 : pf[a].pred_dev;
-            const double pb = std::isnan(pf[b].pred_dev) ? 1e300 : pf[b].pred_dev;
-            return pa < pb;
-        });
-        for (int k = 0; k < std::min(o.top_k, PS_N_POLES); k++) queue(n * PS_N_POLES + order[k]);
-        if (o.margin >= 0)
-            for (int m = 0; m < PS_N_POLES; m++)
-                if (pf[m].pred_dev <= best_pred * (1 + o.margin)) queue(n * PS_N_POLES + m);
+    auto best_done = [&]() {
+        double b = INFINITY;
+        int64_t bn = -1;
+        for (int64_t n = 0; n < sf.nper; n++) {
+            if (!period_done[static_cast<size_t>(n)]) continue;
+            const double r = sf.row(n, c->obj.ndata).rms;
+            if (r < b) {
+                b = r;
+                bn = n;
+            }
+        }
+        return std::make_pair(b, bn);
+    };
+    // (2) completion in the order of the predicted rows, a device's worth
+    // of periods per launch, until the next period's predicted row, lowered
+    // by the margin, cannot beat the best completed row
+    const int64_t batch = o.batch_periods > 0 ? o.batch_periods : std::max<int64_t>(1, c->slots / PS_N_POLES);
+    const double shrink = std::exp(-o.margin);
+    size_t next = 0;
+    std::vector<int64_t> group;
+    for (;;) {
+        const double best = best_done().first;
+        group.clear();
+        while (next < order.size() && static_cast<int64_t>(group.size()) < batch) {
+            const int64_t n = order[next];
+            if (!(pred[static_cast<size_t>(n)] * shrink <= best)) break;
+            group.push_back(n);
+            next++;
+        }
+        if (group.empty()) break;
+        st = complete(group);
+        if (st != PS_OK) return st;
     }
-    st = complete();
-    if (st != PS_OK) return st;
-    // (3) all poles of the periods near the best row (rows of the completed
-    // poles only: an upper bound of the full rows), in the mixed form
-    std::vector<ps_row> rows;
-    sf.rows(rows, c->obj.ndata);
-    int64_t best = ScanFits::best(rows);
-    const double lim = rows[static_cast<size_t>(best)].rms * (1 + o.region_rel);
-    for (int64_t n = 0; n < sf.nper; n++) {
-        if (!(std::llabs(n - best) <= o.region_halfwidth || rows[static_cast<size_t>(n)].rms <= lim)) continue;
-        stt.region_periods++;
-        for (int m = 0; m < PS_N_POLES; m++) queue(n * PS_N_POLES + m);
+    // (3) every period within region_halfwidth of the best completed row,
+    // until the best row no longer moves
+    for (int round = 0; round < 16; round++) {
+        const int64_t bn = best_done().second;
+        if (bn < 0) break;
+        group.clear();
+        for (int64_t n = std::max<int64_t>(0, bn - o.region_halfwidth);
+             n <= std::min<int64_t>(sf.nper - 1, bn + o.region_halfwidth); n++)
+            if (!period_done[static_cast<size_t>(n)]) group.push_back(n);
+        if (group.empty()) break;
+        st = complete(group);
+        if (st != PS_OK) return st;
     }
-    st = complete();
-    if (st != PS_OK) return st;
     for (char d : sf.done) stt.fits_completed += d;
     stt.fits_screened_out = nfits - stt.fits_completed;
     // (4) FP64 refit of the periods nearest the best row
     const int64_t ev0 = stt.evals;
-    st = refit_minimum(c, conw_r, sf, o.refit_rel, o.refit_halfwidth, &stt.refit_ms, &stt.fits_refit, &stt.evals,
-                       &stt.refit_rounds);
+    st = refit_minimum(c, conw_r, sf, o.refit_rel, o.refit_halfwidth, o.fill_refit_waves != 0, &stt.refit_ms,
+                       &stt.fits_refit, &stt.evals, &stt.refit_rounds);
     if (st != PS_OK) return st;
     stt.evals_refit = stt.evals - ev0;
+    std::vector<ps_row> rows;
     sf.rows(rows, c->obj.ndata);
-    best = ScanFits::best(rows);
+    const int64_t best = ScanFits::best(rows);
     for (int64_t n = 0; n < sf.nper; n++) out[n] = rows[static_cast<size_t>(n)];
     if (n_lo == 1) out[0].dark_or_conw = conw_r * c->obj.escl * c->obj.escl;
     stt.best_index = n_lo + best;
@@ -1032,8 +1113,8 @@ ps_status ps_scan_refined(ps_ctx *c, double conw_r, int64_t n_lo, int64_t n_hi, 
     sf.fits = c->h_fits;
     sf.done.assign(static_cast<size_t>(nfits), 1);
     sf.fp64.assign(static_cast<size_t>(sf.nper), c->opt.form == PS_FORM_FP64 ? 1 : 0);
-    st = refit_minimum(c, conw_r, sf, refit_rel, refit_halfwidth, &stt.refit_ms, &stt.fits_refit, &stt.evals,
-                       &stt.refit_rounds);
+    st = refit_minimum(c, conw_r, sf, refit_rel, refit_halfwidth, true, &stt.refit_ms, &stt.fits_refit,
+                       &stt.evals, &stt.refit_rounds);
     if (st != PS_OK) return st;
     stt.evals_refit = stt.evals - stt.evals_complete;
     std::vector<ps_row> rows;
@@ -1231,8 +1312,16 @@ ps_status ps_pack_create(ps_ctx *const *ctxs, int32_t n, int32_t form, ps_pack *
     return PS_OK;
 }
 
-ps_status ps_pack_fit(ps_pack *k, const double *conw_r, int64_t n_fits, const int32_t *object,
-                      const int64_t *period_index, const int32_t *pole, ps_fit *out)
+}  // extern "C"
+
+namespace {
+
+// One packed launch.  iter_limit > 0 stops every fit after that many LM
+// iterations (screening, with the predictor `weights` when given); traj
+// (host, [n_fits][kTrajFloats]) receives the fits' trajectory records.
+ps_status pack_run(ps_pack *k, const double *conw_r, int64_t n_fits, const int32_t *object,
+                   const int64_t *period_index, const int32_t *pole, int iter_limit, int screen_iters,
+                   const float *weights, float *traj, ps_fit *out)
 {
     if (!k || !conw_r || n_fits < 1 || !object || !period_index || !pole || !out) return PS_ERR_ARG;
     const int32_t nobj = static_cast<int32_t>(k->ctx.size());
@@ -1292,6 +1381,25 @@ ps_status ps_pack_fit(ps_pack *k, const double *conw_r, int64_t n_fits, const in
     w.objs = k->d_objs;
     w.cfgs = k->d_cfgs;
     w.object = k->d_obj;
+    w.iter_limit = iter_limit;
+    w.screen_iters = screen_iters;
+    // predictor weights and trajectory records: launch-local device buffers
+    struct Tmp {
+        float *p = nullptr;
+        ~Tmp() { cudaFree(p); }
+    } d_w, d_traj;
+    const size_t traj_bytes = static_cast<size_t>(n_fits) * psg::kTrajFloats * sizeof(float);
+    if (weights) {
+        PSG_PACK_CUDA(k, cudaMalloc(&d_w.p, psg::kMlpFloats * sizeof(float)));
+        PSG_PACK_CUDA(k, cudaMemcpyAsync(d_w.p, weights, psg::kMlpFloats * sizeof(float), cudaMemcpyHostToDevice,
+                                         k->stream));
+        w.mlp = d_w.p;
+    }
+    if (traj) {
+        PSG_PACK_CUDA(k, cudaMalloc(&d_traj.p, traj_bytes));
+        PSG_PACK_CUDA(k, cudaMemsetAsync(d_traj.p, 0, traj_bytes, k->stream));
+        w.traj = d_traj.p;
+    }
     const int grid = static_cast<int>(std::min<int64_t>(k->slots, n_fits));
     PSG_PACK_CUDA(k, cudaEventRecord(k->ev[0], k->stream));
     int e = psg::launch_pack(k->form, w, k->ctx[0]->obj.ncoef, grid, k->P, k->smem, k->dsph_smem, k->stream);
@@ -1300,13 +1408,20 @@ ps_status ps_pack_fit(ps_pack *k, const double *conw_r, int64_t n_fits, const in
     std::vector<ps_fit> sorted(static_cast<size_t>(n_fits));
     PSG_PACK_CUDA(k, cudaMemcpyAsync(sorted.data(), k->d_out, sizeof(ps_fit) * n_fits, cudaMemcpyDeviceToHost,
                                      k->stream));
+    std::vector<float> traj_sorted(traj ? static_cast<size_t>(n_fits) * psg::kTrajFloats : 0);
+    if (traj)
+        PSG_PACK_CUDA(k, cudaMemcpyAsync(traj_sorted.data(), d_traj.p, traj_bytes, cudaMemcpyDeviceToHost, k->stream));
     PSG_PACK_CUDA(k, cudaStreamSynchronize(k->stream));
     float ms = 0;
     cudaEventElapsedTime(&ms, k->ev[0], k->ev[1]);
     int64_t evals = 0;
     for (int64_t i = 0; i < n_fits; i++) {
         const ps_fit &f = sorted[static_cast<size_t>(i)];
-        out[order[static_cast<size_t>(i)]] = f;
+        const int64_t u = order[static_cast<size_t>(i)];
+        out[u] = f;
+        if (traj)
+            std::memcpy(traj + u * psg::kTrajFloats, traj_sorted.data() + i * psg::kTrajFloats,
+                        psg::kTrajFloats * sizeof(float));
         evals += f.niter + 1;
         if (f.err_code == 16) {
             k->err = "a tensor-core wait gave up: fit results are incomplete";
@@ -1320,6 +1435,33 @@ ps_status ps_pack_fit(ps_pack *k, const double *conw_r, int64_t n_fits, const in
     k->timing.evals = evals;
     k->timing.launches = 1;
     return PS_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+ps_status ps_pack_fit(ps_pack *k, const double *conw_r, int64_t n_fits, const int32_t *object,
+                      const int64_t *period_index, const int32_t *pole, ps_fit *out)
+{
+    return pack_run(k, conw_r, n_fits, object, period_index, pole, 0, 0, nullptr, nullptr, out);
+}
+
+ps_status ps_pack_screen(ps_pack *k, const double *conw_r, int64_t n_fits, const int32_t *object,
+                         const int64_t *period_index, const int32_t *pole, int32_t screen_iters,
+                         const float *weights, ps_fit *out)
+{
+    if (!weights || !screen_iters_ok(screen_iters)) return PS_ERR_ARG;
+    return pack_run(k, conw_r, n_fits, object, period_index, pole, screen_iters, screen_iters, weights, nullptr,
+                    out);
+}
+
+ps_status ps_pack_trajectories(ps_pack *k, const double *conw_r, int64_t n_fits, const int32_t *object,
+                               const int64_t *period_index, const int32_t *pole, int32_t feat_iters, float *traj,
+                               ps_fit *out)
+{
+    if (!traj || !screen_iters_ok(feat_iters)) return PS_ERR_ARG;
+    return pack_run(k, conw_r, n_fits, object, period_index, pole, 0, feat_iters, nullptr, traj, out);
 }
 
 ps_status ps_pack_timing(const ps_pack *k, ps_timing *out)
@@ -1375,6 +1517,8 @@ void ps_destroy(ps_ctx *c)
     cudaFree(c->d_pidx);
     cudaFree(c->d_pole);
     cudaFree(c->d_eval);
+    cudaFree(c->d_state);
+    cudaFree(c->d_slot);
     for (auto &e : c->ev)
         if (e) cudaEventDestroy(e);
     if (c->stream) cudaStreamDestroy(c->stream);

@@ -57,8 +57,16 @@ struct FitWork {
     const int *object;
     // learned early stop (all optional)
     int iter_limit;               // > 0: stop every fit after this many LM iterations (screening)
+    int screen_iters;             // iterations after which the predictor's features are taken (a
+                                  // multiple of 4; 0: kScreenIters)
     float *traj;                  // [nfits][kTrajFloats] trajectory records, or nullptr
     const float *mlp;             // stop-predictor weights (layout of kMlp*), or nullptr
+    // resumable fits: the LM state of fit f lives in state[slot][state_stride(ma)]
+    // with slot = state_slot ? state_slot[f] : f; a fit stopped by iter_limit
+    // saves its state there, and with resume != 0 every fit continues from it
+    double *state;
+    const int64_t *state_slot;
+    int resume;
 };
 
 // Learned early stop: features of a fit after kScreenIters LM iterations,
@@ -67,7 +75,7 @@ struct FitWork {
 constexpr int kScreenIters = 4;
 constexpr int kFeat = 10;
 constexpr int kHidden = 64;
-constexpr int kTrajFloats = 16;   // features[10], dev_k, dev_final, niter, spare[3]
+constexpr int kTrajFloats = 16;   // features[10], dev_k, dev_final, niter, dev after 8/16/32 iterations
 constexpr int kMlpMu = 0, kMlpSd = kFeat, kMlpW1 = 2 * kFeat, kMlpB1 = kMlpW1 + kHidden * kFeat,
               kMlpW2 = kMlpB1 + kHidden, kMlpB2 = kMlpW2 + kHidden * kHidden, kMlpW3 = kMlpB2 + kHidden,
               kMlpB3 = kMlpW3 + kHidden, kMlpYMu = kMlpB3 + 1, kMlpYSd = kMlpYMu + 1, kMlpFloats = kMlpYSd + 1;
@@ -119,6 +127,13 @@ constexpr int kMisc = 40;
 constexpr size_t kPrefTim = 0, kPrefGeo = 256, kPrefAcc = 1280, kPrefGeo2 = 2048, kPrefBytes = 3072;
 constexpr size_t kTcAlphaOperands = 32768;   // tensor-core alpha/beta operands: two 128 x 32 TF32 tiles
 
+
+// Saved LM state of a stopped fit: the parameters cg[ma], then lambda,
+// chi^2 of the accepted point, the last trial chi^2, the regularised
+// chi^2, iter_diff, the previous and current rms, the three convexity
+// residuals of the accepted shape, its facet-area sum, the iteration count,
+// the last solver code and the learned prediction.
+PSG_HD constexpr int state_stride(int ma) { return ma + 16; }
 
 // Parked row of a relative lightcurve's point (scratch): the ma model-row
 // entries, the model value, and two values the second pass prepares.

@@ -2093,9 +2093,16 @@ __device__ void run_fit(const DevObject &ob, const FitConfig &cfg, const SlotLay
     const int C = ob.ncoef, ma = ob.ma, mf = ob.mfit;
     const double freq = cfg.freq_start - (n - 1) * cfg.freq_step;
     const double prd = 1 / freq;
+    // learned early stop: features after K iterations (accepted chi^2 and
+    // lambda every K/4 iterations); the saved state of a resumable fit
+    const int K = w.screen_iters > 0 ? w.screen_iters : kScreenIters;
+    const int K4 = K >> 2;
+    double *st = w.state ? w.state + (w.state_slot ? w.state_slot[fidx] : fidx) * state_stride(ma) : nullptr;
+    const bool resume = w.resume && st;
     for (int i = tid; i < ma; i += NT) {
         double v;
-        if (i < C) v = ob.cg_first[i];
+        if (resume) v = st[i];
+        else if (i < C) v = ob.cg_first[i];
         else if (i == C) v = kDeg2Rad * (90 - c_beta_pole[pole - 1]);
         else if (i == C + 1) v = kDeg2Rad * c_lambda_pole[pole - 1];
         else if (i == C + 2) v = 24 * 2 * kPi / prd;
@@ -2115,10 +2122,32 @@ __device__ void run_fit(const DevObject &ob, const FitConfig &cfg, const SlotLay
     double area_first = 0, area_trial = 0, totarea = 0;
     int niter = 0, last_err = 0;
     // learned early stop: accepted chi^2 and lambda of the first iterations
-    double hist[kScreenIters + 1], lam_hist[kScreenIters];
+    double hist[5], lam_hist[4];
     double pred_dev = 0;
     bool screened = false;
-    while (((niter < cfg.n_iter_max) && (iter_diff > cfg.iter_diff_max)) || (niter < cfg.n_iter_min)) {
+    if (resume) {
+        // continue where the fit stopped: alpha and beta are those of the
+        // accepted parameters, recomputed by one evaluation (the same
+        // deterministic evaluation the uninterrupted fit would hold)
+        alamda = st[ma];
+        ochisq = st[ma + 1];
+        chisq = st[ma + 2];
+        rchisq = st[ma + 3];
+        iter_diff = st[ma + 4];
+        dev_old = st[ma + 5];
+        dev_new = st[ma + 6];
+        for (int c = 0; c < 3; c++) chk_acc[c] = st[ma + 7 + c];
+        totarea = st[ma + 10];
+        niter = static_cast<int>(st[ma + 11]);
+        last_err = static_cast<int>(st[ma + 12]);
+        pred_dev = st[ma + 13];
+        evaluate<FORM, KU>(ob, cfg, L, s, s.cg, s.alpha, s.beta, scratch, tcs);
+        if constexpr (kTensor) {
+            if (*s.abort) last_err = kErrTcTimeout;
+        }
+    }
+    while (last_err != kErrTcTimeout &&
+           (((niter < cfg.n_iter_max) && (iter_diff > cfg.iter_diff_max)) || (niter < cfg.n_iter_min))) {
         bool accepted = false;
         if (alamda < 0) {
             alamda = cfg.alamda_start;
@@ -2221,18 +2250,22 @@ __device__ void run_fit(const DevObject &ob, const FitConfig &cfg, const SlotLay
         ochisq = s.misc[M_LM + 1];
         dev_new = s.misc[M_LM + 2];
         iter_diff = s.misc[M_LM + 3];
-        if (niter <= kScreenIters) {
-            hist[niter] = ochisq;
-            lam_hist[niter - 1] = alamda;
+        if (!resume && niter <= K && niter % K4 == 0) {
+            hist[niter / K4] = ochisq;
+            lam_hist[niter / K4 - 1] = alamda;
         }
-        if (niter == kScreenIters && (w.traj || w.mlp)) {
+        // trajectory records: the rms after 8, 16 and 32 iterations as well
+        if (w.traj && tid == 0 && (niter == 8 || niter == 16 || niter == 32))
+            w.traj[static_cast<size_t>(fidx) * kTrajFloats + (niter == 8 ? 13 : niter == 16 ? 14 : 15)] =
+                static_cast<float>(dev_new);
+        if (!resume && niter == K && (w.traj || w.mlp)) {
             // features and prediction on warp 0 only (FP64 logarithms)
             if (tid < 32) {
                 float f[kFeat];
 #pragma unroll
-                for (int i = 0; i < kScreenIters; i++) {
+                for (int i = 0; i < 4; i++) {
                     f[i] = static_cast<float>(log(hist[i + 1] / hist[0]));
-                    f[kScreenIters + i] = static_cast<float>(log10(lam_hist[i]));
+                    f[4 + i] = static_cast<float>(log10(lam_hist[i]));
                 }
                 f[8] = static_cast<float>(log(static_cast<double>(ob.ndata)));
                 f[9] = static_cast<float>(log(prd));
@@ -2241,7 +2274,7 @@ __device__ void run_fit(const DevObject &ob, const FitConfig &cfg, const SlotLay
                     for (int i = 0; i < kFeat; i++) rec[i] = f[i];
                     rec[10] = static_cast<float>(dev_new);
                 }
-                if (w.mlp && w.iter_limit == kScreenIters) {
+                if (w.mlp && w.iter_limit == K) {
                     const float y = mlp_predict_warp(w.mlp, f, reinterpret_cast<float *>(s.pt));
                     if (tid == 0) pred_dev = dev_new * exp(static_cast<double>(y));
                 }
@@ -2250,6 +2283,25 @@ __device__ void run_fit(const DevObject &ob, const FitConfig &cfg, const SlotLay
         }
         if (w.iter_limit > 0 && niter >= w.iter_limit) {
             screened = true;
+            if (st) {
+                // save the state for a later resume (thread 0 holds the
+                // prediction; every thread holds the broadcast scalars)
+                for (int i = tid; i < ma; i += NT) st[i] = s.cg[i];
+                if (tid == 0) {
+                    st[ma] = alamda;
+                    st[ma + 1] = ochisq;
+                    st[ma + 2] = chisq;
+                    st[ma + 3] = rchisq;
+                    st[ma + 4] = iter_diff;
+                    st[ma + 5] = dev_old;
+                    st[ma + 6] = dev_new;
+                    for (int c = 0; c < 3; c++) st[ma + 7 + c] = chk_acc[c];
+                    st[ma + 10] = totarea;
+                    st[ma + 11] = niter;
+                    st[ma + 12] = last_err;
+                    st[ma + 13] = pred_dev;
+                }
+            }
             break;
         }
     }

@@ -1,8 +1,8 @@
 // ps_mlp.cu -- training and inference kernels of the learned early-stop
 // predictor: a 10-64-64-1 multilayer perceptron with GELU activations in
-// FP32.  It maps the first kScreenIters iterations of an LM fit (accepted
-// chi^2 ratios, lambda, Ndata, period) to log(final rms / rms after those
-// iterations).  Parameters live in one float array (layout kMlp* in
+// FP32.  It maps the first K iterations of an LM fit (the screening depth:
+// accepted chi^2 ratios and lambda every K/4 iterations, Ndata, period) to
+// log(final rms / rms after those iterations).  Parameters live in one float array (layout kMlp* in
 // ps_engine.h): input mean/std, W1[64][10], b1, W2[64][64], b2, W3[64], b3,
 // target mean/std.  Standardisation constants are computed on the host;
 // training updates W1..b3 with Adam on mean squared error.

@@ -77,6 +77,40 @@ CONFIGS = {
 }
 
 
+def population_config(rng: np.random.Generator, name: str, ndata_lo: int, ndata_hi: int, per_start: float,
+                      per_end: float, n_periods: int) -> SynthConfig:
+    """One object of a seeded population of work units: Ndata log-uniform
+    in [ndata_lo, ndata_hi]; half the objects sparse calibrated data only,
+    half with 1-8 dense relative lightcurves (3 h, 60 points) plus sparse
+    points (at least 100), as in a survey's mix of work units."""
+    nd = int(round(math.exp(rng.uniform(math.log(ndata_lo), math.log(ndata_hi)))))
+    n_dense = 0
+    if rng.uniform() < 0.5:
+        n_dense = int(min(8, max(1, (nd - 100) // 60), rng.integers(1, 9)))
+        if nd - 60 * n_dense < 100:
+            n_dense = 0
+    return SynthConfig(name=name, n_sparse=nd - 60 * n_dense, n_dense=n_dense, per_start=per_start,
+                       per_end=per_end, n_periods=n_periods, sparse_block=1000)
+
+
+# The multi-object populations: many asteroids with uneven Ndata, each with
+# its own seed (population_config(rng, ...) with rng seeded per object).
+POPULATIONS = {
+    # many asteroids in one launch: Ndata logU[100, 5000], scan 2-20 h
+    "c3": dict(ndata_lo=100, ndata_hi=5000, per_start=2.0, per_end=20.0, n_periods=20000),
+    # the learned early stop's evaluation set: Ndata 200-3000, scan 2-100 h
+    "c5": dict(ndata_lo=200, ndata_hi=3000, per_start=2.0, per_end=100.0, n_periods=60000),
+}
+
+
+def population_object(pop: str, k: int, base_seed: int) -> SynthObject:
+    """Object k of population `pop` (seed base_seed + k for both its
+    configuration and its data)."""
+    rng = np.random.default_rng(base_seed + k)
+    cfg = population_config(rng, f"{pop}_{k}", **POPULATIONS[pop])
+    return make_object(cfg, seed=base_seed + k)
+
+
 def _ylm_norm(l: int, m: int) -> float:
     n = math.sqrt((2 * l + 1) / (4 * math.pi) * factorial(l - m) / factorial(l + m))
     return n * (math.sqrt(2.0) if m > 0 else 1.0)
