@@ -361,6 +361,7 @@ def main():
     ap.add_argument("--eval-objects", type=int, default=2000, help="survey-population evaluation objects")
     ap.add_argument("--device", type=int, default=0)
     ap.add_argument("--processes", type=int, default=16)
+    ap.add_argument("--dump", default="", help="save the collected windows' trajectories (npz) here")
     args = ap.parse_args()
     K = SCREEN_ITERS
     # every object is generated before the GPU is touched (spawned workers)
@@ -377,6 +378,13 @@ def main():
     w_pop_ev, ms_c = collect_windows(pop_eval, 24, K, args.device, around_truth=lambda k: k % 2 == 0, seed=3)
     w_st_ev, ms_d = collect_windows(st_eval, 400, K, args.device, seed=4)
     t1 = time.time()
+    if args.dump:
+        arrs = {}
+        for name, ws in (("pop_train", w_pop), ("st_train", w_st), ("pop_eval", w_pop_ev), ("st_eval", w_st_ev)):
+            arrs[name + "_feat"] = np.concatenate([w["traj"][:, :F] for w in ws]).astype(np.float16)
+            arrs[name + "_dev"] = np.concatenate([w["traj"][:, F:] for w in ws]).astype(np.float32)
+            arrs[name + "_len"] = np.array([len(w["traj"]) for w in ws])
+        np.savez(args.dump, **arrs)
     xs, ys = [], []
     for w in w_pop + w_st:
         x, y, _, _ = samples(w["traj"])
