@@ -57,6 +57,8 @@ struct ps_ctx {
     size_t state_cap = 0;              // fits
     int64_t *d_slot = nullptr;         // state rows of resumed fits
     size_t slot_cap = 0;
+    double *d_alpha_g = nullptr;       // per-slot normal matrices of the wide tensor-core path
+    size_t alpha_g_slots = 0;
     std::vector<ps_fit> h_fits;
     ps_timing timing{};
     std::string err;
@@ -146,13 +148,14 @@ ps_status build_plan(ps_ctx *c, int form, int dsph_smem, int P, int per_sm_cap, 
     PSG_CUDA(c, cudaGetDeviceProperties(&prop, c->opt.device));
     const size_t smem_max = static_cast<size_t>(prop.sharedMemPerBlockOptin);
     if (dsph_smem == psg::kBasisTensor && !psg::tensor_basis_ok(F, o.ncoef, o.mfit, P)) return PS_ERR_LIMIT;
+    if (dsph_smem == psg::kBasisTensorWide && !psg::tensor_wide_ok(F, o.ncoef, o.mfit, P)) return PS_ERR_LIMIT;
     const psg::SlotLayout L = psg::make_layout(form, o.ma, o.mfit, F, o.ncoef, P, dsph_smem);
     if (L.bytes > smem_max) return PS_ERR_LIMIT;
     // A tensor-core slot holds up to 512 Tensor Memory columns for its whole
     // life: request enough shared memory that only one slot fits on an SM.
     const size_t floor_tc = static_cast<size_t>(prop.sharedMemPerMultiprocessor) / 2 + 1024;
     size_t bytes = L.bytes;
-    if (dsph_smem == psg::kBasisTensor) bytes = std::min(smem_max, std::max(bytes, floor_tc));
+    if (psg::basis_on_tensor(dsph_smem)) bytes = std::min(smem_max, std::max(bytes, floor_tc));
     int e = psg::set_kernel_smem(form, bytes, o.ncoef, dsph_smem);
     if (e != 0) return cuda_fail(c, static_cast<cudaError_t>(e), "cudaFuncSetAttribute");
     int per_sm = 0;
@@ -161,7 +164,7 @@ ps_status build_plan(ps_ctx *c, int form, int dsph_smem, int P, int per_sm_cap, 
     int rel_rows = 0;
     if (o.max_rel_points > 0) {
         const psg::SlotLayout Lr = psg::make_layout(form, o.ma, o.mfit, F, o.ncoef, P, dsph_smem, o.max_rel_points);
-        const size_t need = dsph_smem == psg::kBasisTensor ? std::max(Lr.bytes, floor_tc) : Lr.bytes;
+        const size_t need = psg::basis_on_tensor(dsph_smem) ? std::max(Lr.bytes, floor_tc) : Lr.bytes;
         if (Lr.bytes <= smem_max) {
             e = psg::set_kernel_smem(form, need, o.ncoef, dsph_smem);
             if (e != 0) return cuda_fail(c, static_cast<cudaError_t>(e), "cudaFuncSetAttribute");
@@ -181,7 +184,7 @@ ps_status build_plan(ps_ctx *c, int form, int dsph_smem, int P, int per_sm_cap, 
     }
     if (per_sm < 1) return PS_ERR_LIMIT;
     if (per_sm_cap > 0) per_sm = std::min(per_sm, per_sm_cap);
-    if (dsph_smem == psg::kBasisTensor && per_sm > 1) {
+    if (psg::basis_on_tensor(dsph_smem) && per_sm > 1) {
         c->err = "tensor-core fit slots would share an SM";
         return PS_ERR_LIMIT;
     }
@@ -209,6 +212,8 @@ ps_status make_plan(ps_ctx *c, int form)
     if (mixed) {
         if (!(c->opt.flags & PS_FLAG_NO_TENSOR) && psg::tensor_basis_ok(o.shape.nfac, o.ncoef, o.mfit, 32))
             modes[nm++] = psg::kBasisTensor;
+        else if (!(c->opt.flags & PS_FLAG_NO_TENSOR) && psg::tensor_wide_ok(o.shape.nfac, o.ncoef, o.mfit, 32))
+            modes[nm++] = psg::kBasisTensorWide;
         modes[nm++] = psg::kBasisSmem;
     }
     modes[nm++] = psg::kBasisGlobal;
@@ -248,6 +253,19 @@ ps_status run_fits(ps_ctx *c, double conw_r, psg::FitWork w, int form)
     w.scratch_stride = c->scratch_stride;
     w.rel_rows = pl.rel_rows;
     w.out = c->d_out;
+    if (pl.dsph_smem == psg::kBasisTensorWide) {
+        // the wide tensor-core path keeps each slot's normal matrix in global memory
+        const size_t stride = static_cast<size_t>(c->obj.mfit) * c->obj.mfit;
+        if (c->alpha_g_slots < static_cast<size_t>(pl.slots)) {
+            cudaFree(c->d_alpha_g);
+            c->d_alpha_g = nullptr;
+            c->alpha_g_slots = 0;
+            PSG_CUDA(c, cudaMalloc(&c->d_alpha_g, stride * pl.slots * sizeof(double)));
+            c->alpha_g_slots = static_cast<size_t>(pl.slots);
+        }
+        w.alpha_g = c->d_alpha_g;
+        w.alpha_stride = stride;
+    }
     int grid = static_cast<int>(std::min<int64_t>(pl.slots, std::max<int64_t>(w.nfits, 1)));
     PSG_CUDA(c, cudaMemsetAsync(c->d_queue, 0, sizeof(unsigned long long), c->stream));
     PSG_CUDA(c, cudaEventRecord(c->ev[0], c->stream));
@@ -709,7 +727,7 @@ ps_status ps_get_info(const ps_ctx *c, ps_info *out)
     out->slots = c->slots;
     out->h2d_bytes = c->h2d_bytes;
     const FormPlan &pl = c->plan[c->opt.form];
-    out->tensor_cores = pl.ready && pl.dsph_smem == psg::kBasisTensor ? 1 : 0;
+    out->tensor_cores = pl.ready && psg::basis_on_tensor(pl.dsph_smem) ? 1 : 0;
     out->tile_points = pl.ready ? pl.P : 0;
     return PS_OK;
 }
@@ -1161,7 +1179,10 @@ extern "C" ps_status ps_autotune(ps_ctx *c, double conw_r, int32_t sample_fits, 
     }
     std::vector<int> modes;
     if (mixed) {
-        if (!(c->opt.flags & PS_FLAG_NO_TENSOR)) modes.push_back(psg::kBasisTensor);
+        if (!(c->opt.flags & PS_FLAG_NO_TENSOR)) {
+            modes.push_back(psg::kBasisTensor);
+            modes.push_back(psg::kBasisTensorWide);
+        }
         modes.push_back(psg::kBasisSmem);
     }
     modes.push_back(psg::kBasisGlobal);
@@ -1235,6 +1256,7 @@ struct ps_pack {
     psg::FitConfig *d_cfgs = nullptr;
     double *d_scratch = nullptr;
     size_t scratch_stride = 0;
+    double *d_alpha_g = nullptr;       // per-slot normal matrices of the wide tensor-core path
     int slots = 0, P = 0, dsph_smem = 0;
     size_t smem = 0;
     unsigned long long *d_queue = nullptr;
@@ -1305,6 +1327,9 @@ ps_status ps_pack_create(ps_ctx *const *ctxs, int32_t n, int32_t form, ps_pack *
     PSG_PACK_CUDA(k.get(), cudaMalloc(&k->d_cfgs, sizeof(psg::FitConfig) * n));
     PSG_PACK_CUDA(k.get(), cudaMalloc(&k->d_scratch, k->scratch_stride * k->slots * sizeof(double)));
     PSG_PACK_CUDA(k.get(), cudaMalloc(&k->d_queue, sizeof(unsigned long long)));
+    if (k->dsph_smem == psg::kBasisTensorWide)
+        PSG_PACK_CUDA(k.get(), cudaMalloc(&k->d_alpha_g, static_cast<size_t>(c0->obj.mfit) * c0->obj.mfit *
+                                                            k->slots * sizeof(double)));
     std::vector<psg::DevObject> objs(static_cast<size_t>(n));
     for (int32_t i = 0; i < n; i++) objs[static_cast<size_t>(i)] = ctxs[i]->dob;
     PSG_PACK_CUDA(k.get(), cudaMemcpy(k->d_objs, objs.data(), sizeof(psg::DevObject) * n, cudaMemcpyHostToDevice));
@@ -1381,6 +1406,8 @@ ps_status pack_run(ps_pack *k, const double *conw_r, int64_t n_fits, const int32
     w.objs = k->d_objs;
     w.cfgs = k->d_cfgs;
     w.object = k->d_obj;
+    w.alpha_g = k->d_alpha_g;
+    w.alpha_stride = static_cast<size_t>(k->ctx[0]->obj.mfit) * k->ctx[0]->obj.mfit;
     w.iter_limit = iter_limit;
     w.screen_iters = screen_iters;
     // predictor weights and trajectory records: launch-local device buffers
@@ -1481,6 +1508,7 @@ void ps_pack_destroy(ps_pack *k)
     cudaFree(k->d_objs);
     cudaFree(k->d_cfgs);
     cudaFree(k->d_scratch);
+    cudaFree(k->d_alpha_g);
     cudaFree(k->d_queue);
     cudaFree(k->d_obj);
     cudaFree(k->d_pole);
@@ -1519,6 +1547,7 @@ void ps_destroy(ps_ctx *c)
     cudaFree(c->d_eval);
     cudaFree(c->d_state);
     cudaFree(c->d_slot);
+    cudaFree(c->d_alpha_g);
     for (auto &e : c->ev)
         if (e) cudaEventDestroy(e);
     if (c->stream) cudaStreamDestroy(c->stream);

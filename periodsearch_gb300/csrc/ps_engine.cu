@@ -132,12 +132,15 @@ int launch_fits_noalloc(int form, const DevObject &ob, const FitConfig &cfg, Fit
 
 namespace {
 
-// Mixed-form kernel variant: 0 = tensor-core contraction; otherwise the
-// SIMT contraction's coefficient slots per lane, 1 for C <= 64 and 2 up to
-// 128 (the largest Laplace series, L = 10, has 121 coefficients).
+// Mixed-form kernel variant: 0 = tensor-core contraction and alpha; 3 = the
+// wide tensor-core contraction (65..96 coefficients) with the SIMT alpha;
+// otherwise the SIMT contraction's coefficient slots per lane, 1 for C <= 64
+// and 2 up to 128 (the largest Laplace series, L = 10, has 121
+// coefficients).
 inline int ku_of(int ncoef, int dsph_smem)
 {
     if (dsph_smem == kBasisTensor) return 0;
+    if (dsph_smem == kBasisTensorWide) return 3;
     return ncoef <= 64 ? 1 : 2;
 }
 
@@ -147,6 +150,7 @@ cudaError_t for_mixed(int ncoef, int dsph_smem, Fn fn)
     switch (ku_of(ncoef, dsph_smem)) {
     case 0: return fn(std::integral_constant<int, 0>{});
     case 1: return fn(std::integral_constant<int, 1>{});
+    case 3: return fn(std::integral_constant<int, 3>{});
     default: return fn(std::integral_constant<int, 2>{});
     }
 }
@@ -160,11 +164,11 @@ cudaError_t for_mixed(int ncoef, int dsph_smem, Fn fn)
 int set_kernel_smem(int form, size_t smem, int ncoef, int dsph_smem)
 {
     static std::mutex mu;
-    static int raised[64][2][3] = {};
+    static int raised[64][2][4] = {};
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess) return static_cast<int>(e);
-    const int ku = form == PS_FORM_FP64 ? 1 : (dsph_smem == kBasisTensor ? 0 : (ncoef <= 64 ? 1 : 2));
+    const int ku = form == PS_FORM_FP64 ? 1 : ku_of(ncoef, dsph_smem);
     std::lock_guard<std::mutex> lock(mu);
     int *cur = (dev >= 0 && dev < 64 && (form == PS_FORM_FP64 || form == PS_FORM_MIXED)) ? &raised[dev][form][ku] : nullptr;
     if (cur && *cur >= static_cast<int>(smem)) return 0;

@@ -8,6 +8,12 @@
 
 namespace psg {
 
+#if defined(__CUDACC__)
+#define PSG_HD __host__ __device__
+#else
+#define PSG_HD
+#endif
+
 // One object's tables in device memory (all arrays device pointers, 0-based).
 struct DevObject {
     int nfac, ncoef, ma, mfit, npairs, mmax;
@@ -61,6 +67,10 @@ struct FitWork {
                                   // multiple of 4; 0: kScreenIters)
     float *traj;                  // [nfits][kTrajFloats] trajectory records, or nullptr
     const float *mlp;             // stop-predictor weights (layout of kMlp*), or nullptr
+    // kBasisTensorWide: every slot keeps its normal matrix (mfit x mfit
+    // doubles) at alpha_g + blockIdx.x * alpha_stride
+    double *alpha_g;
+    size_t alpha_stride;
     // resumable fits: the LM state of fit f lives in state[slot][state_stride(ma)]
     // with slot = state_slot ? state_slot[f] : f; a fit stopped by iter_limit
     // saves its state there, and with resume != 0 every fit continues from it
@@ -86,7 +96,12 @@ constexpr int kMlpMu = 0, kMlpSd = kFeat, kMlpW1 = 2 * kFeat, kMlpB1 = kMlpW1 + 
 // Where the mixed form's shape contraction takes the basis Dsph from
 // (SlotLayout::dsph_smem): global memory, shared memory (both with the SIMT
 // contraction), or Tensor Memory with the tcgen05 contraction.
-enum BasisMode : int { kBasisGlobal = 0, kBasisSmem = 1, kBasisTensor = 2 };
+// kBasisTensorWide: the tcgen05 contraction for Laplace series of 65 to 96
+// coefficients (L = 8: 81), whose split basis does not fit the 128 Tensor
+// Memory lanes of one region (see tensor_wide_ok), with the alpha/beta
+// accumulation on the SIMT pipes and the kept normal matrix in global memory.
+enum BasisMode : int { kBasisGlobal = 0, kBasisSmem = 1, kBasisTensor = 2, kBasisTensorWide = 3 };
+PSG_HD inline bool basis_on_tensor(int mode) { return mode == kBasisTensor || mode == kBasisTensorWide; }
 
 struct SlotLayout {
     int form, ma, mfit, nfac, ncoef, P, wcols, dsph_smem;
@@ -104,11 +119,6 @@ struct SlotLayout {
     size_t bytes;
 };
 
-#if defined(__CUDACC__)
-#define PSG_HD __host__ __device__
-#else
-#define PSG_HD
-#endif
 
 constexpr int kThreads = 256;   // threads of an FP64-form fit slot
 // Threads of a fit slot: the FP64 form is register-limited to 256; the mixed
@@ -173,14 +183,14 @@ PSG_HD inline SlotLayout make_layout(int form, int ma, int mfit, int nfac, int n
     L.atry = take(ma * d);
     L.beta = take(mfit * d);
     L.da = take(mfit * d);
-    L.alpha = take(static_cast<size_t>(mfit) * mfit * d);
+    L.alpha = take(dsph_smem == kBasisTensorWide ? 0 : static_cast<size_t>(mfit) * mfit * d);
     L.covar = take(static_cast<size_t>(mfit) * mfit * d);
     L.area = take(nfac * d);
     L.gv = take(nfac * d);
     L.areaR = form == PS_FORM_MIXED ? take(nfac * rs) : L.area;
     L.gvR = form == PS_FORM_MIXED ? take(nfac * rs) : L.gv;
     // the tensor-core path writes W straight into the MMA operand
-    L.W = take(dsph_smem == kBasisTensor ? 0 : static_cast<size_t>(P) * L.wcols * rs);
+    L.W = take(basis_on_tensor(dsph_smem) ? 0 : static_cast<size_t>(P) * L.wcols * rs);
     L.J = take(static_cast<size_t>(P) * ma * rs);
     L.pt = take(static_cast<size_t>(P) * kPointStride * rs);
     L.ym = take(P * d);
@@ -190,7 +200,8 @@ PSG_HD inline SlotLayout make_layout(int form, int ma, int mfit, int nfac, int n
     L.misc = take(kMisc * d);
     L.ipiv = take(sizeof(int) * static_cast<size_t>(mfit + 2 + 16));
     L.dsph = dsph_smem == kBasisSmem ? take(static_cast<size_t>(nfac) * ncoef * sizeof(float)) : 0;
-    if (dsph_smem == kBasisTensor) {
+    if (basis_on_tensor(dsph_smem)) {
+        const bool wide = dsph_smem == kBasisTensorWide;
         // B = [W_hi; W_lo]: 2P rows, the low parts right after the high parts
         // (8-row groups stride-byte-offset apart); the accumulator rows are
         // staged over it for the epilogue
@@ -198,11 +209,18 @@ PSG_HD inline SlotLayout make_layout(int form, int ma, int mfit, int nfac, int n
         // operands (two 128 x 32 TF32 tiles) have their own region, so that
         // their MMAs overlap the next tile's facet stage.
         // (FP16 elements, facets padded to tc_kpad)
+        // (wide: the region also stages the second readback and the SIMT
+        // accumulation's weighted rows)
         const size_t tile = static_cast<size_t>(P) * tc_kpad(nfac) * 2;
-        const size_t readback = 128 * 65 * sizeof(float);
+        size_t readback = 128 * 65 * sizeof(float);
+        if (wide) {
+            const size_t wt = static_cast<size_t>(P) * mfit * sizeof(float);
+            readback = 2 * 128 * 33 * sizeof(float);
+            if (wt > readback) readback = wt;
+        }
         L.bhi = take(2 * tile > readback ? 2 * tile : readback);
         L.blo = L.bhi + tile;
-        L.aop = take(kTcAlphaOperands);
+        L.aop = take(wide ? 0 : kTcAlphaOperands);
         L.tcm = take(32);
         L.pt2 = take(static_cast<size_t>(P) * kPointStride * rs);
         L.fac = take(static_cast<size_t>(tc_kpad(nfac)) * 4 * sizeof(float));
@@ -246,6 +264,20 @@ int occupancy_slots(int form, size_t smem, int ncoef, int dsph_smem, int *per_sm
 PSG_HD inline bool tensor_basis_ok(int nfac, int ncoef, int mfit, int P)
 {
     return ncoef <= 64 && mfit <= 63 && (((tc_kpad(nfac) >> 1) + 31) & ~31) + 64 + 128 <= 512 && P == 32;
+}
+// The wide tensor-core path (kBasisTensorWide) for 64 < C <= 96
+// coefficients: region R1 holds the FP16 high parts of all C coefficients
+// (lanes 0..C-1) and the low parts of the first 128 - C (lanes C..127);
+// region R2 holds the low parts of the other n2 = 2C - 128 <= 64, the first
+// half of the facets in lanes 0..n2-1 and the second half in lanes
+// 64..64+n2-1 (Fp/4 columns).  With the two accumulators (64 columns each)
+// the Tensor Memory holds 3 Fp / 4 + 128 <= 512 columns, i.e. up to 512
+// facets (nrows = 8).  The alpha/beta accumulation runs on the SIMT pipes
+// (FP32 partial sums, up to 90 free parameters).
+PSG_HD inline bool tensor_wide_ok(int nfac, int ncoef, int mfit, int P)
+{
+    return ncoef > 64 && ncoef <= 96 && mfit <= 90 && ((3 * (tc_kpad(nfac) >> 2) + 31) & ~31) + 128 <= 512 &&
+           P == 32;
 }
 int measure_fma_peaks(double *fp64_tflops, double *fp32_tflops, void *stream);
 // Learned early stop (ps_mlp.cu).

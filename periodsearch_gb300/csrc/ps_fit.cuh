@@ -127,7 +127,7 @@ __device__ inline Smem<FORM> carve(char *base, const SlotLayout &L)
     s.misc = reinterpret_cast<double *>(base + L.misc);
     s.ipiv = reinterpret_cast<int *>(base + L.ipiv);
     s.dsph = L.dsph_smem == kBasisSmem ? reinterpret_cast<float *>(base + L.dsph) : nullptr;
-    if (L.dsph_smem == kBasisTensor) {
+    if (basis_on_tensor(L.dsph_smem)) {
         s.bhi = reinterpret_cast<unsigned char *>(base + L.bhi);
         s.blo = reinterpret_cast<unsigned char *>(base + L.blo);
         s.mbar = reinterpret_cast<uint64_t *>(base + L.tcm);
@@ -139,6 +139,10 @@ __device__ inline Smem<FORM> carve(char *base, const SlotLayout &L)
         s.aop = reinterpret_cast<unsigned char *>(base + L.aop);
         s.pref = reinterpret_cast<unsigned char *>(base + L.pref);
         s.flist = reinterpret_cast<int *>(base + L.flist);
+        // wide path: the SIMT accumulation's weighted rows are staged in the
+        // operand region (free between a tile's readback and the next
+        // tile's facet stage)
+        if (L.dsph_smem == kBasisTensorWide) s.W = reinterpret_cast<R *>(base + L.bhi);
     } else {
         s.bhi = s.blo = nullptr;
         s.mbar = s.mbar2 = nullptr;
@@ -678,14 +682,22 @@ constexpr int kErrTcTimeout = 16;             // ps_fit.err_code of a fit cut sh
 // Tensor Memory columns: the basis [0, Fp/2) (FP16 pairs of facets, Fp =
 // tc_kpad(F)), the contraction accumulator [tc_dcol, tc_dcol + 64) (column
 // p: A W_hi^T for point p, 32 + p: A W_lo^T) and the alpha accumulator
-// [tc_acol, tc_acol + 128).
-__device__ inline uint32_t tc_dcol(int F) { return static_cast<uint32_t>(((tc_kpad(F) >> 1) + 31) & ~31); }
+// [tc_acol, tc_acol + 128).  The wide path (kBasisTensorWide) has the
+// second basis region R2 at [Fp/2, 3 Fp/4), the accumulator at tc_dcol and
+// R2's accumulator at tc_dcol + 64 (columns 0..31: products with the first
+// half of the facets, 32..63: with the second half), and no alpha
+// accumulator.
+__device__ inline uint32_t tc_r2col(int F) { return static_cast<uint32_t>(tc_kpad(F) >> 1); }
+__device__ inline uint32_t tc_dcol(int F, bool wide = false)
+{
+    return static_cast<uint32_t>(((wide ? 3 * (tc_kpad(F) >> 2) : (tc_kpad(F) >> 1)) + 31) & ~31);
+}
 __device__ inline uint32_t tc_acol(int F) { return tc_dcol(F) + 64; }
 
-__device__ inline uint32_t tc_cols(int F)
+__device__ inline uint32_t tc_cols(int F, bool wide = false)
 {
     uint32_t n = 32;
-    while (n < tc_acol(F) + 128) n <<= 1;
+    while (n < (wide ? tc_dcol(F, true) + 128 : tc_acol(F) + 128)) n <<= 1;
     return n;
 }
 
@@ -698,6 +710,7 @@ struct TcState {
     uint32_t aphase = 0;    // parity of the alpha barrier's next phase
     bool apending = false;  // alpha MMAs committed and not waited for
     bool afresh = true;     // the alpha accumulator holds nothing since the last flush
+    bool wide = false;      // kBasisTensorWide layout
 };
 
 // Waits for the committed alpha MMAs (their operands' shared memory is then
@@ -723,12 +736,12 @@ __device__ inline void tc_alpha_wait(Smem<PS_FORM_MIXED> &s, TcState &t)
 // (the largest magnitude just below 2^14, so that the low parts stay normal
 // FP16 numbers for elements down to 2^-3 of it); column j holds facets 2j
 // and 2j + 1.
-template <int NT>
+template <int NT, bool WIDE = false>
 __device__ void tc_setup(const DevObject &ob, Smem<PS_FORM_MIXED> &s, TcState &t)
 {
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int F = ob.nfac, C = ob.ncoef, Fp = tc_kpad(F);
-    if (warp == 0) tc::tmem_alloc(s.tslot, tc_cols(F));
+    if (warp == 0) tc::tmem_alloc(s.tslot, tc_cols(F, WIDE));
     if (tid == 0) {
         tc::mbar_init(s.mbar, 1);
         tc::mbar_init(s.mbar2, 1);
@@ -749,27 +762,52 @@ __device__ void tc_setup(const DevObject &ob, Smem<PS_FORM_MIXED> &s, TcState &t
     const uint32_t tbase = *s.tslot;
     for (int i = tid; i < Fp; i += NT)
         s.fac[i] = i < F ? make_float4(ob.nx_f[i], ob.ny_f[i], ob.nz_f[i], 0.f) : make_float4(0.f, 0.f, 0.f, 0.f);
-    for (int i = tid; i < static_cast<int>(kTcAlphaOperands / 4); i += NT) reinterpret_cast<uint32_t *>(s.aop)[i] = 0;
+    if constexpr (!WIDE)
+        for (int i = tid; i < static_cast<int>(kTcAlphaOperands / 4); i += NT)
+            reinterpret_cast<uint32_t *>(s.aop)[i] = 0;
     for (int j = tid; j < ob.mfit; j += NT) s.flist[j] = ob.free_list[j];
     if (warp < 4) {
-        const int m = warp * 32 + lane, c = m & 63;
-        const bool low = m >= 64;
+        // lane m of R1: coefficient c, high part (low = false) or low part;
+        // lane m of R2 (wide path): low part of coefficient c2 for the
+        // facet half h2 (-1: unused lane)
+        const int m = warp * 32 + lane;
+        int c, c2 = -1, h2 = 0;
+        bool low;
+        if constexpr (WIDE) {
+            const int L1 = 128 - C, n2 = C - L1;
+            low = m >= C;
+            c = low ? m - C : m;
+            if ((m & 63) < n2) {
+                c2 = L1 + (m & 63);
+                h2 = m >> 6;
+            }
+        } else {
+            c = m & 63;
+            low = m >= 64;
+        }
         const uint32_t row = tbase + (static_cast<uint32_t>(warp * 32) << 16);
+        auto part = [&](int cc, int i, bool lo) {
+            const double d = (cc >= 0 && cc < C && i < F) ? ob.dsph[static_cast<size_t>(i) * C + cc] * bscale : 0.0;
+            const float hi = tc::round_f16(static_cast<float>(d));
+            return lo ? static_cast<float>(d - static_cast<double>(hi)) : hi;
+        };
         for (int j0 = 0; j0 < Fp / 2; j0 += 8) {
             uint32_t v[8];
 #pragma unroll
-            for (int j = 0; j < 8; j++) {
-                float h[2];
-#pragma unroll
-                for (int u = 0; u < 2; u++) {
-                    const int i = 2 * (j0 + j) + u;
-                    const double d = (c < C && i < F) ? ob.dsph[static_cast<size_t>(i) * C + c] * bscale : 0.0;
-                    const float hi = tc::round_f16(static_cast<float>(d));
-                    h[u] = low ? static_cast<float>(d - static_cast<double>(hi)) : hi;
-                }
-                v[j] = tc::pack_f16x2(h[0], h[1]);
-            }
+            for (int j = 0; j < 8; j++) v[j] = tc::pack_f16x2(part(c, 2 * (j0 + j), low), part(c, 2 * (j0 + j) + 1, low));
             tc::tmem_st8(row + static_cast<uint32_t>(j0), v);
+        }
+        if constexpr (WIDE) {
+            // R2 column j: facets 2j, 2j + 1 of the lane's facet half
+            for (int j0 = 0; j0 < Fp / 4; j0 += 8) {
+                uint32_t v[8];
+#pragma unroll
+                for (int j = 0; j < 8; j++) {
+                    const int i = h2 * (Fp / 2) + 2 * (j0 + j);
+                    v[j] = tc::pack_f16x2(part(c2, i, true), part(c2, i + 1, true));
+                }
+                tc::tmem_st8(row + tc_r2col(F) + static_cast<uint32_t>(j0), v);
+            }
         }
         tc::tmem_wait_st();
     }
@@ -778,6 +816,7 @@ __device__ void tc_setup(const DevObject &ob, Smem<PS_FORM_MIXED> &s, TcState &t
     tc::fence_after_sync();
     t.tbase = tbase;
     t.basis_exp = bexp;
+    t.wide = WIDE;
 }
 
 // Releases the Tensor Memory.  After an abandoned wait the MMAs in flight
@@ -790,7 +829,7 @@ __device__ void tc_teardown(Smem<PS_FORM_MIXED> &s, const TcState &t, int F)
     }
     tc::fence_before_sync();
     __syncthreads();
-    if ((threadIdx.x >> 5) == 0) tc::tmem_dealloc(t.tbase, tc_cols(F));
+    if ((threadIdx.x >> 5) == 0) tc::tmem_dealloc(t.tbase, tc_cols(F, t.wide));
 }
 
 // Issues the alpha/beta MMAs of the operands in s.aop (built and fenced,
@@ -821,7 +860,7 @@ __device__ inline void tc_alpha_issue(Smem<PS_FORM_MIXED> &s, TcState &t, int F)
 // barrier.  The facet stage has written the operand: FP16 high parts of W
 // in rows 0..31, low parts in rows 32..63, canonical K-major layout (8-row x
 // 8-facet core matrices, K-adjacent ones 128 bytes apart).
-template <int NT>
+template <int NT, bool WIDE = false>
 __device__ void contract_tc_issue(Smem<PS_FORM_MIXED> &s, int F, TcState &t)
 {
     const int tid = threadIdx.x;
@@ -834,10 +873,23 @@ __device__ void contract_tc_issue(Smem<PS_FORM_MIXED> &s, int F, TcState &t)
         tc::fence_after_sync();
         const uint32_t idesc = tc::idesc_f16(128, 64);
         const uint32_t sbo = static_cast<uint32_t>(kcs) * 128;
-        const uint32_t bh = tc::smem_u32(s.bhi), d = tbase + tc_dcol(F);
+        const uint32_t bh = tc::smem_u32(s.bhi), d = tbase + tc_dcol(F, WIDE);
         for (int ks = 0; ks < Fp / 16; ks++) {
             const uint32_t a = tbase + static_cast<uint32_t>(ks) * 8, off = static_cast<uint32_t>(ks) * 256;
             tc::mma_f16_ts(d, a, tc::smem_desc(bh + off, 128, sbo), idesc, ks > 0);
+        }
+        if constexpr (WIDE) {
+            // R2 against the W_hi rows (N = 32) of each facet half: the
+            // products of lanes 0.. with the first half land in columns
+            // 0..31, those of lanes 64.. with the second half in 32..63
+            const uint32_t idesc32 = tc::idesc_f16(128, 32), d2 = d + 64, a2 = tbase + tc_r2col(F);
+            const int half_steps = Fp / 32;
+            for (int h = 0; h < 2; h++)
+                for (int ks = 0; ks < half_steps; ks++) {
+                    const uint32_t off = static_cast<uint32_t>(h * half_steps + ks) * 256;
+                    tc::mma_f16_ts(d2 + 32u * h, a2 + static_cast<uint32_t>(ks) * 8, tc::smem_desc(bh + off, 128, sbo),
+                                   idesc32, ks > 0);
+                }
         }
         tc::mma_commit(s.mbar);
     }
@@ -996,7 +1048,7 @@ __device__ void conv_rows_tc(const DevObject &ob, Smem<PS_FORM_MIXED> &s, float 
 // + D[64 + k][p] + D[64 + k][32 + p]): basis high and low parts times W high
 // and low parts, jscale undoing the operands' power-of-two scales.  A wait
 // that gives up sets the abort flag; the caller ends the fit.
-template <int NT>
+template <int NT, bool WIDE = false>
 __device__ void contract_tc_finish(Smem<PS_FORM_MIXED> &s, int np, int F, int C, int ma, bool conv, TcState &t,
                                    float jscale)
 {
@@ -1015,9 +1067,10 @@ __device__ void contract_tc_finish(Smem<PS_FORM_MIXED> &s, int np, int F, int C,
     // access Tensor Memory lanes 32 (w % 4) .. + 31), the products with W_hi
     // (column p) and W_lo (column 32 + p) and stages their sum Y[m][p]
     float *Y = reinterpret_cast<float *>(s.bhi);   // [128][33]
+    float *Y2 = Y + 128 * 33;                      // wide path: [128][33] from R2's accumulator
     {
         const int quad = warp & 3, pg = warp >> 2;
-        const uint32_t taddr = tbase + (static_cast<uint32_t>(quad * 32) << 16) + tc_dcol(F) + 8 * pg;
+        const uint32_t taddr = tbase + (static_cast<uint32_t>(quad * 32) << 16) + tc_dcol(F, WIDE) + 8 * pg;
         float *yr = Y + (quad * 32 + lane) * 33 + 8 * pg;
         uint32_t vh[8], vl[8];
         tc::tmem_ld8(taddr, vh);
@@ -1025,8 +1078,33 @@ __device__ void contract_tc_finish(Smem<PS_FORM_MIXED> &s, int np, int F, int C,
         tc::tmem_wait_ld();
 #pragma unroll
         for (int j = 0; j < 8; j++) yr[j] = __uint_as_float(vh[j]) + __uint_as_float(vl[j]);
+        if constexpr (WIDE) {
+            // lanes 0..63 hold the first facet half's products (columns
+            // 0..31), lanes 64..127 the second half's (columns 32..63)
+            uint32_t v2[8];
+            tc::tmem_ld8(taddr + 64 + (quad >= 2 ? 32 : 0), v2);
+            tc::tmem_wait_ld();
+            float *y2 = Y2 + (quad * 32 + lane) * 33 + 8 * pg;
+#pragma unroll
+            for (int j = 0; j < 8; j++) y2[j] = __uint_as_float(v2[j]);
+        }
     }
     __syncthreads();
+    if constexpr (WIDE) {
+        // J[p][k] = Scale_p jscale (high part of k times W_hi and W_lo + low
+        // part of k times W: from R1's lanes C + k for k < 128 - C, else
+        // from R2's two facet halves); thread: k = tid % 128, points
+        // tid / 128 + 4 i
+        const int k = tid & 127, L1 = 128 - C;
+        if (k < C) {
+            for (int p = tid >> 7; p < np; p += NT / 128) {
+                const float sc = (conv ? 1.f : s.pt[p * kPointStride + 24]) * jscale;
+                const float lo = k < L1 ? Y[(C + k) * 33 + p] : Y2[(k - L1) * 33 + p] + Y2[(64 + k - L1) * 33 + p];
+                s.J[p * ma + k] = sc * (Y[k * 33 + p] + lo);
+            }
+        }
+        return;
+    }
     // J[p][k] = Scale_p jscale (Y[k][p] + Y[64 + k][p]); thread: k = tid % 64,
     // points tid / 64 + 8 i (C <= 64 on this path)
     {
@@ -1179,7 +1257,11 @@ __device__ void evaluate(const DevObject &ob, const FitConfig &cfg, const SlotLa
     constexpr bool kFP64 = FORM == PS_FORM_FP64;
     // tensor-core path: the point set-up of the next tile runs on warps 1..15
     // while thread 0 issues the current tile's MMAs
-    constexpr bool kPipe = !kFP64 && KU == 0;
+    constexpr bool kPipe = !kFP64 && (KU == 0 || KU == 3);
+    // alpha/beta on the tensor cores (KU 0), or on the SIMT pipes behind the
+    // wide tensor-core contraction (KU 3: 65..96 coefficients)
+    constexpr bool kTcAlpha = !kFP64 && KU == 0;
+    constexpr bool kWide = !kFP64 && KU == 3;
     constexpr int NT = threads_of<FORM>();
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int F = ob.nfac, C = ob.ncoef, ma = ob.ma, mf = ob.mfit, P = L.P;
@@ -1218,7 +1300,7 @@ __device__ void evaluate(const DevObject &ob, const FitConfig &cfg, const SlotLa
         if constexpr (!kFP64) {
             s.areaR[i] = static_cast<R>(ar);
             s.gvR[i] = static_cast<R>(g);
-            if constexpr (KU == 0) s.fac[i].w = static_cast<float>(ar);
+            if constexpr (kPipe) s.fac[i].w = static_cast<float>(ar);
         }
         asum += ar;
     }
@@ -1330,7 +1412,7 @@ __device__ void evaluate(const DevObject &ob, const FitConfig &cfg, const SlotLa
                     // prefetch for the contraction window: the next tile's
                     // times (warp 1) and geometry (warps 2 and 3, a copy
                     // each), this tile's accumulation data (warp 14)
-                    if (warp == 14) {
+                    if (kTcAlpha && warp == 14) {
                         if (!rel && lane < np) {
                             const int q = start + t0 + lane;
                             double *d = reinterpret_cast<double *>(s.pref + kPrefAcc) + 3 * lane;
@@ -1438,8 +1520,8 @@ __device__ void evaluate(const DevObject &ob, const FitConfig &cfg, const SlotLa
                     for (int i = 0; i < F; i++) acc = acc + Wp[i] * ds[static_cast<size_t>(i) * C];
                     s.J[p * ma + k] = conv ? acc : s.pt[p * kPointStride + 24] * acc;
                 }
-            } else if constexpr (KU == 0) {
-                contract_tc_issue<NT>(s, F, tcs);   // the work below overlaps the MMAs
+            } else if constexpr (kPipe) {
+                contract_tc_issue<NT, kWide>(s, F, tcs);   // the work below overlaps the MMAs
             } else {
                 if (s.dsph)
                     contract_mixed<NT, KU, true>(s, dsphF, np, F, C, ma, wcols, conv);
@@ -1498,7 +1580,7 @@ __device__ void evaluate(const DevObject &ob, const FitConfig &cfg, const SlotLa
                     y = warp_sum(y);
                     if (lane == 0) s.misc[M_AVE] += y;
                 }
-                if (!rel && warp == NT / 32 - 2) {
+                if (kTcAlpha && !rel && warp == NT / 32 - 2) {
                     double c2 = 0;
                     cp_async_wait_all();
                     if (lane < np) {
@@ -1540,7 +1622,7 @@ __device__ void evaluate(const DevObject &ob, const FitConfig &cfg, const SlotLa
                         if (have) setup_mixed_geo(g[0], g[1], s.bmat, ptn, warp - 2);
                     }
                 }
-                contract_tc_finish<NT>(s, np, F, C, ma, conv, tcs, jscale);
+                contract_tc_finish<NT, kWide>(s, np, F, C, ma, conv, tcs, jscale);
             }
             __syncthreads();
             if (next_setup) {
@@ -1586,7 +1668,7 @@ __device__ void evaluate(const DevObject &ob, const FitConfig &cfg, const SlotLa
                 continue;
             }
             // 5. accumulate (mrqcof.c:106-136)
-            if constexpr (kPipe) {
+            if constexpr (kTcAlpha) {
                 accumulate_tile_tc<NT>(ob, s, np, start + t0, conv, conv_sig, tcs, true);
                 if (++tiles_since_flush == kTcTilesPerFlush) {
                     tc_alpha_flush<NT>(ob, s, M, bv, tcs);
@@ -1615,7 +1697,7 @@ __device__ void evaluate(const DevObject &ob, const FitConfig &cfg, const SlotLa
             __syncthreads();
         }
         const double inv_ave = kFP64 ? 0.0 : s.misc[M_INVAVE];
-        if constexpr (kPipe) {
+        if constexpr (kTcAlpha) {
             // The per-point FP64 work of the whole lightcurve at once, one
             // tile per warp (the tiles' FP64 chains on different
             // sub-partitions): renormalisation factor coef and y/ave into
@@ -1656,7 +1738,7 @@ __device__ void evaluate(const DevObject &ob, const FitConfig &cfg, const SlotLa
             // values; the mixed form parks them as FP32); on the tensor-core
             // path they were prepared above, and the tile's residuals and
             // weights go where the accumulation reads them
-            if constexpr (kPipe) {
+            if constexpr (kTcAlpha) {
                 // operands built from the parked rows (renormalised on the way)
                 accumulate_tile_tc<NT>(ob, s, np, start + t0, false, conv_sig, tcs, true, src, RW);
                 if (++tiles_since_flush == kTcTilesPerFlush) {
@@ -1707,7 +1789,7 @@ __device__ void evaluate(const DevObject &ob, const FitConfig &cfg, const SlotLa
             }
         }
     }
-    if constexpr (kPipe) tc_alpha_flush<NT>(ob, s, M, bv, tcs);
+    if constexpr (kTcAlpha) tc_alpha_flush<NT>(ob, s, M, bv, tcs);
     else if constexpr (!kFP64) flush_partials<FORM>(M, bv, mf, accA, accB);
     __syncthreads();
     // mirror the lower triangle (mrqcof.c:139-141)
@@ -2087,7 +2169,7 @@ __device__ void run_fit(const DevObject &ob, const FitConfig &cfg, const SlotLay
                         typename RealOf<FORM>::T *scratch, int64_t n, int pole, ps_fit *out, const FitWork &w,
                         long long fidx, TcState &tcs)
 {
-    constexpr bool kTensor = FORM == PS_FORM_MIXED && KU == 0;
+    constexpr bool kTensor = FORM == PS_FORM_MIXED && (KU == 0 || KU == 3);
     constexpr int NT = threads_of<FORM>();
     const int tid = threadIdx.x;
     const int C = ob.ncoef, ma = ob.ma, mf = ob.mfit;
@@ -2338,11 +2420,13 @@ __global__ void __launch_bounds__(threads_of<FORM>(), 1)
     extern __shared__ __align__(16) char smem[];
     const SlotLayout L = make_layout(FORM, ob.ma, ob.mfit, ob.nfac, ob.ncoef, P, dsph_smem, w.rel_rows);
     Smem<FORM> s = carve<FORM>(smem, L);
-    constexpr bool kTensor = FORM == PS_FORM_MIXED && KU == 0;
+    constexpr bool kTensor = FORM == PS_FORM_MIXED && (KU == 0 || KU == 3);
     if (s.dsph)
         for (int e = threadIdx.x; e < ob.nfac * ob.ncoef; e += NT) s.dsph[e] = ob.dsph_f[e];
     TcState tcs;
-    if constexpr (kTensor) tc_setup<NT>(ob, s, tcs);
+    if constexpr (kTensor) tc_setup<NT, KU == 3>(ob, s, tcs);
+    // the wide tensor-core path keeps the slot's normal matrix in global memory
+    if (L.dsph_smem == kBasisTensorWide) s.alpha = w.alpha_g + static_cast<size_t>(blockIdx.x) * w.alpha_stride;
     R *scratch = L.rels ? reinterpret_cast<R *>(smem + L.rels)
                         : reinterpret_cast<R *>(w.scratch + static_cast<size_t>(blockIdx.x) * w.scratch_stride);
     __shared__ long long next;
@@ -2379,12 +2463,14 @@ __global__ void __launch_bounds__(threads_of<FORM>(), 1) eval_kernel(DevObject o
     extern __shared__ __align__(16) char smem[];
     const SlotLayout L = make_layout(FORM, ob.ma, ob.mfit, ob.nfac, ob.ncoef, P, dsph_smem, rel_rows);
     Smem<FORM> s = carve<FORM>(smem, L);
-    constexpr bool kTensor = FORM == PS_FORM_MIXED && KU == 0;
+    constexpr bool kTensor = FORM == PS_FORM_MIXED && (KU == 0 || KU == 3);
     if (s.dsph)
         for (int e = threadIdx.x; e < ob.nfac * ob.ncoef; e += NT) s.dsph[e] = ob.dsph_f[e];
     TcState tcs;
-    if constexpr (kTensor) tc_setup<NT>(ob, s, tcs);
+    if constexpr (kTensor) tc_setup<NT, KU == 3>(ob, s, tcs);
     for (int i = threadIdx.x; i < ob.ma; i += NT) s.cg[i] = cg[i];
+    // the wide tensor-core path accumulates straight into the output matrix
+    if (L.dsph_smem == kBasisTensorWide) s.alpha = alpha;
     __syncthreads();
     R *rows = L.rels ? reinterpret_cast<R *>(smem + L.rels) : reinterpret_cast<R *>(scratch);
     evaluate<FORM, KU>(ob, cfg, L, s, s.cg, s.alpha, s.beta, rows, tcs);
@@ -2397,7 +2483,8 @@ __global__ void __launch_bounds__(threads_of<FORM>(), 1) eval_kernel(DevObject o
         }
     }
     const int mf = ob.mfit;
-    for (int e = threadIdx.x; e < mf * mf; e += NT) alpha[e] = s.alpha[e];
+    if (L.dsph_smem != kBasisTensorWide)
+        for (int e = threadIdx.x; e < mf * mf; e += NT) alpha[e] = s.alpha[e];
     for (int j = threadIdx.x; j < mf; j += NT) beta[j] = s.beta[j];
     if (area)
         for (int i = threadIdx.x; i < ob.nfac; i += NT) area[i] = s.area[i];

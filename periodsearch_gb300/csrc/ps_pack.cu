@@ -16,7 +16,7 @@ __global__ void __launch_bounds__(threads_of<FORM>(), 1) pack_kernel(FitWork w, 
 {
     using R = typename RealOf<FORM>::T;
     constexpr int NT = threads_of<FORM>();
-    constexpr bool kTensor = FORM == PS_FORM_MIXED && KU == 0;
+    constexpr bool kTensor = FORM == PS_FORM_MIXED && (KU == 0 || KU == 3);
     extern __shared__ __align__(16) char smem[];
     __shared__ DevObject s_ob;
     __shared__ FitConfig s_cfg;
@@ -28,7 +28,8 @@ __global__ void __launch_bounds__(threads_of<FORM>(), 1) pack_kernel(FitWork w, 
     if (s.dsph)
         for (int e = threadIdx.x; e < s_ob.nfac * s_ob.ncoef; e += NT) s.dsph[e] = s_ob.dsph_f[e];
     TcState tcs;
-    if constexpr (kTensor) tc_setup<NT>(s_ob, s, tcs);
+    if constexpr (kTensor) tc_setup<NT, KU == 3>(s_ob, s, tcs);
+    if (dsph_smem == kBasisTensorWide) s.alpha = w.alpha_g + static_cast<size_t>(blockIdx.x) * w.alpha_stride;
     R *scratch = reinterpret_cast<R *>(w.scratch + static_cast<size_t>(blockIdx.x) * w.scratch_stride);
     for (;;) {
         if (threadIdx.x == 0) next = static_cast<long long>(atomicAdd(w.queue, 1ULL));
@@ -56,6 +57,8 @@ cudaError_t for_pack(int form, int ncoef, int dsph_smem, Fn fn)
     if (form == PS_FORM_FP64) return fn(std::integral_constant<int, PS_FORM_FP64>{}, std::integral_constant<int, 1>{});
     if (dsph_smem == kBasisTensor)
         return fn(std::integral_constant<int, PS_FORM_MIXED>{}, std::integral_constant<int, 0>{});
+    if (dsph_smem == kBasisTensorWide)
+        return fn(std::integral_constant<int, PS_FORM_MIXED>{}, std::integral_constant<int, 3>{});
     if (ncoef <= 64) return fn(std::integral_constant<int, PS_FORM_MIXED>{}, std::integral_constant<int, 1>{});
     return fn(std::integral_constant<int, PS_FORM_MIXED>{}, std::integral_constant<int, 2>{});
 }
@@ -68,11 +71,14 @@ int set_pack_smem(int form, size_t smem, int ncoef, int dsph_smem)
 {
     if (form != PS_FORM_FP64 && form != PS_FORM_MIXED) return static_cast<int>(cudaErrorInvalidValue);
     static std::mutex mu;
-    static int raised[64][2][3] = {};
+    static int raised[64][2][4] = {};
     int dev = 0;
     const cudaError_t de = cudaGetDevice(&dev);
     if (de != cudaSuccess) return static_cast<int>(de);
-    const int ku = form == PS_FORM_FP64 ? 1 : (dsph_smem == kBasisTensor ? 0 : (ncoef <= 64 ? 1 : 2));
+    const int ku = form == PS_FORM_FP64 ? 1
+                   : dsph_smem == kBasisTensor ? 0
+                   : dsph_smem == kBasisTensorWide ? 3
+                   : (ncoef <= 64 ? 1 : 2);
     std::lock_guard<std::mutex> lock(mu);
     int *cur = (dev >= 0 && dev < 64) ? &raised[dev][form][ku] : nullptr;
     if (cur && *cur >= static_cast<int>(smem)) return 0;

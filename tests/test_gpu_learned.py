@@ -135,36 +135,34 @@ def _engine_input(obj):
     return read_input(p)
 
 
-def test_trained_network_completes_fewer_fits(engine_lib):
-    """What the committed network gains: on fresh c1-shaped objects (a clear
-    minimum in the period landscape), the learned scan with the network at
-    its calibrated margin and the same cascade without it (the rms after the
-    screening iterations as the prediction, at the margin calibrated for it)
-    both find the full mixed scan's best period, and the network's scan
-    completes measurably fewer fits."""
-    from periodsearch_gb300 import Engine, PS_FORM_MIXED, learned, synth
+def test_trained_network_gain(engine_lib):
+    """What the committed network gains over the same cascade without it
+    (the rms after the screening iterations taken as the final rms), on 160
+    fresh objects of the survey population (Ndata 200-3000, 24-period
+    windows, half around the true period; recorded full trajectories, the
+    cascade's decisions replayed): its log error in the final rms is under
+    half the zero predictor's, and at the network's calibrated margin its
+    scan misses the full scan's best period less than half as often."""
+    from periodsearch_gb300 import learned
 
     P, meta = learned.load_default()
     if P is None or "margin_without_network" not in meta:
         pytest.skip("no trained predictor committed")
-    opts = learned.cascade_defaults()
-    done_net = done_zero = 0
-    for seed in (951, 952):
-        o = synth.make_object("c1", seed=seed)
-        with Engine(_engine_input(o), form=PS_FORM_MIXED) as eng:
-            conw_r = eng.info.conw_r0
-            nt = int(round((eng.info.freq_start - 1 / o.truth["period_h"]) / eng.info.freq_step)) + 1
-            lo, hi = nt - 100, nt + 99
-            full = eng.scan(conw_r, lo, hi)
-            b_full = lo + int(np.argmin(full["rms"]))
-            _, s_net = eng.scan_learned(conw_r, lo, hi, P, **{**opts, "fill_refit_waves": 0})
-            _, s_zero = eng.scan_learned(conw_r, lo, hi, learned.zero_predictor(),
-                                         **{**opts, "margin": meta["margin_without_network"], "fill_refit_waves": 0})
-        assert int(s_net["best_index"]) == b_full
-        assert int(s_zero["best_index"]) == b_full
-        done_net += s_net["fits_completed"]
-        done_zero += s_zero["fits_completed"]
-    assert done_net < 0.8 * done_zero, (done_net, done_zero)
+    objs = learned._population("c5", 160, 70000, processes=8)
+    wins, _ = learned.collect_windows(objs, 24, meta["screen_iters"], around_truth=lambda k: k % 2 == 0, seed=5)
+    x, y = [], []
+    for w in wins:
+        a, b, _, _ = learned.samples(w["traj"])
+        x.append(a)
+        y.append(b)
+    x, y = np.concatenate(x), np.concatenate(y)
+    err_net = np.sqrt(np.mean((learned.predict(P, x) - y) ** 2))
+    err_zero = np.sqrt(np.mean(y ** 2))
+    assert err_net < 0.5 * err_zero, (err_net, err_zero)
+    m = learned.cascade_defaults()["margin"]
+    net = learned.replay_windows(wins, P, m, 15)
+    zero = learned.replay_windows(wins, learned.zero_predictor(), m, 15)
+    assert net["misses"] < 0.5 * max(zero["misses"], 1), (net, zero)
 
 
 def test_learned_scan_keeps_best_period(engine_lib, tmp_path):
