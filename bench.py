@@ -96,6 +96,10 @@ def _args():
     ap.add_argument("--multi-object", type=int, default=0,
                     help="also time K objects of the c3 population (Ndata logU[100, 5000]) packed into one launch "
                          "against one launch per object (512: the many-asteroid configuration)")
+    ap.add_argument("--c2", type=int, default=0,
+                    help="also time the mixed-precision configuration (c1 data with L = M = 8, 81 coefficients, "
+                         "512 facets): a mixed scan of this many periods on the tensor cores, the same on the SIMT "
+                         "pipes and the FP64 form on a tenth of them")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--full-scan", action="store_true",
                     help="also run the whole scan of the workload as one refined scan (rank 0) and report its "
@@ -385,6 +389,60 @@ def multi_object(K: int, form: int, local: int, units_per_object: int = 4) -> di
             e.close()
 
 
+def c2_measurement(periods: int, local: int, peaks: dict) -> dict:
+    """The mixed-precision configuration c2 (c1's data, Laplace series L = M =
+    8 on the 512-facet grid): fits/s of the mixed form with its shape
+    contraction on the tensor cores (the wide path), of the same form with
+    the SIMT contraction, and of the FP64 form, with the tensor form's
+    algorithmic FLOP rate against the measured BF16 peak and its rms error
+    against the FP64 form per period."""
+    import numpy as np
+
+    from periodsearch_gb300 import Engine, PS_FORM_FP64, PS_FORM_MIXED, read_input, synth
+
+    with tempfile.TemporaryDirectory() as td:
+        path = Path(td) / "period_search_in"
+        obj = synth.write_object(path, "c2")
+        data = read_input(path)
+    out = {"workload": "c2: c1 data (Ndata 980), L=M=8 (81 coefficients), 512 facets, 50 LM iterations"}
+    with Engine(data, device=local, form=PS_FORM_MIXED) as eng:
+        info = eng.info
+        n_max = int(info.n_max)
+        lo, hi = window_of(n_max, info.freq_start, info.freq_step, obj.truth["period_h"], periods)
+        conw_r = info.conw_r0
+        eng.scan(conw_r, lo, lo + 9)      # warm-up
+        rows_tc = eng.scan(conw_r, lo, hi)
+        t = eng.timing()
+        fe = flops_per_eval(info.ndata, info.nfac, info.ncoef, info.mfit)
+        flop = t["evals"] * fe + (t["evals"] - t["fits"]) * 2.0 * info.mfit ** 3
+        ach = flop / (t["kernel_ms"] / 1e3) / 1e12
+        bf16 = peaks.get("bf16_tflops")
+        shape = t["evals"] * 2.0 * info.ndata * info.nfac * info.ncoef / (t["kernel_ms"] / 1e3) / 1e12
+        out.update({"tensor_cores": bool(info.tensor_cores), "ncoef": info.ncoef, "nfac": info.nfac,
+                    "mfit": info.mfit, "window": [lo, hi], "fits": t["fits"],
+                    "mixed_tensor_fits_per_s": t["fits"] / (t["kernel_ms"] / 1e3),
+                    "roofline": {"bound": "tensor", "achieved": ach, "peak": bf16, "unit": "TFLOP/s",
+                                 "frac": ach / bf16 if bf16 else None,
+                                 "shape_contraction_tflops": shape,
+                                 "shape_contraction_frac": shape / bf16 if bf16 else None,
+                                 "peak_source": "measured dense BF16 burst of MEASURED_PEAKS.json"}})
+    with Engine(data, device=local, form=PS_FORM_MIXED, tensor_cores=False) as eng:
+        eng.scan(conw_r, lo, hi)
+        t = eng.timing()
+        out["mixed_simt_fits_per_s"] = t["fits"] / (t["kernel_ms"] / 1e3)
+    n64 = max(1, periods // 10)
+    with Engine(data, device=local, form=PS_FORM_FP64) as e64:
+        rows64 = e64.scan(conw_r, lo, lo + n64 - 1)
+        t = e64.timing()
+        out["fp64_fits_per_s"] = t["fits"] / (t["kernel_ms"] / 1e3)
+    rel = (rows_tc["rms"][:n64] - rows64["rms"]) / rows64["rms"]
+    out.update({"tensor_over_simt": out["mixed_tensor_fits_per_s"] / out["mixed_simt_fits_per_s"],
+                "tensor_over_fp64": out["mixed_tensor_fits_per_s"] / out["fp64_fits_per_s"],
+                "rms_rel_vs_fp64_median": float(np.median(np.abs(rel))), "rms_rel_vs_fp64_max": float(np.abs(rel).max()),
+                "fp64_periods": n64})
+    return out
+
+
 def _measured_peaks() -> dict:
     p = ROOT / "MEASURED_PEAKS.json"
     return json.loads(p.read_text()) if p.exists() else {}
@@ -637,6 +695,7 @@ def run_engine_arm(args):
         cascade["device_ms_per_step"] = 1000 * dev_all / args.steps
         cascade["wall_ms_per_step"] = 1000 * statistics.mean(t["wall_s"] for _, t in steps)
         mo = multi_object(args.multi_object, PS_FORM_MIXED, local) if args.multi_object > 0 else None
+        c2 = c2_measurement(args.c2, local, peaks) if args.c2 > 0 else None
         full = None
         if args.full_scan:
             torch.cuda.synchronize()
@@ -666,7 +725,7 @@ def run_engine_arm(args):
                 "e2e": {"value": fits_all / e2e_all, "unit": "fits/s", "h2d_bytes_per_step": h2d,
                         "d2h_bytes_per_step": d2h},
                 "gpu_launches": launches, "roofline": roof, "kernels": kernels, "cascade": cascade,
-                "plain_fp64": fp64, "validation": valid, "multi_object": mo, "full_scan": full,
+                "plain_fp64": fp64, "validation": valid, "multi_object": mo, "c2": c2, "full_scan": full,
                 "cpu_baseline": cb, "clocks": sampler.summary() if sampler else None, "wall_s": wall}
         print(json.dumps(line))
     eng.close()

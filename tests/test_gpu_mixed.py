@@ -195,8 +195,8 @@ def test_cross_build_agreement_report(mixed, engine_lib):
 @pytest.fixture(scope="module")
 def c2_object(tmp_path_factory):
     """A c2-shaped object: Laplace series L = M = 8 (81 coefficients) on the
-    512-facet grid, 200 sparse points -- beyond the tensor-core path, so the
-    mixed form runs its two-coefficients-per-lane SIMT contraction."""
+    512-facet grid, 200 sparse points -- the wide tensor-core path (the split
+    basis in two Tensor Memory regions, alpha/beta on the SIMT pipes)."""
     from periodsearch_gb300 import read_input, synth
 
     cfg = synth.SynthConfig(name="c2s", lmax_truth=8, lmax=8, nrows=8, n_periods=40)
@@ -211,9 +211,10 @@ def test_c2_eval_both_forms_match_oracle(engine_lib, oracle, c2_object):
     ora = oracle.OracleProblem(c2_object)
     conw_r = ora.info()["conw_r"]
     data = read_input(c2_object)
-    for form in (PS_FORM_FP64, PS_FORM_MIXED):
-        with Engine(data, form=form) as eng:
-            assert eng.info.ncoef == 81 and eng.info.nfac == 512 and not eng.info.tensor_cores
+    for form, tensor in ((PS_FORM_FP64, False), (PS_FORM_MIXED, True), (PS_FORM_MIXED, False)):
+        with Engine(data, form=form, tensor_cores=tensor) as eng:
+            assert eng.info.ncoef == 81 and eng.info.nfac == 512
+            assert eng.info.tensor_cores == (1 if form == PS_FORM_MIXED and tensor else 0)
             for n, pole in [(1, 2), (5, 8)]:
                 cg = ora.initial_cg(n, pole)
                 a_g, b_g, x_g, _ = eng.eval(conw_r, cg)
@@ -266,6 +267,38 @@ def test_tensor_path_other_facet_grids(engine_lib, oracle, tmp_path, nrows):
         got = eng.scan(conw_r, 1, 12)
     with Engine(data, form=PS_FORM_FP64) as e64:
         ref = e64.scan(conw_r, 1, 12)
+    signed = (got["rms"] - ref["rms"]) / ref["rms"]
+    assert signed.max() <= MAX_REL and signed.min() >= -MAX_REL_BELOW
+    assert np.median(np.abs(signed)) <= MEDIAN_REL
+
+
+@pytest.mark.parametrize("nrows,n_dense", [(8, 2), (6, 1), (7, 0)])
+def test_wide_tensor_path_against_oracle(engine_lib, oracle, tmp_path, nrows, n_dense):
+    """The wide tensor-core path (L = 8: 81 coefficients; 288, 392 and 512
+    facets), with and without relative lightcurves: evaluations against the
+    oracle within the mixed form's tolerances, a short scan against the FP64
+    form within the mixed scan bounds."""
+    from periodsearch_gb300 import Engine, PS_FORM_FP64, PS_FORM_MIXED, read_input, synth
+
+    path = tmp_path / "period_search_in"
+    cfg = synth.SynthConfig(name=f"wide{nrows}", lmax_truth=8, lmax=8, nrows=nrows, n_sparse=120, n_dense=n_dense,
+                            dense_points=40, n_periods=40)
+    synth.write_object(path, cfg, seed=80 + nrows)
+    data = read_input(path)
+    ora = oracle.OracleProblem(path)
+    conw_r = ora.info()["conw_r"]
+    with Engine(data, form=PS_FORM_MIXED) as eng:
+        assert eng.info.ncoef == 81 and eng.info.nfac == 8 * nrows * nrows and eng.info.tensor_cores == 1
+        for n, pole in [(1, 3), (7, 10)]:
+            cg = ora.initial_cg(n, pole)
+            a_g, b_g, x_g, _ = eng.eval(conw_r, cg)
+            a_o, b_o, x_o, _ = ora.eval(cg)
+            assert abs(x_g - x_o) <= 1e-5 * abs(x_o)
+            assert np.abs(a_g - a_o).max() <= 1e-4 * np.abs(a_o).max()
+            assert np.abs(b_g - b_o).max() <= 1e-3 * np.abs(b_o).max()
+        got = eng.scan(conw_r, 1, 10)
+    with Engine(data, form=PS_FORM_FP64) as e64:
+        ref = e64.scan(conw_r, 1, 10)
     signed = (got["rms"] - ref["rms"]) / ref["rms"]
     assert signed.max() <= MAX_REL and signed.min() >= -MAX_REL_BELOW
     assert np.median(np.abs(signed)) <= MEDIAN_REL
