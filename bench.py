@@ -93,10 +93,10 @@ def _args():
     ap.add_argument("--form", default="learned", choices=["learned", "refined", "mixed", "fp64"])
     ap.add_argument("--window", type=int, default=2000, help="trial periods per step (x 10 poles)")
     ap.add_argument("--no-fp64-compare", action="store_true", help="skip the FP64 scan of the window")
-    ap.add_argument("--multi-object", type=int, default=0,
+    ap.add_argument("--multi-object", type=int, default=512,
                     help="also time K objects of the c3 population (Ndata logU[100, 5000]) packed into one launch "
                          "against one launch per object (512: the many-asteroid configuration)")
-    ap.add_argument("--c2", type=int, default=0,
+    ap.add_argument("--c2", type=int, default=300,
                     help="also time the mixed-precision configuration (c1 data with L = M = 8, 81 coefficients, "
                          "512 facets): a mixed scan of this many periods on the tensor cores, the same on the SIMT "
                          "pipes and the FP64 form on a tenth of them")
@@ -683,9 +683,11 @@ def run_engine_arm(args):
         else:
             ach = fp64_flop / (fp64_ms / 1e3) / 1e12
             tr = _profile_traffic(False)
+            st_last = steps[-1][1]["stats"]
+            per_launch = st_last["fits_refit"] / max(st_last["refit_rounds"], 1)
             roof = {"bound": "fp64", "kernel": "fit_kernel<fp64>", "achieved": ach, "peak": p64.value,
                     "unit": "TFLOP/s", "frac": ach / p64.value,
-                    "traffic": None,
+                    "traffic": tr * per_launch if tr else None,
                     "peak_source": "FP64 FMA ceiling measured live by ps_device_fma_peaks "
                                    "(MEASURED_PEAKS.json has no FP64 figure)",
                     "algorithmic_flop_per_launch": fp64_flop / max(fp64_l, 1)}
