@@ -162,6 +162,8 @@ typedef struct ps_timing {
     int64_t fits;          /* fits computed */
     int64_t evals;         /* model evaluations (mrqcof calls) */
     int32_t launches;      /* kernel launches */
+    int32_t cluster_size;  /* CTAs per fit of the last launch: 1, or 2..4 when FP64 fits were each spread over a
+                              thread-block cluster (fewer fits than fit slots; bit-identical results) */
 } ps_timing;
 
 typedef struct ps_ctx ps_ctx;

@@ -231,6 +231,18 @@ ps_status make_plan(ps_ctx *c, int form)
     return PS_ERR_LIMIT;
 }
 
+// CTAs per fit for a launch: FP64 fits without trajectories, saved states
+// or an iteration limit, fewer than the fit slots, are each spread over a
+// thread-block cluster of 2 or 4 CTAs (the most that the slots hold).
+int split_size(const ps_ctx *c, const psg::FitWork &w, int form)
+{
+    if (form != PS_FORM_FP64 || w.traj || w.state || w.iter_limit > 0 || w.nfits < 1) return 1;
+    const int64_t slots = c->plan[form].slots;
+    if (w.nfits * 4 <= slots) return 4;
+    if (w.nfits * 2 <= slots) return 2;
+    return 1;
+}
+
 // Launches the fits described by w in the given form (queue and outputs
 // filled in here) and copies the results back into c->h_fits.
 ps_status run_fits(ps_ctx *c, double conw_r, psg::FitWork w, int form)
@@ -267,9 +279,21 @@ ps_status run_fits(ps_ctx *c, double conw_r, psg::FitWork w, int form)
         w.alpha_stride = stride;
     }
     int grid = static_cast<int>(std::min<int64_t>(pl.slots, std::max<int64_t>(w.nfits, 1)));
+    // FP64 fits fewer than the slots: each fit spread over a cluster of
+    // CTAs (bit-identical results, a shorter launch)
+    const int cs = split_size(c, w, form);
     PSG_CUDA(c, cudaMemsetAsync(c->d_queue, 0, sizeof(unsigned long long), c->stream));
     PSG_CUDA(c, cudaEventRecord(c->ev[0], c->stream));
-    int e = psg::launch_fits(form, c->dob, cfg, w, grid, pl.P, pl.smem, pl.dsph_smem, c->stream);
+    int e;
+    if (cs > 1) {
+        int clusters = 0;
+        e = psg::split_max_clusters(cs, pl.smem, &clusters);
+        if (e != 0) return cuda_fail(c, static_cast<cudaError_t>(e), "cluster occupancy");
+        clusters = static_cast<int>(std::min<int64_t>(std::max(clusters, 1), w.nfits));
+        e = psg::launch_fits_split(c->dob, cfg, w, clusters, cs, pl.P, pl.smem, c->stream);
+    } else {
+        e = psg::launch_fits(form, c->dob, cfg, w, grid, pl.P, pl.smem, pl.dsph_smem, c->stream);
+    }
     if (e != 0) return cuda_fail(c, static_cast<cudaError_t>(e), "fit kernel launch");
     PSG_CUDA(c, cudaEventRecord(c->ev[1], c->stream));
     c->h_fits.resize(static_cast<size_t>(w.nfits));
@@ -287,6 +311,7 @@ ps_status run_fits(ps_ctx *c, double conw_r, psg::FitWork w, int form)
     for (const ps_fit &f : c->h_fits) evals += f.niter + 1;
     c->timing.evals = evals;
     c->timing.launches = 1;
+    c->timing.cluster_size = cs;
     c->launch_total++;
     for (const ps_fit &f : c->h_fits)
         if (f.err_code == 16) {
@@ -420,9 +445,12 @@ ps_status refit_minimum(ps_ctx *c, double conw_r, ScanFits &sf, double rel, int3
             picked[static_cast<size_t>(n)] = 1;
         }
         if (per.empty()) return PS_OK;
-        // top up the last wave with the lowest remaining rows
+        // top up the last wave with the lowest remaining rows; a set that
+        // leaves half (a quarter) of the slots free runs its fits over 2 (4)
+        // CTAs each, so its wave holds slots / 2 (slots / 4) fits
         const int64_t need = static_cast<int64_t>(per.size()) * PS_N_POLES;
-        const int64_t cap = (need + slots - 1) / slots * slots;
+        const int64_t wave = need * 4 <= slots ? slots / 4 : need * 2 <= slots ? slots / 2 : slots;
+        const int64_t cap = (need + wave - 1) / wave * wave;
         if (fill && need + PS_N_POLES <= cap) {
             order.clear();
             for (int64_t n = 0; n < sf.nper; n++)

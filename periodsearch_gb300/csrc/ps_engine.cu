@@ -177,6 +177,8 @@ int set_kernel_smem(int form, size_t smem, int ncoef, int dsph_smem)
         e = cudaFuncSetAttribute(fit_kernel<PS_FORM_FP64, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
         if (e == cudaSuccess)
             e = cudaFuncSetAttribute(eval_kernel<PS_FORM_FP64, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+        if (e == cudaSuccess)
+            e = cudaFuncSetAttribute(fit_kernel_split, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
     } else if (form == PS_FORM_MIXED) {
         e = for_mixed(ncoef, dsph_smem, [&](auto ku) {
             constexpr int KU = decltype(ku)::value;
@@ -224,6 +226,41 @@ int launch_fits(int form, const DevObject &ob, const FitConfig &cfg, const FitWo
         return static_cast<int>(cudaErrorInvalidValue);
     }
     return static_cast<int>(cudaGetLastError());
+}
+
+namespace {
+cudaLaunchConfig_t split_config(int clusters, int cs, size_t smem, cudaStream_t st, cudaLaunchAttribute *attr)
+{
+    cudaLaunchConfig_t lc = {};
+    lc.gridDim = dim3(static_cast<unsigned>(clusters * cs));
+    lc.blockDim = dim3(static_cast<unsigned>(threads_of<PS_FORM_FP64>()));
+    lc.dynamicSmemBytes = smem;
+    lc.stream = st;
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = static_cast<unsigned>(cs);
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    lc.attrs = attr;
+    lc.numAttrs = 1;
+    return lc;
+}
+}  // namespace
+
+// Clusters of cs CTAs of the split FP64 kernel that the device runs at once
+// (its shared memory attribute must have been raised by set_kernel_smem).
+int split_max_clusters(int cs, size_t smem, int *clusters)
+{
+    cudaLaunchAttribute attr[1];
+    cudaLaunchConfig_t lc = split_config(1, cs, smem, nullptr, attr);
+    return static_cast<int>(cudaOccupancyMaxActiveClusters(clusters, fit_kernel_split, &lc));
+}
+
+int launch_fits_split(const DevObject &ob, const FitConfig &cfg, const FitWork &w, int clusters, int cs, int P,
+                      size_t smem, void *stream)
+{
+    cudaLaunchAttribute attr[1];
+    cudaLaunchConfig_t lc = split_config(clusters, cs, smem, static_cast<cudaStream_t>(stream), attr);
+    return static_cast<int>(cudaLaunchKernelEx(&lc, fit_kernel_split, ob, cfg, w, P));
 }
 
 int launch_eval(int form, const DevObject &ob, const FitConfig &cfg, const double *cg, double *alpha, double *beta,

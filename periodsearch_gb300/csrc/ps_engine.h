@@ -244,6 +244,12 @@ PSG_HD inline SlotLayout make_layout(int form, int ma, int mfit, int nfac, int n
 // Launchers (ps_engine.cu).  All enqueue on `stream`; return cudaError_t as int.
 int launch_fits(int form, const DevObject &ob, const FitConfig &cfg, const FitWork &w, int grid,
                 int P, size_t smem, int dsph_smem, void *stream);
+// FP64 fits each spread over a thread-block cluster of cs CTAs (2..8),
+// bit-identical to launch_fits' FP64 kernel; w without trajectories, saved
+// states or an iteration limit.
+int launch_fits_split(const DevObject &ob, const FitConfig &cfg, const FitWork &w, int clusters, int cs, int P,
+                      size_t smem, void *stream);
+int split_max_clusters(int cs, size_t smem, int *clusters);
 int launch_eval(int form, const DevObject &ob, const FitConfig &cfg, const double *cg, double *alpha,
                 double *beta, double *chisq, double *area, double *scratch, int P, size_t smem,
                 int dsph_smem, int rel_rows, void *stream);

@@ -36,6 +36,7 @@
 // on the SIMT pipes.
 #pragma once
 
+#include <cooperative_groups.h>
 #include <cuda_runtime.h>
 
 #include <cmath>
@@ -1800,6 +1801,312 @@ __device__ void evaluate(const DevObject &ob, const FitConfig &cfg, const SlotLa
     __syncthreads();
 }
 
+// ---------------------------------------------------------------------------
+// FP64 evaluation split over a thread-block cluster (kMaxSplit CTAs at most).
+//
+// One fit's point tiles are dealt round-robin to the cluster's CTAs, which
+// compute their tiles' model rows (point set-up, facet stage, shape
+// contraction, the remaining columns) at the same time; after each round
+// the leader (rank 0) takes the round's tiles in data order -- its own from
+// its shared memory, the others' through distributed shared memory -- and
+// runs everything that sums over points: the relative lightcurves' sums and
+// parked rows, their second pass, the alpha/beta/chi^2 accumulation and the
+// convexity rows.  Every sum therefore runs in the same order as in the
+// single-CTA FP64 form, and the split fit is bit-identical to it.  The
+// leader then copies the normal matrix, beta and the scalars into every
+// CTA, so that all of them take the same LM decisions and keep the same
+// control flow (and the same sequence of cluster barriers).
+// ---------------------------------------------------------------------------
+constexpr int kMaxSplit = 8;
+
+__device__ void evaluate_split(const DevObject &ob, const FitConfig &cfg, const SlotLayout &L, Smem<PS_FORM_FP64> &s,
+                               const double *a, double *M, double *bv, double *scratch)
+{
+    namespace cgr = cooperative_groups;
+    constexpr int NT = threads_of<PS_FORM_FP64>();
+    cgr::cluster_group cl = cgr::this_cluster();
+    const int rank = static_cast<int>(cl.block_rank()), cs = static_cast<int>(cl.num_blocks());
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int F = ob.nfac, C = ob.ncoef, ma = ob.ma, mf = ob.mfit, P = L.P;
+    const int wcols = L.wcols;
+    const int RW = rel_row_stride(ma);
+
+    // curv.c:10-39 and blmatrix.c:9-46 on every CTA (as in evaluate)
+    double asum = 0;
+    for (int i = tid; i < F; i += NT) {
+        double g = 0;
+        for (int q = 0; q < ob.npairs; q++) {
+            int m = ob.pair_m[q], n = ob.pair_n[q];
+            double fsum = a[n] * ob.fc[m * F + i];
+            if (m != 0) fsum = fsum + a[n + 1] * ob.fs[m * F + i];
+            g = g + ob.pleg[q * F + i] * fsum;
+        }
+        g = exp(g);
+        double ar = ob.darea[i] * g;
+        s.area[i] = ar;
+        s.gv[i] = g;
+        asum += ar;
+    }
+    double tot = block_sum<NT>(asum, s.misc + M_RED);
+    if (tid == 0) {
+        s.misc[M_AREA] = tot;
+        s.misc[M_CHISQ] = 0;
+        s.misc[M_CL] = exp(a[ma - 2]);
+        s.misc[M_TRIG] = cos(a[C]);
+        s.misc[M_TRIG + 1] = sin(a[C]);
+        s.misc[M_TRIG + 2] = cos(a[C + 1]);
+        s.misc[M_TRIG + 3] = sin(a[C + 1]);
+    }
+    for (int e = tid; e < mf * mf; e += NT) M[e] = 0;
+    for (int j = tid; j < mf; j += NT) bv[j] = 0;
+    __syncthreads();
+    if (warp == 0) {
+        double v;
+        if (lane < 27) {
+            const int code = c_bl_code[lane];
+            const int fa = code & 3, fb = (code >> 2) & 3;
+            const double va = fa == 1 ? s.misc[M_TRIG] : fa == 2 ? s.misc[M_TRIG + 1] : fa == 3 ? 1.0 : 0.0;
+            const double vb = fb == 1 ? s.misc[M_TRIG + 2] : fb == 2 ? s.misc[M_TRIG + 3] : 1.0;
+            const double p = va * vb;
+            v = (code & 16) ? -p : p;
+        } else {
+            v = lane == 31 ? s.misc[M_CL] : a[lane == 30 ? C + 7 : C + 3 + (lane - 27)];
+        }
+        s.bmat[lane] = v;
+    }
+    const double omg = a[C + 2];
+    __syncthreads();
+    const double cls = s.bmat[30], cl_w = s.bmat[31];
+    const double conv_sig = cfg.conv_sig;
+    float accA[kAccPerThread];
+    float accB = 0.f;
+
+    // model rows of one tile into s.J / s.ym (bright.c:14-126, as in evaluate)
+    auto compute_tile = [&](int lc, int t0, int np, bool conv) {
+        const int start = ob.lc_start[lc];
+        if (!conv) {
+            const int ppw = (P + 3) / 4;
+            const int sp = (lane < ppw && warp < 4) ? warp * ppw + lane : -1;
+            if (sp >= 0 && sp < np)
+                setup_point<PS_FORM_FP64>(ob, cfg, start + t0 + sp, omg, s.bmat, s.pt + sp * kPointStride);
+            __syncthreads();
+            for (int p = warp; p < np; p += NT / 32) {
+                const double *pt = s.pt + p * kPointStride;
+                const double e1 = pt[0], e2 = pt[1], e3 = pt[2];
+                const double f1 = pt[3], f2 = pt[4], f3 = pt[5];
+                double de[9], de0[9];
+#pragma unroll
+                for (int k = 0; k < 9; k++) {
+                    de[k] = pt[6 + k];
+                    de0[k] = pt[15 + k];
+                }
+                double br = 0, r0 = 0, r1 = 0, r2 = 0, dcl = 0, dcls = 0;
+                double *Wp = s.W + static_cast<size_t>(p) * wcols;
+                for (int i = lane; i < F; i += 32) {
+                    const double nx = ob.nx[i], ny = ob.ny[i], nz = ob.nz[i];
+                    const double mu = e1 * nx + e2 * ny + e3 * nz;
+                    const double mu0 = f1 * nx + f2 * ny + f3 * nz;
+                    double w = 0;
+                    if (mu > kTinyMu && mu0 > kTinyMu) {
+                        const double ar = s.area[i];
+                        const LitTerms<double, PS_FORM_FP64> lt(mu, mu0, cl_w, cls);
+                        br = br + ar * lt.sv;
+                        w = ob.darea[i] * lt.sv * s.gv[i];
+                        const double s0 = nx * de[0] + ny * de[3] + nz * de[6];
+                        const double s1 = nx * de[1] + ny * de[4] + nz * de[7];
+                        const double s2 = nx * de[2] + ny * de[5] + nz * de[8];
+                        const double t0v = nx * de0[0] + ny * de0[3] + nz * de0[6];
+                        const double t1v = nx * de0[1] + ny * de0[4] + nz * de0[7];
+                        const double t2v = nx * de0[2] + ny * de0[5] + nz * de0[8];
+                        r0 = r0 + ar * (lt.dsmu * s0 + lt.dsmu0 * t0v);
+                        r1 = r1 + ar * (lt.dsmu * s1 + lt.dsmu0 * t1v);
+                        r2 = r2 + ar * (lt.dsmu * s2 + lt.dsmu0 * t2v);
+                        dcl = dcl + mu * mu0 * ar;
+                        dcls = dcls + ar * lt.dcls_w;
+                    }
+                    Wp[i] = w;
+                }
+                br = warp_sum(br);
+                r0 = warp_sum(r0);
+                r1 = warp_sum(r1);
+                r2 = warp_sum(r2);
+                dcl = warp_sum(dcl);
+                dcls = warp_sum(dcls);
+                if (lane == 0) {
+                    double *rd = s.red + p * kRedStride;
+                    rd[0] = br;
+                    rd[1] = r0;
+                    rd[2] = r1;
+                    rd[3] = r2;
+                    rd[4] = dcl;
+                    rd[5] = dcls;
+                }
+            }
+        } else {
+            for (int p = warp; p < np; p += NT / 32) {
+                const double *nc = (p == 0) ? ob.nx : (p == 1) ? ob.ny : ob.nz;
+                double res = 0;
+                double *Wp = s.W + static_cast<size_t>(p) * wcols;
+                for (int i = lane; i < F; i += 32) {
+                    res = res + s.area[i] * nc[i];
+                    Wp[i] = ob.darea[i] * s.gv[i] * nc[i];
+                }
+                res = warp_sum(res);
+                if (lane == 0) s.red[p * kRedStride] = res;
+            }
+        }
+        __syncthreads();
+        for (int o = tid; o < np * C; o += NT) {
+            const int p = o / C, k = o - p * C;
+            const double *Wp = s.W + static_cast<size_t>(p) * wcols;
+            const double *ds = ob.dsph + k;
+            double acc = 0;
+            for (int i = 0; i < F; i++) acc = acc + Wp[i] * ds[static_cast<size_t>(i) * C];
+            s.J[p * ma + k] = conv ? acc : s.pt[p * kPointStride + 24] * acc;
+        }
+        if (tid < np) {
+            const int p = tid;
+            double *Jp = s.J + p * ma;
+            const double *rd = s.red + p * kRedStride;
+            if (!conv) {
+                const double *pt = s.pt + p * kPointStride;
+                const double scale = pt[24];
+                const double br = rd[0];
+                Jp[C] = scale * rd[1];
+                Jp[C + 1] = scale * rd[2];
+                Jp[C + 2] = scale * rd[3];
+                Jp[C + 3] = br * pt[25];
+                Jp[C + 4] = br * pt[26];
+                Jp[C + 5] = br * pt[27];
+                Jp[C + 6] = scale * rd[4] * cl_w;
+                Jp[C + 7] = scale * rd[5];
+                s.ym[p] = br * scale;
+            } else {
+                for (int k = C; k < ma; k++) Jp[k] = 0;
+                s.ym[p] = rd[0];
+                s.misc[M_CHK + p] = rd[0];
+            }
+        }
+        __syncthreads();
+    };
+
+    // the leader's part of a tile (mrqcof.c:51-136): sums over points in data order
+    auto consume_tile = [&](int lc, int t0, int np) {
+        const int start = ob.lc_start[lc], npts = ob.lc_npts[lc];
+        if (!ob.lc_rel[lc]) {
+            accumulate_tile<PS_FORM_FP64>(ob, s, M, bv, np, start + t0, false, conv_sig, accA, accB);
+            return;
+        }
+        if (t0 == 0) {
+            for (int l = tid; l < ma; l += NT) s.dave[l] = 0;
+            if (tid == 0) s.misc[M_AVE] = 0;
+            __syncthreads();
+        }
+        double *dst = scratch + static_cast<size_t>(t0) * RW;
+        for (int e = tid; e < np * ma; e += NT) {
+            int p = e / ma, l = e - p * ma;
+            dst[static_cast<size_t>(p) * RW + l] = s.J[e];
+        }
+        if (tid < np) dst[static_cast<size_t>(tid) * RW + ma] = s.ym[tid];
+        for (int l = tid; l < ma; l += NT) {
+            double d = s.dave[l];
+            for (int p = 0; p < np; p++) d = d + s.J[p * ma + l];
+            s.dave[l] = d;
+        }
+        if (tid == 0) {
+            double av = s.misc[M_AVE];
+            for (int p = 0; p < np; p++) av = av + s.ym[p];
+            s.misc[M_AVE] = av;
+        }
+        __syncthreads();
+        if (t0 + P < npts) return;
+        // second pass of the lightcurve (mrqcof.c:90-136)
+        const double ave = s.misc[M_AVE];
+        for (int u0 = 0; u0 < npts; u0 += P) {
+            const int nq = min(P, npts - u0);
+            const double *src = scratch + static_cast<size_t>(u0) * RW;
+            if (tid < nq) {
+                const int q = start + u0 + tid;
+                const double yt = src[static_cast<size_t>(tid) * RW + ma];
+                const double coef = ob.sig[q] * npts / ave;
+                s.ym[tid] = coef * yt;
+            }
+            __syncthreads();
+            for (int e = tid; e < nq * ma; e += NT) {
+                const int p = e / ma, l = e - p * ma;
+                const double v = src[static_cast<size_t>(p) * RW + l];
+                const int q = start + u0 + p;
+                const double coef = ob.sig[q] * npts / ave;
+                const double yt = src[static_cast<size_t>(p) * RW + ma];
+                const double out = coef * (v - yt * s.dave[l] / ave);
+                s.J[e] = (l == 0) ? 0.0 : out;
+            }
+            __syncthreads();
+            accumulate_tile<PS_FORM_FP64>(ob, s, M, bv, nq, start + u0, false, conv_sig, accA, accB);
+        }
+    };
+
+    // rounds of cs tiles over the real lightcurves, in data order
+    int rlc[kMaxSplit], rt0[kMaxSplit], rnp[kMaxSplit];
+    int nround = 0;
+    auto flush_round = [&]() {
+        cl.sync();   // every CTA's tile of the round is in its shared memory
+        if (rank == 0) {
+            for (int k = 0; k < nround; k++) {
+                if (k > 0) {
+                    // the rows of rank k's tile, read through distributed shared memory
+                    const double *rJ = cl.map_shared_rank(s.J, k);
+                    const double *rY = cl.map_shared_rank(s.ym, k);
+                    for (int e = tid; e < rnp[k] * ma; e += NT) s.J[e] = rJ[e];
+                    if (tid < rnp[k]) s.ym[tid] = rY[tid];
+                    __syncthreads();
+                }
+                consume_tile(rlc[k], rt0[k], rnp[k]);
+            }
+        }
+        cl.sync();   // the round's tile buffers are free again
+        nround = 0;
+    };
+    const int nreal = ob.n_lc - 1;
+    for (int lc = 0; lc < nreal; lc++) {
+        const int npts = ob.lc_npts[lc];
+        for (int t0 = 0; t0 < npts; t0 += P) {
+            const int np = min(P, npts - t0);
+            rlc[nround] = lc;
+            rt0[nround] = t0;
+            rnp[nround] = np;
+            if (nround == rank) compute_tile(lc, t0, np, false);
+            if (++nround == cs) flush_round();
+        }
+    }
+    if (nround > 0) flush_round();
+    // convexity rows (conv.c:12-29) on the leader
+    if (rank == 0) {
+        const int lc = ob.n_lc - 1, start = ob.lc_start[lc], npts = ob.lc_npts[lc];
+        for (int t0 = 0; t0 < npts; t0 += P) {
+            const int np = min(P, npts - t0);
+            compute_tile(lc, t0, np, true);
+            accumulate_tile<PS_FORM_FP64>(ob, s, M, bv, np, start + t0, true, conv_sig, accA, accB);
+        }
+        // mirror the lower triangle (mrqcof.c:139-141)
+        for (int e = tid; e < mf * mf; e += NT) {
+            const int j = e / mf, k = e - j * mf;
+            if (k > j) M[e] = M[k * mf + j];
+        }
+        __syncthreads();
+        // every CTA gets the result: the same solve and decisions everywhere
+        for (int r = 1; r < cs; r++) {
+            double *rM = cl.map_shared_rank(M, r), *rb = cl.map_shared_rank(bv, r);
+            double *rmisc = cl.map_shared_rank(s.misc, r);
+            for (int e = tid; e < mf * mf; e += NT) rM[e] = M[e];
+            for (int j = tid; j < mf; j += NT) rb[j] = bv[j];
+            if (tid < 3) rmisc[M_CHK + tid] = s.misc[M_CHK + tid];
+            if (tid == 0) rmisc[M_CHISQ] = s.misc[M_CHISQ];
+        }
+    }
+    cl.sync();
+}
+
 // Gauss-Jordan elimination with full pivoting on A (n x n, row-major in
 // shared memory) and right-hand side b (gauss_errc.c:9-73).  Only the
 // solution is needed by the LM step, so the columns that already hold the
@@ -2167,9 +2474,20 @@ __device__ float mlp_predict_warp(const float *W, const float *f, float *sh)
 template <int FORM, int KU>
 __device__ void run_fit(const DevObject &ob, const FitConfig &cfg, const SlotLayout &L, Smem<FORM> &s,
                         typename RealOf<FORM>::T *scratch, int64_t n, int pole, ps_fit *out, const FitWork &w,
-                        long long fidx, TcState &tcs)
+                        long long fidx, TcState &tcs, bool split = false)
 {
     constexpr bool kTensor = FORM == PS_FORM_MIXED && (KU == 0 || KU == 3);
+    // one model evaluation; with split (FP64 form, cluster launch) spread
+    // over the cluster's CTAs (evaluate_split)
+    auto eval = [&](const double *a, double *M, double *bv) {
+        if constexpr (FORM == PS_FORM_FP64) {
+            if (split) {
+                evaluate_split(ob, cfg, L, s, a, M, bv, scratch);
+                return;
+            }
+        }
+        evaluate<FORM, KU>(ob, cfg, L, s, a, M, bv, scratch, tcs);
+    };
     constexpr int NT = threads_of<FORM>();
     const int tid = threadIdx.x;
     const int C = ob.ncoef, ma = ob.ma, mf = ob.mfit;
@@ -2223,7 +2541,7 @@ __device__ void run_fit(const DevObject &ob, const FitConfig &cfg, const SlotLay
         niter = static_cast<int>(st[ma + 11]);
         last_err = static_cast<int>(st[ma + 12]);
         pred_dev = st[ma + 13];
-        evaluate<FORM, KU>(ob, cfg, L, s, s.cg, s.alpha, s.beta, scratch, tcs);
+        eval(s.cg, s.alpha, s.beta);
         if constexpr (kTensor) {
             if (*s.abort) last_err = kErrTcTimeout;
         }
@@ -2233,7 +2551,7 @@ __device__ void run_fit(const DevObject &ob, const FitConfig &cfg, const SlotLay
         bool accepted = false;
         if (alamda < 0) {
             alamda = cfg.alamda_start;
-            evaluate<FORM, KU>(ob, cfg, L, s, s.cg, s.alpha, s.beta, scratch, tcs);
+            eval(s.cg, s.alpha, s.beta);
             if constexpr (kTensor) {
                 if (*s.abort) {
                     last_err = kErrTcTimeout;
@@ -2277,7 +2595,7 @@ __device__ void run_fit(const DevObject &ob, const FitConfig &cfg, const SlotLay
                 s.atry[l] = s.cg[l] + s.da[j];
             }
             __syncthreads();
-            evaluate<FORM, KU>(ob, cfg, L, s, s.atry, s.covar, s.da, scratch, tcs);
+            eval(s.atry, s.covar, s.da);
             if constexpr (kTensor) {
                 if (*s.abort) {
                     last_err = kErrTcTimeout;
@@ -2406,7 +2724,7 @@ __device__ void run_fit(const DevObject &ob, const FitConfig &cfg, const SlotLay
         r.pred_dev = pred_dev;
         r.screened = screened ? 1 : 0;
         r.reserved = 0;
-        *out = r;
+        if (out) *out = r;
     }
     __syncthreads();
 }
@@ -2451,6 +2769,45 @@ __global__ void __launch_bounds__(threads_of<FORM>(), 1)
         run_fit<FORM, KU>(ob, cfg, L, s, scratch, n, pole, w.out + f, w, f, tcs);
     }
     if constexpr (kTensor) tc_teardown(s, tcs, ob.nfac);
+}
+
+// FP64 fits, each spread over a thread-block cluster (evaluate_split): the
+// cluster's leader takes fits from the work counter and hands every fit to
+// all of the cluster's CTAs, which run the same LM loop together; the
+// leader writes the result.  Bit-identical to fit_kernel<FP64>.
+__global__ void __launch_bounds__(threads_of<PS_FORM_FP64>(), 1)
+    fit_kernel_split(DevObject ob, FitConfig cfg, FitWork w, int P)
+{
+    namespace cgr = cooperative_groups;
+    cgr::cluster_group cl = cgr::this_cluster();
+    const int rank = static_cast<int>(cl.block_rank()), cs = static_cast<int>(cl.num_blocks());
+    extern __shared__ __align__(16) char smem[];
+    const SlotLayout L = make_layout(PS_FORM_FP64, ob.ma, ob.mfit, ob.nfac, ob.ncoef, P, 0, w.rel_rows);
+    Smem<PS_FORM_FP64> s = carve<PS_FORM_FP64>(smem, L);
+    TcState tcs;
+    double *scratch = L.rels ? reinterpret_cast<double *>(smem + L.rels)
+                             : w.scratch + static_cast<size_t>(blockIdx.x) * w.scratch_stride;
+    __shared__ long long next;
+    for (;;) {
+        if (rank == 0 && threadIdx.x == 0) {
+            const long long f = static_cast<long long>(atomicAdd(w.queue, 1ULL));
+            for (int r = 0; r < cs; r++) *cl.map_shared_rank(&next, r) = f;
+        }
+        cl.sync();
+        const long long f = next;
+        cl.sync();
+        if (f >= w.nfits) break;
+        int64_t n;
+        int pole;
+        if (w.period_index) {
+            n = w.period_index[f];
+            pole = w.pole[f];
+        } else {
+            n = w.n_lo + f / PS_N_POLES;
+            pole = static_cast<int>(f % PS_N_POLES) + 1;
+        }
+        run_fit<PS_FORM_FP64, 1>(ob, cfg, L, s, scratch, n, pole, rank == 0 ? w.out + f : nullptr, w, f, tcs, true);
+    }
 }
 
 template <int FORM, int KU>
