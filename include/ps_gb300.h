@@ -187,7 +187,10 @@ ps_status ps_prepare(const ps_problem *prob, const ps_options *opt, ps_ctx **out
 ps_status ps_get_info(const ps_ctx *ctx, ps_info *out);
 /* Convexity-weight optimisation (period_search_BOINC.cpp:487-715).  On entry
  * *conw_r is ignored; on exit it holds the final conw_r and *new_conw tells
- * whether the loop accepted it.  Replaces CUDAPrecalc. */
+ * whether the loop accepted it.  Its fits run in the FP64 form whatever the
+ * context's form, so that every form scans at the reference's conw_r (the
+ * loop compares a mean over 100 fits with a threshold).  Replaces
+ * CUDAPrecalc. */
 ps_status ps_precalc_conw(ps_ctx *ctx, double *conw_r, int32_t *new_conw);
 /* Rows for period indices n_lo..n_hi (1-based, inclusive) at convexity weight
  * conw_r.  out has n_hi-n_lo+1 rows.  Replaces CUDAStart. */
@@ -397,8 +400,9 @@ ps_status ps_prepare_state(const ps_state *state, const ps_options *opt, ps_ctx 
 
 /* One round of the convexity-weight pre-pass at *conw_r (the CUDA port's
  * CUDAPrecalc, start_CUDA.cu:248-521): fits the first min(10, n_max)
- * periods, then sets *new_conw = 1 when their mean dark-facet statistic is
- * below 1, else doubles *conw_r.  ps_precalc_conw repeats it. */
+ * periods in the FP64 form, then sets *new_conw = 1 when their mean
+ * dark-facet statistic is below 1, else doubles *conw_r.  ps_precalc_conw
+ * repeats it. */
 ps_status ps_precalc_step(ps_ctx *ctx, double *conw_r, int32_t *new_conw);
 
 /* ---- autotuner ---- */

@@ -326,7 +326,10 @@ ps_status scan_rows(ps_ctx *c, double conw_r, int64_t n_lo, int64_t n_hi, ps_row
     psg::FitWork w{};
     w.n_lo = n_lo;
     w.nfits = (n_hi - n_lo + 1) * PS_N_POLES;
-    ps_status st = run_fits(c, conw_r, w, c->opt.form);
+    // the convexity-weight pre-pass always takes the FP64 form: its decision
+    // is a threshold on a mean over few fits, which the mixed form's
+    // rounding can move across on an object that sits near it
+    ps_status st = run_fits(c, conw_r, w, prepass ? PS_FORM_FP64 : c->opt.form);
     if (st != PS_OK) return st;
     for (int64_t n = n_lo; n <= n_hi; n++) {
         ps_row r = psg::best_of_poles(&c->h_fits[static_cast<size_t>(n - n_lo) * PS_N_POLES], c->obj.ndata);

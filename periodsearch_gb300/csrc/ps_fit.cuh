@@ -90,7 +90,7 @@ struct Smem {
     // Memory address slot and the abort flag set when a wait gives up
     unsigned char *bhi, *blo;
     uint64_t *mbar, *mbar2;   // completion of the contraction MMAs / of the alpha MMAs
-    float4 *fac;              // per facet: nx, ny, nz and the evaluation's Area = Darea g
+    float4 *fac;              // per facet pair (2j, 2j + 1): {nx, nx', ny, ny'}, {nz, nz', Area, Area'} (fac_at)
     float *fpart;             // [4][P][9] facet-sum partials of the four facet quarters
     unsigned char *aop;       // alpha/beta MMA operands
     unsigned char *pref;      // per-point data prefetched for the contraction window
@@ -172,6 +172,16 @@ enum : int {
     M_LM = 32,     // 4 doubles: lambda, ochisq, dev, iter_diff of the fit, broadcast from thread 0
     M_WEXP = 36    // tensor-core path: exponent of the evaluation's W scale
 };
+
+// Facet table of the tensor-core path, interleaved by facet pairs so that
+// the facet stage loads each pair's components as FP32x2 register pairs:
+// float4 2j = {nx_2j, nx_2j+1, ny_2j, ny_2j+1}, float4 2j + 1 = {nz_2j,
+// nz_2j+1, Area_2j, Area_2j+1}.  Component c (0 nx, 1 ny, 2 nz, 3 Area) of
+// facet i:
+__device__ inline float &fac_at(float4 *fac, int i, int c)
+{
+    return reinterpret_cast<float *>(fac)[(i >> 1) * 8 + 2 * c + (i & 1)];
+}
 
 // Row j of packed lower-triangle element e (j*(j+1)/2 <= e < (j+1)*(j+2)/2),
 // from an FP32 square root corrected in integers.
@@ -761,8 +771,12 @@ __device__ void tc_setup(const DevObject &ob, Smem<PS_FORM_MIXED> &s, TcState &t
     const int bexp = (mx > 0.0 && mx < 1e300) ? 13 - ilogb(mx) : 0;
     const double bscale = ldexp(1.0, bexp);
     const uint32_t tbase = *s.tslot;
-    for (int i = tid; i < Fp; i += NT)
-        s.fac[i] = i < F ? make_float4(ob.nx_f[i], ob.ny_f[i], ob.nz_f[i], 0.f) : make_float4(0.f, 0.f, 0.f, 0.f);
+    for (int i = tid; i < Fp; i += NT) {
+        fac_at(s.fac, i, 0) = i < F ? ob.nx_f[i] : 0.f;
+        fac_at(s.fac, i, 1) = i < F ? ob.ny_f[i] : 0.f;
+        fac_at(s.fac, i, 2) = i < F ? ob.nz_f[i] : 0.f;
+        fac_at(s.fac, i, 3) = 0.f;
+    }
     if constexpr (!WIDE)
         for (int i = tid; i < static_cast<int>(kTcAlphaOperands / 4); i += NT)
             reinterpret_cast<uint32_t *>(s.aop)[i] = 0;
@@ -932,44 +946,65 @@ __device__ void facet_stage_tc(const DevObject &ob, Smem<PS_FORM_MIXED> &s, int 
     // E_k)) over the lit facets are D_k . U + E_k . V with U = sum Area dsmu
     // n and V = sum Area dsmu0 n (D_k, E_k: the derivative directions of the
     // Earth and Sun vectors), so the facet loop accumulates U and V.
-    float br = 0, dcl = 0, dcls = 0, ux = 0, uy = 0, uz = 0, vx = 0, vy = 0, vz = 0;
+    // A lane's two facets of each 8 run as the halves of FP32x2 operations
+    // (one paired instruction each, on the facet table's interleaved pairs),
+    // each half summing its own facets; the halves are added at the end.
+    const float2 E1 = make_float2(e1, e1), E2 = make_float2(e2, e2), E3 = make_float2(e3, e3);
+    const float2 F1 = make_float2(f1, f1), F2 = make_float2(f2, f2), F3 = make_float2(f3, f3);
+    const float2 CL = make_float2(cl, cl), CLS = make_float2(cls, cls), WS = make_float2(wscale, wscale);
+    const float2 z2 = make_float2(0.f, 0.f);
+    float2 br = z2, dcl = z2, dcls = z2, ux = z2, uy = z2, uz = z2, vx = z2, vy = z2, vz = z2;
     uint32_t *bh = reinterpret_cast<uint32_t *>(s.bhi), *bl = reinterpret_cast<uint32_t *>(s.blo);
     for (int kc = quarter * cq; kc < (quarter + 1) * cq; kc++) {
         const int i = kc * 8 + 2 * fl;
         const int cm = g * kcs + kc;    // core matrix (8-point group, 8-facet group)
-        float wv[2];
-#pragma unroll
-        for (int u = 0; u < 2; u++) {
-            const float4 n = s.fac[i + u];
-            const float mu = e1 * n.x + e2 * n.y + e3 * n.z;
-            const float mu0 = f1 * n.x + f2 * n.y + f3 * n.z;
-            // Branch-free: the 8 points of a warp see different lit facets,
-            // so a branch would diverge on almost every step (and a
-            // warp-uniform skip of groups unlit for all 8 points measured
-            // slower, twice); unlit and padding facets get zero area (every
-            // term vanishes) and a safe denominator.
-            const bool lit = mu > float(kTinyMu) && mu0 > float(kTinyMu);
-            // Area (= Darea g, also the weight of W: the Lambert and
-            // Lommel-Seeliger terms share it)
-            const float ax = lit ? n.w : 0.f;
-            const LitTerms<float, PS_FORM_MIXED> lt(lit ? mu : 1.f, lit ? mu0 : 1.f, cl, cls);
-            br = fmaf(ax, lt.sv, br);
-            wv[u] = ax * lt.sv * wscale;
-            const float cu = ax * lt.dsmu, cv = ax * lt.dsmu0;
-            ux = fmaf(cu, n.x, ux);
-            uy = fmaf(cu, n.y, uy);
-            uz = fmaf(cu, n.z, uz);
-            vx = fmaf(cv, n.x, vx);
-            vy = fmaf(cv, n.y, vy);
-            vz = fmaf(cv, n.z, vz);
-            dcl = fmaf(mu * mu0, ax, dcl);
-            dcls = fmaf(ax, lt.dcls_w, dcls);
-        }
-        const uint32_t hp = tc::pack_f16x2(wv[0], wv[1]);
+        const float4 fa = s.fac[i], fb = s.fac[i + 1];
+        const float2 nx = make_float2(fa.x, fa.y), ny = make_float2(fa.z, fa.w), nz = make_float2(fb.x, fb.y);
+        float2 mu = __fmul2_rn(E1, nx), mu0 = __fmul2_rn(F1, nx);
+        mu = __ffma2_rn(E2, ny, mu);
+        mu0 = __ffma2_rn(F2, ny, mu0);
+        mu = __ffma2_rn(E3, nz, mu);
+        mu0 = __ffma2_rn(F3, nz, mu0);
+        // Branch-free: the 8 points of a warp see different lit facets,
+        // so a branch would diverge on almost every step (and a
+        // warp-uniform skip of groups unlit for all 8 points measured
+        // slower, twice); unlit and padding facets get zero area (every
+        // term vanishes) and a safe denominator.
+        const bool lit0 = mu.x > float(kTinyMu) && mu0.x > float(kTinyMu);
+        const bool lit1 = mu.y > float(kTinyMu) && mu0.y > float(kTinyMu);
+        // Area (= Darea g, also the weight of W: the Lambert and
+        // Lommel-Seeliger terms share it)
+        const float2 ax = make_float2(lit0 ? fb.z : 0.f, lit1 ? fb.w : 0.f);
+        const float2 m = make_float2(lit0 ? mu.x : 1.f, lit1 ? mu.y : 1.f);
+        const float2 m0 = make_float2(lit0 ? mu0.x : 1.f, lit1 ? mu0.y : 1.f);
+        // LitTerms<float, PS_FORM_MIXED> on both halves
+        const float2 dnom = __fadd2_rn(m, m0);
+        float2 r;
+        asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r.x) : "f"(dnom.x));
+        asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r.y) : "f"(dnom.y));
+        const float2 mm = __fmul2_rn(m, m0);
+        const float2 sv = __fmul2_rn(mm, __ffma2_rn(CLS, r, CL));
+        const float2 q0 = __fmul2_rn(m0, r), q1 = __fmul2_rn(m, r);
+        const float2 dsmu = __ffma2_rn(CLS, __fmul2_rn(q0, q0), __fmul2_rn(CL, m0));
+        const float2 dsmu0 = __ffma2_rn(CLS, __fmul2_rn(q1, q1), __fmul2_rn(CL, m));
+        const float2 axs = __fmul2_rn(ax, sv);
+        br = __fadd2_rn(br, axs);
+        const float2 wv = __fmul2_rn(axs, WS);
+        const float2 cu = __fmul2_rn(ax, dsmu), cv = __fmul2_rn(ax, dsmu0);
+        ux = __ffma2_rn(cu, nx, ux);
+        uy = __ffma2_rn(cu, ny, uy);
+        uz = __ffma2_rn(cu, nz, uz);
+        vx = __ffma2_rn(cv, nx, vx);
+        vy = __ffma2_rn(cv, ny, vy);
+        vz = __ffma2_rn(cv, nz, vz);
+        dcl = __ffma2_rn(mm, ax, dcl);
+        dcls = __ffma2_rn(ax, __fmul2_rn(mm, r), dcls);
+        const uint32_t hp = tc::pack_f16x2(wv.x, wv.y);
         bh[cm * 32 + lane] = hp;
-        bl[cm * 32 + lane] = tc::pack_f16x2(wv[0] - tc::f16_lo(hp), wv[1] - tc::f16_hi(hp));
+        bl[cm * 32 + lane] = tc::pack_f16x2(wv.x - tc::f16_lo(hp), wv.y - tc::f16_hi(hp));
     }
-    float v[9] = {br, dcl, dcls, ux, uy, uz, vx, vy, vz};
+    float v[9] = {br.x + br.y, dcl.x + dcl.y, dcls.x + dcls.y, ux.x + ux.y, uy.x + uy.y,
+                  uz.x + uz.y, vx.x + vx.y, vy.x + vy.y, vz.x + vz.y};
 #pragma unroll
     for (int k = 0; k < 9; k++) {
         v[k] += __shfl_xor_sync(0xffffffffu, v[k], 1);
@@ -1301,7 +1336,7 @@ __device__ void evaluate(const DevObject &ob, const FitConfig &cfg, const SlotLa
         if constexpr (!kFP64) {
             s.areaR[i] = static_cast<R>(ar);
             s.gvR[i] = static_cast<R>(g);
-            if constexpr (kPipe) s.fac[i].w = static_cast<float>(ar);
+            if constexpr (kPipe) fac_at(s.fac, i, 3) = static_cast<float>(ar);
         }
         asum += ar;
     }
@@ -1342,7 +1377,7 @@ __device__ void evaluate(const DevObject &ob, const FitConfig &cfg, const SlotLa
         // convexity rows' W <= Darea g, so 2^k puts the evaluation's largest
         // W just below 2^14.
         float mx = 0.f;
-        for (int i = lane; i < F; i += 32) mx = fmaxf(mx, s.fac[i].w);
+        for (int i = lane; i < F; i += 32) mx = fmaxf(mx, fac_at(s.fac, i, 3));
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
         const float wmax =
