@@ -116,6 +116,7 @@ struct SlotLayout {
     size_t rels;            // relative-lightcurve rows in shared memory, or 0 (global scratch)
     size_t pref;            // tensor-core path: per-point data prefetched for the contraction window
     size_t flist;           // tensor-core path: the free parameters' columns
+    size_t lit;             // FP64 form: per point of a tile, its lit-facet count, then its lit facets
     size_t bytes;
 };
 
@@ -237,6 +238,8 @@ PSG_HD inline SlotLayout make_layout(int form, int ma, int mfit, int nfac, int n
     L.davef = form == PS_FORM_MIXED ? take(static_cast<size_t>(ma) * sizeof(float)) : 0;
     L.bmat = take(32 * rs);
     L.rels = rel_rows > 0 ? take(static_cast<size_t>(rel_rows) * rel_row_stride(ma) * rs) : 0;
+    // FP64 form: P counts (int) and P x wcols facet indices (uint16_t)
+    L.lit = form == PS_FORM_FP64 ? take(static_cast<size_t>(P) * (4 + 2 * L.wcols)) : 0;
     L.bytes = o;
     return L;
 }

@@ -95,6 +95,10 @@ struct Smem {
     unsigned char *aop;       // alpha/beta MMA operands
     unsigned char *pref;      // per-point data prefetched for the contraction window
     int *flist;               // the free parameters' columns (tensor-core path)
+    // FP64 form: lit-facet count of each point of the tile, and its lit
+    // facets in increasing order ([P][wcols], the W row holds their values)
+    int *nlit;
+    uint16_t *lidx;
     uint32_t *tslot;
     int *abort;
 };
@@ -127,6 +131,9 @@ __device__ inline Smem<FORM> carve(char *base, const SlotLayout &L)
     s.col = reinterpret_cast<double *>(base + L.col);
     s.misc = reinterpret_cast<double *>(base + L.misc);
     s.ipiv = reinterpret_cast<int *>(base + L.ipiv);
+    s.nlit = L.form == PS_FORM_FP64 ? reinterpret_cast<int *>(base + L.lit) : nullptr;
+    s.lidx = L.form == PS_FORM_FP64 ? reinterpret_cast<uint16_t *>(base + L.lit + 4 * static_cast<size_t>(L.P))
+                                     : nullptr;
     s.dsph = L.dsph_smem == kBasisSmem ? reinterpret_cast<float *>(base + L.dsph) : nullptr;
     if (basis_on_tensor(L.dsph_smem)) {
         s.bhi = reinterpret_cast<unsigned char *>(base + L.bhi);
@@ -257,6 +264,40 @@ __device__ inline float rotation_phase_mixed(double omg, double t, double phi0)
     if (ff < 0.f) ff += kTwoPiF;
     if (ff >= kTwoPiF) ff -= kTwoPiF;
     return ff;
+}
+
+// FP64 form: appends the warp's lit facets of one 32-facet round (facet i
+// on each lane) to a point's list in increasing facet order, their W values
+// in the point's W row and their indices in idx; returns the new count (the
+// same on every lane).  Every lane of the warp calls it.
+__device__ inline int list_lit(double *Wp, uint16_t *idx, int n, int i, bool lit, double w, int lane)
+{
+    const unsigned m = __ballot_sync(0xffffffffu, lit);
+    if (lit) {
+        const int pos = n + __popc(m & ((1u << lane) - 1u));
+        Wp[pos] = w;
+        idx[pos] = static_cast<uint16_t>(i);
+    }
+    return n + __popc(m);
+}
+
+// FP64 form: sum_i W[p][i] Dsph[i][k] (ds = Dsph + k) for point p of the
+// tile.  Model rows sum over the point's lit facets, in increasing order as
+// bright.c:79-86 does (a dense sum over all facets adds only exact zeros,
+// so the two agree bit for bit); convexity rows sum over every facet.
+template <class S>
+__device__ inline double contract_fp64(const S &s, const double *ds, int p, int C, int F, int wcols, bool conv)
+{
+    const double *Wp = s.W + static_cast<size_t>(p) * wcols;
+    double acc = 0;
+    if (conv) {
+        for (int i = 0; i < F; i++) acc = acc + Wp[i] * ds[static_cast<size_t>(i) * C];
+    } else {
+        const uint16_t *idx = s.lidx + static_cast<size_t>(p) * wcols;
+        const int n = s.nlit[p];
+        for (int j = 0; j < n; j++) acc = acc + Wp[j] * ds[static_cast<size_t>(idx[j]) * C];
+    }
+    return acc;
 }
 
 // Lit-facet terms of the Lommel-Seeliger + Lambert law (bright.c:65-74,
@@ -1487,12 +1528,17 @@ __device__ void evaluate(const DevObject &ob, const FitConfig &cfg, const SlotLa
                     }
                     R br = 0, r0 = 0, r1 = 0, r2 = 0, dcl = 0, dcls = 0;
                     R *Wp = s.W + static_cast<size_t>(p) * wcols;
-                    for (int i = lane; i < F; i += 32) {
+                    int nl = 0;   // FP64 form: lit facets listed so far
+                    for (int i0 = 0; i0 < F; i0 += 32) {
+                        const int i = i0 + lane;
+                        R w = 0;
+                        bool lit = false;
+                        if (i < F) {
                         const R nx = nxR[i], ny = nyR[i], nz = nzR[i];
                         const R mu = e1 * nx + e2 * ny + e3 * nz;
                         const R mu0 = f1 * nx + f2 * ny + f3 * nz;
-                        R w = 0;
-                        if (mu > R(kTinyMu) && mu0 > R(kTinyMu)) {
+                        lit = mu > R(kTinyMu) && mu0 > R(kTinyMu);
+                        if (lit) {
                             const R ar = s.areaR[i];
                             const LitTerms<R, FORM> lt(mu, mu0, cl, cls);
                             br = br + ar * lt.sv;
@@ -1509,8 +1555,14 @@ __device__ void evaluate(const DevObject &ob, const FitConfig &cfg, const SlotLa
                             dcl = dcl + mu * mu0 * ar;
                             dcls = dcls + ar * lt.dcls_w;
                         }
-                        Wp[i] = w;
+                        }
+                        if constexpr (kFP64) {
+                            nl = list_lit(Wp, s.lidx + p * wcols, nl, i, lit, w, lane);
+                        } else if (i < F) {
+                            Wp[i] = w;
+                        }
                     }
+                    if (kFP64 && lane == 0) s.nlit[p] = nl;
                     br = warp_sum(br);
                     r0 = warp_sum(r0);
                     r1 = warp_sum(r1);
@@ -1550,10 +1602,7 @@ __device__ void evaluate(const DevObject &ob, const FitConfig &cfg, const SlotLa
             if constexpr (kFP64) {
                 for (int o = tid; o < np * C; o += NT) {
                     const int p = o / C, k = o - p * C;
-                    const R *Wp = s.W + static_cast<size_t>(p) * wcols;
-                    const R *ds = dsphR + k;
-                    R acc = 0;
-                    for (int i = 0; i < F; i++) acc = acc + Wp[i] * ds[static_cast<size_t>(i) * C];
+                    const double acc = contract_fp64(s, dsphR + k, p, C, F, wcols, conv);
                     s.J[p * ma + k] = conv ? acc : s.pt[p * kPointStride + 24] * acc;
                 }
             } else if constexpr (kPipe) {
@@ -1646,7 +1695,6 @@ __device__ void evaluate(const DevObject &ob, const FitConfig &cfg, const SlotLa
                 next_setup = nlc < ob.n_lc - 1;   // the last lightcurve is the convexity rows
                 if (next_setup && warp >= 1 && warp <= 3) {
                     const bool have = lane < min(P, ob.lc_npts[nlc] - nt0);
-                    const int q = ob.lc_start[nlc] + nt0 + lane;
                     float *ptn = s.pt2 + lane * kPointStride;
                     cp_async_wait_all();
                     if (warp == 1) {
@@ -1937,12 +1985,17 @@ __device__ void evaluate_split(const DevObject &ob, const FitConfig &cfg, const 
                 }
                 double br = 0, r0 = 0, r1 = 0, r2 = 0, dcl = 0, dcls = 0;
                 double *Wp = s.W + static_cast<size_t>(p) * wcols;
-                for (int i = lane; i < F; i += 32) {
+                int nl = 0;   // lit facets listed so far
+                for (int i0 = 0; i0 < F; i0 += 32) {
+                    const int i = i0 + lane;
+                    double w = 0;
+                    bool lit = false;
+                    if (i < F) {
                     const double nx = ob.nx[i], ny = ob.ny[i], nz = ob.nz[i];
                     const double mu = e1 * nx + e2 * ny + e3 * nz;
                     const double mu0 = f1 * nx + f2 * ny + f3 * nz;
-                    double w = 0;
-                    if (mu > kTinyMu && mu0 > kTinyMu) {
+                    lit = mu > kTinyMu && mu0 > kTinyMu;
+                    if (lit) {
                         const double ar = s.area[i];
                         const LitTerms<double, PS_FORM_FP64> lt(mu, mu0, cl_w, cls);
                         br = br + ar * lt.sv;
@@ -1959,8 +2012,10 @@ __device__ void evaluate_split(const DevObject &ob, const FitConfig &cfg, const 
                         dcl = dcl + mu * mu0 * ar;
                         dcls = dcls + ar * lt.dcls_w;
                     }
-                    Wp[i] = w;
+                    }
+                    nl = list_lit(Wp, s.lidx + p * wcols, nl, i, lit, w, lane);
                 }
+                if (lane == 0) s.nlit[p] = nl;
                 br = warp_sum(br);
                 r0 = warp_sum(r0);
                 r1 = warp_sum(r1);
@@ -1993,10 +2048,7 @@ __device__ void evaluate_split(const DevObject &ob, const FitConfig &cfg, const 
         __syncthreads();
         for (int o = tid; o < np * C; o += NT) {
             const int p = o / C, k = o - p * C;
-            const double *Wp = s.W + static_cast<size_t>(p) * wcols;
-            const double *ds = ob.dsph + k;
-            double acc = 0;
-            for (int i = 0; i < F; i++) acc = acc + Wp[i] * ds[static_cast<size_t>(i) * C];
+            const double acc = contract_fp64(s, ob.dsph + k, p, C, F, wcols, conv);
             s.J[p * ma + k] = conv ? acc : s.pt[p * kPointStride + 24] * acc;
         }
         if (tid < np) {
