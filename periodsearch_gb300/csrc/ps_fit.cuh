@@ -266,21 +266,6 @@ __device__ inline float rotation_phase_mixed(double omg, double t, double phi0)
     return ff;
 }
 
-// FP64 form: appends the warp's lit facets of one 32-facet round (facet i
-// on each lane) to a point's list in increasing facet order, their W values
-// in the point's W row and their indices in idx; returns the new count (the
-// same on every lane).  Every lane of the warp calls it.
-__device__ inline int list_lit(double *Wp, uint16_t *idx, int n, int i, bool lit, double w, int lane)
-{
-    const unsigned m = __ballot_sync(0xffffffffu, lit);
-    if (lit) {
-        const int pos = n + __popc(m & ((1u << lane) - 1u));
-        Wp[pos] = w;
-        idx[pos] = static_cast<uint16_t>(i);
-    }
-    return n + __popc(m);
-}
-
 // FP64 form: sum_i W[p][i] Dsph[i][k] (ds = Dsph + k) for point p of the
 // tile.  Model rows sum over the point's lit facets, in increasing order as
 // bright.c:79-86 does (a dense sum over all facets adds only exact zeros,
@@ -326,6 +311,83 @@ struct LitTerms {
         }
     }
 };
+
+// FP64 facet stage of point p of the tile (bright.c:59-120), one warp.  A
+// first pass lists the point's lit facets in increasing order (s.lidx,
+// s.nlit); the law and the facet sums then run over that list with every
+// lane busy (an FP64 instruction holds its sub-partition's FP64 unit for
+// the whole warp, however few lanes are active), lane l taking the list's
+// entries l, l + 32, ...  W is left in the W row at the list positions.
+// The facet sums go to s.red[p * kRedStride + 0..5]: brightness, the three
+// rotation derivatives, the Lambert and the scattering-weight derivatives.
+__device__ inline void facet_point_fp64(const DevObject &ob, Smem<PS_FORM_FP64> &s, int p, int wcols, double cl,
+                                        double cls)
+{
+    const int lane = threadIdx.x & 31, F = ob.nfac;
+    const double *pt = s.pt + p * kPointStride;
+    const double e1 = pt[0], e2 = pt[1], e3 = pt[2];
+    const double f1 = pt[3], f2 = pt[4], f3 = pt[5];
+    uint16_t *idx = s.lidx + static_cast<size_t>(p) * wcols;
+    int n = 0;
+    for (int i0 = 0; i0 < F; i0 += 32) {
+        const int i = i0 + lane;
+        bool lit = false;
+        if (i < F) {
+            const double mu = e1 * ob.nx[i] + e2 * ob.ny[i] + e3 * ob.nz[i];
+            const double mu0 = f1 * ob.nx[i] + f2 * ob.ny[i] + f3 * ob.nz[i];
+            lit = mu > kTinyMu && mu0 > kTinyMu;
+        }
+        const unsigned m = __ballot_sync(0xffffffffu, lit);
+        if (lit) idx[n + __popc(m & ((1u << lane) - 1u))] = static_cast<uint16_t>(i);
+        n += __popc(m);
+    }
+    __syncwarp();
+    double de[9], de0[9];
+#pragma unroll
+    for (int k = 0; k < 9; k++) {
+        de[k] = pt[6 + k];
+        de0[k] = pt[15 + k];
+    }
+    double br = 0, r0 = 0, r1 = 0, r2 = 0, dcl = 0, dcls = 0;
+    double *Wp = s.W + static_cast<size_t>(p) * wcols;
+    for (int j = lane; j < n; j += 32) {
+        const int i = idx[j];
+        const double nx = ob.nx[i], ny = ob.ny[i], nz = ob.nz[i];
+        const double mu = e1 * nx + e2 * ny + e3 * nz;
+        const double mu0 = f1 * nx + f2 * ny + f3 * nz;
+        const double ar = s.area[i];
+        const LitTerms<double, PS_FORM_FP64> lt(mu, mu0, cl, cls);
+        br = br + ar * lt.sv;
+        Wp[j] = ob.darea[i] * lt.sv * s.gv[i];
+        const double s0 = nx * de[0] + ny * de[3] + nz * de[6];
+        const double s1 = nx * de[1] + ny * de[4] + nz * de[7];
+        const double s2 = nx * de[2] + ny * de[5] + nz * de[8];
+        const double t0v = nx * de0[0] + ny * de0[3] + nz * de0[6];
+        const double t1v = nx * de0[1] + ny * de0[4] + nz * de0[7];
+        const double t2v = nx * de0[2] + ny * de0[5] + nz * de0[8];
+        r0 = r0 + ar * (lt.dsmu * s0 + lt.dsmu0 * t0v);
+        r1 = r1 + ar * (lt.dsmu * s1 + lt.dsmu0 * t1v);
+        r2 = r2 + ar * (lt.dsmu * s2 + lt.dsmu0 * t2v);
+        dcl = dcl + mu * mu0 * ar;
+        dcls = dcls + ar * lt.dcls_w;
+    }
+    br = warp_sum(br);
+    r0 = warp_sum(r0);
+    r1 = warp_sum(r1);
+    r2 = warp_sum(r2);
+    dcl = warp_sum(dcl);
+    dcls = warp_sum(dcls);
+    if (lane == 0) {
+        double *rd = s.red + p * kRedStride;
+        rd[0] = br;
+        rd[1] = r0;
+        rd[2] = r1;
+        rd[3] = r2;
+        rd[4] = dcl;
+        rd[5] = dcls;
+        s.nlit[p] = n;
+    }
+}
 
 // Accumulates the rows J[0..np) (model values in ym) of one tile into the
 // normal matrix M (lower triangle), bv and chi^2 (mrqcof.c:106-136).  The
@@ -1515,6 +1577,9 @@ __device__ void evaluate(const DevObject &ob, const FitConfig &cfg, const SlotLa
                     }
                     facet_stage_tc<NT>(ob, s, np, cl, cls, wscale);
                 }
+                else if constexpr (kFP64) {
+                    for (int p = warp; p < np; p += NT / 32) facet_point_fp64(ob, s, p, wcols, cl, cls);
+                }
                 else
                 for (int p = warp; p < np; p += NT / 32) {
                     const R *pt = s.pt + p * kPointStride;
@@ -1528,17 +1593,12 @@ __device__ void evaluate(const DevObject &ob, const FitConfig &cfg, const SlotLa
                     }
                     R br = 0, r0 = 0, r1 = 0, r2 = 0, dcl = 0, dcls = 0;
                     R *Wp = s.W + static_cast<size_t>(p) * wcols;
-                    int nl = 0;   // FP64 form: lit facets listed so far
-                    for (int i0 = 0; i0 < F; i0 += 32) {
-                        const int i = i0 + lane;
-                        R w = 0;
-                        bool lit = false;
-                        if (i < F) {
+                    for (int i = lane; i < F; i += 32) {
                         const R nx = nxR[i], ny = nyR[i], nz = nzR[i];
                         const R mu = e1 * nx + e2 * ny + e3 * nz;
                         const R mu0 = f1 * nx + f2 * ny + f3 * nz;
-                        lit = mu > R(kTinyMu) && mu0 > R(kTinyMu);
-                        if (lit) {
+                        R w = 0;
+                        if (mu > R(kTinyMu) && mu0 > R(kTinyMu)) {
                             const R ar = s.areaR[i];
                             const LitTerms<R, FORM> lt(mu, mu0, cl, cls);
                             br = br + ar * lt.sv;
@@ -1555,14 +1615,8 @@ __device__ void evaluate(const DevObject &ob, const FitConfig &cfg, const SlotLa
                             dcl = dcl + mu * mu0 * ar;
                             dcls = dcls + ar * lt.dcls_w;
                         }
-                        }
-                        if constexpr (kFP64) {
-                            nl = list_lit(Wp, s.lidx + p * wcols, nl, i, lit, w, lane);
-                        } else if (i < F) {
-                            Wp[i] = w;
-                        }
+                        Wp[i] = w;
                     }
-                    if (kFP64 && lane == 0) s.nlit[p] = nl;
                     br = warp_sum(br);
                     r0 = warp_sum(r0);
                     r1 = warp_sum(r1);
@@ -1973,65 +2027,7 @@ __device__ void evaluate_split(const DevObject &ob, const FitConfig &cfg, const 
             if (sp >= 0 && sp < np)
                 setup_point<PS_FORM_FP64>(ob, cfg, start + t0 + sp, omg, s.bmat, s.pt + sp * kPointStride);
             __syncthreads();
-            for (int p = warp; p < np; p += NT / 32) {
-                const double *pt = s.pt + p * kPointStride;
-                const double e1 = pt[0], e2 = pt[1], e3 = pt[2];
-                const double f1 = pt[3], f2 = pt[4], f3 = pt[5];
-                double de[9], de0[9];
-#pragma unroll
-                for (int k = 0; k < 9; k++) {
-                    de[k] = pt[6 + k];
-                    de0[k] = pt[15 + k];
-                }
-                double br = 0, r0 = 0, r1 = 0, r2 = 0, dcl = 0, dcls = 0;
-                double *Wp = s.W + static_cast<size_t>(p) * wcols;
-                int nl = 0;   // lit facets listed so far
-                for (int i0 = 0; i0 < F; i0 += 32) {
-                    const int i = i0 + lane;
-                    double w = 0;
-                    bool lit = false;
-                    if (i < F) {
-                    const double nx = ob.nx[i], ny = ob.ny[i], nz = ob.nz[i];
-                    const double mu = e1 * nx + e2 * ny + e3 * nz;
-                    const double mu0 = f1 * nx + f2 * ny + f3 * nz;
-                    lit = mu > kTinyMu && mu0 > kTinyMu;
-                    if (lit) {
-                        const double ar = s.area[i];
-                        const LitTerms<double, PS_FORM_FP64> lt(mu, mu0, cl_w, cls);
-                        br = br + ar * lt.sv;
-                        w = ob.darea[i] * lt.sv * s.gv[i];
-                        const double s0 = nx * de[0] + ny * de[3] + nz * de[6];
-                        const double s1 = nx * de[1] + ny * de[4] + nz * de[7];
-                        const double s2 = nx * de[2] + ny * de[5] + nz * de[8];
-                        const double t0v = nx * de0[0] + ny * de0[3] + nz * de0[6];
-                        const double t1v = nx * de0[1] + ny * de0[4] + nz * de0[7];
-                        const double t2v = nx * de0[2] + ny * de0[5] + nz * de0[8];
-                        r0 = r0 + ar * (lt.dsmu * s0 + lt.dsmu0 * t0v);
-                        r1 = r1 + ar * (lt.dsmu * s1 + lt.dsmu0 * t1v);
-                        r2 = r2 + ar * (lt.dsmu * s2 + lt.dsmu0 * t2v);
-                        dcl = dcl + mu * mu0 * ar;
-                        dcls = dcls + ar * lt.dcls_w;
-                    }
-                    }
-                    nl = list_lit(Wp, s.lidx + p * wcols, nl, i, lit, w, lane);
-                }
-                if (lane == 0) s.nlit[p] = nl;
-                br = warp_sum(br);
-                r0 = warp_sum(r0);
-                r1 = warp_sum(r1);
-                r2 = warp_sum(r2);
-                dcl = warp_sum(dcl);
-                dcls = warp_sum(dcls);
-                if (lane == 0) {
-                    double *rd = s.red + p * kRedStride;
-                    rd[0] = br;
-                    rd[1] = r0;
-                    rd[2] = r1;
-                    rd[3] = r2;
-                    rd[4] = dcl;
-                    rd[5] = dcls;
-                }
-            }
+            for (int p = warp; p < np; p += NT / 32) facet_point_fp64(ob, s, p, wcols, cl_w, cls);
         } else {
             for (int p = warp; p < np; p += NT / 32) {
                 const double *nc = (p == 0) ? ob.nx : (p == 1) ? ob.ny : ob.nz;
