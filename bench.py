@@ -115,7 +115,20 @@ def _dist():
 
 
 def flops_per_eval(ndata, nfac, ncoef, mfit):
+    """Dense count of one evaluation: the mixed form's tensor-core
+    contraction and branch-free facet stage compute every facet."""
     return 2.0 * ndata * nfac * ncoef + 60.0 * ndata * nfac + ndata * mfit * (mfit + 1) + 9.0 * nfac * ncoef
+
+
+def flops_fp64(info, evals: int, fits: int, lit: int) -> float:
+    """The reference's own work over `evals` FP64 evaluations with `lit`
+    lit (point, facet) pairs in all (the engine's count): the two dot
+    products of every pair (10), the facet law and its sums on the lit pairs
+    (70) and the shape contraction over the lit facets (2 C), as bright.c
+    does; the normal equations and the curvature; 2 m^3 per solve."""
+    n, f, c, m = info.ndata, info.nfac, info.ncoef, info.mfit
+    return ((70.0 + 2.0 * c) * lit + evals * (10.0 * n * f + n * m * (m + 1) + 9.0 * f * c) +
+            (evals - fits) * 2.0 * m ** 3)
 
 
 def window_of(n_max: int, freq_start: float, freq_step: float, truth_h: float, width: int, rank: int = 0):
@@ -468,6 +481,7 @@ class Scanner:
 
     def __init__(self, form: str, eng, eng64, conw_r: float, fe: float, fs: float):
         self.form, self.eng, self.eng64, self.conw_r, self.fe, self.fs = form, eng, eng64, conw_r, fe, fs
+        self.info = eng.info
 
     def __call__(self, lo: int, hi: int):
         from periodsearch_gb300 import learned
@@ -475,12 +489,15 @@ class Scanner:
         nfits = (hi - lo + 1) * 10
         if self.form == "learned":
             rows, st = self.eng.scan_learned(self.conw_r, lo, hi, **learned.cascade_defaults())
+            lit = self.eng.timing()["lit_facets"]
         elif self.form == "refined":
             rows, st = self.eng.scan_refined(self.conw_r, lo, hi)
+            lit = self.eng.timing()["lit_facets"]
         else:
             eng = self.eng64 if self.form == "fp64" else self.eng
             rows = eng.scan(self.conw_r, lo, hi)
             t = eng.timing()
+            lit = t["lit_facets"]
             key = "refit" if self.form == "fp64" else "complete"
             st = {"fits_total": nfits, "launches": t["launches"], "screen_ms": 0.0, "complete_ms": 0.0,
                   "refit_ms": 0.0, "evals_screen": 0, "evals_complete": 0, "evals_refit": 0, "fits_completed": 0,
@@ -492,7 +509,7 @@ class Scanner:
         mixed_ms = st["screen_ms"] + st["complete_ms"]
         mixed_flop = ((st["evals_screen"] + st["evals_complete"]) * self.fe +
                       (st["evals_screen"] - screen_fits + st["evals_complete"] - st["fits_completed"]) * self.fs)
-        fp64_flop = st["evals_refit"] * self.fe + (st["evals_refit"] - st["fits_refit"]) * self.fs
+        fp64_flop = flops_fp64(self.info, st["evals_refit"], st["fits_refit"], lit)
         # the FP64 refit launches are the refit rounds; every other launch is the mixed kernel
         mixed_launches = st["launches"] - st["refit_rounds"]
         if self.form in ("mixed", "fp64"):
@@ -621,13 +638,15 @@ def run_engine_arm(args):
             t64 = eng64.timing()
             b64 = lo + int(np.argmin(r64["rms"]))
             pv = wfits / (t64["kernel_ms"] / 1e3)
-            pflop = t64["evals"] * fe + (t64["evals"] - t64["fits"]) * fs
+            pflop = flops_fp64(info, t64["evals"], t64["fits"], t64["lit_facets"])
             pa = pflop / (t64["kernel_ms"] / 1e3) / 1e12
             fp64 = {"value": pv, "unit": "fits/s", "window": [lo, hi], "fits": wfits,
                     "seconds": t64["kernel_ms"] / 1e3, "best_index": b64,
                     "speedup_chosen_over_fp64": value / pv,
+                    "lit_fraction": t64["lit_facets"] / (t64["evals"] * info.ndata * info.nfac),
                     "roofline": {"bound": "fp64", "achieved": pa, "peak": p64.value, "unit": "TFLOP/s",
                                  "frac": pa / p64.value,
+                                 "count": "the reference's lit-facet work (flops_fp64)",
                                  "peak_source": "FP64 FMA ceiling measured live by ps_device_fma_peaks"}}
             rows_c = steps[-1][0]
             bc = best_steps[-1]

@@ -164,6 +164,9 @@ typedef struct ps_timing {
     int32_t launches;      /* kernel launches */
     int32_t cluster_size;  /* CTAs per fit of the last launch: 1, or 2..4 when FP64 fits were each spread over a
                               thread-block cluster (fewer fits than fit slots; bit-identical results) */
+    int64_t lit_facets;    /* FP64 form: (point, facet) pairs on the lit side over all evaluations, the work of
+                              the facet law and of the shape contraction (bright.c runs both on lit facets
+                              only); 0 for the mixed form, whose tensor-core contraction is dense */
 } ps_timing;
 
 typedef struct ps_ctx ps_ctx;

@@ -122,7 +122,7 @@ TRAJ_FLOATS = 16
 
 class Timing(C.Structure):
     _fields_ = [("kernel_ms", C.c_double), ("total_ms", C.c_double), ("fits", C.c_int64), ("evals", C.c_int64),
-                ("launches", C.c_int32), ("cluster_size", C.c_int32)]
+                ("launches", C.c_int32), ("cluster_size", C.c_int32), ("lit_facets", C.c_int64)]
 
 
 # Every symbol the header declares, with its ctypes signature.

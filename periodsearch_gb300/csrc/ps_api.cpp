@@ -261,6 +261,7 @@ ps_status run_fits(ps_ctx *c, double conw_r, psg::FitWork w, int form)
     st = ensure_out(c, static_cast<size_t>(w.nfits));
     if (st != PS_OK) return st;
     w.queue = c->d_queue;
+    w.lit = c->d_queue + 1;   // the lit facet-point counter of the FP64 form
     w.scratch = c->d_scratch;
     w.scratch_stride = c->scratch_stride;
     w.rel_rows = pl.rel_rows;
@@ -282,7 +283,7 @@ ps_status run_fits(ps_ctx *c, double conw_r, psg::FitWork w, int form)
     // FP64 fits fewer than the slots: each fit spread over a cluster of
     // CTAs (bit-identical results, a shorter launch)
     const int cs = split_size(c, w, form);
-    PSG_CUDA(c, cudaMemsetAsync(c->d_queue, 0, sizeof(unsigned long long), c->stream));
+    PSG_CUDA(c, cudaMemsetAsync(c->d_queue, 0, 2 * sizeof(unsigned long long), c->stream));
     PSG_CUDA(c, cudaEventRecord(c->ev[0], c->stream));
     int e;
     if (cs > 1) {
@@ -299,6 +300,8 @@ ps_status run_fits(ps_ctx *c, double conw_r, psg::FitWork w, int form)
     c->h_fits.resize(static_cast<size_t>(w.nfits));
     PSG_CUDA(c, cudaMemcpyAsync(c->h_fits.data(), c->d_out, w.nfits * sizeof(ps_fit), cudaMemcpyDeviceToHost,
                                 c->stream));
+    unsigned long long lit = 0;
+    PSG_CUDA(c, cudaMemcpyAsync(&lit, c->d_queue + 1, sizeof(lit), cudaMemcpyDeviceToHost, c->stream));
     PSG_CUDA(c, cudaEventRecord(c->ev[2], c->stream));
     PSG_CUDA(c, cudaStreamSynchronize(c->stream));
     float k_ms = 0, t_ms = 0;
@@ -312,6 +315,7 @@ ps_status run_fits(ps_ctx *c, double conw_r, psg::FitWork w, int form)
     c->timing.evals = evals;
     c->timing.launches = 1;
     c->timing.cluster_size = cs;
+    c->timing.lit_facets = static_cast<int64_t>(lit);
     c->launch_total++;
     for (const ps_fit &f : c->h_fits)
         if (f.err_code == 16) {
@@ -423,7 +427,7 @@ struct ScanFits {
 // periods that a later round would likely have needed come at no extra
 // time, and fewer rounds run.
 ps_status refit_minimum(ps_ctx *c, double conw_r, ScanFits &sf, double rel, int32_t halfwidth, bool fill,
-                        double *ms, int64_t *nrefit, int64_t *evals, int32_t *rounds)
+                        double *ms, int64_t *nrefit, int64_t *evals, int32_t *rounds, int64_t *lit)
 {
     ps_status st = make_plan(c, PS_FORM_FP64);
     if (st != PS_OK) return st;
@@ -477,6 +481,7 @@ ps_status refit_minimum(ps_ctx *c, double conw_r, ScanFits &sf, double rel, int3
         if (st != PS_OK) return st;
         *ms += c->timing.kernel_ms;
         *evals += c->timing.evals;
+        *lit += c->timing.lit_facets;
         *nrefit += static_cast<int64_t>(pidx.size());
         *rounds += 1;
         for (size_t k = 0; k < per.size(); k++) {
@@ -789,7 +794,7 @@ ps_status ps_precalc_conw(ps_ctx *c, double *conw_r, int32_t *new_conw)
     int32_t nc = 0;
     const int64_t ntest = std::min<int64_t>(10, o.n_max);
     double launches = 0, kms = 0, tms = 0;
-    int64_t fits = 0, evals = 0;
+    int64_t fits = 0, evals = 0, lit = 0;
     while (nc != 1 && (cw * o.escl * o.escl) < 10.0) {
         if (ntest < 1) break;
         ps_status st = ps_precalc_step(c, &cw, &nc);
@@ -799,11 +804,13 @@ ps_status ps_precalc_conw(ps_ctx *c, double *conw_r, int32_t *new_conw)
         tms += c->timing.total_ms;
         fits += c->timing.fits;
         evals += c->timing.evals;
+        lit += c->timing.lit_facets;
     }
     c->timing.kernel_ms = kms;
     c->timing.total_ms = tms;
     c->timing.fits = fits;
     c->timing.evals = evals;
+    c->timing.lit_facets = lit;
     c->timing.launches = static_cast<int32_t>(launches);
     *conw_r = cw;
     *new_conw = nc;
@@ -1118,8 +1125,9 @@ ps_status ps_scan_learned(ps_ctx *c, double conw_r, int64_t n_lo, int64_t n_hi, 
     stt.fits_screened_out = nfits - stt.fits_completed;
     // (4) FP64 refit of the periods nearest the best row
     const int64_t ev0 = stt.evals;
+    int64_t lit = 0;
     st = refit_minimum(c, conw_r, sf, o.refit_rel, o.refit_halfwidth, o.fill_refit_waves != 0, &stt.refit_ms,
-                       &stt.fits_refit, &stt.evals, &stt.refit_rounds);
+                       &stt.fits_refit, &stt.evals, &stt.refit_rounds, &lit);
     if (st != PS_OK) return st;
     stt.evals_refit = stt.evals - ev0;
     std::vector<ps_row> rows;
@@ -1131,6 +1139,7 @@ ps_status ps_scan_learned(ps_ctx *c, double conw_r, int64_t n_lo, int64_t n_hi, 
     c->timing.kernel_ms = stt.screen_ms + stt.complete_ms + stt.refit_ms;
     c->timing.fits = nfits;
     c->timing.evals = stt.evals;
+    c->timing.lit_facets = lit;   // the FP64 refit's
     c->timing.launches = static_cast<int32_t>(c->launch_total - launch0);
     stt.launches = c->timing.launches;
     if (stats) *stats = stt;
@@ -1162,8 +1171,9 @@ ps_status ps_scan_refined(ps_ctx *c, double conw_r, int64_t n_lo, int64_t n_hi, 
     sf.fits = c->h_fits;
     sf.done.assign(static_cast<size_t>(nfits), 1);
     sf.fp64.assign(static_cast<size_t>(sf.nper), c->opt.form == PS_FORM_FP64 ? 1 : 0);
+    int64_t lit = c->opt.form == PS_FORM_FP64 ? c->timing.lit_facets : 0;
     st = refit_minimum(c, conw_r, sf, refit_rel, refit_halfwidth, true, &stt.refit_ms, &stt.fits_refit,
-                       &stt.evals, &stt.refit_rounds);
+                       &stt.evals, &stt.refit_rounds, &lit);
     if (st != PS_OK) return st;
     stt.evals_refit = stt.evals - stt.evals_complete;
     std::vector<ps_row> rows;
@@ -1174,6 +1184,7 @@ ps_status ps_scan_refined(ps_ctx *c, double conw_r, int64_t n_lo, int64_t n_hi, 
     c->timing.kernel_ms = stt.complete_ms + stt.refit_ms;
     c->timing.fits = nfits;
     c->timing.evals = stt.evals;
+    c->timing.lit_facets = lit;   // the FP64 form's
     c->timing.launches = static_cast<int32_t>(c->launch_total - launch0);
     stt.launches = c->timing.launches;
     if (stats) *stats = stt;
@@ -1357,7 +1368,7 @@ ps_status ps_pack_create(ps_ctx *const *ctxs, int32_t n, int32_t form, ps_pack *
     PSG_PACK_CUDA(k.get(), cudaMalloc(&k->d_objs, sizeof(psg::DevObject) * n));
     PSG_PACK_CUDA(k.get(), cudaMalloc(&k->d_cfgs, sizeof(psg::FitConfig) * n));
     PSG_PACK_CUDA(k.get(), cudaMalloc(&k->d_scratch, k->scratch_stride * k->slots * sizeof(double)));
-    PSG_PACK_CUDA(k.get(), cudaMalloc(&k->d_queue, sizeof(unsigned long long)));
+    PSG_PACK_CUDA(k.get(), cudaMalloc(&k->d_queue, 2 * sizeof(unsigned long long)));
     if (k->dsph_smem == psg::kBasisTensorWide)
         PSG_PACK_CUDA(k.get(), cudaMalloc(&k->d_alpha_g, static_cast<size_t>(c0->obj.mfit) * c0->obj.mfit *
                                                             k->slots * sizeof(double)));
@@ -1424,13 +1435,14 @@ ps_status pack_run(ps_pack *k, const double *conw_r, int64_t n_fits, const int32
     PSG_PACK_CUDA(k, cudaMemcpyAsync(k->d_pole, h_pole.data(), sizeof(int) * n_fits, cudaMemcpyHostToDevice, k->stream));
     PSG_PACK_CUDA(k, cudaMemcpyAsync(k->d_pidx, h_pidx.data(), sizeof(int64_t) * n_fits, cudaMemcpyHostToDevice,
                                      k->stream));
-    PSG_PACK_CUDA(k, cudaMemsetAsync(k->d_queue, 0, sizeof(unsigned long long), k->stream));
+    PSG_PACK_CUDA(k, cudaMemsetAsync(k->d_queue, 0, 2 * sizeof(unsigned long long), k->stream));
     psg::FitWork w{};
     w.n_lo = 1;
     w.nfits = n_fits;
     w.period_index = k->d_pidx;
     w.pole = k->d_pole;
     w.queue = k->d_queue;
+    w.lit = k->d_queue + 1;
     w.scratch = k->d_scratch;
     w.scratch_stride = k->scratch_stride;
     w.out = k->d_out;
@@ -1469,6 +1481,8 @@ ps_status pack_run(ps_pack *k, const double *conw_r, int64_t n_fits, const int32
     std::vector<float> traj_sorted(traj ? static_cast<size_t>(n_fits) * psg::kTrajFloats : 0);
     if (traj)
         PSG_PACK_CUDA(k, cudaMemcpyAsync(traj_sorted.data(), d_traj.p, traj_bytes, cudaMemcpyDeviceToHost, k->stream));
+    unsigned long long lit = 0;
+    PSG_PACK_CUDA(k, cudaMemcpyAsync(&lit, k->d_queue + 1, sizeof(lit), cudaMemcpyDeviceToHost, k->stream));
     PSG_PACK_CUDA(k, cudaStreamSynchronize(k->stream));
     float ms = 0;
     cudaEventElapsedTime(&ms, k->ev[0], k->ev[1]);
@@ -1492,6 +1506,7 @@ ps_status pack_run(ps_pack *k, const double *conw_r, int64_t n_fits, const int32
     k->timing.fits = n_fits;
     k->timing.evals = evals;
     k->timing.launches = 1;
+    k->timing.lit_facets = static_cast<int64_t>(lit);
     return PS_OK;
 }
 

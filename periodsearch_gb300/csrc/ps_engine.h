@@ -77,6 +77,9 @@ struct FitWork {
     double *state;
     const int64_t *state_slot;
     int resume;
+    // FP64 form, optional: every CTA adds its count of lit facet-point pairs
+    // (the facet law's and the shape contraction's work) when it ends
+    unsigned long long *lit;
 };
 
 // Learned early stop: features of a fit after kScreenIters LM iterations,

@@ -177,8 +177,15 @@ enum : int {
     M_PIV = 12,    // pivot broadcast of the solvers (2 doubles + status)
     M_RED = 16,    // 16 doubles of block-reduction scratch
     M_LM = 32,     // 4 doubles: lambda, ochisq, dev, iter_diff of the fit, broadcast from thread 0
-    M_WEXP = 36    // tensor-core path: exponent of the evaluation's W scale
+    M_WEXP = 36,   // tensor-core path: exponent of the evaluation's W scale
+    M_LIT = 37     // FP64 form: the CTA's count of lit facet-point pairs (an unsigned 64-bit integer)
 };
+
+// FP64 form: the CTA's lit facet-point counter in misc.
+__device__ inline unsigned long long *lit_counter(double *misc)
+{
+    return reinterpret_cast<unsigned long long *>(misc + M_LIT);
+}
 
 // Facet table of the tensor-core path, interleaved by facet pairs so that
 // the facet stage loads each pair's components as FP32x2 register pairs:
@@ -328,14 +335,31 @@ __device__ inline void facet_point_fp64(const DevObject &ob, Smem<PS_FORM_FP64> 
     const double e1 = pt[0], e2 = pt[1], e3 = pt[2];
     const double f1 = pt[3], f2 = pt[4], f3 = pt[5];
     uint16_t *idx = s.lidx + static_cast<size_t>(p) * wcols;
+    // The lit test in FP32 where it is decided beyond its rounding: the FP32
+    // dot products of the FP32-rounded unit vectors are within ~4e-7 of the
+    // FP64 ones, so outside a 1e-4 band (scaled by the direction's 1-norm)
+    // around kTinyMu the FP64 test gives the same answer; inside it the FP64
+    // test runs (on the FP64 unit, which the first pass then leaves alone).
+    const float e1f = static_cast<float>(e1), e2f = static_cast<float>(e2), e3f = static_cast<float>(e3);
+    const float f1f = static_cast<float>(f1), f2f = static_cast<float>(f2), f3f = static_cast<float>(f3);
+    const float band_e = 1e-4f * fmaxf(1.f, fabsf(e1f) + fabsf(e2f) + fabsf(e3f));
+    const float band_f = 1e-4f * fmaxf(1.f, fabsf(f1f) + fabsf(f2f) + fabsf(f3f));
+    const float tiny = static_cast<float>(kTinyMu);
     int n = 0;
     for (int i0 = 0; i0 < F; i0 += 32) {
         const int i = i0 + lane;
         bool lit = false;
         if (i < F) {
-            const double mu = e1 * ob.nx[i] + e2 * ob.ny[i] + e3 * ob.nz[i];
-            const double mu0 = f1 * ob.nx[i] + f2 * ob.ny[i] + f3 * ob.nz[i];
-            lit = mu > kTinyMu && mu0 > kTinyMu;
+            const float nxf = ob.nx_f[i], nyf = ob.ny_f[i], nzf = ob.nz_f[i];
+            const float muf = e1f * nxf + e2f * nyf + e3f * nzf;
+            const float mu0f = f1f * nxf + f2f * nyf + f3f * nzf;
+            if (muf > tiny + band_e && mu0f > tiny + band_f) {
+                lit = true;
+            } else if (!(muf < tiny - band_e || mu0f < tiny - band_f)) {
+                const double mu = e1 * ob.nx[i] + e2 * ob.ny[i] + e3 * ob.nz[i];
+                const double mu0 = f1 * ob.nx[i] + f2 * ob.ny[i] + f3 * ob.nz[i];
+                lit = mu > kTinyMu && mu0 > kTinyMu;
+            }
         }
         const unsigned m = __ballot_sync(0xffffffffu, lit);
         if (lit) idx[n + __popc(m & ((1u << lane) - 1u))] = static_cast<uint16_t>(i);
@@ -386,6 +410,7 @@ __device__ inline void facet_point_fp64(const DevObject &ob, Smem<PS_FORM_FP64> 
         rd[4] = dcl;
         rd[5] = dcls;
         s.nlit[p] = n;
+        atomicAdd(lit_counter(s.misc), static_cast<unsigned long long>(n));
     }
 }
 
@@ -2830,6 +2855,7 @@ __global__ void __launch_bounds__(threads_of<FORM>(), 1)
     if (L.dsph_smem == kBasisTensorWide) s.alpha = w.alpha_g + static_cast<size_t>(blockIdx.x) * w.alpha_stride;
     R *scratch = L.rels ? reinterpret_cast<R *>(smem + L.rels)
                         : reinterpret_cast<R *>(w.scratch + static_cast<size_t>(blockIdx.x) * w.scratch_stride);
+    if (FORM == PS_FORM_FP64 && threadIdx.x == 0) *lit_counter(s.misc) = 0;
     __shared__ long long next;
     for (;;) {
         if (threadIdx.x == 0) next = static_cast<long long>(atomicAdd(w.queue, 1ULL));
@@ -2852,6 +2878,7 @@ __global__ void __launch_bounds__(threads_of<FORM>(), 1)
         run_fit<FORM, KU>(ob, cfg, L, s, scratch, n, pole, w.out + f, w, f, tcs);
     }
     if constexpr (kTensor) tc_teardown(s, tcs, ob.nfac);
+    if (FORM == PS_FORM_FP64 && threadIdx.x == 0 && w.lit) atomicAdd(w.lit, *lit_counter(s.misc));
 }
 
 // FP64 fits, each spread over a thread-block cluster (evaluate_split): the
@@ -2870,6 +2897,7 @@ __global__ void __launch_bounds__(threads_of<PS_FORM_FP64>(), 1)
     TcState tcs;
     double *scratch = L.rels ? reinterpret_cast<double *>(smem + L.rels)
                              : w.scratch + static_cast<size_t>(blockIdx.x) * w.scratch_stride;
+    if (threadIdx.x == 0) *lit_counter(s.misc) = 0;
     __shared__ long long next;
     for (;;) {
         if (rank == 0 && threadIdx.x == 0) {
@@ -2891,6 +2919,7 @@ __global__ void __launch_bounds__(threads_of<PS_FORM_FP64>(), 1)
         }
         run_fit<PS_FORM_FP64, 1>(ob, cfg, L, s, scratch, n, pole, rank == 0 ? w.out + f : nullptr, w, f, tcs, true);
     }
+    if (threadIdx.x == 0 && w.lit) atomicAdd(w.lit, *lit_counter(s.misc));
 }
 
 template <int FORM, int KU>
@@ -2909,6 +2938,7 @@ __global__ void __launch_bounds__(threads_of<FORM>(), 1) eval_kernel(DevObject o
     TcState tcs;
     if constexpr (kTensor) tc_setup<NT, KU == 3>(ob, s, tcs);
     for (int i = threadIdx.x; i < ob.ma; i += NT) s.cg[i] = cg[i];
+    if (FORM == PS_FORM_FP64 && threadIdx.x == 0) *lit_counter(s.misc) = 0;
     // the wide tensor-core path accumulates straight into the output matrix
     if (L.dsph_smem == kBasisTensorWide) s.alpha = alpha;
     __syncthreads();

@@ -31,6 +31,7 @@ __global__ void __launch_bounds__(threads_of<FORM>(), 1) pack_kernel(FitWork w, 
     if constexpr (kTensor) tc_setup<NT, KU == 3>(s_ob, s, tcs);
     if (dsph_smem == kBasisTensorWide) s.alpha = w.alpha_g + static_cast<size_t>(blockIdx.x) * w.alpha_stride;
     R *scratch = reinterpret_cast<R *>(w.scratch + static_cast<size_t>(blockIdx.x) * w.scratch_stride);
+    if (FORM == PS_FORM_FP64 && threadIdx.x == 0) *lit_counter(s.misc) = 0;
     for (;;) {
         if (threadIdx.x == 0) next = static_cast<long long>(atomicAdd(w.queue, 1ULL));
         __syncthreads();
@@ -49,6 +50,7 @@ __global__ void __launch_bounds__(threads_of<FORM>(), 1) pack_kernel(FitWork w, 
         run_fit<FORM, KU>(s_ob, s_cfg, L, s, scratch, w.period_index[f], w.pole[f], w.out + f, w, f, tcs);
     }
     if constexpr (kTensor) tc_teardown(s, tcs, s_ob.nfac);
+    if (FORM == PS_FORM_FP64 && threadIdx.x == 0 && w.lit) atomicAdd(w.lit, *lit_counter(s.misc));
 }
 
 template <class Fn>
