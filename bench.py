@@ -27,23 +27,27 @@ value      fits of the window per second of device time of the step's
            fit-kernel launches (CUDA events on the engine's stream), the
            object resident in HBM; the plain FP64 scan of the SAME window is
            timed beside it (plain_fp64), and every step's best period is
-           compared with the FP64 scan's (validation.same_best_period), its
-           chi^2 there with the FP64 form's and with the CPU oracle's (the
-           reference's FP64 algorithm) at that period;
+           compared with the FP64 scan's (validation.same_best_period) and
+           its chi^2 there with the FP64 form's;
 e2e        the same steps through the C ABI with host buffers: ps_prepare
            (host -> device copy of the tables), the scan (rows back to the
            host) and ps_destroy per step, wall clock;
 roofline   the kernel with the largest share of the step's device time:
-           algorithmic FLOP of its launches (2 N F C + 60 N F + N m(m+1) +
-           9 F C per evaluation, 2 m^3 per solve) over their time, against
-           the measured dense BF16 rate (mixed kernel: its contractions run
-           on the tensor cores) or the FP64 FMA ceiling measured live (FP64
-           kernel; MEASURED_PEAKS.json has no FP64 figure); every kernel's
-           share in kernels;
+           algorithmic FLOP of its launches over their time (mixed kernel:
+           the dense count 2 N F C + 60 N F + N m(m+1) + 9 F C per
+           evaluation and 2 m^3 per solve, against the measured dense BF16
+           rate, its contractions running on the tensor cores; FP64 kernel:
+           the reference's lit-facet work, flops_fp64, against the FP64 FMA
+           ceiling measured live, MEASURED_PEAKS.json having no FP64
+           figure); every kernel's share in kernels;
 cpu_baseline  the reference's own CPU app (oracle/_ref/ps_ref, built from
            its sources) on all host cores, one process per core, each
            fitting one trial period of the window (10 fits) through the
-           reference's resume path.
+           reference's resume path.  The same leg runs the CPU oracle (the
+           reference's FP64 algorithm) as the checker: the headline's row
+           at its best period (validation.vs_oracle_at_best: relative error
+           in rms, chi^2 and the fitted period, lambda/beta differences) and
+           c2's rows at five periods of its window (c2.vs_oracle).
 
 `--impl reference` times that CPU app alone as the reference arm.  Between
 timed steps a 256 MiB buffer is rewritten to flush the 126 MB L2.
@@ -417,6 +421,7 @@ def c2_measurement(periods: int, local: int, peaks: dict) -> dict:
         path = Path(td) / "period_search_in"
         obj = synth.write_object(path, "c2")
         data = read_input(path)
+        text = path.read_text()
     out = {"workload": "c2: c1 data (Ndata 980), L=M=8 (81 coefficients), 512 facets, 50 LM iterations"}
     with Engine(data, device=local, form=PS_FORM_MIXED) as eng:
         info = eng.info
@@ -453,6 +458,12 @@ def c2_measurement(periods: int, local: int, peaks: dict) -> dict:
                 "tensor_over_fp64": out["mixed_tensor_fits_per_s"] / out["fp64_fits_per_s"],
                 "rms_rel_vs_fp64_median": float(np.median(np.abs(rel))), "rms_rel_vs_fp64_max": float(np.abs(rel).max()),
                 "fp64_periods": n64})
+    # for the CPU-baseline leg's oracle check: the tensor form's best period
+    # and four more spread over the window
+    best = lo + int(np.argmin(rows_tc["rms"]))
+    periods = sorted({best, *(lo + (hi - lo) * k // 4 for k in range(4))})
+    out["_check"] = {"text": text, "conw_r": conw_r, "periods": periods, "best": best, "ndata": info.ndata,
+                     "rows": {n: rows_tc[n - lo] for n in periods}}
     return out
 
 
@@ -522,17 +533,46 @@ class Scanner:
                       "fp64_evals": st["evals_refit"], "stats": st}
 
 
-def _oracle_at(path: Path, conw_r: float, n: int) -> dict:
-    """The CPU oracle's row at period index n (10 poles, one thread each)."""
+def oracle_rows(path: Path, conw_r: float, periods: list[int], cores: int, ndata: int) -> dict:
+    """The CPU oracle's rows at the given period indices (all ten poles of
+    each, the best pole kept; chi^2 = rms^2 Ndata as in the output rows), on
+    `cores` threads.  The checker of the CPU-baseline leg."""
     sys.path.insert(0, str(ROOT / "tests"))
     import oracle_binding
 
-    probs = [oracle_binding.OracleProblem(path) for _ in range(10)]
+    oracle_binding.build_oracle()
+    jobs = [(n, m) for n in periods for m in range(1, 11)]
+    nw = max(1, min(cores, len(jobs)))
+    probs = [oracle_binding.OracleProblem(path) for _ in range(nw)]
     for p in probs:
         p.setup(conw_r)
-    with ThreadPoolExecutor(10) as ex:
-        fits = list(ex.map(lambda m: probs[m - 1].fit_n(n, m), range(1, 11)))
-    return {"rms": min(f["dev"] for f in fits)}
+    fits = {}
+
+    def work(w):
+        for k in range(w, len(jobs), nw):
+            fits[jobs[k]] = probs[w].fit_n(*jobs[k])
+
+    with ThreadPoolExecutor(nw) as ex:
+        list(ex.map(work, range(nw)))
+    for p in probs:
+        p.close()
+    out = {}
+    for n in periods:
+        f = min((fits[(n, m)] for m in range(1, 11)), key=lambda f: f["dev"])
+        out[n] = {"rms": f["dev"], "chi2": f["dev"] ** 2 * ndata, "period_h": 24.0 * f["prd"], "lambda_deg": f["la"],
+                  "beta_deg": f["be"]}
+    return out
+
+
+def versus_oracle(row, orc: dict) -> dict:
+    """Relative errors of an engine row against the oracle's row (rms, chi^2,
+    the fitted period) and the pole's angular differences in degrees."""
+    dl = abs(float(row["lambda_deg"]) - orc["lambda_deg"]) % 360.0
+    return {"rms_rel": abs(float(row["rms"]) - orc["rms"]) / orc["rms"],
+            "chi2_rel": abs(float(row["chi2"]) - orc["chi2"]) / orc["chi2"],
+            "period_rel": abs(float(row["period_h"]) - orc["period_h"]) / orc["period_h"],
+            "lambda_deg_diff": min(dl, 360.0 - dl),
+            "beta_deg_diff": abs(float(row["beta_deg"]) - orc["beta_deg"])}
 
 
 def run_engine_arm(args):
@@ -650,14 +690,12 @@ def run_engine_arm(args):
                                  "peak_source": "FP64 FMA ceiling measured live by ps_device_fma_peaks"}}
             rows_c = steps[-1][0]
             bc = best_steps[-1]
-            orc = _oracle_at(path, conw_r, bc)
             valid.update({
                 "best_index_fp64": b64, "same_best_period": all(b == b64 for b in best_steps),
                 "best_period_h": float(rows_c["period_h"][bc - lo]),
                 "chi2_rel_at_best_vs_fp64_form": float(abs(rows_c["chi2"][bc - lo] - r64["chi2"][b64 - lo]) /
                                                        r64["chi2"][b64 - lo]),
-                "rms_rel_at_best_vs_oracle": float(abs(rows_c["rms"][bc - lo] - orc["rms"]) / orc["rms"]),
-                "oracle_rms_at_best": orc["rms"], "rms_at_best": float(rows_c["rms"][bc - lo])})
+                "rms_at_best": float(rows_c["rms"][bc - lo])})
             # the other forms on the same window
             others = {}
             for f in ("learned", "refined", "mixed"):
@@ -729,10 +767,29 @@ def run_engine_arm(args):
                     "seconds": t_full, "fits_per_s": n_max * 10 / t_full, "best_index": b,
                     "best_period_h": float(rows_f["period_h"][b - 1]), "truth_period_h": truth["period_h"]}
         cb = None
+        c2_check = c2.pop("_check", None) if c2 else None
         if not args.no_cpu_baseline and world == 1:
             cores = os.cpu_count() or 1
             cb = cpu_rate(path, text, [lo + (i * 7919) % (hi - lo + 1) for i in range(cores)], cores)
             cb.pop("wall_s", None)
+            # the CPU oracle as the checker: the headline's row at its best
+            # period, and c2's rows at five periods of its window
+            bc = best_steps[-1]
+            orc = oracle_rows(path, conw_r, [bc], cores, info.ndata)[bc]
+            valid["vs_oracle_at_best"] = {"period_index": bc, "oracle": orc,
+                                          **versus_oracle(steps[-1][0][bc - lo], orc)}
+            if c2_check:
+                with tempfile.TemporaryDirectory() as td:
+                    p2 = Path(td) / "period_search_in"
+                    p2.write_text(c2_check["text"])
+                    o2 = oracle_rows(p2, c2_check["conw_r"], c2_check["periods"], cores, c2_check["ndata"])
+                per = [{"period_index": n, **versus_oracle(c2_check["rows"][n], o2[n])} for n in c2_check["periods"]]
+                c2["vs_oracle"] = {"periods": per, "best_index": c2_check["best"],
+                                   "rms_rel_max": max(x["rms_rel"] for x in per),
+                                   "chi2_rel_max": max(x["chi2_rel"] for x in per),
+                                   "period_rel_max": max(x["period_rel"] for x in per),
+                                   "lambda_deg_diff_max": max(x["lambda_deg_diff"] for x in per),
+                                   "beta_deg_diff_max": max(x["beta_deg_diff"] for x in per)}
         line = {"metric": METRIC, "value": value, "unit": "fits/s", "n_gpus": world, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": 1000 * dev_all / args.steps, "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None,
