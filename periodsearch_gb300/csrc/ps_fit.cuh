@@ -1451,11 +1451,22 @@ __device__ void evaluate(const DevObject &ob, const FitConfig &cfg, const SlotLa
     double asum = 0;
     for (int i = tid; i < F; i += NT) {
         double g = 0;
-        for (int q = 0; q < ob.npairs; q++) {
-            int m = ob.pair_m[q], n = ob.pair_n[q];
-            double fsum = a[n] * ob.fc[m * F + i];
-            if (m != 0) fsum = fsum + a[n + 1] * ob.fs[m * F + i];
-            g = g + ob.pleg[q * F + i] * fsum;
+        if constexpr (kFP64) {
+            for (int q = 0; q < ob.npairs; q++) {
+                int m = ob.pair_m[q], n = ob.pair_n[q];
+                double fsum = a[n] * ob.fc[m * F + i];
+                if (m != 0) fsum = fsum + a[n + 1] * ob.fs[m * F + i];
+                g = g + ob.pleg[q * F + i] * fsum;
+            }
+        } else {
+            // the same sum as the dot product of the facet's FP64 basis row
+            // (Dsph[i][n] = P_l^m cos(m phi_i), Dsph[i][n + 1] = P_l^m
+            // sin(m phi_i)) with the shape coefficients: independent loads
+            // instead of a pair-index chain per term; it rounds differently
+            // from curv.c's order by about 1e-16
+            const double *drow = ob.dsph + static_cast<size_t>(i) * ob.ncoef;
+#pragma unroll 7
+            for (int k = 0; k < ob.ncoef; k++) g = fma(drow[k], a[k], g);
         }
         g = exp(g);
         double ar = ob.darea[i] * g;
