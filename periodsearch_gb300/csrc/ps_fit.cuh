@@ -366,13 +366,12 @@ __device__ inline void facet_point_fp64(const DevObject &ob, Smem<PS_FORM_FP64> 
         n += __popc(m);
     }
     __syncwarp();
-    double de[9], de0[9];
-#pragma unroll
-    for (int k = 0; k < 9; k++) {
-        de[k] = pt[6 + k];
-        de0[k] = pt[15 + k];
-    }
-    double br = 0, r0 = 0, r1 = 0, r2 = 0, dcl = 0, dcls = 0;
+    // The rotation derivatives sum_i Area_i (dsmu_i (n_i . D_k) + dsmu0_i
+    // (n_i . E_k)) (bright.c:87-104; D_k, E_k: the derivative directions of
+    // the Earth and Sun vectors) are D_k . U + E_k . V with U = sum Area
+    // dsmu n and V = sum Area dsmu0 n: the law accumulates U and V, the six
+    // dot products run once per point.
+    double br = 0, ux = 0, uy = 0, uz = 0, vx = 0, vy = 0, vz = 0, dcl = 0, dcls = 0;
     double *Wp = s.W + static_cast<size_t>(p) * wcols;
     for (int j = lane; j < n; j += 32) {
         const int i = idx[j];
@@ -383,30 +382,33 @@ __device__ inline void facet_point_fp64(const DevObject &ob, Smem<PS_FORM_FP64> 
         const LitTerms<double, PS_FORM_FP64> lt(mu, mu0, cl, cls);
         br = br + ar * lt.sv;
         Wp[j] = ob.darea[i] * lt.sv * s.gv[i];
-        const double s0 = nx * de[0] + ny * de[3] + nz * de[6];
-        const double s1 = nx * de[1] + ny * de[4] + nz * de[7];
-        const double s2 = nx * de[2] + ny * de[5] + nz * de[8];
-        const double t0v = nx * de0[0] + ny * de0[3] + nz * de0[6];
-        const double t1v = nx * de0[1] + ny * de0[4] + nz * de0[7];
-        const double t2v = nx * de0[2] + ny * de0[5] + nz * de0[8];
-        r0 = r0 + ar * (lt.dsmu * s0 + lt.dsmu0 * t0v);
-        r1 = r1 + ar * (lt.dsmu * s1 + lt.dsmu0 * t1v);
-        r2 = r2 + ar * (lt.dsmu * s2 + lt.dsmu0 * t2v);
+        const double cu = ar * lt.dsmu, cv = ar * lt.dsmu0;
+        ux = ux + cu * nx;
+        uy = uy + cu * ny;
+        uz = uz + cu * nz;
+        vx = vx + cv * nx;
+        vy = vy + cv * ny;
+        vz = vz + cv * nz;
         dcl = dcl + mu * mu0 * ar;
         dcls = dcls + ar * lt.dcls_w;
     }
     br = warp_sum(br);
-    r0 = warp_sum(r0);
-    r1 = warp_sum(r1);
-    r2 = warp_sum(r2);
+    ux = warp_sum(ux);
+    uy = warp_sum(uy);
+    uz = warp_sum(uz);
+    vx = warp_sum(vx);
+    vy = warp_sum(vy);
+    vz = warp_sum(vz);
     dcl = warp_sum(dcl);
     dcls = warp_sum(dcls);
     if (lane == 0) {
+        // D_k = (de[k], de[3 + k], de[6 + k]), E_k likewise from de0
+        const double *de = pt + 6, *de0 = pt + 15;
         double *rd = s.red + p * kRedStride;
         rd[0] = br;
-        rd[1] = r0;
-        rd[2] = r1;
-        rd[3] = r2;
+#pragma unroll
+        for (int k = 0; k < 3; k++)
+            rd[1 + k] = de[k] * ux + de[3 + k] * uy + de[6 + k] * uz + de0[k] * vx + de0[3 + k] * vy + de0[6 + k] * vz;
         rd[4] = dcl;
         rd[5] = dcls;
         s.nlit[p] = n;
