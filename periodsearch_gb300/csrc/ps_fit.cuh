@@ -293,8 +293,10 @@ __device__ inline double contract_fp64(const S &s, const double *ds, int p, int 
 }
 
 // Lit-facet terms of the Lommel-Seeliger + Lambert law (bright.c:65-74,
-// 116-117).  The FP64 form divides as the reference does; the mixed form
-// multiplies by one approximate reciprocal.
+// 116-117).  The reference divides four times by mu + mu0; both forms
+// multiply by one reciprocal instead (the FP64 form's correctly rounded, so
+// each quotient is within an ulp of the reference's; the mixed form's
+// approximate).
 template <class R, int FORM>
 struct LitTerms {
     R sv, dsmu, dsmu0, dcls_w;  // s, ds/dmu, ds/dmu0, mu*mu0/(mu+mu0)
@@ -302,11 +304,12 @@ struct LitTerms {
     {
         const R dnom = mu + mu0;
         if constexpr (FORM == PS_FORM_FP64) {
-            sv = mu * mu0 * (cl + cls / dnom);
-            const R q0 = mu0 / dnom, q1 = mu / dnom;
+            const R r = 1.0 / dnom;
+            sv = mu * mu0 * (cl + cls * r);
+            const R q0 = mu0 * r, q1 = mu * r;
             dsmu = cls * (q0 * q0) + cl * mu0;
             dsmu0 = cls * (q1 * q1) + cl * mu;
-            dcls_w = mu * mu0 / dnom;
+            dcls_w = mu * mu0 * r;
         } else {
             R r;
             asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(dnom));   // ~1 ulp: the mixed form's budget
