@@ -124,13 +124,13 @@ struct SlotLayout {
 };
 
 
-constexpr int kThreads = 256;   // threads of an FP64-form fit slot
+constexpr int kThreads = 384;   // threads of an FP64-form fit slot
 // Threads of a fit slot: the FP64 form is register-limited to 256; the mixed
 // form runs 512 (16 warps) to hide FP32/shared-memory latency.
 template <int FORM>
 PSG_HD constexpr int threads_of()
 {
-    return FORM == PS_FORM_MIXED ? 512 : 256;
+    return FORM == PS_FORM_MIXED ? 512 : 384;
 }
 constexpr int kPointStride = 33;   // reals of per-point set-up (odd: a warp with one point per lane hits 32 banks)
 constexpr int kRedStride = 8;      // doubles of per-point facet sums
