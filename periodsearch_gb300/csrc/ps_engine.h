@@ -125,8 +125,9 @@ struct SlotLayout {
 
 
 constexpr int kThreads = 384;   // threads of an FP64-form fit slot
-// Threads of a fit slot: the FP64 form is register-limited to 256; the mixed
-// form runs 512 (16 warps) to hide FP32/shared-memory latency.
+// Threads of a fit slot: the FP64 form runs 384 (12 warps at up to 170
+// registers: more warps to hide its FP64 latency than 256, 512 would spill);
+// the mixed form runs 512 (16 warps) to hide FP32/shared-memory latency.
 template <int FORM>
 PSG_HD constexpr int threads_of()
 {
