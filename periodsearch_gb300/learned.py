@@ -362,8 +362,12 @@ def main():
     ap.add_argument("--device", type=int, default=0)
     ap.add_argument("--processes", type=int, default=16)
     ap.add_argument("--dump", default="", help="save the collected windows' trajectories (npz) here")
+    ap.add_argument("--screen-iters", type=int, default=SCREEN_ITERS,
+                    help="LM iterations before the prediction (a multiple of 4)")
     args = ap.parse_args()
-    K = SCREEN_ITERS
+    K = args.screen_iters
+    if K < 4 or K % 4:
+        ap.error("--screen-iters must be a positive multiple of 4")
     # every object is generated before the GPU is touched (spawned workers)
     pop_train = _population("c5", args.train_objects, 60000, args.processes)
     pop_eval = _population("c5", args.eval_objects, 50000, args.processes)
@@ -416,7 +420,7 @@ def main():
             "loss_first": float(hist[0]), "loss_last": float(hist[-1]),
             "val_rmse_log": float(np.sqrt(np.mean((pv - yv) ** 2))),
             "val_rmse_log_without_network": float(np.sqrt(np.mean(yv ** 2))),
-            "cascade": {**DEFAULT_CASCADE, "margin": m_net}, "margin_without_network": m_zero,
+            "cascade": {**DEFAULT_CASCADE, "screen_iters": K, "margin": m_net}, "margin_without_network": m_zero,
             "windows": {"train_population": len(w_pop), "train_structured": len(w_st),
                         "eval_population": len(w_pop_ev), "eval_structured": len(w_st_ev)},
             "evaluation": ev, "collect_s": t1 - t0, "collect_kernel_s": (ms_a + ms_b + ms_c + ms_d) / 1e3,
