@@ -195,7 +195,10 @@ PSG_HD inline SlotLayout make_layout(int form, int ma, int mfit, int nfac, int n
     L.areaR = form == PS_FORM_MIXED ? take(nfac * rs) : L.area;
     L.gvR = form == PS_FORM_MIXED ? take(nfac * rs) : L.gv;
     // the tensor-core path writes W straight into the MMA operand
-    L.W = take(basis_on_tensor(dsph_smem) ? 0 : static_cast<size_t>(P) * L.wcols * rs);
+    // (FP64 form: room for the accumulation weights of a tile, [P][mfit],
+    // and a staged tile of rows and model values, [P][ma] + [P], behind them)
+    const int wrow = form == PS_FORM_FP64 && mfit + ma + 1 > L.wcols ? mfit + ma + 1 : L.wcols;
+    L.W = take(basis_on_tensor(dsph_smem) ? 0 : static_cast<size_t>(P) * wrow * rs);
     L.J = take(static_cast<size_t>(P) * ma * rs);
     L.pt = take(static_cast<size_t>(P) * kPointStride * rs);
     L.ym = take(P * d);

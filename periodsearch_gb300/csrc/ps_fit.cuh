@@ -491,7 +491,9 @@ __device__ inline void flush_partials(double *M, double *bv, int mf, float (&acc
 
 template <int FORM>
 __device__ void accumulate_tile(const DevObject &ob, Smem<FORM> &s, double *M, double *bv, int np, int q0pt,
-                                bool conv, double conv_sig, float (&accA)[kAccPerThread], float &accB)
+                                bool conv, double conv_sig, float (&accA)[kAccPerThread], float &accB,
+                                const double *Jrows = nullptr, const double *ymv = nullptr, int part = 0,
+                                int parts = 1)
 {
     using R = typename RealOf<FORM>::T;
     constexpr int NT = threads_of<FORM>();
@@ -499,12 +501,18 @@ __device__ void accumulate_tile(const DevObject &ob, Smem<FORM> &s, double *M, d
     const int ma = ob.ma, mf = ob.mfit;
     R *wt = s.W;  // [np][mf], reuses the facet-weight tile
     if constexpr (FORM == PS_FORM_FP64) {
+        // FP64 form: the tile's rows and model values (Jrows, ymv: another
+        // CTA's tile staged here, by default the CTA's own), and of the
+        // normal matrix only the elements e = part NT + tid (mod parts NT);
+        // chi^2 is summed whole
+        if (!Jrows) Jrows = s.J;
+        if (!ymv) ymv = s.ym;
         for (int e = tid; e < np * mf; e += NT) {
             const int p = e / mf, j = e - p * mf;
             const int q = q0pt + p;
             const double sig2i = conv ? 1 / (conv_sig * conv_sig) : ob.sig2i[q];
             const double wg = ob.weight[q];
-            wt[p * mf + j] = s.J[p * ma + ob.free_list[j]] * sig2i * wg;
+            wt[p * mf + j] = Jrows[p * ma + ob.free_list[j]] * sig2i * wg;
         }
     } else {
         // per point: FP32 weight sig2i*w and residual; chi^2 of the tile
@@ -534,19 +542,19 @@ __device__ void accumulate_tile(const DevObject &ob, Smem<FORM> &s, double *M, d
     __syncthreads();
     const int ntri = mf * (mf + 1) / 2;
     if constexpr (FORM == PS_FORM_FP64) {
-        for (int e = tid; e < ntri; e += NT) {
+        for (int e = part * NT + tid; e < ntri; e += parts * NT) {
             const int j = tri_row(e);
             const int k = e - j * (j + 1) / 2;
             const int lk = ob.free_list[k];
             double acc = M[j * mf + k];
-            for (int p = 0; p < np; p++) acc = acc + wt[p * mf + j] * s.J[p * ma + lk];
+            for (int p = 0; p < np; p++) acc = acc + wt[p * mf + j] * Jrows[p * ma + lk];
             M[j * mf + k] = acc;
         }
-        for (int j = tid; j < mf; j += NT) {
+        for (int j = part * NT + tid; j < mf; j += parts * NT) {
             double acc = bv[j];
             for (int p = 0; p < np; p++) {
                 const double y = conv ? 0.0 : ob.bright[q0pt + p];
-                acc = acc + (y - s.ym[p]) * wt[p * mf + j];
+                acc = acc + (y - ymv[p]) * wt[p * mf + j];
             }
             bv[j] = acc;
         }
@@ -571,12 +579,13 @@ __device__ void accumulate_tile(const DevObject &ob, Smem<FORM> &s, double *M, d
         }
     }
     if (FORM == PS_FORM_FP64 && tid == NT - 1) {
+        const double *yv = ymv ? ymv : s.ym;
         double c2 = s.misc[M_CHISQ];
         for (int p = 0; p < np; p++) {
             const int q = q0pt + p;
             const double sig2i = conv ? 1 / (conv_sig * conv_sig) : ob.sig2i[q];
             const double y = conv ? 0.0 : ob.bright[q];
-            const double dy = y - s.ym[p];
+            const double dy = y - yv[p];
             c2 = c2 + dy * dy * sig2i * ob.weight[q];
         }
         s.misc[M_CHISQ] = c2;
@@ -2022,15 +2031,15 @@ __device__ void evaluate(const DevObject &ob, const FitConfig &cfg, const SlotLa
 // One fit's point tiles are dealt round-robin to the cluster's CTAs, which
 // compute their tiles' model rows (point set-up, facet stage, shape
 // contraction, the remaining columns) at the same time; after each round
-// the leader (rank 0) takes the round's tiles in data order -- its own from
-// its shared memory, the others' through distributed shared memory -- and
-// runs everything that sums over points: the relative lightcurves' sums and
-// parked rows, their second pass, the alpha/beta/chi^2 accumulation and the
-// convexity rows.  Every sum therefore runs in the same order as in the
-// single-CTA FP64 form, and the split fit is bit-identical to it.  The
-// leader then copies the normal matrix, beta and the scalars into every
-// CTA, so that all of them take the same LM decisions and keep the same
-// control flow (and the same sequence of cluster barriers).
+// every CTA takes the round's tiles in data order -- its own from its shared
+// memory, the others' through distributed shared memory -- and runs what
+// sums over points: the relative lightcurves' sums, parked rows and second
+// pass, and chi^2 in full, the normal matrix and beta for its share of the
+// elements only.  Every sum therefore runs in the same order as in the
+// single-CTA FP64 form, and the split fit is bit-identical to it.  Every
+// CTA computes the convexity rows; then each copies its share of the matrix
+// into the others, so that all of them take the same LM decisions and keep
+// the same control flow (and the same sequence of cluster barriers).
 // ---------------------------------------------------------------------------
 constexpr int kMaxSplit = 8;
 
@@ -2151,11 +2160,19 @@ __device__ void evaluate_split(const DevObject &ob, const FitConfig &cfg, const 
         __syncthreads();
     };
 
-    // the leader's part of a tile (mrqcof.c:51-136): sums over points in data order
-    auto consume_tile = [&](int lc, int t0, int np) {
+    // A tile's sums (mrqcof.c:51-136), over points in data order, on every
+    // CTA: the relative lightcurves' sums and rows and chi^2 in full, of the
+    // normal matrix only the CTA's share of the elements (accumulate_tile's
+    // part).  Jt, yt: the tile's rows and model values (the CTA's own tile,
+    // or another CTA's staged in Jst/ymst); the second pass stages its
+    // renormalised rows there too, so that s.J, which the other CTAs read
+    // during the round, stays as computed.
+    double *Jst = s.W + static_cast<size_t>(P) * mf, *ymst = Jst + static_cast<size_t>(P) * ma;
+    auto consume_tile = [&](int lc, int t0, int np, const double *Jt, const double *yt) {
         const int start = ob.lc_start[lc], npts = ob.lc_npts[lc];
         if (!ob.lc_rel[lc]) {
-            accumulate_tile<PS_FORM_FP64>(ob, s, M, bv, np, start + t0, false, conv_sig, accA, accB);
+            accumulate_tile<PS_FORM_FP64>(ob, s, M, bv, np, start + t0, false, conv_sig, accA, accB, Jt, yt, rank,
+                                          cs);
             return;
         }
         if (t0 == 0) {
@@ -2166,17 +2183,17 @@ __device__ void evaluate_split(const DevObject &ob, const FitConfig &cfg, const 
         double *dst = scratch + static_cast<size_t>(t0) * RW;
         for (int e = tid; e < np * ma; e += NT) {
             int p = e / ma, l = e - p * ma;
-            dst[static_cast<size_t>(p) * RW + l] = s.J[e];
+            dst[static_cast<size_t>(p) * RW + l] = Jt[e];
         }
-        if (tid < np) dst[static_cast<size_t>(tid) * RW + ma] = s.ym[tid];
+        if (tid < np) dst[static_cast<size_t>(tid) * RW + ma] = yt[tid];
         for (int l = tid; l < ma; l += NT) {
             double d = s.dave[l];
-            for (int p = 0; p < np; p++) d = d + s.J[p * ma + l];
+            for (int p = 0; p < np; p++) d = d + Jt[p * ma + l];
             s.dave[l] = d;
         }
         if (tid == 0) {
             double av = s.misc[M_AVE];
-            for (int p = 0; p < np; p++) av = av + s.ym[p];
+            for (int p = 0; p < np; p++) av = av + yt[p];
             s.misc[M_AVE] = av;
         }
         __syncthreads();
@@ -2188,22 +2205,22 @@ __device__ void evaluate_split(const DevObject &ob, const FitConfig &cfg, const 
             const double *src = scratch + static_cast<size_t>(u0) * RW;
             if (tid < nq) {
                 const int q = start + u0 + tid;
-                const double yt = src[static_cast<size_t>(tid) * RW + ma];
+                const double ytv = src[static_cast<size_t>(tid) * RW + ma];
                 const double coef = ob.sig[q] * npts / ave;
-                s.ym[tid] = coef * yt;
+                ymst[tid] = coef * ytv;
             }
-            __syncthreads();
             for (int e = tid; e < nq * ma; e += NT) {
                 const int p = e / ma, l = e - p * ma;
                 const double v = src[static_cast<size_t>(p) * RW + l];
                 const int q = start + u0 + p;
                 const double coef = ob.sig[q] * npts / ave;
-                const double yt = src[static_cast<size_t>(p) * RW + ma];
-                const double out = coef * (v - yt * s.dave[l] / ave);
-                s.J[e] = (l == 0) ? 0.0 : out;
+                const double ytv = src[static_cast<size_t>(p) * RW + ma];
+                const double out = coef * (v - ytv * s.dave[l] / ave);
+                Jst[e] = (l == 0) ? 0.0 : out;
             }
             __syncthreads();
-            accumulate_tile<PS_FORM_FP64>(ob, s, M, bv, nq, start + u0, false, conv_sig, accA, accB);
+            accumulate_tile<PS_FORM_FP64>(ob, s, M, bv, nq, start + u0, false, conv_sig, accA, accB, Jst, ymst, rank,
+                                          cs);
         }
     };
 
@@ -2212,18 +2229,19 @@ __device__ void evaluate_split(const DevObject &ob, const FitConfig &cfg, const 
     int nround = 0;
     auto flush_round = [&]() {
         cl.sync();   // every CTA's tile of the round is in its shared memory
-        if (rank == 0) {
-            for (int k = 0; k < nround; k++) {
-                if (k > 0) {
-                    // the rows of rank k's tile, read through distributed shared memory
-                    const double *rJ = cl.map_shared_rank(s.J, k);
-                    const double *rY = cl.map_shared_rank(s.ym, k);
-                    for (int e = tid; e < rnp[k] * ma; e += NT) s.J[e] = rJ[e];
-                    if (tid < rnp[k]) s.ym[tid] = rY[tid];
-                    __syncthreads();
-                }
-                consume_tile(rlc[k], rt0[k], rnp[k]);
+        for (int k = 0; k < nround; k++) {
+            const double *Jt = s.J, *yt = s.ym;
+            if (k != rank) {
+                // rank k's tile, read through distributed shared memory
+                const double *rJ = cl.map_shared_rank(s.J, k);
+                const double *rY = cl.map_shared_rank(s.ym, k);
+                for (int e = tid; e < rnp[k] * ma; e += NT) Jst[e] = rJ[e];
+                if (tid < rnp[k]) ymst[tid] = rY[tid];
+                __syncthreads();
+                Jt = Jst;
+                yt = ymst;
             }
+            consume_tile(rlc[k], rt0[k], rnp[k], Jt, yt);
         }
         cl.sync();   // the round's tile buffers are free again
         nround = 0;
@@ -2241,31 +2259,37 @@ __device__ void evaluate_split(const DevObject &ob, const FitConfig &cfg, const 
         }
     }
     if (nround > 0) flush_round();
-    // convexity rows (conv.c:12-29) on the leader
-    if (rank == 0) {
+    // convexity rows (conv.c:12-29) on every CTA, each accumulating its share
+    {
         const int lc = ob.n_lc - 1, start = ob.lc_start[lc], npts = ob.lc_npts[lc];
         for (int t0 = 0; t0 < npts; t0 += P) {
             const int np = min(P, npts - t0);
             compute_tile(lc, t0, np, true);
-            accumulate_tile<PS_FORM_FP64>(ob, s, M, bv, np, start + t0, true, conv_sig, accA, accB);
+            accumulate_tile<PS_FORM_FP64>(ob, s, M, bv, np, start + t0, true, conv_sig, accA, accB, s.J, s.ym, rank,
+                                          cs);
         }
-        // mirror the lower triangle (mrqcof.c:139-141)
-        for (int e = tid; e < mf * mf; e += NT) {
-            const int j = e / mf, k = e - j * mf;
-            if (k > j) M[e] = M[k * mf + j];
-        }
-        __syncthreads();
-        // every CTA gets the result: the same solve and decisions everywhere
-        for (int r = 1; r < cs; r++) {
+    }
+    // every CTA copies its share of the lower triangle and of bv into the
+    // others, then mirrors (mrqcof.c:139-141): the same matrix, solve and
+    // decisions everywhere
+    {
+        const int ntri = mf * (mf + 1) / 2;
+        for (int r = 0; r < cs; r++) {
+            if (r == rank) continue;
             double *rM = cl.map_shared_rank(M, r), *rb = cl.map_shared_rank(bv, r);
-            double *rmisc = cl.map_shared_rank(s.misc, r);
-            for (int e = tid; e < mf * mf; e += NT) rM[e] = M[e];
-            for (int j = tid; j < mf; j += NT) rb[j] = bv[j];
-            if (tid < 3) rmisc[M_CHK + tid] = s.misc[M_CHK + tid];
-            if (tid == 0) rmisc[M_CHISQ] = s.misc[M_CHISQ];
+            for (int e = rank * NT + tid; e < ntri; e += cs * NT) {
+                const int j = tri_row(e), k = e - j * (j + 1) / 2;
+                rM[j * mf + k] = M[j * mf + k];
+            }
+            for (int j = rank * NT + tid; j < mf; j += cs * NT) rb[j] = bv[j];
         }
     }
     cl.sync();
+    for (int e = tid; e < mf * mf; e += NT) {
+        const int j = e / mf, k = e - j * mf;
+        if (k > j) M[e] = M[k * mf + j];
+    }
+    __syncthreads();
 }
 
 // Gauss-Jordan elimination with full pivoting on A (n x n, row-major in
