@@ -1,8 +1,9 @@
 """FP64 fits spread over a thread-block cluster (evaluate_split): when a
 launch has fewer FP64 fits than half (a quarter) of the fit slots, each fit
-runs on a cluster of 2 (4) CTAs whose leader sums every quantity over the
-points in data order, so the fits are bit-identical to the one-CTA kernel's
--- and so to the FP64 form's parity with the CPU oracle."""
+runs on a cluster of 2 (4) CTAs, every one of which sums over the points in
+data order (each its share of the normal matrix), so the fits are
+bit-identical to the one-CTA kernel's -- and so to the FP64 form's parity
+with the CPU oracle."""
 from __future__ import annotations
 
 import numpy as np
@@ -77,3 +78,34 @@ def test_refined_scan_with_split_refits(engine_lib):
     assert st["fits_refit"] >= 30
     assert rows["rms"][b] == full["rms"][b]
     assert int(np.argmin(full["rms"])) == b
+
+
+def test_lit_facet_count(engine_lib):
+    """ps_timing.lit_facets: the FP64 kernels' count of lit (point, facet)
+    pairs.  A fraction of all pairs in the FP64 form, the same whether the
+    fits run one CTA each or over 4-CTA clusters (three quarter-slot batches
+    against their union), and 0 for the mixed form."""
+    from periodsearch_gb300 import Engine, PS_FORM_FP64, PS_FORM_MIXED, read_input
+
+    data = read_input(_path("c1"))
+    with Engine(data, form=PS_FORM_FP64) as eng:
+        conw_r = eng.info.conw_r0
+        q = eng.info.slots // 4
+        rng = np.random.default_rng(5)
+        per = rng.integers(20000, 26000, size=3 * q).astype(np.int64)
+        pole = rng.integers(1, 11, size=3 * q).astype(np.int32)
+        eng.fit_batch(conw_r, per, pole)
+        t = eng.timing()
+        assert t["cluster_size"] == 1
+        frac = t["lit_facets"] / (t["evals"] * eng.info.ndata * eng.info.nfac)
+        assert 0.2 < frac < 0.8
+        parts = 0
+        for b in range(3):
+            eng.fit_batch(conw_r, per[b * q:(b + 1) * q], pole[b * q:(b + 1) * q])
+            tb = eng.timing()
+            assert tb["cluster_size"] == 4
+            parts += tb["lit_facets"]
+        assert parts == t["lit_facets"]
+    with Engine(data, form=PS_FORM_MIXED) as eng:
+        eng.fit_batch(eng.info.conw_r0, per[:8], pole[:8])
+        assert eng.timing()["lit_facets"] == 0
