@@ -2306,14 +2306,18 @@ __device__ int gauss_jordan(double *A, double *b, int n, double *col, int *ipiv,
     __syncthreads();
     for (int step = 0; step < n; step++) {
         // pivot search: largest |a| over unpivoted rows and columns; ties go
-        // to the last element in row-major order (the reference's >=).
-        double bv = -1.0;
+        // to the last element in row-major order (the reference's >=).  The
+        // bits of |a| order as its values do (NaN patterns, above +inf's,
+        // skipped as v >= 0 skips them), so the search compares 64-bit
+        // integers, off the FP64 unit, and picks the same pivots.
+        constexpr long long kInfBits = 0x7ff0000000000000LL;
+        long long bv = -1;
         int bi = -1;
         for (int e = tid; e < n * n; e += NT) {
             const int j = e / n, k = e - j * n;
             if (ipiv[j] != 1 && ipiv[k] == 0) {
-                const double v = fabs(A[e]);
-                if (v >= 0.0 && (v > bv || (v == bv && e > bi))) {
+                const long long v = __double_as_longlong(A[e]) & 0x7fffffffffffffffLL;
+                if (v <= kInfBits && (v > bv || (v == bv && e > bi))) {
                     bv = v;
                     bi = e;
                 }
@@ -2321,23 +2325,24 @@ __device__ int gauss_jordan(double *A, double *b, int n, double *col, int *ipiv,
         }
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) {
-            const double ov = __shfl_xor_sync(0xffffffffu, bv, o);
+            const long long ov = __shfl_xor_sync(0xffffffffu, bv, o);
             const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
             if (ov > bv || (ov == bv && oi > bi)) {
                 bv = ov;
                 bi = oi;
             }
         }
+        long long *redk = reinterpret_cast<long long *>(red);
         if (lane == 0) {
-            red[warp] = bv;
+            redk[warp] = bv;
             ipiv[n + 2 + warp] = bi;
         }
         __syncthreads();
         if (tid == 0) {
-            double v = red[0];
+            long long v = redk[0];
             int idx = ipiv[n + 2];
             for (int w = 1; w < NT / 32; w++) {
-                const double ov = red[w];
+                const long long ov = redk[w];
                 const int oi = ipiv[n + 2 + w];
                 if (ov > v || (ov == v && oi > idx)) {
                     v = ov;
