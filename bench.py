@@ -106,8 +106,8 @@ def _args():
                          "pipes and the FP64 form on a tenth of them")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--full-scan", action="store_true",
-                    help="also run the whole scan of the workload as one refined scan (rank 0) and report its "
-                         "time and best period (full_scan)")
+                    help="also run the whole scan of the workload (rank 0) as one refined scan and as one learned "
+                         "cascade and report their times and best periods (full_scan)")
     return ap.parse_args()
 
 
@@ -757,15 +757,23 @@ def run_engine_arm(args):
         c2 = c2_measurement(args.c2, local, peaks) if args.c2 > 0 else None
         full = None
         if args.full_scan:
-            torch.cuda.synchronize()
-            t_full0 = time.perf_counter()
-            rows_f, stf = eng.scan_refined(conw_r, 1, n_max)
-            torch.cuda.synchronize()
-            t_full = time.perf_counter() - t_full0
-            b = int(stf["best_index"])
-            full = {"periods": n_max, "fits": n_max * 10, "fp64_refits": int(stf["fits_refit"]),
-                    "seconds": t_full, "fits_per_s": n_max * 10 / t_full, "best_index": b,
-                    "best_period_h": float(rows_f["period_h"][b - 1]), "truth_period_h": truth["period_h"]}
+            from periodsearch_gb300 import learned
+
+            # the whole job: every period of the object, by the refined scan
+            # and by the learned cascade (the chosen form)
+            full = {"periods": n_max, "fits": n_max * 10, "truth_period_h": truth["period_h"]}
+            for key, run in (("refined", lambda: eng.scan_refined(conw_r, 1, n_max)),
+                             ("learned", lambda: eng.scan_learned(conw_r, 1, n_max, **learned.cascade_defaults()))):
+                torch.cuda.synchronize()
+                t_full0 = time.perf_counter()
+                rows_f, stf = run()
+                torch.cuda.synchronize()
+                t_full = time.perf_counter() - t_full0
+                b = int(stf["best_index"])
+                full[key] = {"seconds": t_full, "fits_per_s": n_max * 10 / t_full, "best_index": b,
+                             "best_period_h": float(rows_f["period_h"][b - 1]),
+                             "fits_completed": int(stf["fits_completed"]), "fp64_refits": int(stf["fits_refit"])}
+            full["same_best_period"] = full["refined"]["best_index"] == full["learned"]["best_index"]
         cb = None
         c2_check = c2.pop("_check", None) if c2 else None
         if not args.no_cpu_baseline and world == 1:
